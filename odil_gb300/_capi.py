@@ -1,0 +1,126 @@
+"""ctypes binding of libodil_gb300.so (the C ABI declared in include/odil_gb300.h).
+
+The library is the only compute path: if it is missing, every call raises.
+Arguments are raw device pointers (``tensor.data_ptr()``), sizes and the
+current torch stream handle; nothing here copies or allocates on its own.
+"""
+import ctypes
+import os
+
+import torch
+
+from . import _build
+
+ODIL_OK = 0
+_STATUS = {
+    -1: "ODIL_ERR_SHAPE",
+    -2: "ODIL_ERR_DTYPE",
+    -3: "ODIL_ERR_ALIGN",
+    -4: "ODIL_ERR_LAUNCH",
+    -5: "ODIL_ERR_TIMEOUT",
+    -6: "ODIL_ERR_NONFINITE",
+    -7: "ODIL_ERR_WORKSPACE",
+    -8: "ODIL_ERR_ARG",
+}
+
+
+class OdilError(RuntimeError):
+    """A libodil_gb300 entry point returned a negative status."""
+
+    def __init__(self, fn, status, text):
+        super().__init__("%s failed: %s (%d): %s" %
+                         (fn, _STATUS.get(status, "?"), status, text))
+        self.status = status
+
+
+class OdilWaveParams(ctypes.Structure):
+    _fields_ = [
+        ("nt", ctypes.c_int64),
+        ("nx", ctypes.c_int64),
+        ("dt", ctypes.c_double),
+        ("dx", ctypes.c_double),
+        ("c", ctypes.c_double),
+        ("init_u", ctypes.c_void_p),
+        ("init_ut", ctypes.c_void_p),
+        ("left_u", ctypes.c_void_p),
+        ("right_u", ctypes.c_void_p),
+    ]
+
+
+_P = ctypes.c_void_p
+_I64 = ctypes.c_int64
+_D = ctypes.c_double
+_INT = ctypes.c_int
+
+# name -> (restype, argtypes)
+SIGNATURES = {
+    "odil_version": (_INT, []),
+    "odil_status_string": (ctypes.c_char_p, [_INT]),
+    "odil_wave_workspace_bytes": (_I64, [_P]),
+    "odil_wave_residual_f32": (_INT, [_P, _P, _P, _P]),
+    "odil_wave_residual_f64": (_INT, [_P, _P, _P, _P]),
+    "odil_wave_loss_grad_f32": (_INT, [_P, _P, _P, _P, _P, _I64, _P]),
+    "odil_wave_loss_grad_f64": (_INT, [_P, _P, _P, _P, _P, _I64, _P]),
+    "odil_wave_jv_f32": (_INT, [_P, _P, _P, _P]),
+    "odil_wave_jv_f64": (_INT, [_P, _P, _P, _P]),
+    "odil_wave_jtv_f32": (_INT, [_P, _P, _P, _P]),
+    "odil_wave_jtv_f64": (_INT, [_P, _P, _P, _P]),
+    "odil_wave_march_f32": (_INT, [_P, _P, _P, _P]),
+    "odil_wave_march_f64": (_INT, [_P, _P, _P, _P]),
+    "odil_wave_refine_mixed": (_INT, [_P, _P, _P, _P]),
+}
+
+_lib = None
+
+
+def lib_path():
+    return os.path.join(_build.LIBDIR, _build.LIBNAME)
+
+
+def load():
+    """Loads libodil_gb300.so once; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = lib_path()
+    if not os.path.exists(path):
+        raise RuntimeError(
+            "libodil_gb300.so is not built (%s); run "
+            "`python -c 'import __graft_entry__ as g; g.build()'` first. "
+            "There is no CPU fallback." % path)
+    lib = ctypes.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def exported_symbols():
+    return list(SIGNATURES)
+
+
+def stream_handle(device=None):
+    return ctypes.c_void_p(torch.cuda.current_stream(device).cuda_stream)
+
+
+def call(name, *args):
+    """Calls entry point `name`; raises OdilError on a negative status."""
+    lib = load()
+    st = getattr(lib, name)(*args)
+    if st != ODIL_OK:
+        text = lib.odil_status_string(st).decode()
+        raise OdilError(name, st, text)
+    return st
+
+
+def ptr(t):
+    """Device pointer of a CUDA tensor (None -> NULL)."""
+    if t is None:
+        return None
+    if not t.is_cuda:
+        raise ValueError("expected a CUDA tensor, got device %s" % t.device)
+    if not t.is_contiguous():
+        raise ValueError("expected a contiguous tensor")
+    return ctypes.c_void_p(t.data_ptr())

@@ -1,0 +1,109 @@
+// Shared device helpers of libodil_gb300: status handling, index wrapping and
+// the deterministic two-level FP64 reduction used by every loss kernel.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/odil_gb300.h"
+
+#define ODIL_API extern "C" __attribute__((visibility("default")))
+
+namespace odil {
+
+inline int launch_status() {
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? ODIL_OK : ODIL_ERR_LAUNCH;
+}
+
+inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+// Periodic wrap of an index that is at most one period outside [0, n).
+__device__ __forceinline__ int wrap1(int i, int n) {
+    return i < 0 ? i + n : (i >= n ? i - n : i);
+}
+// Periodic wrap of an arbitrary index.
+__device__ __forceinline__ int wrapn(int i, int n) {
+    int r = i % n;
+    return r < 0 ? r + n : r;
+}
+
+template <typename T>
+__device__ __forceinline__ T ldg(const T* p) { return __ldg(p); }
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Sum over the block; the result is valid in every thread.  Fixed tree, so
+// the result is bitwise reproducible for a fixed blockDim.
+__device__ __forceinline__ double block_sum(double v) {
+    __shared__ double red[32];
+    __shared__ double total;
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    const int nwarp = (blockDim.x + 31) >> 5;
+    v = warp_sum(v);
+    __syncthreads();  // protect `red` and `total` against a previous call
+    if (lane == 0) red[warp] = v;
+    __syncthreads();
+    if (warp == 0) {
+        double w = lane < nwarp ? red[lane] : 0.0;
+        w = warp_sum(w);
+        if (lane == 0) total = w;
+    }
+    __syncthreads();
+    return total;
+}
+
+// Workspace layout of a reduction: [counter | pad to 256 B | partials...].
+struct ReduceWs {
+    unsigned* counter;
+    double* partials;
+};
+
+constexpr int64_t kReduceHeader = 256;
+
+inline int64_t reduce_ws_bytes(int64_t nblocks) {
+    return kReduceHeader + nblocks * (int64_t)sizeof(double);
+}
+
+inline ReduceWs reduce_ws(void* ws) {
+    ReduceWs r;
+    r.counter = reinterpret_cast<unsigned*>(ws);
+    r.partials = reinterpret_cast<double*>(reinterpret_cast<char*>(ws) + kReduceHeader);
+    return r;
+}
+
+// Called by every thread of every block with the thread's partial sum.  Block
+// `bid` of `nblocks` stores its sum; the last block to arrive adds the partial
+// sums in index order (deterministic), writes out[0] = sum * scale and resets
+// the counter to zero for the next call.
+__device__ __forceinline__ void reduce_finish(double v, int64_t bid, int64_t nblocks,
+                                              ReduceWs ws, double scale, double* out) {
+    __shared__ bool is_last;
+    v = block_sum(v);
+    if (threadIdx.x == 0) {
+        ws.partials[bid] = v;
+        __threadfence();
+        unsigned prev = atomicAdd(ws.counter, 1u);
+        is_last = (prev == (unsigned)(nblocks - 1));
+    }
+    __syncthreads();
+    if (is_last) {
+        __threadfence();
+        double s = 0.0;
+        for (int64_t k = threadIdx.x; k < nblocks; k += blockDim.x) {
+            s += __ldcg(ws.partials + k);
+        }
+        s = block_sum(s);
+        if (threadIdx.x == 0) {
+            out[0] = s * scale;
+            *ws.counter = 0u;
+        }
+    }
+}
+
+}  // namespace odil

@@ -1,0 +1,476 @@
+// 1D wave operator on the (t, x) space-time grid: residual, fused loss+adjoint
+// gradient, matrix-free J v / J^T w, and the forward-substitution direct solve.
+//
+// Reference: wave.py:67-122 (operator_fd), util_op.py:508-563 (roll semantics
+// of Context.field), util_op.py:585-614 (per-shift Jacobian), util_op.py:
+// 627-654 (loss), linsolver.py:28-45 (Newton linear solve).
+//
+// Jacobian in stencil form.  Row (i, j) of J couples to five "slots":
+//   u = (i, j), tm = (i-1, j), tmm = (i-2, j), xm = (i-1, j-1), xp = (i-1, j+1)
+// (indices periodic, as tf.roll).  With A = 1/dt^2, B = c^2/dx^2:
+//   row 0:   c_u = 1, all other slots 0
+//   row >=1: c_u = A, c_tm = -(1 or 2) A + B k_tm, c_tmm = (0 or 1) A,
+//            c_xm = -B k_xm, c_xp = -B k_xp
+// where (k_tm, k_xm, k_xp) depend on the column class through the quadratic
+// extrapolation of the x-halo: interior (2, 1, 1), j = 0 (4, 0, 4/3),
+// j = nx-1 (4, 4/3, 0), nx = 1 (20/3, 0, 4/9).  These are the derivatives
+// tf.GradientTape returns for each rolled argument, including the zero
+// gradient through the branch tf.where did not take.
+#include "common.cuh"
+
+namespace odil {
+namespace {
+
+template <typename T>
+struct WaveDev {
+    int nt, nx;
+    T inv_dt, inv_dx2, c2, half_dt;
+    T A, B;       // 1/dt^2, c^2/dx^2
+    T dt2, lam2;  // dt^2, c^2 dt^2 / dx^2
+    const T* init_u;
+    const T* init_ut;
+    const T* left_u;
+    const T* right_u;
+};
+
+template <typename T>
+int make_dev(const odil_wave_params* p, WaveDev<T>* g, bool with_bc) {
+    if (!p) return ODIL_ERR_ARG;
+    if (p->nt < 1 || p->nx < 1 || p->nt > (1 << 30) || p->nx > (1 << 30) ||
+        p->nt * p->nx > (int64_t(1) << 31) - 1)
+        return ODIL_ERR_SHAPE;
+    if (!(p->dt > 0) || !(p->dx > 0)) return ODIL_ERR_ARG;
+    g->nt = (int)p->nt;
+    g->nx = (int)p->nx;
+    const double inv_dt = 1.0 / p->dt;
+    const double inv_dx2 = 1.0 / (p->dx * p->dx);
+    g->inv_dt = (T)inv_dt;
+    g->inv_dx2 = (T)inv_dx2;
+    g->c2 = (T)(p->c * p->c);
+    g->half_dt = (T)(0.5 * p->dt);
+    g->A = (T)(inv_dt * inv_dt);
+    g->B = (T)(p->c * p->c * inv_dx2);
+    g->dt2 = (T)(p->dt * p->dt);
+    g->lam2 = (T)(p->c * p->c * p->dt * p->dt * inv_dx2);
+    g->init_u = with_bc ? (const T*)p->init_u : nullptr;
+    g->init_ut = with_bc ? (const T*)p->init_ut : nullptr;
+    g->left_u = with_bc ? (const T*)p->left_u : nullptr;
+    g->right_u = with_bc ? (const T*)p->right_u : nullptr;
+    return ODIL_OK;
+}
+
+template <typename T>
+__device__ __forceinline__ T opt_ld(const T* p, int k) {
+    return p ? __ldg(p + k) : T(0);
+}
+
+// Residual of cell (i, j) from its five stencil values, in the operation order
+// of wave.py:106-118.
+template <typename T>
+__device__ __forceinline__ T wave_f(const WaveDev<T>& g, int i, int j, T u, T utm, T utmm,
+                                    T uxm, T uxp) {
+    if (i == 0) {
+        return u - (opt_ld(g.init_u, j) + g.half_dt * opt_ld(g.init_ut, j));
+    }
+    if (j == 0) uxm = (uxp - T(6) * utm + T(8) * opt_ld(g.left_u, i - 1)) / T(3);
+    if (j == g.nx - 1) uxp = (uxm - T(6) * utm + T(8) * opt_ld(g.right_u, i - 1)) / T(3);
+    const T u_t_tm = (u - utm) * g.inv_dt;
+    const T u_t_tmm = (i == 1) ? opt_ld(g.init_ut, j) : (utm - utmm) * g.inv_dt;
+    const T u_tt = (u_t_tm - u_t_tmm) * g.inv_dt;
+    const T u_xx = (uxm - T(2) * utm + uxp) * g.inv_dx2;
+    return u_tt - g.c2 * u_xx;
+}
+
+// Column-class factors of d(u_xx_raw)/d(slot) (see the header comment).
+template <typename T>
+__device__ __forceinline__ T k_tm(int col, int nx) {
+    if (nx == 1) return T(20.0 / 3.0);
+    return (col == 0 || col == nx - 1) ? T(4) : T(2);
+}
+template <typename T>
+__device__ __forceinline__ T k_xm(int col, int nx) {
+    if (nx == 1 || col == 0) return T(0);
+    return col == nx - 1 ? T(4.0 / 3.0) : T(1);
+}
+template <typename T>
+__device__ __forceinline__ T k_xp(int col, int nx) {
+    if (nx == 1) return T(4.0 / 9.0);
+    if (col == nx - 1) return T(0);
+    return col == 0 ? T(4.0 / 3.0) : T(1);
+}
+
+// Gather of J^T at cell (a, b): sum over the rows that read u[a, b].
+// f_* are the values of the multiplied vector at the dependent rows.
+template <typename T>
+__device__ __forceinline__ T wave_gather(const WaveDev<T>& g, int a, int b, T f_u, T f_tm,
+                                         T f_tmm, T f_xm, T f_xp) {
+    const int nt = g.nt, nx = g.nx;
+    T s = (a == 0 ? T(1) : g.A) * f_u;
+    if (a + 1 < nt) {
+        const T ctm = (a + 1 == 1 ? -g.A : T(-2) * g.A) + g.B * k_tm<T>(b, nx);
+        s += ctm * f_tm;
+        const int bp = (b + 1 == nx) ? 0 : b + 1;
+        const int bm = (b == 0) ? nx - 1 : b - 1;
+        s -= g.B * (k_xm<T>(bp, nx) * f_xm + k_xp<T>(bm, nx) * f_xp);
+    }
+    if (a + 2 < nt) s += g.A * f_tmm;
+    return s;
+}
+
+// ---------------------------------------------------------------------------
+// Residual / J v: one thread per cell, stencil values through the read-only
+// cache (each u is reused by 5 neighbouring threads; DRAM sees it once).
+template <typename T>
+__global__ void __launch_bounds__(256) wave_residual_kernel(WaveDev<T> g, const T* __restrict__ u,
+                                                            T* __restrict__ f) {
+    const int nx = g.nx;
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= nx) return;
+    for (int i = blockIdx.y; i < g.nt; i += gridDim.y) {
+        const T uc = __ldg(u + (int64_t)i * nx + j);
+        T utm = 0, utmm = 0, uxm = 0, uxp = 0;
+        if (i >= 1) {
+            const T* r1 = u + (int64_t)(i - 1) * nx;
+            utm = __ldg(r1 + j);
+            uxm = __ldg(r1 + (j == 0 ? nx - 1 : j - 1));
+            uxp = __ldg(r1 + (j + 1 == nx ? 0 : j + 1));
+        }
+        if (i >= 2) utmm = __ldg(u + (int64_t)(i - 2) * nx + j);
+        f[(int64_t)i * nx + j] = wave_f(g, i, j, uc, utm, utmm, uxm, uxp);
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) wave_jtv_kernel(WaveDev<T> g, const T* __restrict__ w,
+                                                       T* __restrict__ out) {
+    const int nx = g.nx, nt = g.nt;
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= nx) return;
+    const int bp = (b + 1 == nx) ? 0 : b + 1;
+    const int bm = (b == 0) ? nx - 1 : b - 1;
+    for (int a = blockIdx.y; a < nt; a += gridDim.y) {
+        const T fu = __ldg(w + (int64_t)a * nx + b);
+        T ftm = 0, fxm = 0, fxp = 0, ftmm = 0;
+        if (a + 1 < nt) {
+            const T* r1 = w + (int64_t)(a + 1) * nx;
+            ftm = __ldg(r1 + b);
+            fxm = __ldg(r1 + bp);
+            fxp = __ldg(r1 + bm);
+        }
+        if (a + 2 < nt) ftmm = __ldg(w + (int64_t)(a + 2) * nx + b);
+        out[(int64_t)a * nx + b] = wave_gather(g, a, b, fu, ftm, ftmm, fxm, fxp);
+    }
+}
+
+template <typename T>
+void grid_rows(const WaveDev<T>& g, dim3* grid, dim3* block) {
+    const int bx = g.nx >= 256 ? 256 : ((g.nx + 31) / 32) * 32;
+    *block = dim3(bx);
+    int gy = g.nt < 65535 ? g.nt : 65535;
+    *grid = dim3((g.nx + bx - 1) / bx, gy);
+}
+
+// ---------------------------------------------------------------------------
+// Fused loss + adjoint gradient.  A block owns a TY x TX tile of the gradient:
+// it stages u with a halo of 2 rows/cols in shared memory, evaluates the
+// residual on the (TY+2) x (TX+2) cells whose rows read the tile, keeps those
+// residuals in shared memory only, and gathers J^T f.  The tile's own
+// residuals feed the FP64 loss partial.
+constexpr int LG_TY = 16;
+constexpr int LG_TX = 64;
+constexpr int LG_THREADS = 256;
+
+template <typename T>
+__global__ void __launch_bounds__(LG_THREADS) wave_loss_grad_kernel(WaveDev<T> g,
+                                                                    const T* __restrict__ u,
+                                                                    T* __restrict__ grad,
+                                                                    ReduceWs ws, double* loss,
+                                                                    T gscale, double lscale) {
+    constexpr int UY = LG_TY + 4, UX = LG_TX + 4;
+    constexpr int FY = LG_TY + 2, FX = LG_TX + 2;
+    __shared__ T su[UY][UX + 1];
+    __shared__ T sf[FY][FX + 1];
+    const int nt = g.nt, nx = g.nx;
+    const int a0 = blockIdx.y * LG_TY;
+    const int b0 = blockIdx.x * LG_TX;
+    const bool col_inner = (b0 >= 2) && (b0 + LG_TX + 2 <= nx);
+    const bool row_inner = (a0 >= 2) && (a0 + LG_TY + 2 <= nt);
+
+    // Stage u rows a0-2 .. a0+TY+1, cols b0-2 .. b0+TX+1 (periodic, as tf.roll).
+    for (int k = threadIdx.x; k < UY * UX; k += LG_THREADS) {
+        const int rr = k / UX, cc = k - rr * UX;
+        int r = a0 - 2 + rr, c = b0 - 2 + cc;
+        if (!row_inner) r = wrapn(r, nt);
+        if (!col_inner) c = wrapn(c, nx);
+        su[rr][cc] = __ldg(u + (int64_t)r * nx + c);
+    }
+    __syncthreads();
+
+    // Residuals of rows a0 .. a0+TY+1, cols b0-1 .. b0+TX.
+    for (int k = threadIdx.x; k < FY * FX; k += LG_THREADS) {
+        const int rr = k / FX, cc = k - rr * FX;
+        const int r = a0 + rr;
+        T val = T(0);
+        if (r < nt) {
+            int c = b0 - 1 + cc;
+            if (!col_inner) c = wrapn(c, nx);
+            val = wave_f(g, r, c, su[rr + 2][cc + 1], su[rr + 1][cc + 1], su[rr][cc + 1],
+                         su[rr + 1][cc], su[rr + 1][cc + 2]);
+        }
+        sf[rr][cc] = val;
+    }
+    __syncthreads();
+
+    double lsum = 0.0;
+    for (int k = threadIdx.x; k < LG_TY * LG_TX; k += LG_THREADS) {
+        const int rr = k / LG_TX, cc = k - rr * LG_TX;
+        const int a = a0 + rr, b = b0 + cc;
+        if (a < nt && b < nx) {
+            const T fu = sf[rr][cc + 1];
+            lsum += (double)fu * (double)fu;
+            const T gs = wave_gather(g, a, b, fu, sf[rr + 1][cc + 1], sf[rr + 2][cc + 1],
+                                     sf[rr + 1][cc + 2], sf[rr + 1][cc]);
+            grad[(int64_t)a * nx + b] = gs * gscale;
+        }
+    }
+    const int64_t bid = (int64_t)blockIdx.y * gridDim.x + blockIdx.x;
+    const int64_t nb = (int64_t)gridDim.x * gridDim.y;
+    reduce_finish(lsum, bid, nb, ws, lscale, loss);
+}
+
+inline dim3 lg_grid(int nt, int nx) {
+    return dim3((nx + LG_TX - 1) / LG_TX, (nt + LG_TY - 1) / LG_TY);
+}
+
+// ---------------------------------------------------------------------------
+// Forward substitution J x = b, one block marching the rows.  Thread t owns
+// columns t, t + blockDim, ... (CPT of them); row i-1 lives in a double
+// buffer in shared memory for the x-neighbours, rows i-1 and i-2 of the own
+// columns stay in registers.  Right-hand sides are prefetched PF rows ahead.
+// REFINE: b is the FP64 residual r (rhs = -r) and the solution is added to
+// the FP64 field `u` in place.
+constexpr int MARCH_PF = 4;
+
+template <typename TS, typename TB, bool REFINE, int CPT>
+__global__ void __launch_bounds__(1024) wave_march_kernel(WaveDev<TS> g, const TB* __restrict__ b,
+                                                          void* __restrict__ xout) {
+    extern __shared__ unsigned char smem_raw[];
+    TS* buf = reinterpret_cast<TS*>(smem_raw);  // [2][nx]
+    const int nx = g.nx, nt = g.nt;
+    const int nthr = blockDim.x;
+    TS kxm[CPT], ktm[CPT], kxp[CPT], d1[CPT], d2[CPT];
+    int jm[CPT], jp[CPT];
+#pragma unroll
+    for (int c = 0; c < CPT; ++c) {
+        const int j = threadIdx.x + c * nthr;
+        const int jj = j < nx ? j : 0;
+        ktm[c] = k_tm<TS>(jj, nx);
+        kxm[c] = k_xm<TS>(jj, nx);
+        kxp[c] = k_xp<TS>(jj, nx);
+        jm[c] = jj == 0 ? nx - 1 : jj - 1;
+        jp[c] = jj + 1 == nx ? 0 : jj + 1;
+        d1[c] = TS(0);
+        d2[c] = TS(0);
+    }
+    TB pre[MARCH_PF][CPT];
+    double upre[REFINE ? MARCH_PF : 1][CPT];
+#pragma unroll
+    for (int s = 0; s < MARCH_PF; ++s) {
+#pragma unroll
+        for (int c = 0; c < CPT; ++c) {
+            const int j = threadIdx.x + c * nthr;
+            const bool ok = (s < nt) && (j < nx);
+            pre[s][c] = ok ? __ldcs(b + (int64_t)s * nx + j) : TB(0);
+            if constexpr (REFINE) {
+                upre[s][c] = ok ? __ldcs(reinterpret_cast<double*>(xout) + (int64_t)s * nx + j) : 0.0;
+            }
+        }
+    }
+    for (int i0 = 0; i0 < nt; i0 += MARCH_PF) {
+#pragma unroll
+        for (int s = 0; s < MARCH_PF; ++s) {
+            const int i = i0 + s;
+            if (i >= nt) break;
+            TS* cur = buf + (i & 1) * nx;
+            const TS* prv = buf + ((i & 1) ^ 1) * nx;
+            TS dnew[CPT];
+#pragma unroll
+            for (int c = 0; c < CPT; ++c) {
+                const int j = threadIdx.x + c * nthr;
+                TS rhs = REFINE ? TS(-(double)pre[s][c]) : TS(pre[s][c]);
+                TS v;
+                if (i == 0) {
+                    v = rhs;
+                } else {
+                    const TS tprev = (i == 1) ? d1[c] : TS(2) * d1[c] - d2[c];
+                    TS xm = TS(0), xp = TS(0);
+                    if (j < nx) {
+                        xm = prv[jm[c]];
+                        xp = prv[jp[c]];
+                    }
+                    v = g.dt2 * rhs + tprev + g.lam2 * (kxm[c] * xm - ktm[c] * d1[c] + kxp[c] * xp);
+                }
+                dnew[c] = v;
+            }
+            // Prefetch row i + PF into the slot just consumed.
+            {
+                const int ip = i + MARCH_PF;
+#pragma unroll
+                for (int c = 0; c < CPT; ++c) {
+                    const int j = threadIdx.x + c * nthr;
+                    if (j < nx) {
+                        if constexpr (REFINE) {
+                            double* uo = reinterpret_cast<double*>(xout) + (int64_t)i * nx + j;
+                            *uo = upre[s][c] + (double)dnew[c];
+                        } else {
+                            reinterpret_cast<TS*>(xout)[(int64_t)i * nx + j] = dnew[c];
+                        }
+                    }
+                    const bool ok = (ip < nt) && (j < nx);
+                    pre[s][c] = ok ? __ldcs(b + (int64_t)ip * nx + j) : TB(0);
+                    if constexpr (REFINE) {
+                        upre[s][c] = ok ? __ldcs(reinterpret_cast<double*>(xout) + (int64_t)ip * nx + j)
+                                        : 0.0;
+                    }
+                    d2[c] = d1[c];
+                    d1[c] = dnew[c];
+                    if (j < nx) cur[j] = dnew[c];
+                }
+            }
+            __syncthreads();
+        }
+    }
+}
+
+template <typename TS, typename TB, bool REFINE>
+int launch_march(const WaveDev<TS>& g, const TB* b, void* x, cudaStream_t st) {
+    const int nx = g.nx;
+    if (nx > 2048) return ODIL_ERR_SHAPE;
+    const int cpt = nx > 1024 ? 2 : 1;
+    int threads = (nx + cpt - 1) / cpt;
+    threads = ((threads + 31) / 32) * 32;
+    const size_t smem = 2 * (size_t)nx * sizeof(TS);
+    auto go = [&](auto kern) {
+        if (smem > 48 * 1024) {
+            cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        }
+        kern<<<1, threads, smem, st>>>(g, b, x);
+    };
+    if (cpt == 1) {
+        go(wave_march_kernel<TS, TB, REFINE, 1>);
+    } else {
+        go(wave_march_kernel<TS, TB, REFINE, 2>);
+    }
+    return launch_status();
+}
+
+template <typename T>
+int residual_impl(const odil_wave_params* p, const T* u, T* f, void* stream, bool with_bc) {
+    WaveDev<T> g;
+    int st = make_dev<T>(p, &g, with_bc);
+    if (st) return st;
+    if (!u || !f) return ODIL_ERR_ARG;
+    dim3 grid, block;
+    grid_rows(g, &grid, &block);
+    wave_residual_kernel<T><<<grid, block, 0, as_stream(stream)>>>(g, u, f);
+    return launch_status();
+}
+
+template <typename T>
+int jtv_impl(const odil_wave_params* p, const T* w, T* out, void* stream) {
+    WaveDev<T> g;
+    int st = make_dev<T>(p, &g, false);
+    if (st) return st;
+    if (!w || !out) return ODIL_ERR_ARG;
+    dim3 grid, block;
+    grid_rows(g, &grid, &block);
+    wave_jtv_kernel<T><<<grid, block, 0, as_stream(stream)>>>(g, w, out);
+    return launch_status();
+}
+
+template <typename T>
+int loss_grad_impl(const odil_wave_params* p, const T* u, T* grad, double* loss, void* ws,
+                   int64_t ws_bytes, void* stream) {
+    WaveDev<T> g;
+    int st = make_dev<T>(p, &g, true);
+    if (st) return st;
+    if (!u || !grad || !loss) return ODIL_ERR_ARG;
+    const dim3 grid = lg_grid(g.nt, g.nx);
+    if (grid.y > 65535) return ODIL_ERR_SHAPE;
+    const int64_t nb = (int64_t)grid.x * grid.y;
+    if (!ws || ws_bytes < reduce_ws_bytes(nb)) return ODIL_ERR_WORKSPACE;
+    const double n = (double)g.nt * (double)g.nx;
+    wave_loss_grad_kernel<T><<<grid, LG_THREADS, 0, as_stream(stream)>>>(
+        g, u, grad, reduce_ws(ws), loss, (T)(2.0 / n), 1.0 / n);
+    return launch_status();
+}
+
+}  // namespace
+}  // namespace odil
+
+using namespace odil;
+
+ODIL_API int64_t odil_wave_workspace_bytes(const odil_wave_params* p) {
+    if (!p || p->nt < 1 || p->nx < 1) return 0;
+    const dim3 grid = lg_grid((int)p->nt, (int)p->nx);
+    return reduce_ws_bytes((int64_t)grid.x * grid.y);
+}
+
+ODIL_API int odil_wave_residual_f32(const odil_wave_params* p, const float* u, float* f,
+                                    void* stream) {
+    return residual_impl<float>(p, u, f, stream, true);
+}
+ODIL_API int odil_wave_residual_f64(const odil_wave_params* p, const double* u, double* f,
+                                    void* stream) {
+    return residual_impl<double>(p, u, f, stream, true);
+}
+ODIL_API int odil_wave_jv_f32(const odil_wave_params* p, const float* v, float* out,
+                              void* stream) {
+    return residual_impl<float>(p, v, out, stream, false);
+}
+ODIL_API int odil_wave_jv_f64(const odil_wave_params* p, const double* v, double* out,
+                              void* stream) {
+    return residual_impl<double>(p, v, out, stream, false);
+}
+ODIL_API int odil_wave_jtv_f32(const odil_wave_params* p, const float* w, float* out,
+                               void* stream) {
+    return jtv_impl<float>(p, w, out, stream);
+}
+ODIL_API int odil_wave_jtv_f64(const odil_wave_params* p, const double* w, double* out,
+                               void* stream) {
+    return jtv_impl<double>(p, w, out, stream);
+}
+ODIL_API int odil_wave_loss_grad_f32(const odil_wave_params* p, const float* u, float* grad,
+                                     double* loss, void* workspace, int64_t workspace_bytes,
+                                     void* stream) {
+    return loss_grad_impl<float>(p, u, grad, loss, workspace, workspace_bytes, stream);
+}
+ODIL_API int odil_wave_loss_grad_f64(const odil_wave_params* p, const double* u, double* grad,
+                                     double* loss, void* workspace, int64_t workspace_bytes,
+                                     void* stream) {
+    return loss_grad_impl<double>(p, u, grad, loss, workspace, workspace_bytes, stream);
+}
+ODIL_API int odil_wave_march_f32(const odil_wave_params* p, const float* b, float* x,
+                                 void* stream) {
+    WaveDev<float> g;
+    int st = make_dev<float>(p, &g, false);
+    if (st) return st;
+    if (!b || !x) return ODIL_ERR_ARG;
+    return launch_march<float, float, false>(g, b, x, as_stream(stream));
+}
+ODIL_API int odil_wave_march_f64(const odil_wave_params* p, const double* b, double* x,
+                                 void* stream) {
+    WaveDev<double> g;
+    int st = make_dev<double>(p, &g, false);
+    if (st) return st;
+    if (!b || !x) return ODIL_ERR_ARG;
+    return launch_march<double, double, false>(g, b, x, as_stream(stream));
+}
+ODIL_API int odil_wave_refine_mixed(const odil_wave_params* p, const double* r, double* u,
+                                    void* stream) {
+    WaveDev<float> g;
+    int st = make_dev<float>(p, &g, false);
+    if (st) return st;
+    if (!r || !u) return ODIL_ERR_ARG;
+    return launch_march<float, double, true>(g, r, u, as_stream(stream));
+}

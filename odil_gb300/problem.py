@@ -1,0 +1,237 @@
+"""ODIL problem: operator evaluation, loss and gradient, linearization.
+
+Same API as util_op.py:432-973 (``Context``, ``Problem``): a user operator
+``operator(mod, ctx)`` returns a list of residual arrays, the loss is the sum
+of their mean squares (``Problem.Raw`` terms are averaged as given), and the
+gradient is the adjoint of that sum.
+
+Two routes:
+  * registered operator families (objects with ``bind(domain)``, e.g.
+    ``WaveOperator``) run the fused CUDA kernels of libodil_gb300;
+  * any other operator runs op by op as torch CUDA tensors with autograd
+    (``mod`` is the tf-style namespace of ``odil_gb300.mod``).
+Both run on the GPU; CPU tensors are rejected.
+"""
+import numpy as np
+import torch
+
+from .domain import State
+from .mod import TorchMod
+
+
+def _torch_dtype(np_dtype):
+    return torch.float32 if np.dtype(np_dtype) == np.float32 else torch.float64
+
+
+class Context:
+    """util_op.py:432-563 over torch tensors.
+
+    ``field(name, *shift)`` returns the field rolled by ``-shift``
+    (``field('u', -1, 0)[i, j] == u[i-1, j]``, periodic), ``freeze=True``
+    detaches it.
+    """
+
+    def __init__(self, domain, state_fields, epoch=0, extra=None, mod=None):
+        self.domain = domain
+        self.state_fields = state_fields
+        self.epoch = epoch
+        self.extra = extra
+        self.dtype = _torch_dtype(domain.dtype)
+        self.mod = mod
+
+    def cast(self, value, dtype=None):
+        return self.mod.cast(value, dtype or self.dtype)
+
+    def size(self, i):
+        return self.domain.size(i)
+
+    def step(self, i):
+        return self.domain.step(i)
+
+    def cell_index(self, i):
+        return self.domain.cell_index(i)
+
+    def node_index(self, i):
+        return self.domain.node_index(i)
+
+    def cell_center(self, i):
+        return self.domain.cell_center(i)
+
+    def neural_net(self, name, *inputs, **kw):
+        raise KeyError("Weights with name '{:}' not found in domain.neuralnets"
+                       .format(name))
+
+    def field(self, name, *shift, freeze=False):
+        domain = self.domain
+        assert len(shift) <= domain.ndim, "Shift is too long {:}".format(shift)
+        shift = tuple(shift) + (0, ) * (domain.ndim - len(shift))
+        if name == "zeros":
+            return self.mod.zeros(domain.shape)
+        if name == "ones":
+            return self.mod.ones(domain.shape)
+        if name not in domain.fieldnames:
+            raise ValueError("Unknown field name '" + name + "'")
+        u = self.state_fields[name]
+        if freeze:
+            u = u.detach()
+        if any(shift):
+            u = torch.roll(u, tuple(-s for s in shift), tuple(range(domain.ndim)))
+        return u
+
+
+class FusedLoss(torch.autograd.Function):
+    """loss = sum_k mean(f_k^2) of a registered family, with the gradient from
+    the fused adjoint kernel (residuals recomputed in-tile, never stored)."""
+
+    @staticmethod
+    def forward(ctx, u, kernels):
+        loss, grad = kernels.loss_grad(u.detach())
+        ctx.save_for_backward(grad)
+        return loss.reshape(()).clone()
+
+    @staticmethod
+    def backward(ctx, gout):
+        grad, = ctx.saved_tensors
+        return grad * gout.to(grad.dtype), None
+
+
+class Jacobian:
+    """Matrix-free Jacobian of a registered family (the stencil form of the
+    CSR matrix util_op.py:859-937 assembles).  ``matvec``/``rmatvec`` act on
+    packed vectors; ``solve`` is the direct Newton solve."""
+
+    def __init__(self, kernels, shape):
+        self.kernels = kernels
+        self.shape = shape
+
+    def matvec(self, v):
+        return self.kernels.jv(v.reshape(self.kernels.shape)).reshape(-1)
+
+    def rmatvec(self, w):
+        return self.kernels.jtv(w.reshape(self.kernels.shape)).reshape(-1)
+
+    def solve(self, rhs):
+        return self.kernels.march(rhs.reshape(self.kernels.shape)).reshape(-1)
+
+
+class Problem:
+    """util_op.py:566-973."""
+
+    class Raw:
+        """A pre-reduced loss term: averaged as given, not squared."""
+
+        def __init__(self, value):
+            self.value = value
+
+    def __init__(self, operator, domain, extra=None):
+        self.domain = domain
+        self.operator = operator
+        self.extra = extra
+        self.kernels = operator.bind(domain) if hasattr(operator, "bind") \
+            else None
+        self.mod = TorchMod(device=domain.device,
+                            dtype=_torch_dtype(domain.dtype))
+
+    # -- state handling (util_op.py:733-857) --------------------------------
+    @property
+    def tdtype(self):
+        return _torch_dtype(self.domain.dtype)
+
+    def init_missing(self, state):
+        for name in self.domain.fieldnames:
+            if name not in state.fields:
+                state.fields[name] = torch.zeros(self.domain.shape,
+                                                 dtype=self.tdtype,
+                                                 device=self.domain.device)
+            elif not isinstance(state.fields[name], torch.Tensor):
+                state.fields[name] = torch.as_tensor(
+                    np.asarray(state.fields[name]), dtype=self.tdtype,
+                    device=self.domain.device)
+
+    def pack_fields(self, fields):
+        return torch.cat([fields[n].reshape(-1)
+                          for n in self.domain.fieldnames])
+
+    def unpack_fields(self, packed):
+        n = self.domain.cells()
+        return {name: packed[i * n:(i + 1) * n].reshape(self.domain.shape)
+                for i, name in enumerate(self.domain.fieldnames)}
+
+    def pack_state(self, state, with_frozen=False):
+        return self.pack_fields(state.fields)
+
+    def unpack_state(self, packed, with_frozen=False):
+        return State(fields=self.unpack_fields(packed))
+
+    # -- evaluation ---------------------------------------------------------
+    def _check_device(self, state):
+        for name in self.domain.fieldnames:
+            if not state.fields[name].is_cuda:
+                raise RuntimeError(
+                    "field '%s' is on %s: the ODIL engine runs on CUDA only" %
+                    (name, state.fields[name].device))
+
+    def _generic(self, fields, epoch):
+        ctx = Context(self.domain, fields, epoch=epoch, extra=self.extra,
+                      mod=self.mod)
+        ff = self.operator(self.mod, ctx)
+        if not isinstance(ff, (list, tuple)):
+            ff = [ff]
+        return list(ff)
+
+    def eval_operator(self, state, epoch=0):
+        """util_op.py:968-973: list of residual fields."""
+        self.init_missing(state)
+        self._check_device(state)
+        if self.kernels is not None:
+            u = state.fields[self.domain.fieldnames[0]]
+            return [self.kernels.residual(u)]
+        with torch.no_grad():
+            ff = self._generic(state.fields, epoch)
+        return [f.value if isinstance(f, Problem.Raw) else f for f in ff]
+
+    def eval_loss_grad(self, state, epoch=0):
+        """util_op.py:939-966: (loss, grads, wgrads, loss_split)."""
+        self.init_missing(state)
+        self._check_device(state)
+        names = self.domain.fieldnames
+        if self.kernels is not None:
+            u = state.fields[names[0]]
+            loss, grad = self.kernels.loss_grad(u)
+            loss = loss.reshape(()).clone()
+            return loss, {names[0]: grad}, {}, [loss]
+        fields = {k: v.detach().requires_grad_(True)
+                  for k, v in state.fields.items()}
+        ff = self._generic(fields, epoch)
+        loss_split = [
+            torch.mean(f.value) if isinstance(f, Problem.Raw) else
+            torch.mean(torch.square(f)) for f in ff
+        ]
+        loss = sum(loss_split)
+        gg = torch.autograd.grad(loss, [fields[n] for n in names],
+                                 allow_unused=True)
+        grads = {n: (g if g is not None else torch.zeros_like(fields[n]))
+                 for n, g in zip(names, gg)}
+        return loss.detach(), grads, {}, [l.detach() for l in loss_split]
+
+    def loss(self, u):
+        """Differentiable loss of the packed state (torch.autograd.Function
+        over the fused adjoint for registered families)."""
+        if self.kernels is not None:
+            return FusedLoss.apply(u.reshape(self.kernels.shape), self.kernels)
+        fields = self.unpack_fields(u)
+        ff = self._generic(fields, 0)
+        return sum(torch.mean(f.value) if isinstance(f, Problem.Raw) else
+                   torch.mean(torch.square(f)) for f in ff)
+
+    def linearize(self, state, epoch=0):
+        """util_op.py:859-937: (const, J) with J matrix-free on the GPU."""
+        self.init_missing(state)
+        self._check_device(state)
+        if self.kernels is None:
+            raise NotImplementedError(
+                "linearize needs a registered operator family; generic "
+                "operators use eval_loss_grad")
+        const = self.eval_operator(state, epoch)
+        n = self.domain.cells()
+        return const, Jacobian(self.kernels, (len(const) * n, n))

@@ -1,0 +1,184 @@
+"""1D wave operator family: the registered, fused-kernel form of
+wave.py:67-122 (operator_fd) of the reference.
+
+``WaveOperator`` is a drop-in ``operator(mod, ctx)``: called with the torch
+``mod`` it evaluates the residual op by op (generic path, used to validate the
+fused path), and ``Problem`` binds it to ``WaveKernels``, which run the
+hand-written kernels of libodil_gb300 on the GPU.
+"""
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _capi
+from ._capi import call, ptr, stream_handle
+
+
+def extrap_quadh(u0, u1, u1p):
+    """util_op.py:1017-1023: quadratic extrapolation to the face value."""
+    return (u0 - 6 * u1 + 8 * u1p) / 3
+
+
+class WaveOperator:
+    """Registered operator family "wave".
+
+    Boundary data as wave.py:457-464 builds them: ``init_u``, ``init_ut``
+    ([nx], at t=0 and x cell centres), ``left_u``/``right_u`` ([nt], at
+    x = lower/upper and t cell centres).  ``c`` is the wave speed (the
+    reference has c = 1).
+    """
+    family = "wave"
+
+    def __init__(self, init_u, init_ut, left_u, right_u, c=1.0):
+        self.init_u = np.asarray(init_u, np.float64)
+        self.init_ut = np.asarray(init_ut, np.float64)
+        self.left_u = np.asarray(left_u, np.float64)
+        self.right_u = np.asarray(right_u, np.float64)
+        self.c = float(c)
+
+    def bind(self, domain):
+        assert domain.ndim == 2 and len(domain.fieldnames) == 1, \
+            "the wave family has one field on a (t, x) grid"
+        nt, nx = domain.shape
+        return WaveKernels(nt, nx, domain.step(0), domain.step(1), self.c,
+                           self.init_u, self.init_ut, self.left_u,
+                           self.right_u, device=domain.device)
+
+    def __call__(self, mod, ctx):
+        """Op-by-op form of wave.py:67-122 (generic path)."""
+        dt = ctx.step(0)
+        dx = ctx.step(1)
+        it = ctx.cell_index(0)
+        ix = ctx.cell_index(1)
+        nx = ctx.size(1)
+        key = ctx.domain.fieldnames[0]
+        st = [
+            ctx.field(key),
+            ctx.field(key, -1, 0),
+            ctx.field(key, -2, 0),
+            ctx.field(key, -1, -1),
+            ctx.field(key, -1, 1)
+        ]
+        left_utm = mod.roll(self.left_u, 1, axis=0)
+        right_utm = mod.roll(self.right_u, 1, axis=0)
+        st[3] = mod.where(ix == 0, extrap_quadh(st[4], st[1], left_utm[:, None]),
+                          st[3])
+        st[4] = mod.where(ix == nx - 1,
+                          extrap_quadh(st[3], st[1], right_utm[:, None]),
+                          st[4])
+        u, utm, utmm, uxm, uxp = st
+        init_ut = mod.constant(self.init_ut)
+        u_t_tm = (u - utm) / dt
+        u_t_tmm = (utm - utmm) / dt
+        u_t_tmm = mod.where(it == 1, init_ut[None, :], u_t_tmm)
+        u_tt = (u_t_tm - u_t_tmm) / dt
+        u_xx = (uxm - 2 * utm + uxp) / (dx**2)
+        fu = u_tt - self.c**2 * u_xx
+        u0 = mod.constant(self.init_u + 0.5 * dt * self.init_ut)
+        fu = mod.where(it == 0, u - u0[None, :], fu)
+        return [fu]
+
+
+class WaveKernels:
+    """Device-side state of one wave instance and its fused kernels.
+
+    Holds the boundary data in FP64 and FP32 copies, the C-ABI parameter
+    structs and the loss workspace.  One instance per CUDA stream: the
+    workspace is reused by every loss call.
+    """
+
+    def __init__(self, nt, nx, dt, dx, c, init_u, init_ut, left_u, right_u,
+                 device="cuda"):
+        _capi.load()
+        self.nt, self.nx = int(nt), int(nx)
+        self.shape = (self.nt, self.nx)
+        self.n = self.nt * self.nx
+        self.dt, self.dx, self.c = float(dt), float(dx), float(c)
+        self.device = torch.device(device)
+        bc = [init_u, init_ut, left_u, right_u]
+        sizes = [self.nx, self.nx, self.nt, self.nt]
+        for a, s in zip(bc, sizes):
+            if np.asarray(a).shape != (s, ):
+                raise ValueError("boundary array has shape %s, expected (%d,)"
+                                 % (np.asarray(a).shape, s))
+        self.bc64 = [torch.as_tensor(np.asarray(a, np.float64),
+                                     device=self.device) for a in bc]
+        self.bc32 = [a.float() for a in self.bc64]
+        self.p64 = self._params(self.bc64)
+        self.p32 = self._params(self.bc32)
+        nbytes = _capi.load().odil_wave_workspace_bytes(ctypes.byref(self.p64))
+        self.workspace = torch.zeros(int(nbytes), dtype=torch.uint8,
+                                     device=self.device)
+        self.loss_buf = torch.zeros(1, dtype=torch.float64, device=self.device)
+
+    def _params(self, bc):
+        p = _capi.OdilWaveParams()
+        p.nt, p.nx, p.dt, p.dx, p.c = self.nt, self.nx, self.dt, self.dx, self.c
+        p.init_u, p.init_ut, p.left_u, p.right_u = [t.data_ptr() for t in bc]
+        return p
+
+    def _pp(self, t):
+        if t.dtype == torch.float64:
+            return ctypes.byref(self.p64), "f64"
+        if t.dtype == torch.float32:
+            return ctypes.byref(self.p32), "f32"
+        raise TypeError("wave kernels take float32 or float64, got %s" % t.dtype)
+
+    def _check(self, t):
+        if tuple(t.shape) != self.shape and t.numel() != self.n:
+            raise ValueError("field has shape %s, expected %s" %
+                             (tuple(t.shape), self.shape))
+        if t.device != self.device and not (t.is_cuda and
+                                            self.device.type == "cuda"):
+            raise ValueError("field on %s, kernels on %s" %
+                             (t.device, self.device))
+
+    def residual(self, u, out=None):
+        self._check(u)
+        p, sfx = self._pp(u)
+        out = torch.empty_like(u) if out is None else out
+        call("odil_wave_residual_" + sfx, p, ptr(u), ptr(out), stream_handle())
+        return out
+
+    def jv(self, v, out=None):
+        self._check(v)
+        p, sfx = self._pp(v)
+        out = torch.empty_like(v) if out is None else out
+        call("odil_wave_jv_" + sfx, p, ptr(v), ptr(out), stream_handle())
+        return out
+
+    def jtv(self, w, out=None):
+        self._check(w)
+        p, sfx = self._pp(w)
+        out = torch.empty_like(w) if out is None else out
+        call("odil_wave_jtv_" + sfx, p, ptr(w), ptr(out), stream_handle())
+        return out
+
+    def loss_grad(self, u, grad=None, loss=None):
+        """Fused loss+adjoint: returns (loss [1] float64 tensor, grad)."""
+        self._check(u)
+        p, sfx = self._pp(u)
+        grad = torch.empty_like(u) if grad is None else grad
+        loss = self.loss_buf if loss is None else loss
+        call("odil_wave_loss_grad_" + sfx, p, ptr(u), ptr(grad), ptr(loss),
+             ptr(self.workspace), self.workspace.numel(), stream_handle())
+        return loss, grad
+
+    def march(self, b, out=None):
+        """Direct solve of J x = b by forward substitution."""
+        self._check(b)
+        p, sfx = self._pp(b)
+        out = torch.empty_like(b) if out is None else out
+        call("odil_wave_march_" + sfx, p, ptr(b), ptr(out), stream_handle())
+        return out
+
+    def refine_mixed(self, r, u):
+        """u += J^{-1}(-r) with the solve in FP32 (r, u FP64)."""
+        self._check(r)
+        self._check(u)
+        if r.dtype != torch.float64 or u.dtype != torch.float64:
+            raise TypeError("refine_mixed takes FP64 residual and field")
+        call("odil_wave_refine_mixed", ctypes.byref(self.p64), ptr(r), ptr(u),
+             stream_handle())
+        return u

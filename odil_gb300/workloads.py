@@ -1,0 +1,80 @@
+"""Seeded synthetic problem instances (the benchmark workloads).
+
+No dataset is involved: every input is generated from a seed.
+
+Wave (wave.py:380-483 of the reference, plus a wave speed and a seeded
+profile): u_tt = c^2 u_xx on t in [0, 1], x in [-1, 1].
+  * profile "cos": the reference's fixed 5-mode cosine profile
+    (wave.py:27-39), u_t(x, 0) != 0, c = 1;
+  * profile "sine": f(x) = sum_k a_k sin(k pi (x + 1) / 2), a_k ~ N(0,1)/k from
+    numpy default_rng(seed); exact solution u = (f(x - ct) + f(x + ct)) / 2
+    (odd-periodic extension, zero Dirichlet values, u_t(x, 0) = 0).
+"""
+import numpy as np
+
+from .domain import Domain
+from .wave import WaveOperator
+
+
+def cell_centers(lower, upper, n):
+    x = np.linspace(lower, upper, n, endpoint=False, dtype=np.float64)
+    h = (x[1] - x[0]) if n > 1 else (upper - lower)
+    return x + h * 0.5
+
+
+def wave_exact_cos(t, x):
+    """u and u_t of the reference profile (u_t analytically)."""
+    u = np.zeros(np.broadcast(t, x).shape)
+    ut = np.zeros_like(u)
+    for i in (1, 2, 3, 4, 5):
+        k = i * np.pi
+        u = u + np.cos((x - t + 0.5) * k) + np.cos((x + t - 0.5) * k)
+        ut = ut + k * np.sin((x - t + 0.5) * k) - k * np.sin((x + t - 0.5) * k)
+    return u / 10.0, ut / 10.0
+
+
+def sine_amplitudes(seed, nmodes):
+    rng = np.random.default_rng(seed)
+    return rng.standard_normal(nmodes) / np.arange(1, nmodes + 1)
+
+
+def wave_exact_sine(t, x, amps, c=1.0):
+    t = np.asarray(t, np.float64)
+    x = np.asarray(x, np.float64)
+    u = np.zeros(np.broadcast(t, x).shape)
+    ut = np.zeros_like(u)
+    for k, a in enumerate(amps, start=1):
+        w = k * np.pi / 2
+        u = u + a * (np.sin(w * (x - c * t + 1)) + np.sin(w * (x + c * t + 1)))
+        ut = ut + a * c * w * (-np.cos(w * (x - c * t + 1)) +
+                               np.cos(w * (x + c * t + 1)))
+    return 0.5 * u, 0.5 * ut
+
+
+class WaveInstance:
+    """Domain, operator and exact solution of one wave problem."""
+
+    def __init__(self, nt, nx, profile="sine", seed=0, nmodes=5, c=1.0,
+                 dtype=np.float64, device="cuda"):
+        self.nt, self.nx = int(nt), int(nx)
+        self.profile, self.seed, self.nmodes, self.c = profile, seed, nmodes, c
+        self.domain = Domain(ndim=2, shape=(nt, nx), lower=(0, -1),
+                             upper=(1, 1), varnames=('t', 'x'),
+                             fieldnames=('u', ), dtype=dtype, device=device)
+        t1 = cell_centers(0.0, 1.0, nt)
+        x1 = cell_centers(-1.0, 1.0, nx)
+        if profile == "cos":
+            if c != 1.0:
+                raise ValueError("the reference cosine profile has c = 1")
+            ex = wave_exact_cos
+        elif profile == "sine":
+            amps = sine_amplitudes(seed, nmodes)
+            ex = lambda t, x: wave_exact_sine(t, x, amps, c)
+        else:
+            raise ValueError("Unknown profile=" + profile)
+        left_u, _ = ex(t1, t1 * 0 - 1.0)
+        right_u, _ = ex(t1, t1 * 0 + 1.0)
+        init_u, init_ut = ex(x1 * 0, x1)
+        tt, xx = np.meshgrid(t1, x1, indexing="ij")
+        self.exact_u, _ = ex(tt, xx)
+        self.operator = WaveOperator(init_u, init_ut, left_u, right_u, c=c)

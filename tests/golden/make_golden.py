@@ -1,0 +1,132 @@
+#!/usr/bin/env python3
+"""Regenerates the golden fixtures in this folder from the reference checkout.
+
+Run from the repository root, on a machine that has the reference at
+/root/reference (it does not exist on the GPU machines, which only read the
+committed JSON/NPZ files):
+
+    python tests/golden/make_golden.py [--ref /root/reference]
+
+Fixtures
+  wave_fd_newton.json   N and ref_du_l2 after 2 Newton epochs, read from the
+                        reference's cases/wave_cost/precomputed/fd_newton/
+                        lines.pickle (fields N, error).
+  wave_fd_lbfgsb.json   same for the L-BFGS-B runs (fd_lbfgsb/lines.pickle).
+  multigrid_ref.npz     outputs of the reference's multigrid.py (NumPy
+                        backend) on small odd grids: restriction and
+                        interpolation operators, stencil products, Galerkin
+                        coarsening, transposed products (see make_multigrid).
+  cavity_N128.npz       u, v, p fields of the reference's FP64 Newton cavity
+                        solutions cases/cavity_stream/cavity_N128_Re{100,400}.
+"""
+import argparse
+import json
+import os
+import pickle
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def load_lines(ref, name):
+    path = os.path.join(ref, "code/cases/wave_cost/precomputed", name,
+                        "lines.pickle")
+    with open(path, "rb") as f:
+        d = pickle.load(f)
+    return {
+        "source": "code/cases/wave_cost/precomputed/%s/lines.pickle" % name,
+        "N": [int(n) for n in d.N],
+        "error": [float(e) for e in d.error],
+        "time_epoch": [float(t) for t in d.time_epoch],
+        "epochs": [float(e) for e in d.epochs],
+    }
+
+
+def make_multigrid(ref):
+    """Evaluates the reference's multigrid.py on deterministic inputs."""
+    sys.path.insert(0, os.path.join(ref, "code"))
+    import types
+    sys.modules.setdefault("multigrid_plot", types.ModuleType("multigrid_plot"))
+    import scipy.sparse as sp
+    import multigrid as mg
+
+    mod = mg.ModNumpy(np, sp)
+    out = {}
+    dtype = np.float64
+
+    def field(nw, seed):
+        n = int(np.prod(nw))
+        return np.sin(seed * 0.123 + np.linspace(0, 3, n)).reshape(nw)
+
+    for nw in [(9,), (17,), (9, 9), (5, 9), (17, 17), (5, 5, 9)]:
+        key = "x".join(map(str, nw))
+        nw_a = np.array(nw)
+        R = mg.MultigridOp.get_R(nw_a, mod=mod, dtype=dtype)
+        TT = mg.MultigridOp.get_TT(nw_a, mod=mod, dtype=dtype)
+        u = field(nw, 1)
+        uh = field(R.nwh, 2)
+        out["R_%s" % key] = R.mul_field(u)
+        out["T_%s" % key] = TT.mul_transpose_field(uh)
+        out["Rcsr_%s" % key] = R.tocsr().toarray() if np.prod(nw) <= 81 \
+            else np.zeros(1)
+        # A generic stencil operator with random coefficient fields.
+        dim = len(nw)
+        shifts = [tuple(s) for s in np.array(np.meshgrid(
+            *[[-1, 0, 1]] * dim, indexing="ij")).reshape(dim, -1).T]
+        stf = {}
+        for i, s in enumerate(shifts):
+            stf[s] = field(nw, 10 + i)
+        A = mg.SparseOperator(stf, nw_a, mod=mod, dtype=dtype)
+        out["A_shifts_%s" % key] = np.array(shifts)
+        out["A_coefs_%s" % key] = np.stack([stf[s] for s in shifts])
+        out["Au_%s" % key] = A.mul_field(u)
+        out["ATu_%s" % key] = A.mul_transpose_field(u)
+        AtA = A.mul_transpose_op(A)
+        out["AtA_shifts_%s" % key] = np.array(
+            [list(k) for k in AtA.shift_to_field.keys()])
+        out["AtA_coefs_%s" % key] = np.stack(
+            [np.asarray(c).reshape(nw) for c in AtA.shift_to_field.values()])
+        Ah = mg.MultigridOp.coarsen_sparse_operator(A, R, TT, mod=mod,
+                                                    dtype=dtype)
+        out["Ah_shifts_%s" % key] = np.array(
+            [list(k) for k in Ah.shift_to_field.keys()])
+        out["Ah_coefs_%s" % key] = np.stack([
+            np.asarray(c).reshape(Ah.nwh) for c in Ah.shift_to_field.values()
+        ])
+    return out
+
+
+def make_cavity(ref):
+    res = {}
+    for re_ in (100, 400):
+        path = os.path.join(ref, "code/cases/cavity_stream",
+                            "cavity_N128_Re%d.pickle" % re_)
+        with open(path, "rb") as f:
+            s = pickle.load(f)
+        for k in ("u", "v", "p"):
+            res["Re%d_%s" % (re_, k)] = np.asarray(s["fields"][k], np.float64)
+    return res
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--only", default=None)
+    a = ap.parse_args()
+    todo = a.only.split(",") if a.only else ["wave", "multigrid", "cavity"]
+    if "wave" in todo:
+        for name in ("fd_newton", "fd_lbfgsb"):
+            with open(os.path.join(HERE, "wave_%s.json" % name), "w") as f:
+                json.dump(load_lines(a.ref, name), f, indent=1)
+    if "multigrid" in todo:
+        np.savez_compressed(os.path.join(HERE, "multigrid_ref.npz"),
+                            **make_multigrid(a.ref))
+    if "cavity" in todo:
+        np.savez_compressed(os.path.join(HERE, "cavity_N128.npz"),
+                            **make_cavity(a.ref))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,211 @@
+"""GPU parity tests of the wave kernels against the CPU oracle.
+
+Tolerances: FP64 kernels agree with the FP64 oracle to 1e-10 relative to the
+field's max (different but equivalent operation order); FP32 kernels to
+2e-5 relative on the residual/J v/J^T w (cancellation of O(1/dt^2) terms),
+and FP32 gradients to 1e-4 relative.
+"""
+import numpy as np
+import pytest
+import torch
+
+from oracle import wave as W
+from oracle import autodiff as AD
+
+pytestmark = pytest.mark.gpu
+
+SHAPES = [(1, 5), (2, 3), (3, 1), (4, 2), (17, 33), (64, 64), (70, 130),
+          (129, 257), (256, 96)]
+
+
+def _setup(nt, nx, seed=0, c=1.3):
+    rng = np.random.default_rng(seed)
+    return W.WaveSetup(nt, nx, rng.standard_normal(nx), rng.standard_normal(nx),
+                       rng.standard_normal(nt), rng.standard_normal(nt), c=c)
+
+
+def _kernels(s, dev):
+    from odil_gb300.wave import WaveKernels
+    return WaveKernels(s.nt, s.nx, s.dt, s.dx, s.c, s.init_u, s.init_ut,
+                       s.left_u, s.right_u, device=dev)
+
+
+def _rel(a, b):
+    return np.abs(np.asarray(a) - np.asarray(b)).max() / max(
+        np.abs(np.asarray(b)).max(), 1e-300)
+
+
+@pytest.mark.parametrize("shape", SHAPES)
+def test_residual_f64_f32(cuda, shape):
+    s = _setup(*shape)
+    k = _kernels(s, cuda)
+    u = np.random.default_rng(1).standard_normal(shape)
+    fo = W.residual(s, u)
+    f64 = k.residual(torch.as_tensor(u, device=cuda)).cpu().numpy()
+    assert _rel(f64, fo) < 1e-12
+    f32 = k.residual(torch.as_tensor(u, dtype=torch.float32,
+                                     device=cuda)).cpu().numpy()
+    fo32 = W.residual(s, u.astype(np.float32).astype(np.float64))
+    assert _rel(f32, fo32) < 2e-5
+
+
+@pytest.mark.parametrize("shape", SHAPES)
+def test_jv_jtv_against_csr(cuda, shape):
+    s = _setup(*shape, seed=2)
+    k = _kernels(s, cuda)
+    rng = np.random.default_rng(3)
+    v = rng.standard_normal(shape)
+    w = rng.standard_normal(shape)
+    _, J = W.linearize(s, np.zeros(shape))
+    jv_o = J.dot(v.ravel()).reshape(shape)
+    jtw_o = J.T.dot(w.ravel()).reshape(shape)
+    jv = k.jv(torch.as_tensor(v, device=cuda)).cpu().numpy()
+    jtw = k.jtv(torch.as_tensor(w, device=cuda)).cpu().numpy()
+    assert _rel(jv, jv_o) < 1e-12
+    assert _rel(jtw, jtw_o) < 1e-12
+    # Adjoint identity <J v, w> = <v, J^T w> in FP64.
+    a = float(np.sum(jv * w))
+    b = float(np.sum(v * jtw))
+    assert abs(a - b) <= 1e-12 * (abs(a) + np.abs(jv).max() * np.abs(w).sum())
+    jv32 = k.jv(torch.as_tensor(v, dtype=torch.float32, device=cuda)).cpu()
+    jtw32 = k.jtv(torch.as_tensor(w, dtype=torch.float32, device=cuda)).cpu()
+    assert _rel(jv32.numpy(), jv_o) < 2e-5
+    assert _rel(jtw32.numpy(), jtw_o) < 2e-5
+
+
+@pytest.mark.parametrize("shape", SHAPES)
+def test_loss_grad_fused(cuda, shape):
+    s = _setup(*shape, seed=4)
+    k = _kernels(s, cuda)
+    u = np.random.default_rng(5).standard_normal(shape)
+    lo, go = W.loss_grad(s, u)
+    loss, grad = k.loss_grad(torch.as_tensor(u, device=cuda))
+    assert abs(loss.item() - lo) <= 1e-12 * lo
+    assert _rel(grad.cpu().numpy(), go) < 1e-12
+    loss32, grad32 = k.loss_grad(torch.as_tensor(u, dtype=torch.float32,
+                                                 device=cuda))
+    u32 = u.astype(np.float32).astype(np.float64)
+    lo32, go32 = W.loss_grad(s, u32)
+    assert abs(loss32.item() - lo32) <= 1e-5 * lo32
+    assert _rel(grad32.cpu().numpy(), go32) < 1e-4
+
+
+def test_loss_grad_deterministic_and_workspace_reset(cuda):
+    s = _setup(300, 200, seed=6)
+    k = _kernels(s, cuda)
+    u = torch.as_tensor(np.random.default_rng(7).standard_normal((300, 200)),
+                        device=cuda)
+    vals = []
+    for _ in range(5):
+        loss, grad = k.loss_grad(u)
+        vals.append((loss.item(), grad.sum().item()))
+    assert all(v == vals[0] for v in vals)
+    # The reduction counter is back to zero after every call.
+    assert int(k.workspace[:4].view(torch.int32).item()) == 0
+
+
+def test_gradient_against_autodiff_and_fd(cuda):
+    """Fused FP32 adjoint gradient vs (a) the FP64 autodiff gradient of the
+    op-by-op operator and (b) central finite differences (step 1e-3, FP64) on
+    64 seeded coordinates."""
+    nt = nx = 96
+    s = W.make_setup(nt, nx, "sine", seed=1, nmodes=16)
+    k = _kernels(s, cuda)
+    rng = np.random.default_rng(11)
+    u = W.solve_march(s) + 0.05 * rng.standard_normal((nt, nx))
+    u32 = u.astype(np.float32).astype(np.float64)
+    _, g_ad = AD.wave_loss_grad_autodiff(s, u32)
+    _, g = k.loss_grad(torch.as_tensor(u32, dtype=torch.float32, device=cuda))
+    g = g.cpu().numpy().astype(np.float64)
+    assert _rel(g, g_ad) < 1e-4
+    idx = rng.choice(nt * nx, 64, replace=False)
+    h = 1e-3
+    for q in idx:
+        e = np.zeros(nt * nx)
+        e[q] = h
+        e = e.reshape(nt, nx)
+        fd = (np.mean(W.residual(s, u32 + e)**2) -
+              np.mean(W.residual(s, u32 - e)**2)) / (2 * h)
+        assert abs(g.ravel()[q] - fd) <= 1e-3 * np.abs(g).max() + 1e-4 * abs(fd)
+
+
+@pytest.mark.parametrize("shape", [(1, 4), (2, 1), (3, 2), (64, 64), (100, 37),
+                                   (257, 1024), (64, 2048)])
+def test_march_direct_solve(cuda, shape):
+    s = _setup(*shape, seed=8, c=0.9)
+    k = _kernels(s, cuda)
+    b = np.random.default_rng(9).standard_normal(shape)
+    xo = W.march(s, b)
+    x = k.march(torch.as_tensor(b, device=cuda)).cpu().numpy()
+    assert _rel(x, xo) < 1e-10
+    x32 = k.march(torch.as_tensor(b, dtype=torch.float32, device=cuda))
+    assert _rel(x32.cpu().numpy(), xo) < 1e-3
+
+
+def test_mixed_newton_reaches_oracle(cuda):
+    """Mixed precision (FP64 residual, FP32 solve) converges to the FP64
+    discrete solution of the 1024^2 benchmark wave to <= 1e-5 (here 1e-9)."""
+    n = 1024
+    s = W.make_setup(n, n, "sine", seed=1, nmodes=16)
+    ref = W.solve_march(s)
+    k = _kernels(s, cuda)
+    x = torch.zeros((n, n), dtype=torch.float64, device=cuda)
+    errs = []
+    for _ in range(4):
+        r = k.residual(x)
+        k.refine_mixed(r, x)
+        errs.append(W.rel_err(x.cpu().numpy(), ref))
+    assert errs[1] <= 1e-5, errs
+    assert errs[-1] <= 1e-9, errs
+
+
+def test_generic_operator_matches_fused(cuda):
+    """The op-by-op torch path of WaveOperator equals the fused kernels."""
+    from odil_gb300.workloads import WaveInstance
+    from odil_gb300.problem import Problem
+    inst = WaveInstance(40, 30, profile="sine", seed=3, nmodes=5, c=1.1,
+                        device=cuda)
+    fused = Problem(inst.operator, inst.domain)
+
+    def op(mod, ctx):
+        return inst.operator(mod, ctx)
+
+    generic = Problem(op, inst.domain)
+    from odil_gb300.domain import State
+    rng = np.random.default_rng(0)
+    st = State(fields={"u": torch.as_tensor(rng.standard_normal((40, 30)),
+                                            device=cuda)})
+    f1 = fused.eval_operator(st)[0]
+    f2 = generic.eval_operator(st)[0]
+    assert _rel(f1.cpu().numpy(), f2.cpu().numpy()) < 1e-12
+    l1, g1, _, _ = fused.eval_loss_grad(st)
+    l2, g2, _, _ = generic.eval_loss_grad(st)
+    assert abs(l1.item() - l2.item()) <= 1e-12 * l2.item()
+    assert _rel(g1["u"].cpu().numpy(), g2["u"].cpu().numpy()) < 1e-12
+
+
+def test_autograd_function_backward(cuda):
+    from odil_gb300.workloads import WaveInstance
+    from odil_gb300.problem import Problem
+    inst = WaveInstance(32, 32, profile="cos", device=cuda)
+    prob = Problem(inst.operator, inst.domain)
+    u = torch.randn(32 * 32, dtype=torch.float64, device=cuda,
+                    requires_grad=True)
+    loss = prob.loss(u)
+    loss.backward()
+    _, g = prob.kernels.loss_grad(u.detach().reshape(32, 32))
+    assert torch.equal(u.grad.reshape(32, 32), g)
+
+
+def test_errors_are_loud(cuda):
+    from odil_gb300._capi import OdilError
+    s = _setup(8, 8)
+    k = _kernels(s, cuda)
+    with pytest.raises(ValueError):
+        k.residual(torch.zeros((8, 8)))  # CPU tensor
+    with pytest.raises(TypeError):
+        k.residual(torch.zeros((8, 8), dtype=torch.float16, device=cuda))
+    s2 = _setup(4, 4096)
+    k2 = _kernels(s2, cuda)
+    with pytest.raises(OdilError):
+        k2.march(torch.zeros((4, 4096), dtype=torch.float64, device=cuda))
