@@ -4,9 +4,11 @@
 Workload: 1D wave u_tt = c^2 u_xx on a 1024 x 1024 (t, x) grid, c = 1, seeded
 16-mode sine profile (seed 1), exact Dirichlet data (the 1024^2 wave
 configuration of the benchmark set).  One "solve" takes u = 0 to the discrete
-solution with the mixed-precision Newton method (FP64 residual + FP32 direct
-solve per epoch, 3 epochs).  Beside it: the plain FP64 GPU method (FP64
-residual + FP64 direct solve, 2 epochs as the reference runs Newton).
+solution with the mixed-precision Newton method (per epoch: FP64 residual on
+all SMs + FP32 direct solve by forward substitution; 2 epochs as the reference
+runs Newton).  Beside it: the plain FP64 GPU method (FP64 residual + FP64
+direct solve, 2 epochs), and the workload's optimizer runs (L-BFGS m=50 and
+Adam lr=1e-3, 2000 iterations each, FP32 fused adjoint gradient).
 
 Prints one JSON line (rank 0).  ``--impl reference`` times the reference's
 CPU method instead (linearize + normal equations + SuperLU MMD_ATA, the
@@ -28,7 +30,8 @@ sys.path.insert(0, HERE)
 
 NT = NX = 1024
 SEED, NMODES, C = 1, 16, 1.0
-MIXED_EPOCHS, FP64_EPOCHS = 3, 2
+MIXED_EPOCHS = FP64_EPOCHS = 2
+OPT_ITERS = 2000
 L2_FLUSH_BYTES = 256 << 20
 WORKLOAD = "wave1d_1024x1024_sine16_seed1"
 METRIC = "ODIL solves/s at rel err <=1e-5 vs FP64 oracle"
@@ -41,6 +44,11 @@ def parse():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=("ours", "reference"))
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--case", default=None,
+                    choices=("march", "march64", "update_residual", "loss_grad",
+                             "loss_grad64", "lbfgs_iter", "adam_iter"),
+                    help="run one kernel of the workload --steps times (for "
+                    "profiler captures) instead of the benchmark")
     return ap.parse_args()
 
 
@@ -165,6 +173,47 @@ class Clocks:
                 "reasons": sorted(reasons), "samples": len(rows)}
 
 
+def run_optimizers(problem, inst, dev, with_oracle):
+    """L-BFGS (m=50) and Adam (lr=1e-3), OPT_ITERS iterations each from u=0,
+    FP32 state and fused FP32 adjoint gradient; wall time per iteration and
+    the error against the exact solution (and the FP64 oracle)."""
+    import torch
+    from odil_gb300.optimizer import make_optimizer
+    from odil_gb300.problem import Problem
+    from odil_gb300.workloads import WaveInstance
+    inst32 = WaveInstance(NT, NX, profile="sine", seed=SEED, nmodes=NMODES,
+                          c=C, dtype=np.float32, device=dev)
+    prob = Problem(inst32.operator, inst32.domain)
+    kk = prob.kernels
+    grad = torch.empty(NT * NX, dtype=torch.float32, device=dev)
+
+    def lg(x, epoch):
+        loss, g = kk.loss_grad(x.reshape(NT, NX), grad=torch.empty_like(grad))
+        return loss, g.reshape(-1), [loss]
+
+    res = {}
+    ref = oracle_solution() if with_oracle else None
+    for name in ("lbfgsb", "adam"):
+        opt = make_optimizer(name)
+        x0 = torch.zeros(NT * NX, dtype=torch.float32, device=dev)
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        x, info = opt.run(x0, lg, epochs=OPT_ITERS, lr=1e-3)
+        torch.cuda.synchronize(dev)
+        wall = time.perf_counter() - t0
+        xs = x.double().cpu().numpy().reshape(NT, NX)
+        loss, _ = kk.loss_grad(x.reshape(NT, NX))
+        ent = {"iterations": int(info.epochs), "evals": int(info.evals),
+               "wall_s": wall, "ms_per_iter": 1000 * wall / max(1, info.epochs),
+               "final_loss": float(loss.item()),
+               "err_vs_exact_l2": float(np.mean((xs - inst.exact_u)**2)**0.5)}
+        if ref is not None:
+            ent["rel_err_vs_oracle"] = float(np.linalg.norm(xs - ref) /
+                                             np.linalg.norm(ref))
+        res[name] = ent
+    return res
+
+
 def run_ours(args):
     import torch
     import torch.distributed as dist
@@ -230,15 +279,22 @@ def run_ours(args):
     t_fp64 = timed(solve_fp64, max(3, args.steps // 2), max(3, args.warmup))
     u_fp64 = u.cpu().numpy()
 
-    # Dominant kernel: the fused FP32 forward substitution with FP64 update.
-    r = k.residual(u)
-    v = u.clone()
-    t_march = timed(lambda: k.refine_mixed(r, v), 20, 3)
-    t_res = timed(lambda: k.residual(u, out=r), 20, 3)
-    # Fused loss+adjoint (FP32) of the same grid, for the kernel table.
+    # Per-kernel times (same stream, CUDA events, L2 flushed before each).
+    rhs = torch.empty((NT, NX), dtype=torch.float32, device=dev)
+    d32 = torch.empty_like(rhs)
+    ub = torch.empty_like(u)
+    k.update_residual_mixed(u, None, None, rhs)
+    t_march = timed(lambda: k.march(rhs, out=d32), 20, 3)
+    t_upd = timed(lambda: k.update_residual_mixed(u, d32, ub, rhs), 20, 3)
+    r64 = torch.empty_like(u)
+    t_march64 = timed(lambda: k.march(r64, out=ub), 5, 2)
     u32 = u.float()
     g32 = torch.empty_like(u32)
     t_lg = timed(lambda: k.loss_grad(u32, grad=g32), 20, 3)
+
+    # The workload's optimizer runs (FP32 fused adjoint gradient).
+    opt_info = run_optimizers(problem, inst, dev, rank == 0 and
+                              not args.no_cpu_baseline)
 
     # End to end through the public API: boundary data from pinned host
     # memory each step, solution back to pinned host memory.
@@ -270,9 +326,10 @@ def run_ours(args):
     e2e_ms = statistics.mean(t_e2e)
     fp64_ms = statistics.mean(t_fp64)
     march_ms = statistics.mean(t_march)
+    upd_ms = statistics.mean(t_upd)
     n = NT * NX
-    march_bytes = 24 * n  # read r (8), read u (8), write u (8) per cell
-    res_bytes = 16 * n    # read u, write r (FP64)
+    march_bytes = 8 * n   # read rhs (4), write d (4) per cell, FP32
+    upd_bytes = 28 * n    # read u (8), d (4); write u_out (8), rhs (4)... + r
     lg_bytes = 8 * n      # read u, write grad (FP32)
 
     peaks = {}
@@ -302,7 +359,7 @@ def run_ours(args):
                              "substitution), %d epochs" % MIXED_EPOCHS,
                    "l2": "flushed (256 MiB write) before every timed solve",
                    "parallelism": "replicas" if world > 1 else "single"},
-        "gpu_launches": 2 * MIXED_EPOCHS * args.steps,
+        "gpu_launches": (2 * MIXED_EPOCHS + 1) * args.steps,
         "clocks": clk,
         "e2e": {"value": 1000.0 / e2e_ms, "unit": "solves/s",
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
@@ -310,20 +367,22 @@ def run_ours(args):
         "plain_fp64": {"value": 1000.0 / fp64_ms, "unit": "solves/s",
                        "epochs": FP64_EPOCHS,
                        "speedup_mixed_over_fp64": fp64_ms / (total_ms / args.steps)},
-        "roofline": {"kernel": "wave_march_kernel<float,double,REFINE>",
+        "roofline": {"kernel": "wave_march_kernel<float>",
                      "bound": "hbm", "achieved": march_bytes / (march_ms * 1e6),
                      "peak": hbm, "unit": "GB/s",
                      "frac": march_bytes / (march_ms * 1e6) / hbm,
                      "traffic": None, "peak_source": peak_src,
                      "note": "latency-bound: one block marches 1024 dependent "
-                             "rows"},
+                             "rows (algorithmic bytes 8 per cell)"},
         "kernels": {
-            "refine_mixed_ms": march_ms,
-            "residual_f64_ms": statistics.mean(t_res),
-            "residual_f64_GBs": res_bytes / (statistics.mean(t_res) * 1e6),
+            "march_f32_ms": march_ms,
+            "update_residual_mixed_ms": upd_ms,
+            "update_residual_mixed_GBs": upd_bytes / (upd_ms * 1e6),
+            "march_f64_ms": statistics.mean(t_march64),
             "loss_grad_f32_ms": statistics.mean(t_lg),
             "loss_grad_f32_GBs": lg_bytes / (statistics.mean(t_lg) * 1e6),
         },
+        "optimizers": opt_info,
     }
     if rank == 0 and not args.no_cpu_baseline:
         ref = oracle_solution()
@@ -339,9 +398,56 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+def run_case(args):
+    """Runs one kernel of the 1024^2 workload (warmup + steps launches)."""
+    import torch
+    from odil_gb300.problem import Problem
+    from odil_gb300.workloads import WaveInstance
+    from odil_gb300 import vec
+    dev = torch.device("cuda", 0)
+    inst = WaveInstance(NT, NX, profile="sine", seed=SEED, nmodes=NMODES, c=C,
+                        device=dev)
+    k = Problem(inst.operator, inst.domain).kernels
+    u = torch.as_tensor(inst.exact_u, device=dev)
+    rhs = torch.empty((NT, NX), dtype=torch.float32, device=dev)
+    d32 = torch.zeros_like(rhs)
+    ub = torch.empty_like(u)
+    u32 = u.float()
+    g32 = torch.empty_like(u32)
+    g64 = torch.empty_like(u)
+    n = NT * NX
+    m = 50
+    H = torch.randn((2 * m, n), dtype=torch.float32, device=dev)
+    md = vec.MultiDot(n, 2 * m, 3, device=dev)
+    coef = torch.randn(2 * m + 1, dtype=torch.float64, device=dev)
+    mm = torch.zeros(n, dtype=torch.float32, device=dev)
+    vv = torch.zeros(n, dtype=torch.float32, device=dev)
+    k.update_residual_mixed(u, None, None, rhs)
+    fn = {
+        "march": lambda: k.march(rhs, out=d32),
+        "march64": lambda: k.march(u, out=ub),
+        "update_residual": lambda: k.update_residual_mixed(u, d32, ub, rhs),
+        "loss_grad": lambda: k.loss_grad(u32, grad=g32),
+        "loss_grad64": lambda: k.loss_grad(u, grad=g64),
+        "lbfgs_iter": lambda: (md(H, 2 * m, [u32.reshape(-1), g32.reshape(-1),
+                                              d32.reshape(-1)]),
+                               vec.lincomb(g32.reshape(-1), u32.reshape(-1), H,
+                                           2 * m, coef)),
+        "adam_iter": lambda: vec.adam_step(u32.reshape(-1), g32.reshape(-1),
+                                           mm, vv, 1e-3, 0.9, 0.999, 1e-7),
+    }[args.case]
+    for _ in range(args.warmup + args.steps):
+        fn()
+    torch.cuda.synchronize(dev)
+    print(json.dumps({"case": args.case, "launch_groups": args.warmup +
+                      args.steps}))
+
+
 def main():
     args = parse()
-    if args.impl == "reference":
+    if args.case:
+        run_case(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)

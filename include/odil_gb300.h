@@ -105,11 +105,63 @@ int odil_wave_march_f32(const odil_wave_params* p, const float* b, float* x,
 int odil_wave_march_f64(const odil_wave_params* p, const double* b, double* x,
                         void* stream);
 
-/* One mixed-precision iterative-refinement update of a Newton step
- * (util.py:242-268 with linsolver.py:28-45): given the FP64 residual r = F(u),
- * solves J d = -r in FP32 by forward substitution and applies u += d in FP64. */
-int odil_wave_refine_mixed(const odil_wave_params* p, const double* r,
-                           double* u, void* stream);
+/* One fully parallel FP64 step of a mixed-precision Newton epoch
+ * (util.py:242-268 with linsolver.py:28-45, the FP64 residual of the
+ * iterative refinement): u_out = u + d (d = FP32 correction from
+ * odil_wave_march_f32, or NULL: then u_out is not written and u is used),
+ * r = F(u_out) in FP64, rhs = (float)(-r) for the next FP32 solve, and, if
+ * rnorm2 != NULL, *rnorm2 = sum(r^2) (FP64, deterministic; needs the
+ * workspace).  u_out must not alias u.  `p` carries FP64 boundary data. */
+int64_t odil_wave_update_residual_workspace_bytes(const odil_wave_params* p);
+int odil_wave_update_residual_mixed(const odil_wave_params* p, const double* u,
+                                    const float* d, double* u_out, float* rhs,
+                                    double* rnorm2, void* workspace,
+                                    int64_t workspace_bytes, void* stream);
+
+/* ------------------------------------------------------------------------
+ * Optimizer vector kernels (n elements, contiguous).
+ * ---------------------------------------------------------------------- */
+
+/* Fused Adam step, the update of optimizer.py:301-314 (AdamNativeOptimizer,
+ * the Keras Adam equations):
+ *   m += (g - m)(1 - beta1);  v += (g^2 - v)(1 - beta2);
+ *   x -= alpha m / (sqrt(v) + epsilon),
+ * alpha = lr sqrt(1 - beta2^t) / (1 - beta1^t) computed by the caller. */
+int odil_adam_step_f32(float* x, const float* g, float* m, float* v, int64_t n,
+                       double alpha, double beta1, double beta2,
+                       double epsilon, void* stream);
+int odil_adam_step_f64(double* x, const double* g, double* m, double* v,
+                       int64_t n, double alpha, double beta1, double beta2,
+                       double epsilon, void* stream);
+
+/* z = a x + b y (z may alias x or y); the GD update of optimizer.py:260 and
+ * the line-search trial points of the L-BFGS driver. */
+int odil_axpby_f32(float* z, const float* x, const float* y, int64_t n,
+                   double a, double b, void* stream);
+int odil_axpby_f64(double* z, const double* x, const double* y, int64_t n,
+                   double a, double b, void* stream);
+
+/* Multi-dot: out[i*r + j] = sum_e M[i*ld + e] * q[j][e] for i < k, j < r
+ * (r <= 4), in one pass over M.  FP64 accumulation, deterministic order.
+ * This and odil_lincomb_* are the two streaming passes of the compact L-BFGS
+ * direction that replaces scipy's fmin_l_bfgs_b (optimizer.py:61-99):
+ * [S; Y] . g (plus the new correction pair's products), then
+ * d = c0 g + sum_i coef[i] [S; Y]_i. */
+int64_t odil_multidot_workspace_bytes(int64_t n, int k, int r);
+int odil_multidot_f32(const float* M, int64_t ld, int k, const void* const* q,
+                      int r, int64_t n, double* out, void* workspace,
+                      int64_t workspace_bytes, void* stream);
+int odil_multidot_f64(const double* M, int64_t ld, int k,
+                      const void* const* q, int r, int64_t n, double* out,
+                      void* workspace, int64_t workspace_bytes, void* stream);
+
+/* out = coef[k] * x + sum_{i<k} coef[i] * M[i*ld ...]; coef is a device array
+ * of k+1 doubles; k <= 256. */
+int odil_lincomb_f32(float* out, const float* x, const float* M, int64_t ld,
+                     int k, const double* coef, int64_t n, void* stream);
+int odil_lincomb_f64(double* out, const double* x, const double* M,
+                     int64_t ld, int k, const double* coef, int64_t n,
+                     void* stream);
 
 #ifdef __cplusplus
 }

@@ -67,7 +67,20 @@ SIGNATURES = {
     "odil_wave_jtv_f64": (_INT, [_P, _P, _P, _P]),
     "odil_wave_march_f32": (_INT, [_P, _P, _P, _P]),
     "odil_wave_march_f64": (_INT, [_P, _P, _P, _P]),
-    "odil_wave_refine_mixed": (_INT, [_P, _P, _P, _P]),
+    "odil_wave_update_residual_workspace_bytes": (_I64, [_P]),
+    "odil_wave_update_residual_mixed": (_INT, [_P, _P, _P, _P, _P, _P, _P, _I64,
+                                               _P]),
+    "odil_adam_step_f32": (_INT, [_P, _P, _P, _P, _I64, _D, _D, _D, _D, _P]),
+    "odil_adam_step_f64": (_INT, [_P, _P, _P, _P, _I64, _D, _D, _D, _D, _P]),
+    "odil_axpby_f32": (_INT, [_P, _P, _P, _I64, _D, _D, _P]),
+    "odil_axpby_f64": (_INT, [_P, _P, _P, _I64, _D, _D, _P]),
+    "odil_multidot_workspace_bytes": (_I64, [_I64, _INT, _INT]),
+    "odil_multidot_f32": (_INT, [_P, _I64, _INT, _P, _INT, _I64, _P, _P, _I64,
+                                 _P]),
+    "odil_multidot_f64": (_INT, [_P, _I64, _INT, _P, _INT, _I64, _P, _P, _I64,
+                                 _P]),
+    "odil_lincomb_f32": (_INT, [_P, _P, _P, _I64, _INT, _P, _I64, _P]),
+    "odil_lincomb_f64": (_INT, [_P, _P, _P, _I64, _INT, _P, _I64, _P]),
 }
 
 _lib = None

@@ -1,0 +1,347 @@
+// Vector kernels of the optimizers: fused Adam update, deterministic dot and
+// multi-dot products, linear combinations (L-BFGS compact direction), axpby.
+//
+// Reference: optimizer.py:301-314 (AdamNativeOptimizer update, the Keras Adam
+// equations), optimizer.py:61-99 (L-BFGS-B with m = 50 correction pairs, run
+// here in the compact representation of Byrd, Nocedal & Schnabel 1994).
+// All passes are HBM-bound streaming loops with 16-byte vector accesses where
+// the pointers allow it.
+#include "common.cuh"
+
+namespace odil {
+namespace {
+
+constexpr int VT = 256;  // threads per block of the streaming kernels
+
+inline int sm_count() {
+    static int n = 0;
+    if (!n) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        if (n <= 0) n = 132;
+    }
+    return n;
+}
+
+inline int stream_blocks(int64_t n, int per_thread) {
+    int64_t need = (n + (int64_t)VT * per_thread - 1) / ((int64_t)VT * per_thread);
+    int64_t cap = (int64_t)sm_count() * 8;
+    if (need < 1) need = 1;
+    return (int)(need < cap ? need : cap);
+}
+
+template <typename T>
+struct Vec;
+template <>
+struct Vec<float> {
+    using V = float4;
+    static constexpr int W = 4;
+};
+template <>
+struct Vec<double> {
+    using V = double2;
+    static constexpr int W = 2;
+};
+
+inline bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
+
+// ---------------------------------------------------------------------------
+// Adam (optimizer.py:301-314):
+//   m += (g - m)(1 - b1);  v += (g^2 - v)(1 - b2);  x -= alpha m / (sqrt(v) + eps)
+template <typename T>
+__device__ __forceinline__ void adam1(T& x, T g, T& m, T& v, T alpha, T b1c, T b2c, T eps) {
+    m += (g - m) * b1c;
+    v += (g * g - v) * b2c;
+    x -= (m * alpha) / (sqrt(v) + eps);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(VT) adam_kernel(T* __restrict__ x, const T* __restrict__ g,
+                                                  T* __restrict__ m, T* __restrict__ v,
+                                                  int64_t n, T alpha, T b1c, T b2c, T eps,
+                                                  bool vec) {
+    using V = typename Vec<T>::V;
+    constexpr int W = Vec<T>::W;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int64_t nv = vec ? n / W : 0;
+    for (int64_t i = tid; i < nv; i += stride) {
+        V xv = reinterpret_cast<V*>(x)[i];
+        V gv = __ldcs(reinterpret_cast<const V*>(g) + i);
+        V mv = reinterpret_cast<V*>(m)[i];
+        V vv = reinterpret_cast<V*>(v)[i];
+        T* xs = reinterpret_cast<T*>(&xv);
+        T* gs = reinterpret_cast<T*>(&gv);
+        T* ms = reinterpret_cast<T*>(&mv);
+        T* vs = reinterpret_cast<T*>(&vv);
+#pragma unroll
+        for (int k = 0; k < W; ++k) adam1(xs[k], gs[k], ms[k], vs[k], alpha, b1c, b2c, eps);
+        reinterpret_cast<V*>(x)[i] = xv;
+        reinterpret_cast<V*>(m)[i] = mv;
+        reinterpret_cast<V*>(v)[i] = vv;
+    }
+    for (int64_t i = nv * W + tid; i < n; i += stride) {
+        T xs = x[i], ms = m[i], vs = v[i];
+        adam1(xs, g[i], ms, vs, alpha, b1c, b2c, eps);
+        x[i] = xs;
+        m[i] = ms;
+        v[i] = vs;
+    }
+}
+
+// z = a x + b y  (z may alias x or y)
+template <typename T>
+__global__ void __launch_bounds__(VT) axpby_kernel(T* z, const T* x, const T* y, int64_t n, T a,
+                                                   T b, bool vec) {
+    using V = typename Vec<T>::V;
+    constexpr int W = Vec<T>::W;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int64_t nv = vec ? n / W : 0;
+    for (int64_t i = tid; i < nv; i += stride) {
+        V xv = reinterpret_cast<const V*>(x)[i];
+        V yv = reinterpret_cast<const V*>(y)[i];
+        T* xs = reinterpret_cast<T*>(&xv);
+        const T* ys = reinterpret_cast<const T*>(&yv);
+#pragma unroll
+        for (int k = 0; k < W; ++k) xs[k] = a * xs[k] + b * ys[k];
+        reinterpret_cast<V*>(z)[i] = xv;
+    }
+    for (int64_t i = nv * W + tid; i < n; i += stride) z[i] = a * x[i] + b * y[i];
+}
+
+// ---------------------------------------------------------------------------
+// Multi-dot: D[i*r + j] = sum_e M[i*ld + e] * Q_j[e], i < k, j < r <= 4.
+// Block (i, c) reduces row i over column chunk c; the last block adds the
+// chunk partials in order (deterministic).  Rows of one chunk run on
+// consecutive block ids so the Q chunk is reused from L2.
+constexpr int MD_MAXR = 4;
+
+struct QPtrs {
+    const void* q[MD_MAXR];
+};
+
+template <typename T>
+__global__ void __launch_bounds__(VT) multidot_kernel(const T* __restrict__ M, int64_t ld, int k,
+                                                      QPtrs qs, int r, int64_t n, int64_t chunk,
+                                                      double* __restrict__ partials,
+                                                      unsigned* counter, double* __restrict__ out,
+                                                      bool vec) {
+    using V = typename Vec<T>::V;
+    constexpr int W = Vec<T>::W;
+    const int i = blockIdx.x;       // row
+    const int64_t c = blockIdx.y;   // chunk
+    const int64_t e0 = c * chunk;
+    int64_t e1 = e0 + chunk;
+    if (e1 > n) e1 = n;
+    const T* row = M + (int64_t)i * ld;
+    // Per-thread partial sums in the working precision (a thread adds at most
+    // chunk / (VT * W) products), FP64 across threads and blocks: the FP64
+    // pipe stays off the streaming loop.
+    T acc[MD_MAXR] = {T(0), T(0), T(0), T(0)};
+    if (vec) {
+        const int64_t v0 = e0 / W, v1 = e1 / W;
+        for (int64_t e = v0 + threadIdx.x; e < v1; e += VT) {
+            V mv = __ldcs(reinterpret_cast<const V*>(row) + e);
+            const T* ms = reinterpret_cast<const T*>(&mv);
+#pragma unroll
+            for (int j = 0; j < MD_MAXR; ++j) {
+                if (j < r) {
+                    V qv = __ldg(reinterpret_cast<const V*>(qs.q[j]) + e);
+                    const T* qq = reinterpret_cast<const T*>(&qv);
+#pragma unroll
+                    for (int w = 0; w < W; ++w) acc[j] += ms[w] * qq[w];
+                }
+            }
+        }
+        for (int64_t e = v1 * W + threadIdx.x; e < e1; e += VT) {
+            const T mval = row[e];
+            for (int j = 0; j < r; ++j) acc[j] += mval * ((const T*)qs.q[j])[e];
+        }
+    } else {
+        for (int64_t e = e0 + threadIdx.x; e < e1; e += VT) {
+            const T mval = row[e];
+            for (int j = 0; j < r; ++j) acc[j] += mval * ((const T*)qs.q[j])[e];
+        }
+    }
+    const int64_t nchunk = gridDim.y;
+    for (int j = 0; j < r; ++j) {
+        double s = block_sum((double)acc[j]);
+        if (threadIdx.x == 0) partials[((int64_t)i * r + j) * nchunk + c] = s;
+    }
+    __shared__ bool is_last;
+    if (threadIdx.x == 0) {
+        __threadfence();
+        unsigned prev = atomicAdd(counter, 1u);
+        is_last = (prev == (unsigned)((int64_t)gridDim.x * gridDim.y - 1));
+    }
+    __syncthreads();
+    if (!is_last) return;
+    __threadfence();
+    // One warp per (row, column) output, chunk partials added in order.
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = VT / 32;
+    for (int o = warp; o < k * r; o += nw) {
+        double s = 0.0;
+        for (int64_t q = lane; q < nchunk; q += 32) s += __ldcg(partials + (int64_t)o * nchunk + q);
+        s = warp_sum(s);
+        if (lane == 0) out[o] = s;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) *counter = 0u;
+}
+
+// out = c0 * x + sum_i coef[i] * M_i  (coef, c0 read from device memory).
+template <typename T>
+__global__ void __launch_bounds__(VT) lincomb_kernel(T* __restrict__ out, const T* __restrict__ x,
+                                                     const T* __restrict__ M, int64_t ld, int k,
+                                                     const double* __restrict__ coef,
+                                                     int64_t n, bool vec) {
+    using V = typename Vec<T>::V;
+    constexpr int W = Vec<T>::W;
+    __shared__ T sc[257];
+    for (int i = threadIdx.x; i <= k; i += blockDim.x) sc[i] = (T)coef[i];
+    __syncthreads();
+    const T c0 = sc[k];
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t nv = vec ? n / W : 0;
+    for (int64_t e = tid; e < nv; e += stride) {
+        V xv = __ldcs(reinterpret_cast<const V*>(x) + e);
+        T* acc = reinterpret_cast<T*>(&xv);
+#pragma unroll
+        for (int w = 0; w < W; ++w) acc[w] *= c0;
+        for (int i = 0; i < k; ++i) {
+            V mv = __ldcs(reinterpret_cast<const V*>(M + (int64_t)i * ld) + e);
+            const T* ms = reinterpret_cast<const T*>(&mv);
+            const T ci = sc[i];
+#pragma unroll
+            for (int w = 0; w < W; ++w) acc[w] += ci * ms[w];
+        }
+        reinterpret_cast<V*>(out)[e] = xv;
+    }
+    for (int64_t e = nv * W + tid; e < n; e += stride) {
+        T acc = c0 * x[e];
+        for (int i = 0; i < k; ++i) acc += sc[i] * M[(int64_t)i * ld + e];
+        out[e] = acc;
+    }
+}
+
+template <typename T>
+int adam_impl(T* x, const T* g, T* m, T* v, int64_t n, double alpha, double beta1, double beta2,
+              double eps, void* stream) {
+    if (n < 0) return ODIL_ERR_SHAPE;
+    if (n == 0) return ODIL_OK;
+    if (!x || !g || !m || !v) return ODIL_ERR_ARG;
+    const bool vec = aligned16(x) && aligned16(g) && aligned16(m) && aligned16(v);
+    const int blocks = stream_blocks(n, Vec<T>::W);
+    adam_kernel<T><<<blocks, VT, 0, as_stream(stream)>>>(x, g, m, v, n, (T)alpha,
+                                                         (T)(1.0 - beta1), (T)(1.0 - beta2),
+                                                         (T)eps, vec);
+    return launch_status();
+}
+
+template <typename T>
+int axpby_impl(T* z, const T* x, const T* y, int64_t n, double a, double b, void* stream) {
+    if (n < 0) return ODIL_ERR_SHAPE;
+    if (n == 0) return ODIL_OK;
+    if (!z || !x || !y) return ODIL_ERR_ARG;
+    const bool vec = aligned16(z) && aligned16(x) && aligned16(y);
+    axpby_kernel<T><<<stream_blocks(n, Vec<T>::W), VT, 0, as_stream(stream)>>>(z, x, y, n, (T)a,
+                                                                               (T)b, vec);
+    return launch_status();
+}
+
+inline int64_t md_chunk(int64_t n) {
+    // ~2 waves of blocks per row group; chunks are multiples of 1024 elements.
+    int64_t chunk = 1 << 16;
+    if (n < chunk) chunk = ((n + 1023) / 1024) * 1024;
+    if (chunk < 1024) chunk = 1024;
+    return chunk;
+}
+
+inline int64_t md_ws_bytes(int64_t n, int k, int r) {
+    const int64_t nchunk = (n + md_chunk(n) - 1) / md_chunk(n);
+    return kReduceHeader + (int64_t)k * r * nchunk * (int64_t)sizeof(double);
+}
+
+template <typename T>
+int multidot_impl(const T* M, int64_t ld, int k, const void* const* q, int r, int64_t n,
+                  double* out, void* ws, int64_t ws_bytes, void* stream) {
+    if (k < 1 || r < 1 || r > MD_MAXR || n < 1 || ld < n || k > 65535) return ODIL_ERR_SHAPE;
+    if (!M || !q || !out) return ODIL_ERR_ARG;
+    if (!ws || ws_bytes < md_ws_bytes(n, k, r)) return ODIL_ERR_WORKSPACE;
+    QPtrs qs = {};
+    bool vec = aligned16(M) && ((ld * (int64_t)sizeof(T)) % 16 == 0);
+    for (int j = 0; j < r; ++j) {
+        if (!q[j]) return ODIL_ERR_ARG;
+        qs.q[j] = q[j];
+        vec = vec && aligned16(q[j]);
+    }
+    const int64_t chunk = md_chunk(n);
+    const int64_t nchunk = (n + chunk - 1) / chunk;
+    if (nchunk > 65535) return ODIL_ERR_SHAPE;
+    ReduceWs w = reduce_ws(ws);
+    dim3 grid(k, (unsigned)nchunk);
+    multidot_kernel<T><<<grid, VT, 0, as_stream(stream)>>>(M, ld, k, qs, r, n, chunk, w.partials,
+                                                           w.counter, out, vec);
+    return launch_status();
+}
+
+template <typename T>
+int lincomb_impl(T* out, const T* x, const T* M, int64_t ld, int k, const double* coef, int64_t n,
+                 void* stream) {
+    if (k < 0 || k > 256 || n < 1 || (k > 0 && ld < n)) return ODIL_ERR_SHAPE;
+    if (!out || !x || !coef || (k > 0 && !M)) return ODIL_ERR_ARG;
+    const bool vec = aligned16(out) && aligned16(x) && (k == 0 || (aligned16(M) &&
+                                                                  (ld * (int64_t)sizeof(T)) % 16 == 0));
+    lincomb_kernel<T><<<stream_blocks(n, Vec<T>::W), VT, 0, as_stream(stream)>>>(out, x, M, ld, k,
+                                                                                 coef, n, vec);
+    return launch_status();
+}
+
+}  // namespace
+}  // namespace odil
+
+using namespace odil;
+
+ODIL_API int odil_adam_step_f32(float* x, const float* g, float* m, float* v, int64_t n,
+                                double alpha, double beta1, double beta2, double epsilon,
+                                void* stream) {
+    return adam_impl<float>(x, g, m, v, n, alpha, beta1, beta2, epsilon, stream);
+}
+ODIL_API int odil_adam_step_f64(double* x, const double* g, double* m, double* v, int64_t n,
+                                double alpha, double beta1, double beta2, double epsilon,
+                                void* stream) {
+    return adam_impl<double>(x, g, m, v, n, alpha, beta1, beta2, epsilon, stream);
+}
+ODIL_API int odil_axpby_f32(float* z, const float* x, const float* y, int64_t n, double a,
+                            double b, void* stream) {
+    return axpby_impl<float>(z, x, y, n, a, b, stream);
+}
+ODIL_API int odil_axpby_f64(double* z, const double* x, const double* y, int64_t n, double a,
+                            double b, void* stream) {
+    return axpby_impl<double>(z, x, y, n, a, b, stream);
+}
+ODIL_API int64_t odil_multidot_workspace_bytes(int64_t n, int k, int r) {
+    if (n < 1 || k < 1 || r < 1) return 0;
+    return md_ws_bytes(n, k, r);
+}
+ODIL_API int odil_multidot_f32(const float* M, int64_t ld, int k, const void* const* q, int r,
+                               int64_t n, double* out, void* workspace, int64_t workspace_bytes,
+                               void* stream) {
+    return multidot_impl<float>(M, ld, k, q, r, n, out, workspace, workspace_bytes, stream);
+}
+ODIL_API int odil_multidot_f64(const double* M, int64_t ld, int k, const void* const* q, int r,
+                               int64_t n, double* out, void* workspace, int64_t workspace_bytes,
+                               void* stream) {
+    return multidot_impl<double>(M, ld, k, q, r, n, out, workspace, workspace_bytes, stream);
+}
+ODIL_API int odil_lincomb_f32(float* out, const float* x, const float* M, int64_t ld, int k,
+                              const double* coef, int64_t n, void* stream) {
+    return lincomb_impl<float>(out, x, M, ld, k, coef, n, stream);
+}
+ODIL_API int odil_lincomb_f64(double* out, const double* x, const double* M, int64_t ld, int k,
+                              const double* coef, int64_t n, void* stream) {
+    return lincomb_impl<double>(out, x, M, ld, k, coef, n, stream);
+}

@@ -243,125 +243,239 @@ inline dim3 lg_grid(int nt, int nx) {
 }
 
 // ---------------------------------------------------------------------------
-// Forward substitution J x = b, one block marching the rows.  Thread t owns
-// columns t, t + blockDim, ... (CPT of them); row i-1 lives in a double
-// buffer in shared memory for the x-neighbours, rows i-1 and i-2 of the own
-// columns stay in registers.  Right-hand sides are prefetched PF rows ahead.
-// REFINE: b is the FP64 residual r (rhs = -r) and the solution is added to
-// the FP64 field `u` in place.
-constexpr int MARCH_PF = 4;
+// Forward substitution J x = b, one block marching the rows (the rows are a
+// dependency chain; the parallelism is across x).  Thread t owns the CPT
+// contiguous columns [CPT t, CPT t + CPT).  Row i-1 lives in a double buffer in
+// shared memory for the x-neighbours at the ends of a thread's run; rows i-1
+// and i-2 of the own columns stay in registers.  Right-hand-side rows stream
+// into a PF-row shared-memory ring with cp.async (one CPT-wide copy per thread
+// and row, PF-1 rows ahead of the march), so the HBM latency is off the
+// dependency chain.  Each thread copies and later reads only its own columns,
+// so cp.async.wait_group alone orders the ring; one __syncthreads per row
+// publishes the new row to the neighbours.  The row loop is unrolled by PF so
+// ring slots are compile-time constants.  No FP64 arithmetic in the FP32
+// instance: GB300's FP64 pipe would bound the chain.
+__device__ __forceinline__ void cp_async_n(void* smem, const void* gmem, int bytes) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    if (bytes == 16) {
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem));
+    } else if (bytes == 8) {
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem));
+    } else {
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem));
+    }
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(N));
+}
 
-template <typename TS, typename TB, bool REFINE, int CPT>
-__global__ void __launch_bounds__(1024) wave_march_kernel(WaveDev<TS> g, const TB* __restrict__ b,
-                                                          void* __restrict__ xout) {
-    extern __shared__ unsigned char smem_raw[];
-    TS* buf = reinterpret_cast<TS*>(smem_raw);  // [2][nx]
+template <typename T, int CPT>
+struct Chunk {
+    T v[CPT];
+};
+
+// VEC: the thread's CPT columns are contiguous and 16/8/4-byte aligned in
+// global memory (nx % CPT == 0 and aligned pointers), so the ring copy and the
+// solution store are single vector accesses.
+template <typename T, int CPT, int PF, bool VEC>
+__global__ void __launch_bounds__(1024) wave_march_kernel(WaveDev<T> g, const T* __restrict__ b,
+                                                          T* __restrict__ x) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
     const int nx = g.nx, nt = g.nt;
-    const int nthr = blockDim.x;
-    TS kxm[CPT], ktm[CPT], kxp[CPT], d1[CPT], d2[CPT];
-    int jm[CPT], jp[CPT];
+    T* buf = reinterpret_cast<T*>(smem_raw);  // [2][nx] rows i-1 / i
+    T* ring = buf + 2 * nx;                   // [PF][nx] right-hand sides
+    const int j0 = threadIdx.x * CPT;
+    const bool active = j0 < nx;
+    T kxm[CPT], ktm[CPT], kxp[CPT], d1[CPT], d2[CPT];
 #pragma unroll
     for (int c = 0; c < CPT; ++c) {
-        const int j = threadIdx.x + c * nthr;
+        const int j = j0 + c;
         const int jj = j < nx ? j : 0;
-        ktm[c] = k_tm<TS>(jj, nx);
-        kxm[c] = k_xm<TS>(jj, nx);
-        kxp[c] = k_xp<TS>(jj, nx);
-        jm[c] = jj == 0 ? nx - 1 : jj - 1;
-        jp[c] = jj + 1 == nx ? 0 : jj + 1;
-        d1[c] = TS(0);
-        d2[c] = TS(0);
+        ktm[c] = k_tm<T>(jj, nx);
+        kxm[c] = k_xm<T>(jj, nx);
+        kxp[c] = k_xp<T>(jj, nx);
+        d1[c] = T(0);
+        d2[c] = T(0);
     }
-    TB pre[MARCH_PF][CPT];
-    double upre[REFINE ? MARCH_PF : 1][CPT];
+    const int jl = j0 == 0 ? nx - 1 : j0 - 1;       // left neighbour of the run
+    const int jr = j0 + CPT >= nx ? (j0 + CPT) % nx : j0 + CPT;  // right neighbour
+    auto issue = [&](int row, int slot) {
+        if (active && row < nt) {
+            const T* src = b + (int64_t)row * nx + j0;
+            T* dst = ring + slot * nx + j0;
+            if constexpr (VEC) {
+                constexpr int bytes = CPT * (int)sizeof(T);
+                if constexpr (bytes <= 16) {
+                    cp_async_n(dst, src, bytes);
+                } else {
 #pragma unroll
-    for (int s = 0; s < MARCH_PF; ++s) {
+                    for (int off = 0; off < bytes; off += 16)
+                        cp_async_n(reinterpret_cast<char*>(dst) + off,
+                                   reinterpret_cast<const char*>(src) + off, 16);
+                }
+            } else {
 #pragma unroll
-        for (int c = 0; c < CPT; ++c) {
-            const int j = threadIdx.x + c * nthr;
-            const bool ok = (s < nt) && (j < nx);
-            pre[s][c] = ok ? __ldcs(b + (int64_t)s * nx + j) : TB(0);
-            if constexpr (REFINE) {
-                upre[s][c] = ok ? __ldcs(reinterpret_cast<double*>(xout) + (int64_t)s * nx + j) : 0.0;
+                for (int c = 0; c < CPT; ++c)
+                    if (j0 + c < nx) cp_async_n(dst + c, src + c, (int)sizeof(T));
             }
         }
-    }
-    for (int i0 = 0; i0 < nt; i0 += MARCH_PF) {
+        cp_async_commit();
+    };
 #pragma unroll
-        for (int s = 0; s < MARCH_PF; ++s) {
+    for (int s = 0; s < PF - 1; ++s) issue(s, s);
+    for (int i0 = 0; i0 < nt; i0 += PF) {
+#pragma unroll
+        for (int s = 0; s < PF; ++s) {
             const int i = i0 + s;
             if (i >= nt) break;
-            TS* cur = buf + (i & 1) * nx;
-            const TS* prv = buf + ((i & 1) ^ 1) * nx;
-            TS dnew[CPT];
-#pragma unroll
-            for (int c = 0; c < CPT; ++c) {
-                const int j = threadIdx.x + c * nthr;
-                TS rhs = REFINE ? TS(-(double)pre[s][c]) : TS(pre[s][c]);
-                TS v;
-                if (i == 0) {
-                    v = rhs;
+            issue(i + PF - 1, (s + PF - 1) % PF);
+            cp_async_wait<PF - 1>();  // this thread's copy of row i has landed
+            const T* rrow = ring + s * nx;
+            T* cur = buf + (i & 1) * nx;
+            const T* prv = buf + ((i & 1) ^ 1) * nx;
+            if (active) {
+                Chunk<T, CPT> rhs;
+                if constexpr (VEC) {
+                    rhs = *reinterpret_cast<const Chunk<T, CPT>*>(rrow + j0);
                 } else {
-                    const TS tprev = (i == 1) ? d1[c] : TS(2) * d1[c] - d2[c];
-                    TS xm = TS(0), xp = TS(0);
-                    if (j < nx) {
-                        xm = prv[jm[c]];
-                        xp = prv[jp[c]];
-                    }
-                    v = g.dt2 * rhs + tprev + g.lam2 * (kxm[c] * xm - ktm[c] * d1[c] + kxp[c] * xp);
-                }
-                dnew[c] = v;
-            }
-            // Prefetch row i + PF into the slot just consumed.
-            {
-                const int ip = i + MARCH_PF;
 #pragma unroll
-                for (int c = 0; c < CPT; ++c) {
-                    const int j = threadIdx.x + c * nthr;
-                    if (j < nx) {
-                        if constexpr (REFINE) {
-                            double* uo = reinterpret_cast<double*>(xout) + (int64_t)i * nx + j;
-                            *uo = upre[s][c] + (double)dnew[c];
-                        } else {
-                            reinterpret_cast<TS*>(xout)[(int64_t)i * nx + j] = dnew[c];
+                    for (int c = 0; c < CPT; ++c) rhs.v[c] = j0 + c < nx ? rrow[j0 + c] : T(0);
+                }
+                Chunk<T, CPT> out;
+                if (i == 0) {
+#pragma unroll
+                    for (int c = 0; c < CPT; ++c) out.v[c] = rhs.v[c];
+                } else {
+                    const T left = prv[jl];
+                    const T right = prv[jr];
+#pragma unroll
+                    for (int c = 0; c < CPT; ++c) {
+                        const T xm = c == 0 ? left : d1[c - 1];
+                        const T xp = c == CPT - 1 ? right : d1[c + 1];
+                        const T tprev = (i == 1) ? d1[c] : T(2) * d1[c] - d2[c];
+                        out.v[c] = g.dt2 * rhs.v[c] + tprev +
+                                   g.lam2 * (kxm[c] * xm - ktm[c] * d1[c] + kxp[c] * xp);
+                    }
+                }
+                if constexpr (VEC) {
+                    *reinterpret_cast<Chunk<T, CPT>*>(x + (int64_t)i * nx + j0) = out;
+                    *reinterpret_cast<Chunk<T, CPT>*>(cur + j0) = out;
+                } else {
+#pragma unroll
+                    for (int c = 0; c < CPT; ++c) {
+                        if (j0 + c < nx) {
+                            x[(int64_t)i * nx + j0 + c] = out.v[c];
+                            cur[j0 + c] = out.v[c];
                         }
                     }
-                    const bool ok = (ip < nt) && (j < nx);
-                    pre[s][c] = ok ? __ldcs(b + (int64_t)ip * nx + j) : TB(0);
-                    if constexpr (REFINE) {
-                        upre[s][c] = ok ? __ldcs(reinterpret_cast<double*>(xout) + (int64_t)ip * nx + j)
-                                        : 0.0;
-                    }
+                }
+#pragma unroll
+                for (int c = 0; c < CPT; ++c) {
                     d2[c] = d1[c];
-                    d1[c] = dnew[c];
-                    if (j < nx) cur[j] = dnew[c];
+                    d1[c] = out.v[c];
                 }
             }
             __syncthreads();
         }
     }
+    cp_async_wait<0>();
 }
 
-template <typename TS, typename TB, bool REFINE>
-int launch_march(const WaveDev<TS>& g, const TB* b, void* x, cudaStream_t st) {
+// Columns per thread for a row of nx cells (at most 1024 threads).
+inline int march_cpt(int nx) {
+    if (nx <= 128) return 1;
+    if (nx <= 1024) return 2;
+    return 4;
+}
+
+template <typename T, int CPT, int PF>
+int launch_march_cfg(const WaveDev<T>& g, const T* b, T* x, cudaStream_t st) {
     const int nx = g.nx;
-    if (nx > 2048) return ODIL_ERR_SHAPE;
-    const int cpt = nx > 1024 ? 2 : 1;
-    int threads = (nx + cpt - 1) / cpt;
+    const bool vec = (nx % CPT == 0) &&
+                     ((reinterpret_cast<uintptr_t>(b) | reinterpret_cast<uintptr_t>(x)) %
+                      (CPT * sizeof(T))) == 0;
+    int threads = (nx + CPT - 1) / CPT;
     threads = ((threads + 31) / 32) * 32;
-    const size_t smem = 2 * (size_t)nx * sizeof(TS);
+    if (threads > 1024) return ODIL_ERR_SHAPE;
+    const size_t smem = (2 + PF) * (size_t)nx * sizeof(T);
     auto go = [&](auto kern) {
-        if (smem > 48 * 1024) {
-            cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        }
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         kern<<<1, threads, smem, st>>>(g, b, x);
     };
-    if (cpt == 1) {
-        go(wave_march_kernel<TS, TB, REFINE, 1>);
+    if (vec) {
+        go(wave_march_kernel<T, CPT, PF, true>);
     } else {
-        go(wave_march_kernel<TS, TB, REFINE, 2>);
+        go(wave_march_kernel<T, CPT, PF, false>);
     }
     return launch_status();
+}
+
+template <typename T>
+int launch_march(const WaveDev<T>& g, const T* b, T* x, cudaStream_t st) {
+    const int nx = g.nx;
+    if (nx > 2048) return ODIL_ERR_SHAPE;
+    // Ring depth: 16 rows when it fits in shared memory, else 8.
+    const bool deep = (2 + 16) * (size_t)nx * sizeof(T) <= 200 * 1024;
+    switch (march_cpt(nx)) {
+        case 1: return deep ? launch_march_cfg<T, 1, 16>(g, b, x, st)
+                            : launch_march_cfg<T, 1, 8>(g, b, x, st);
+        case 2: return deep ? launch_march_cfg<T, 2, 16>(g, b, x, st)
+                            : launch_march_cfg<T, 2, 8>(g, b, x, st);
+        default: return deep ? launch_march_cfg<T, 4, 16>(g, b, x, st)
+                             : launch_march_cfg<T, 4, 8>(g, b, x, st);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// One fully parallel FP64 step of mixed-precision Newton: u_out = u + d (d is
+// the FP32 correction of the previous march, or absent), r = F(u_out) in FP64,
+// rhs = float(-r) for the next FP32 march, optionally sum(r^2) in FP64.  The
+// stencil reads u + d at the five neighbours itself, so u_out must not alias u.
+template <bool HAS_D, bool NORM>
+__global__ void __launch_bounds__(256) wave_update_residual_kernel(
+    WaveDev<double> g, const double* __restrict__ u, const float* __restrict__ d,
+    double* __restrict__ uout, float* __restrict__ rhs, ReduceWs ws, double* rnorm2) {
+    const int nx = g.nx, nt = g.nt;
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    double acc = 0.0;
+    if (j < nx) {
+        const int jm = j == 0 ? nx - 1 : j - 1;
+        const int jp = j + 1 == nx ? 0 : j + 1;
+        for (int i = blockIdx.y; i < nt; i += gridDim.y) {
+            auto val = [&](int ii, int jj) -> double {
+                const int64_t k = (int64_t)ii * nx + jj;
+                double v = __ldg(u + k);
+                if constexpr (HAS_D) v += (double)__ldg(d + k);
+                return v;
+            };
+            const double uc = val(i, j);
+            double utm = 0, utmm = 0, uxm = 0, uxp = 0;
+            if (i >= 1) {
+                utm = val(i - 1, j);
+                uxm = val(i - 1, jm);
+                uxp = val(i - 1, jp);
+            }
+            if (i >= 2) utmm = val(i - 2, j);
+            const double f = wave_f(g, i, j, uc, utm, utmm, uxm, uxp);
+            const int64_t k = (int64_t)i * nx + j;
+            if constexpr (HAS_D) uout[k] = uc;
+            rhs[k] = (float)(-f);
+            if constexpr (NORM) acc += f * f;
+        }
+    }
+    if constexpr (NORM) {
+        const int64_t bid = (int64_t)blockIdx.y * gridDim.x + blockIdx.x;
+        reduce_finish(acc, bid, (int64_t)gridDim.x * gridDim.y, ws, 1.0, rnorm2);
+    }
+}
+
+inline dim3 ur_grid(int nt, int nx, dim3* block) {
+    const int bx = nx >= 256 ? 256 : ((nx + 31) / 32) * 32;
+    *block = dim3(bx);
+    const int gy = nt < 4096 ? nt : 4096;
+    return dim3((nx + bx - 1) / bx, gy);
 }
 
 template <typename T>
@@ -456,7 +570,7 @@ ODIL_API int odil_wave_march_f32(const odil_wave_params* p, const float* b, floa
     int st = make_dev<float>(p, &g, false);
     if (st) return st;
     if (!b || !x) return ODIL_ERR_ARG;
-    return launch_march<float, float, false>(g, b, x, as_stream(stream));
+    return launch_march<float>(g, b, x, as_stream(stream));
 }
 ODIL_API int odil_wave_march_f64(const odil_wave_params* p, const double* b, double* x,
                                  void* stream) {
@@ -464,13 +578,42 @@ ODIL_API int odil_wave_march_f64(const odil_wave_params* p, const double* b, dou
     int st = make_dev<double>(p, &g, false);
     if (st) return st;
     if (!b || !x) return ODIL_ERR_ARG;
-    return launch_march<double, double, false>(g, b, x, as_stream(stream));
+    return launch_march<double>(g, b, x, as_stream(stream));
 }
-ODIL_API int odil_wave_refine_mixed(const odil_wave_params* p, const double* r, double* u,
-                                    void* stream) {
-    WaveDev<float> g;
-    int st = make_dev<float>(p, &g, false);
+ODIL_API int64_t odil_wave_update_residual_workspace_bytes(const odil_wave_params* p) {
+    if (!p || p->nt < 1 || p->nx < 1) return 0;
+    dim3 block;
+    const dim3 grid = ur_grid((int)p->nt, (int)p->nx, &block);
+    return reduce_ws_bytes((int64_t)grid.x * grid.y);
+}
+ODIL_API int odil_wave_update_residual_mixed(const odil_wave_params* p, const double* u,
+                                             const float* d, double* u_out, float* rhs,
+                                             double* rnorm2, void* workspace,
+                                             int64_t workspace_bytes, void* stream) {
+    WaveDev<double> g;
+    int st = make_dev<double>(p, &g, true);
     if (st) return st;
-    if (!r || !u) return ODIL_ERR_ARG;
-    return launch_march<float, double, true>(g, r, u, as_stream(stream));
+    if (!u || !rhs || (d && !u_out)) return ODIL_ERR_ARG;
+    if (d && u_out == u) return ODIL_ERR_ARG;
+    dim3 block;
+    const dim3 grid = ur_grid(g.nt, g.nx, &block);
+    ReduceWs ws = {};
+    if (rnorm2) {
+        if (!workspace || workspace_bytes < reduce_ws_bytes((int64_t)grid.x * grid.y))
+            return ODIL_ERR_WORKSPACE;
+        ws = reduce_ws(workspace);
+    }
+    cudaStream_t s = as_stream(stream);
+    if (d) {
+        if (rnorm2)
+            wave_update_residual_kernel<true, true><<<grid, block, 0, s>>>(g, u, d, u_out, rhs, ws, rnorm2);
+        else
+            wave_update_residual_kernel<true, false><<<grid, block, 0, s>>>(g, u, d, u_out, rhs, ws, rnorm2);
+    } else {
+        if (rnorm2)
+            wave_update_residual_kernel<false, true><<<grid, block, 0, s>>>(g, u, d, u_out, rhs, ws, rnorm2);
+        else
+            wave_update_residual_kernel<false, false><<<grid, block, 0, s>>>(g, u, d, u_out, rhs, ws, rnorm2);
+    }
+    return launch_status();
 }

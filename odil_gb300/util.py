@@ -1,0 +1,135 @@
+"""Solver loops with the reference's entry points (util.py:109-370):
+
+    optimize(args, optname, problem, state, callback)
+
+dispatches to ``optimize_newton`` (Newton with ``linsolver.solve``) or to
+``optimize_opt`` (generic optimizers over ``loss_grad``).  The callback
+protocol is the reference's: ``callback(packed, epoch, dhistory=None,
+opt=None)``.  States and packed vectors stay on the GPU.
+"""
+import time
+from collections import defaultdict
+
+import torch
+
+from . import linsolver
+from . import optimizer as optimizer_mod
+
+
+class Timer:
+    """util.py:78-99: named wall-clock counters (push/pop)."""
+
+    def __init__(self):
+        self._starts = []
+        self.counters = dict()
+
+    def push(self, key=None):
+        self._starts.append((key, time.time()))
+
+    def pop(self, key=None):
+        start = self._starts.pop()
+        assert start[0] is None or key is None or start[0] == key
+        key = start[0] if key is None else key
+        self.counters[key] = self.counters.get(key, 0.) + time.time() - start[1]
+
+    def append(self, timer):
+        for k, v in timer.counters.items():
+            self.counters[k] = self.counters.get(k, 0.) + v
+
+
+def optimize_newton(args, problem, state, callback=None):
+    """util.py:242-268: epochs of linearize -> linsolver.solve -> update.
+
+    With ``args.precision == "mixed"`` (and the default linsolver) the solve
+    runs in FP32 on the FP64 residual: every epoch is one step of
+    mixed-precision iterative refinement."""
+    opt = optimizer_mod.Optimizer(name='newton', displayname='Newton')
+    problem.init_missing(state)
+    packed = problem.pack_state(state)
+    dhistory = defaultdict(list)
+    name = getattr(args, "linsolver", "direct")
+    if getattr(args, "precision", "fp64") == "mixed" and name == "direct":
+        name = "mixed"
+    for epoch in range(getattr(args, "epoch_start", 0), args.epochs + 1):
+        s = problem.unpack_state(packed)
+        problem.domain.assign_active_state(state, s)
+        const, m = problem.linearize(state, epoch=epoch)
+        opt.last_loss = sum(torch.mean(c**2) for c in const)
+        opt.last_residual = [torch.mean(c**2)**0.5 for c in const]
+        if callback:
+            callback(packed, epoch, dhistory=dhistory, opt=opt)
+        if epoch == args.epochs:
+            break
+        opt.evals += 1
+        rhs = -torch.cat([c.reshape(-1) for c in const])
+        timer = Timer()
+        timer.push('linsolver')
+        dpacked = linsolver.solve(m, rhs, args, dhistory, name)
+        timer.pop()
+        packed += dpacked
+    s = problem.unpack_state(packed)
+    problem.domain.assign_active_state(state, s)
+    return packed
+
+
+def optimize_opt(args, optname, problem, state, callback=None, **kwargs):
+    """util.py:271-317: run a generic optimizer over the packed state."""
+    problem.init_missing(state)
+
+    def loss_grad(packed, epoch):
+        fields = problem.unpack_fields(packed)
+        s = type(state)(fields=fields)
+        loss, grads, _, loss_split = problem.eval_loss_grad(s, epoch=epoch)
+        g = problem.pack_fields(grads)
+        last_residual = [v**0.5 if v >= 0 else v for v in loss_split]
+        return loss, g, last_residual
+
+    packed = problem.pack_state(state)
+    if getattr(args, "bfgs_m", None) is not None:
+        kwargs['m'] = args.bfgs_m
+    for key, attr in (('epsilon', 'adam_epsilon'), ('beta_1', 'adam_beta_1'),
+                      ('beta_2', 'adam_beta_2')):
+        if getattr(args, attr, None) is not None:
+            kwargs[key] = getattr(args, attr)
+    opt = optimizer_mod.make_optimizer(optname, dtype=problem.domain.dtype,
+                                       **kwargs)
+    epoch_start = getattr(args, "epoch_start", 0)
+    loss, _, residual = loss_grad(packed, epoch_start)
+    opt.last_loss = loss
+    opt.last_residual = residual
+    if callback:
+        callback(packed, epoch=epoch_start, opt=opt)
+    packed, info = opt.run(packed, loss_grad=loss_grad,
+                           epochs=args.epochs - epoch_start,
+                           callback=callback, epoch_start=epoch_start,
+                           lr=getattr(args, "lr", 1e-3), **kwargs)
+    s = problem.unpack_state(packed)
+    problem.domain.assign_active_state(state, s)
+    return packed, info
+
+
+def optimize(args, optname, problem, state, callback=None, **kwargs):
+    """util.py:365-370."""
+    if optname == 'newton':
+        return optimize_newton(args, problem, state, callback)
+    return optimize_opt(args, optname, problem, state, callback, **kwargs)
+
+
+def add_arguments(parser):
+    """The solver flags of util.py:109-239 that the GPU engine uses."""
+    parser.add_argument('--epochs', type=int, default=None,
+                        help="Maximum epochs")
+    parser.add_argument('--epoch_start', type=int, default=0,
+                        help="Index of the first epoch")
+    parser.add_argument('--optimizer', type=str, default='newton',
+                        help="Optimizer: newton, lbfgsb, lbfgs, adam, adamn, gd")
+    parser.add_argument('--seed', type=int, default=None, help="Seed")
+    parser.add_argument('--double', type=int, default=1,
+                        help="Use FP64 fields")
+    parser.add_argument('--bfgs_m', type=int, default=50,
+                        help="L-BFGS history size")
+    parser.add_argument('--adam_epsilon', type=float, default=None)
+    parser.add_argument('--adam_beta_1', type=float, default=None)
+    parser.add_argument('--adam_beta_2', type=float, default=None)
+    parser.add_argument('--outdir', type=str, default='.',
+                        help="Output directory")

@@ -111,6 +111,7 @@ class WaveKernels:
         self.workspace = torch.zeros(int(nbytes), dtype=torch.uint8,
                                      device=self.device)
         self.loss_buf = torch.zeros(1, dtype=torch.float64, device=self.device)
+        self.ur_workspace = None
 
     def _params(self, bc):
         p = _capi.OdilWaveParams()
@@ -173,12 +174,22 @@ class WaveKernels:
         call("odil_wave_march_" + sfx, p, ptr(b), ptr(out), stream_handle())
         return out
 
-    def refine_mixed(self, r, u):
-        """u += J^{-1}(-r) with the solve in FP32 (r, u FP64)."""
-        self._check(r)
+    def update_residual_mixed(self, u, d, u_out, rhs, rnorm2=None):
+        """u_out = u + d (d FP32 or None), rhs = float32(-F(u_out)) with the
+        residual in FP64; optionally rnorm2[0] = sum(F^2)."""
         self._check(u)
-        if r.dtype != torch.float64 or u.dtype != torch.float64:
-            raise TypeError("refine_mixed takes FP64 residual and field")
-        call("odil_wave_refine_mixed", ctypes.byref(self.p64), ptr(r), ptr(u),
+        if u.dtype != torch.float64 or rhs.dtype != torch.float32:
+            raise TypeError("FP64 field and FP32 right-hand side expected")
+        if d is not None and (d.dtype != torch.float32 or u_out is None):
+            raise TypeError("FP32 correction and an FP64 output expected")
+        if rnorm2 is not None and self.ur_workspace is None:
+            nb = _capi.load().odil_wave_update_residual_workspace_bytes(
+                ctypes.byref(self.p64))
+            self.ur_workspace = torch.zeros(int(nb), dtype=torch.uint8,
+                                            device=self.device)
+        ws = self.ur_workspace if rnorm2 is not None else None
+        call("odil_wave_update_residual_mixed", ctypes.byref(self.p64), ptr(u),
+             ptr(d), ptr(u_out if d is not None else None), ptr(rhs),
+             ptr(rnorm2), ptr(ws), 0 if ws is None else ws.numel(),
              stream_handle())
-        return u
+        return rhs

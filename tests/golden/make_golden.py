@@ -88,13 +88,31 @@ def make_multigrid(ref):
             [list(k) for k in AtA.shift_to_field.keys()])
         out["AtA_coefs_%s" % key] = np.stack(
             [np.asarray(c).reshape(nw) for c in AtA.shift_to_field.values()])
-        Ah = mg.MultigridOp.coarsen_sparse_operator(A, R, TT, mod=mod,
-                                                    dtype=dtype)
-        out["Ah_shifts_%s" % key] = np.array(
-            [list(k) for k in Ah.shift_to_field.keys()])
-        out["Ah_coefs_%s" % key] = np.stack([
-            np.asarray(c).reshape(Ah.nwh) for c in Ah.shift_to_field.values()
-        ])
+        # Galerkin coarsening as the reference defines it for CSR matrices
+        # (Multigrid.update_A, multigrid.py:125-131: A_{l+1} = R A_l T with
+        # R, T from Multigrid.get_R / get_T).  The reference's stencil path
+        # (coarsen_sparse_operator) agrees with it only for the zero-padded
+        # constant Laplacian of its test_coarsen, stored separately below.
+        Rc = mg.Multigrid.get_R(nw_a, mod=mod, dtype=dtype)
+        Tc = mg.Multigrid.get_T(nw_a, mod=mod, dtype=dtype)
+        out["AhCSR_%s" % key] = (Rc @ A.tocsr() @ Tc).toarray()
+    # test_multigrid.py:197-249: the 11x11 padded Laplacian through the
+    # stencil coarsening.
+    nw = np.array((11, 11))
+    pad = [[1, 1]] * 2
+    Aop = mg.SparseOperator(
+        {
+            (0, 0): 4 * np.ones(nw),
+            (-1, 0): -np.pad(np.ones(nw - 2), pad),
+            (1, 0): -np.pad(np.ones(nw - 2), pad),
+            (0, -1): -np.pad(np.ones(nw - 2), pad),
+            (0, 1): -np.pad(np.ones(nw - 2), pad),
+        }, nw, mod=mod, dtype=dtype)
+    Rop = mg.MultigridOp.get_R(nw, mod=mod, dtype=dtype)
+    TTop = mg.MultigridOp.get_TT(nw, mod=mod, dtype=dtype)
+    Ahop = mg.MultigridOp.coarsen_sparse_operator(Aop, Rop, TTop, mod=mod,
+                                                  dtype=dtype)
+    out["lap11_Ah"] = Ahop.tocsr().toarray()
     return out
 
 
