@@ -32,6 +32,7 @@ NT = NX = 1024
 SEED, NMODES, C = 1, 16, 1.0
 MIXED_EPOCHS = FP64_EPOCHS = 2
 OPT_ITERS = 2000
+BIG = 8192
 L2_FLUSH_BYTES = 256 << 20
 WORKLOAD = "wave1d_1024x1024_sine16_seed1"
 METRIC = "ODIL solves/s at rel err <=1e-5 vs FP64 oracle"
@@ -291,6 +292,15 @@ def run_ours(args):
     u32 = u.float()
     g32 = torch.empty_like(u32)
     t_lg = timed(lambda: k.loss_grad(u32, grad=g32), 20, 3)
+    # The same fused loss+adjoint kernel on an 8192^2 grid (256 MiB in,
+    # 256 MiB out): HBM-bound, so its roofline fraction is meaningful.
+    big = WaveInstance(BIG, BIG, profile="sine", seed=SEED, nmodes=NMODES,
+                       c=C, dtype=np.float32, device=dev)
+    kb = Problem(big.operator, big.domain).kernels
+    ubig = torch.randn((BIG, BIG), dtype=torch.float32, device=dev)
+    gbig = torch.empty_like(ubig)
+    t_lg_big = timed(lambda: kb.loss_grad(ubig, grad=gbig), 10, 3)
+    del ubig, gbig, kb
 
     # The workload's optimizer runs (FP32 fused adjoint gradient).
     opt_info = run_optimizers(problem, inst, dev, rank == 0 and
@@ -381,6 +391,11 @@ def run_ours(args):
             "march_f64_ms": statistics.mean(t_march64),
             "loss_grad_f32_ms": statistics.mean(t_lg),
             "loss_grad_f32_GBs": lg_bytes / (statistics.mean(t_lg) * 1e6),
+            "loss_grad_f32_8192sq_ms": statistics.mean(t_lg_big),
+            "loss_grad_f32_8192sq_GBs": 8 * BIG * BIG /
+                                        (statistics.mean(t_lg_big) * 1e6),
+            "loss_grad_f32_8192sq_frac_of_measured_hbm": 8 * BIG * BIG /
+                (statistics.mean(t_lg_big) * 1e6) / (hbm or 6800.0),
         },
         "optimizers": opt_info,
     }

@@ -119,6 +119,145 @@ int odil_wave_update_residual_mixed(const odil_wave_params* p, const double* u,
                                     int64_t workspace_bytes, void* stream);
 
 /* ------------------------------------------------------------------------
+ * 2D linear advection on the (t, x, y) space-time grid, periodic in x, y.
+ *
+ * Replaces advection_2d.py:103-223 (operator, direct problem, --periodic 1,
+ * first-order upwind on the frozen velocity) for a constant velocity:
+ *   f = (p - ptm)/dt + ax p_x + ay p_y, ptm = p[i-1], row 0: ptm = p_init,
+ *   p_x = (p - p[x-1])/dx if ax > 0 else (p[x+1] - p)/dx (same in y).
+ * ---------------------------------------------------------------------- */
+typedef struct odil_advect_params {
+    int64_t nt, nx, ny;  /* grid cells; nt, nx <= 65535 */
+    double dt, dx, dy;
+    double ax, ay;       /* constant velocity */
+    const void* p_init;  /* [nx*ny] previous value of row 0 (the reference's
+                            exact_pp[0]); kernel precision; NULL = 0 */
+} odil_advect_params;
+
+int64_t odil_advect_workspace_bytes(const odil_advect_params* p);
+int odil_advect_residual_f32(const odil_advect_params* p, const float* u,
+                             float* f, void* stream);
+int odil_advect_residual_f64(const odil_advect_params* p, const double* u,
+                             double* f, void* stream);
+int odil_advect_jv_f32(const odil_advect_params* p, const float* v,
+                       float* out, void* stream);
+int odil_advect_jv_f64(const odil_advect_params* p, const double* v,
+                       double* out, void* stream);
+int odil_advect_jtv_f32(const odil_advect_params* p, const float* w,
+                        float* out, void* stream);
+int odil_advect_jtv_f64(const odil_advect_params* p, const double* w,
+                        double* out, void* stream);
+/* Fused loss + adjoint (util_op.py:627-654): *loss = mean(f^2),
+ * grad = (2/N) J^T f. */
+int odil_advect_loss_grad_f32(const odil_advect_params* p, const float* u,
+                              float* grad, double* loss, void* workspace,
+                              int64_t workspace_bytes, void* stream);
+int odil_advect_loss_grad_f64(const odil_advect_params* p, const double* u,
+                              double* grad, double* loss, void* workspace,
+                              int64_t workspace_bytes, void* stream);
+/* FP64 step of the mixed-precision Newton loop, as
+ * odil_wave_update_residual_mixed. */
+int odil_advect_update_residual_mixed(const odil_advect_params* p,
+                                      const double* u, const float* d,
+                                      double* u_out, float* rhs,
+                                      double* rnorm2, void* workspace,
+                                      int64_t workspace_bytes, void* stream);
+/* Matrix-free FP32 multigrid on the same operator (the V-cycle of
+ * multigrid.py:567-602 with rediscretised coarse operators; coarse levels
+ * pass their own params with doubled steps).  Damped Jacobi
+ * (multigrid.py:543-552): x_out = x + omega (b - J x)/diag(J); x = NULL means
+ * a zero iterate.  r_out (optional, needs x) receives b - J x. */
+int odil_advect_mg_jacobi(const odil_advect_params* p, const float* x,
+                          const float* b, float* x_out, float omega,
+                          float* r_out, void* stream);
+/* Full-weighting restriction (nt, nx, ny) -> halves: weights
+ * (1, 3, 3, 1)/8 per axis, x and y periodic, t clamped. */
+int odil_advect_mg_restrict(int64_t nt, int64_t nx, int64_t ny,
+                            const float* r, float* rc, void* stream);
+/* x += trilinear prolongation of the half-size correction e. */
+int odil_advect_mg_prolong_add(int64_t nt, int64_t nx, int64_t ny,
+                               const float* e, float* x, void* stream);
+/* Dense FP64 matrix of the operator (nt*nx*ny <= 1024), for the coarsest
+ * level's direct solve. */
+int odil_advect_dense(const odil_advect_params* p, double* A, void* stream);
+/* x = Ainv b with a dense FP64 n x n matrix (n <= 1024): the coarsest-level
+ * direct solve (multigrid.py:307-310) by the precomputed inverse. */
+int odil_dense_apply_f64(int64_t n, const double* Ainv, const float* b,
+                         float* x, void* stream);
+
+/* ------------------------------------------------------------------------
+ * Operators in stencil form (the reference's SparseOperator,
+ * multigrid.py:877-1214): shifts s with one coefficient field C_s each on the
+ * output grid,  (A u)[c] = sum_s C_s[c] u[stride*c + s], zero outside the
+ * grid on non-periodic axes and wrapped on periodic ones.
+ * ---------------------------------------------------------------------- */
+#define ODIL_STENCIL_MAXS 128
+
+typedef struct odil_stencil {
+    int32_t dim;                         /* 1..3 */
+    int32_t stride;                      /* 1, or 2 for restriction-type ops */
+    int32_t periodic[3];                 /* per axis: 1 = periodic */
+    int64_t nw[3];                       /* input (fine) grid */
+    int32_t nshift;                      /* <= ODIL_STENCIL_MAXS */
+    int32_t shifts[ODIL_STENCIL_MAXS][3];
+    void* coef;                          /* device [nshift][output cells],
+                                            output grid nwh = (nw-1)/stride+1
+                                            (nw/2 on periodic stride-2 axes) */
+} odil_stencil;
+
+/* out = beta out + alpha A u  (multigrid.py:958-969, mul_field) */
+int odil_stencil_apply_f32(const odil_stencil* A, const float* u, float* out,
+                           double alpha, double beta, void* stream);
+int odil_stencil_apply_f64(const odil_stencil* A, const double* u,
+                           double* out, double alpha, double beta,
+                           void* stream);
+/* out = beta out + alpha A^T uh  (multigrid.py:1006-1027) */
+int odil_stencil_apply_t_f32(const odil_stencil* A, const float* uh,
+                             float* out, double alpha, double beta,
+                             void* stream);
+int odil_stencil_apply_t_f64(const odil_stencil* A, const double* uh,
+                             double* out, double alpha, double beta,
+                             void* stream);
+/* Small device scratch for the two set-up products below. */
+int64_t odil_stencil_pair_workspace_bytes(void);
+/* C = A^T B as a stencil (multigrid.py:1035-1071); C->shifts must list every
+ * difference b - a of the shifts of A and B; C->coef is written.  Set-up
+ * call: synchronizes the stream. */
+int odil_stencil_mul_transpose_op_f32(const odil_stencil* A,
+                                      const odil_stencil* B, odil_stencil* C,
+                                      void* workspace, int64_t workspace_bytes,
+                                      void* stream);
+int odil_stencil_mul_transpose_op_f64(const odil_stencil* A,
+                                      const odil_stencil* B, odil_stencil* C,
+                                      void* workspace, int64_t workspace_bytes,
+                                      void* stream);
+/* Ac = R A T with T = TT^T, in stencil form: the Galerkin coarse operator of
+ * Multigrid.update_A (multigrid.py:125-131).  Ac->shifts list the coarse
+ * shifts to produce (|shift| <= 4).  Set-up call: synchronizes the stream. */
+int odil_stencil_galerkin_f32(const odil_stencil* R, const odil_stencil* A,
+                              const odil_stencil* TT, odil_stencil* Ac,
+                              void* workspace, int64_t workspace_bytes,
+                              void* stream);
+int odil_stencil_galerkin_f64(const odil_stencil* R, const odil_stencil* A,
+                              const odil_stencil* TT, odil_stencil* Ac,
+                              void* workspace, int64_t workspace_bytes,
+                              void* stream);
+/* One block row of a coupled system (nterm <= 4 terms A_ij u_j):
+ *   r = f - sum_j A_ij u_j  (r_out, optional; f may be NULL = 0),
+ *   u_out = u_i + omega r / diag   (optional; damped Jacobi of
+ *   multigrid.py:543-552). */
+int odil_stencil_block_row_f32(int nterm, const odil_stencil* const* ops,
+                               const void* const* us, const float* f,
+                               const float* u_i, const float* diag,
+                               float* u_out, float* r_out, double omega,
+                               void* stream);
+int odil_stencil_block_row_f64(int nterm, const odil_stencil* const* ops,
+                               const void* const* us, const double* f,
+                               const double* u_i, const double* diag,
+                               double* u_out, double* r_out, double omega,
+                               void* stream);
+
+/* ------------------------------------------------------------------------
  * Optimizer vector kernels (n elements, contiguous).
  * ---------------------------------------------------------------------- */
 

@@ -47,6 +47,35 @@ class OdilWaveParams(ctypes.Structure):
     ]
 
 
+class OdilAdvectParams(ctypes.Structure):
+    _fields_ = [
+        ("nt", ctypes.c_int64),
+        ("nx", ctypes.c_int64),
+        ("ny", ctypes.c_int64),
+        ("dt", ctypes.c_double),
+        ("dx", ctypes.c_double),
+        ("dy", ctypes.c_double),
+        ("ax", ctypes.c_double),
+        ("ay", ctypes.c_double),
+        ("p_init", ctypes.c_void_p),
+    ]
+
+
+STENCIL_MAXS = 128
+
+
+class OdilStencil(ctypes.Structure):
+    _fields_ = [
+        ("dim", ctypes.c_int32),
+        ("stride", ctypes.c_int32),
+        ("periodic", ctypes.c_int32 * 3),
+        ("nw", ctypes.c_int64 * 3),
+        ("nshift", ctypes.c_int32),
+        ("shifts", (ctypes.c_int32 * 3) * STENCIL_MAXS),
+        ("coef", ctypes.c_void_p),
+    ]
+
+
 _P = ctypes.c_void_p
 _I64 = ctypes.c_int64
 _D = ctypes.c_double
@@ -70,6 +99,35 @@ SIGNATURES = {
     "odil_wave_update_residual_workspace_bytes": (_I64, [_P]),
     "odil_wave_update_residual_mixed": (_INT, [_P, _P, _P, _P, _P, _P, _P, _I64,
                                                _P]),
+    "odil_advect_workspace_bytes": (_I64, [_P]),
+    "odil_advect_residual_f32": (_INT, [_P, _P, _P, _P]),
+    "odil_advect_residual_f64": (_INT, [_P, _P, _P, _P]),
+    "odil_advect_jv_f32": (_INT, [_P, _P, _P, _P]),
+    "odil_advect_jv_f64": (_INT, [_P, _P, _P, _P]),
+    "odil_advect_jtv_f32": (_INT, [_P, _P, _P, _P]),
+    "odil_advect_jtv_f64": (_INT, [_P, _P, _P, _P]),
+    "odil_advect_loss_grad_f32": (_INT, [_P, _P, _P, _P, _P, _I64, _P]),
+    "odil_advect_loss_grad_f64": (_INT, [_P, _P, _P, _P, _P, _I64, _P]),
+    "odil_advect_update_residual_mixed": (_INT, [_P, _P, _P, _P, _P, _P, _P,
+                                                 _I64, _P]),
+    "odil_advect_mg_jacobi": (_INT, [_P, _P, _P, _P, ctypes.c_float, _P, _P]),
+    "odil_advect_mg_restrict": (_INT, [_I64, _I64, _I64, _P, _P, _P]),
+    "odil_advect_mg_prolong_add": (_INT, [_I64, _I64, _I64, _P, _P, _P]),
+    "odil_advect_dense": (_INT, [_P, _P, _P]),
+    "odil_dense_apply_f64": (_INT, [_I64, _P, _P, _P, _P]),
+    "odil_stencil_apply_f32": (_INT, [_P, _P, _P, _D, _D, _P]),
+    "odil_stencil_apply_f64": (_INT, [_P, _P, _P, _D, _D, _P]),
+    "odil_stencil_apply_t_f32": (_INT, [_P, _P, _P, _D, _D, _P]),
+    "odil_stencil_apply_t_f64": (_INT, [_P, _P, _P, _D, _D, _P]),
+    "odil_stencil_pair_workspace_bytes": (_I64, []),
+    "odil_stencil_mul_transpose_op_f32": (_INT, [_P, _P, _P, _P, _I64, _P]),
+    "odil_stencil_mul_transpose_op_f64": (_INT, [_P, _P, _P, _P, _I64, _P]),
+    "odil_stencil_galerkin_f32": (_INT, [_P, _P, _P, _P, _P, _I64, _P]),
+    "odil_stencil_galerkin_f64": (_INT, [_P, _P, _P, _P, _P, _I64, _P]),
+    "odil_stencil_block_row_f32": (_INT, [_INT, _P, _P, _P, _P, _P, _P, _P, _D,
+                                          _P]),
+    "odil_stencil_block_row_f64": (_INT, [_INT, _P, _P, _P, _P, _P, _P, _P, _D,
+                                          _P]),
     "odil_adam_step_f32": (_INT, [_P, _P, _P, _P, _I64, _D, _D, _D, _D, _P]),
     "odil_adam_step_f64": (_INT, [_P, _P, _P, _P, _I64, _D, _D, _D, _D, _P]),
     "odil_axpby_f32": (_INT, [_P, _P, _P, _I64, _D, _D, _P]),

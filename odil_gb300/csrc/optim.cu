@@ -142,7 +142,34 @@ __global__ void __launch_bounds__(VT) multidot_kernel(const T* __restrict__ M, i
     T acc[MD_MAXR] = {T(0), T(0), T(0), T(0)};
     if (vec) {
         const int64_t v0 = e0 / W, v1 = e1 / W;
-        for (int64_t e = v0 + threadIdx.x; e < v1; e += VT) {
+        // Four vector elements per thread per step, all loads issued first:
+        // enough bytes in flight per SM to cover the HBM latency.
+        constexpr int U = 4;
+        int64_t e = v0 + threadIdx.x;
+        for (; e + (U - 1) * VT < v1; e += U * VT) {
+            V mv[U], qv[MD_MAXR][U];
+#pragma unroll
+            for (int uu = 0; uu < U; ++uu) mv[uu] = __ldcs(reinterpret_cast<const V*>(row) + e + uu * VT);
+#pragma unroll
+            for (int j = 0; j < MD_MAXR; ++j)
+                if (j < r)
+#pragma unroll
+                    for (int uu = 0; uu < U; ++uu)
+                        qv[j][uu] = __ldg(reinterpret_cast<const V*>(qs.q[j]) + e + uu * VT);
+#pragma unroll
+            for (int uu = 0; uu < U; ++uu) {
+                const T* ms = reinterpret_cast<const T*>(&mv[uu]);
+#pragma unroll
+                for (int j = 0; j < MD_MAXR; ++j) {
+                    if (j < r) {
+                        const T* qq = reinterpret_cast<const T*>(&qv[j][uu]);
+#pragma unroll
+                        for (int w = 0; w < W; ++w) acc[j] += ms[w] * qq[w];
+                    }
+                }
+            }
+        }
+        for (; e < v1; e += VT) {
             V mv = __ldcs(reinterpret_cast<const V*>(row) + e);
             const T* ms = reinterpret_cast<const T*>(&mv);
 #pragma unroll

@@ -171,66 +171,95 @@ void grid_rows(const WaveDev<T>& g, dim3* grid, dim3* block) {
 }
 
 // ---------------------------------------------------------------------------
-// Fused loss + adjoint gradient.  A block owns a TY x TX tile of the gradient:
-// it stages u with a halo of 2 rows/cols in shared memory, evaluates the
-// residual on the (TY+2) x (TX+2) cells whose rows read the tile, keeps those
-// residuals in shared memory only, and gathers J^T f.  The tile's own
-// residuals feed the FP64 loss partial.
-constexpr int LG_TY = 16;
-constexpr int LG_TX = 64;
-constexpr int LG_THREADS = 256;
+// Fused loss + adjoint gradient, one warp per 32-column strip marching down a
+// tile of rows.  Lane l holds column c0 - 1 + l; lanes 1..30 produce outputs,
+// lanes 0 and 31 are the halo.  Per row the warp loads u once (coalesced; the
+// two halo lanes load one extra neighbour), gets the x-neighbours of the
+// previous row by shuffles, evaluates the residual of the row (kept in
+// registers, never stored), and gathers J^T f for the row two above:
+//   g(a, b) = sum over the rows (a, b), (a+1, b), (a+2, b), (a+1, b-1),
+//             (a+1, b+1) that read u(a, b), of coefficient * f.
+// Warps whose rows and columns avoid the boundary classes use the constant
+// interior coefficients; the others use the general class functions.
+constexpr int LG_WARPS = 4;
+constexpr int LG_OUT = 30;  // output columns per warp
 
-template <typename T>
-__global__ void __launch_bounds__(LG_THREADS) wave_loss_grad_kernel(WaveDev<T> g,
-                                                                    const T* __restrict__ u,
-                                                                    T* __restrict__ grad,
-                                                                    ReduceWs ws, double* loss,
-                                                                    T gscale, double lscale) {
-    constexpr int UY = LG_TY + 4, UX = LG_TX + 4;
-    constexpr int FY = LG_TY + 2, FX = LG_TX + 2;
-    __shared__ T su[UY][UX + 1];
-    __shared__ T sf[FY][FX + 1];
+template <typename T, int TY>
+__global__ void __launch_bounds__(LG_WARPS * 32) wave_loss_grad_kernel(
+    WaveDev<T> g, const T* __restrict__ u, T* __restrict__ grad, ReduceWs ws, double* loss,
+    T gscale, double lscale) {
     const int nt = g.nt, nx = g.nx;
-    const int a0 = blockIdx.y * LG_TY;
-    const int b0 = blockIdx.x * LG_TX;
-    const bool col_inner = (b0 >= 2) && (b0 + LG_TX + 2 <= nx);
-    const bool row_inner = (a0 >= 2) && (a0 + LG_TY + 2 <= nt);
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    const int c0 = (blockIdx.x * LG_WARPS + warp) * LG_OUT;  // first output column
+    const int a0 = blockIdx.y * TY;
+    const int col = c0 - 1 + lane;
+    const bool out_lane = lane >= 1 && lane <= LG_OUT && col < nx;
+    const int colw = wrapn(col, nx);
+    const int colm = wrapn(col - 1, nx);  // lane 0's extra load
+    const int colp = wrapn(col + 1, nx);  // lane 31's extra load
+    const bool fast = (c0 >= 2) && (c0 + LG_OUT + 2 <= nx) && (a0 >= 1) && (a0 + TY + 2 < nt);
+    const T A = g.A, B = g.B;
+    const T ctm_int = T(-2) * A + T(2) * B;
 
-    // Stage u rows a0-2 .. a0+TY+1, cols b0-2 .. b0+TX+1 (periodic, as tf.roll).
-    for (int k = threadIdx.x; k < UY * UX; k += LG_THREADS) {
-        const int rr = k / UX, cc = k - rr * UX;
-        int r = a0 - 2 + rr, c = b0 - 2 + cc;
-        if (!row_inner) r = wrapn(r, nt);
-        if (!col_inner) c = wrapn(c, nx);
-        su[rr][cc] = __ldg(u + (int64_t)r * nx + c);
-    }
-    __syncthreads();
-
-    // Residuals of rows a0 .. a0+TY+1, cols b0-1 .. b0+TX.
-    for (int k = threadIdx.x; k < FY * FX; k += LG_THREADS) {
-        const int rr = k / FX, cc = k - rr * FX;
-        const int r = a0 + rr;
-        T val = T(0);
-        if (r < nt) {
-            int c = b0 - 1 + cc;
-            if (!col_inner) c = wrapn(c, nx);
-            val = wave_f(g, r, c, su[rr + 2][cc + 1], su[rr + 1][cc + 1], su[rr][cc + 1],
-                         su[rr + 1][cc], su[rr + 1][cc + 2]);
-        }
-        sf[rr][cc] = val;
-    }
-    __syncthreads();
-
+    T u1 = 0, u2 = 0, e1 = 0;   // u rows r-1, r-2 at this lane; e1: lane-0/31 extra of row r-1
+    T f1 = 0, f2 = 0;           // f rows r-1, r-2
+    T f1m = 0, f1p = 0;         // f row r-1 at col-1, col+1
     double lsum = 0.0;
-    for (int k = threadIdx.x; k < LG_TY * LG_TX; k += LG_THREADS) {
-        const int rr = k / LG_TX, cc = k - rr * LG_TX;
-        const int a = a0 + rr, b = b0 + cc;
-        if (a < nt && b < nx) {
-            const T fu = sf[rr][cc + 1];
-            lsum += (double)fu * (double)fu;
-            const T gs = wave_gather(g, a, b, fu, sf[rr + 1][cc + 1], sf[rr + 2][cc + 1],
-                                     sf[rr + 1][cc + 2], sf[rr + 1][cc]);
-            grad[(int64_t)a * nx + b] = gs * gscale;
+    // Rows are loaded LGQ at a time before any of them is used, so each warp
+    // keeps LGQ row loads in flight (the march itself is a dependency chain
+    // through the shuffles).
+    constexpr int LGQ = 4;
+    static_assert((TY + 4) % LGQ == 0, "row chunking");
+    for (int q0 = 0; q0 < TY + 4; q0 += LGQ) {
+        T uq[LGQ], eq[LGQ];
+#pragma unroll
+        for (int j = 0; j < LGQ; ++j) {
+            const int r = a0 - 2 + q0 + j;
+            uq[j] = T(0);
+            eq[j] = T(0);
+            if (r >= 0 && r < nt) {
+                const T* row = u + (int64_t)r * nx;
+                uq[j] = __ldg(row + colw);
+                if (lane == 0) eq[j] = __ldg(row + colm);
+                if (lane == 31) eq[j] = __ldg(row + colp);
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < LGQ; ++j) {
+            const int q = q0 + j;
+            const int r = a0 - 2 + q;
+            const T u0 = uq[j], e0 = eq[j];
+            // x-neighbours of row r-1 at this lane.
+            T um = __shfl_up_sync(0xffffffffu, u1, 1);
+            T up = __shfl_down_sync(0xffffffffu, u1, 1);
+            if (lane == 0) um = e1;
+            if (lane == 31) up = e1;
+            if (q >= 2) {
+                T f0 = T(0);
+                if (r < nt) f0 = wave_f(g, r, colw, u0, u1, u2, um, up);
+                // Gradient of row a = r - 2 (f rows a, a+1 with neighbours, a+2).
+                if (q >= 4 && out_lane) {
+                    const int a = r - 2;
+                    if (a < nt) {
+                        T gs;
+                        if (fast) {
+                            gs = A * (f2 + f0) + ctm_int * f1 - B * (f1p + f1m);
+                        } else {
+                            gs = wave_gather(g, a, col, f2, f1, f0, f1p, f1m);
+                        }
+                        grad[(int64_t)a * nx + col] = gs * gscale;
+                        lsum += (double)f2 * (double)f2;
+                    }
+                }
+                f2 = f1;
+                f1 = f0;
+                f1m = __shfl_up_sync(0xffffffffu, f0, 1);
+                f1p = __shfl_down_sync(0xffffffffu, f0, 1);
+            }
+            u2 = u1;
+            u1 = u0;
+            e1 = e0;
         }
     }
     const int64_t bid = (int64_t)blockIdx.y * gridDim.x + blockIdx.x;
@@ -238,8 +267,12 @@ __global__ void __launch_bounds__(LG_THREADS) wave_loss_grad_kernel(WaveDev<T> g
     reduce_finish(lsum, bid, nb, ws, lscale, loss);
 }
 
+inline int lg_ty(int nt, int nx) { return (int64_t)nt * nx < (4 << 20) ? 16 : 32; }
+
 inline dim3 lg_grid(int nt, int nx) {
-    return dim3((nx + LG_TX - 1) / LG_TX, (nt + LG_TY - 1) / LG_TY);
+    const int ty = lg_ty(nt, nx);
+    const int cols = LG_WARPS * LG_OUT;
+    return dim3((nx + cols - 1) / cols, (nt + ty - 1) / ty);
 }
 
 // ---------------------------------------------------------------------------
@@ -514,8 +547,13 @@ int loss_grad_impl(const odil_wave_params* p, const T* u, T* grad, double* loss,
     const int64_t nb = (int64_t)grid.x * grid.y;
     if (!ws || ws_bytes < reduce_ws_bytes(nb)) return ODIL_ERR_WORKSPACE;
     const double n = (double)g.nt * (double)g.nx;
-    wave_loss_grad_kernel<T><<<grid, LG_THREADS, 0, as_stream(stream)>>>(
-        g, u, grad, reduce_ws(ws), loss, (T)(2.0 / n), 1.0 / n);
+    if (lg_ty(g.nt, g.nx) == 16) {
+        wave_loss_grad_kernel<T, 16><<<grid, LG_WARPS * 32, 0, as_stream(stream)>>>(
+            g, u, grad, reduce_ws(ws), loss, (T)(2.0 / n), 1.0 / n);
+    } else {
+        wave_loss_grad_kernel<T, 32><<<grid, LG_WARPS * 32, 0, as_stream(stream)>>>(
+            g, u, grad, reduce_ws(ws), loss, (T)(2.0 / n), 1.0 / n);
+    }
     return launch_status();
 }
 

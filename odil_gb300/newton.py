@@ -43,6 +43,12 @@ def solve(problem, state, precision="mixed", epochs=None, rnorm2=None):
     u = state.fields[name]
     if u.dtype != torch.float64:
         raise TypeError("Newton runs on an FP64 state")
+    if hasattr(k, "solve_mixed"):
+        if precision != "mixed":
+            raise ValueError("this family solves in mixed precision only")
+        k.solve_mixed(u, epochs=3 if epochs is None else epochs,
+                      rnorm2=rnorm2)
+        return u
     epochs = 2 if epochs is None else epochs
     if precision == "mixed":
         rhs = _scratch(k, "rhs32", torch.float32)

@@ -170,6 +170,7 @@ class LbfgsOptimizer(Optimizer):
             x, xt = xt, x
             g.copy_(gt)
             f = ft
+            self.last_loss = f
             self.epoch += 1
             info.epochs += 1
             if callback:

@@ -78,3 +78,52 @@ class WaveInstance:
         tt, xx = np.meshgrid(t1, x1, indexing="ij")
         self.exact_u, _ = ex(tt, xx)
         self.operator = WaveOperator(init_u, init_ut, left_u, right_u, c=c)
+
+
+# -- 2D advection (advection_2d.py of the reference) -------------------------
+def advect_blob_params(seed, nblobs=8):
+    """Velocity |a| <= 1 (direction uniform, magnitude in [0.2, 1]) and 8
+    Gaussian blobs: centres in [0,1)^2, widths in [0.05, 0.15], amplitudes in
+    [0.5, 1], from numpy default_rng(seed)."""
+    rng = np.random.default_rng(seed)
+    ang = rng.uniform(0, 2 * np.pi)
+    mag = rng.uniform(0.2, 1.0)
+    a = (mag * np.cos(ang), mag * np.sin(ang))
+    centres = rng.uniform(0, 1, (nblobs, 2))
+    widths = rng.uniform(0.05, 0.15, nblobs)
+    amps = rng.uniform(0.5, 1.0, nblobs)
+    return a, centres, widths, amps
+
+
+def periodic_blobs(x, y, centres, widths, amps):
+    p = np.zeros(np.broadcast(x, y).shape)
+    for (cx, cy), w, A in zip(centres, widths, amps):
+        dx = (x - cx + 0.5) % 1.0 - 0.5
+        dy = (y - cy + 0.5) % 1.0 - 0.5
+        p = p + A * np.exp(-(dx * dx + dy * dy) / (2 * w * w))
+    return p
+
+
+class AdvectInstance:
+    """(nt, n, n) grid on t in [0, 1], x, y in [0, 1) periodic; the row-0
+    previous value is the exact field at the first time cell centre
+    (advection_2d.py:196-202); exact solution p0(x - ax t, y - ay t)."""
+
+    def __init__(self, n, seed=0, nt=None, dtype=np.float64, device="cuda"):
+        from .advection import AdvectionOperator
+        nt = n if nt is None else nt
+        (ax, ay), c, w, A = advect_blob_params(seed)
+        self.a = (ax, ay)
+        self.domain = Domain(ndim=3, shape=(nt, n, n), lower=(0, 0, 0),
+                             upper=(1, 1, 1), varnames=('t', 'x', 'y'),
+                             fieldnames=('p', ), dtype=dtype, device=device)
+        t1 = cell_centers(0.0, 1.0, nt)
+        x1 = cell_centers(0.0, 1.0, n)
+        xx, yy = np.meshgrid(x1, x1, indexing="ij")
+        p_init = periodic_blobs(xx - ax * t1[0], yy - ay * t1[0], c, w, A)
+        self.operator = AdvectionOperator(ax, ay, p_init)
+        self._exact = lambda: np.stack(
+            [periodic_blobs(xx - ax * t, yy - ay * t, c, w, A) for t in t1])
+
+    def exact(self):
+        return self._exact()

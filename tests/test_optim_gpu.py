@@ -139,7 +139,12 @@ def test_lbfgs_fp32_wave_1024_runs(cuda):
         losses.append(float(opt.last_loss))
 
     x0 = torch.zeros(n * n, dtype=torch.float32, device=cuda)
+    l0 = prob.kernels.loss_grad(x0.reshape(n, n))[0].item()
     opt = make_optimizer("lbfgsb")
     x, info = opt.run(x0, lg, epochs=30, callback=cb)
     assert info.epochs == 30, info
-    assert losses[-1] <= losses[0]
+    # The initial-row residual is removed in the first iterations; after that
+    # the FP32 loss sits near its rounding floor (kappa(J^T J) ~ 1e12), and
+    # accepted steps stay within the approximate-Wolfe tolerance.
+    assert min(losses) < 0.01 * l0
+    assert losses[-1] <= min(losses) * (1 + 1e-5)
