@@ -47,7 +47,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--case", default=None,
                     choices=("march", "march64", "update_residual", "loss_grad",
-                             "loss_grad64", "lbfgs_iter", "adam_iter"),
+                             "loss_grad64", "loss_grad_big", "lbfgs_iter",
+                             "adam_iter", "batch"),
                     help="run one kernel of the workload --steps times (for "
                     "profiler captures) instead of the benchmark")
     return ap.parse_args()
@@ -215,6 +216,85 @@ def run_optimizers(problem, inst, dev, with_oracle):
     return res
 
 
+def run_batch(dev, with_oracle, steps=5):
+    """512 wave instances, sides U{64..512}, c in [0.5, 2], 5-mode profiles:
+    mixed Newton for the whole batch as one CUDA-graph replay (FP64
+    update/residual + persistent FP32 forward substitution, 2 epochs), against
+    the plain FP64 method run instance by instance on the same GPU."""
+    import torch
+    from odil_gb300.batch import WaveBatch
+    from odil_gb300.workloads import wave_batch_instances
+    from odil_gb300.wave import WaveKernels
+    from odil_gb300 import vec
+    insts = wave_batch_instances(count=512)
+    b = WaveBatch(insts, device=dev)
+    cfg = b.tune()
+    b.capture()
+    st = torch.cuda.current_stream(dev)
+    for _ in range(3):
+        b.replay()
+    torch.cuda.synchronize(dev)
+    ts = []
+    for _ in range(steps):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        b.replay()
+        e1.record(st)
+        ts.append((e0, e1))
+    torch.cuda.synchronize(dev)
+    ms = statistics.mean(a.elapsed_time(c) for a, c in ts)
+    # Plain FP64 method, one instance after the other (2 Newton epochs each).
+    kk = [WaveKernels(i["nt"], i["nx"], i["dt"], i["dx"], i["c"], i["init_u"],
+                      i["init_ut"], i["left_u"], i["right_u"], device=dev)
+          for i in insts]
+    us = [torch.zeros((i["nt"], i["nx"]), dtype=torch.float64, device=dev)
+          for i in insts]
+    rs = [torch.empty_like(u) for u in us]
+    ds = [torch.empty_like(u) for u in us]
+
+    def plain():
+        for k, u, r, d in zip(kk, us, rs, ds):
+            u.zero_()
+            for _ in range(FP64_EPOCHS):
+                k.residual(u, out=r)
+                k.march(r, out=d)
+                vec.axpby(u, 1.0, u, -1.0, d)
+
+    plain()
+    torch.cuda.synchronize(dev)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    plain()
+    e1.record(st)
+    torch.cuda.synchronize(dev)
+    plain_ms = e0.elapsed_time(e1)
+    cells = sum(i["nt"] * i["nx"] for i in insts)
+    out = {"instances": len(insts), "cells": cells,
+           "ms_per_batch": ms, "value": len(insts) / (ms / 1000.0),
+           "unit": "solves/s", "march_cfg": cfg,
+           "launches_per_batch": 2 * MIXED_EPOCHS + 1 + MIXED_EPOCHS,
+           "plain_fp64_per_instance": {"ms": plain_ms,
+                                       "value": len(insts) / (plain_ms / 1e3)},
+           "speedup_vs_plain_fp64": plain_ms / ms}
+    if with_oracle:
+        from oracle import wave as W
+        errs = []
+        for inst, u in zip(insts, b.unpack()):
+            s = W.WaveSetup(inst["nt"], inst["nx"], inst["init_u"],
+                            inst["init_ut"], inst["left_u"], inst["right_u"],
+                            c=inst["c"])
+            errs.append(W.rel_err(u, W.solve_march(s, rounds=2)))
+        out["rel_err_vs_oracle_max"] = max(errs)
+        errs_p = [W.rel_err(u.cpu().numpy(), W.solve_march(W.WaveSetup(
+            i["nt"], i["nx"], i["init_u"], i["init_ut"], i["left_u"],
+            i["right_u"], c=i["c"]), rounds=2)) for i, u in
+            list(zip(insts, us))[:16]]
+        out["plain_rel_err_vs_oracle_max_first16"] = max(errs_p)
+    return out
+
+
 def run_ours(args):
     import torch
     import torch.distributed as dist
@@ -301,6 +381,9 @@ def run_ours(args):
     gbig = torch.empty_like(ubig)
     t_lg_big = timed(lambda: kb.loss_grad(ubig, grad=gbig), 10, 3)
     del ubig, gbig, kb
+
+    # The batched configuration: 512 uneven instances in one graph replay.
+    batch_info = run_batch(dev, rank == 0 and not args.no_cpu_baseline)
 
     # The workload's optimizer runs (FP32 fused adjoint gradient).
     opt_info = run_optimizers(problem, inst, dev, rank == 0 and
@@ -398,6 +481,7 @@ def run_ours(args):
                 (statistics.mean(t_lg_big) * 1e6) / (hbm or 6800.0),
         },
         "optimizers": opt_info,
+        "batched": batch_info,
     }
     if rank == 0 and not args.no_cpu_baseline:
         ref = oracle_solution()
@@ -438,7 +522,20 @@ def run_case(args):
     mm = torch.zeros(n, dtype=torch.float32, device=dev)
     vv = torch.zeros(n, dtype=torch.float32, device=dev)
     k.update_residual_mixed(u, None, None, rhs)
+    if args.case == "loss_grad_big":
+        big = WaveInstance(BIG, BIG, profile="sine", seed=SEED, nmodes=NMODES,
+                           c=C, dtype=np.float32, device=dev)
+        kb = Problem(big.operator, big.domain).kernels
+        ubig = torch.randn((BIG, BIG), dtype=torch.float32, device=dev)
+        gbig = torch.empty_like(ubig)
+    if args.case == "batch":
+        from odil_gb300.batch import WaveBatch
+        from odil_gb300.workloads import wave_batch_instances
+        wb = WaveBatch(wave_batch_instances(count=512), device=dev)
+        wb.update_residual(wb.u, None, None, wb.rhs)
     fn = {
+        "loss_grad_big": lambda: kb.loss_grad(ubig, grad=gbig),
+        "batch": lambda: wb.solve_mixed(),
         "march": lambda: k.march(rhs, out=d32),
         "march64": lambda: k.march(u, out=ub),
         "update_residual": lambda: k.update_residual_mixed(u, d32, ub, rhs),

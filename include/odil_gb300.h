@@ -119,6 +119,54 @@ int odil_wave_update_residual_mixed(const odil_wave_params* p, const double* u,
                                     int64_t workspace_bytes, void* stream);
 
 /* ------------------------------------------------------------------------
+ * Batched wave instances of uneven sizes (the reference runs them as
+ * separate processes, vary_wave.py:7-43).  Fields of all instances are
+ * packed back to back in one array; each instance's first cell `offset` is
+ * a multiple of 4.
+ * ---------------------------------------------------------------------- */
+typedef struct odil_wave_instance {
+    int64_t nt, nx;
+    double dt, dx, c;
+    int64_t offset;    /* first cell in the packed field arrays */
+    int64_t offset_x;  /* first entry in packed init_u / init_ut */
+    int64_t offset_t;  /* first entry in packed left_u / right_u */
+    /* Derived constants, filled on the device by odil_wave_batch_setup. */
+    double inv_dt, inv_dx2, c2, dt2, lam2;
+} odil_wave_instance;
+
+typedef struct odil_wave_batch {
+    int32_t ninst;
+    int32_t max_nx;                  /* largest nx of the batch (<= 4096) */
+    int64_t total_cells;             /* packed array length */
+    odil_wave_instance* inst;        /* device [ninst], sorted by offset */
+    const int32_t* order;            /* device [ninst]: march order */
+    const void* init_u;              /* device, packed, FP64 */
+    const void* init_ut;
+    const void* left_u;
+    const void* right_u;
+} odil_wave_batch;
+
+/* Fills the derived constants of a device descriptor array. */
+int odil_wave_batch_setup(odil_wave_instance* inst, int32_t ninst,
+                          void* stream);
+int64_t odil_wave_batch_workspace_bytes(const odil_wave_batch* b);
+/* FP64 step of a mixed Newton epoch for every instance: as
+ * odil_wave_update_residual_mixed on the packed arrays. */
+int odil_wave_batch_update_residual_mixed(const odil_wave_batch* b,
+                                          const double* u, const float* d,
+                                          double* u_out, float* rhs,
+                                          void* stream);
+/* FP32 forward substitution of every instance in one persistent launch:
+ * blocks_per_sm x #SM blocks of `threads` threads take instances from an
+ * atomic work queue in `order`; threads * cpt >= max_nx; (cpt, pf) in
+ * {1, 2, 4} x {8, 16} (pf = prefetched right-hand-side rows). */
+int odil_wave_batch_march_f32(const odil_wave_batch* b, const float* rhs,
+                              float* x, int32_t threads, int32_t cpt,
+                              int32_t pf, int32_t blocks_per_sm,
+                              void* workspace, int64_t workspace_bytes,
+                              void* stream);
+
+/* ------------------------------------------------------------------------
  * 2D linear advection on the (t, x, y) space-time grid, periodic in x, y.
  *
  * Replaces advection_2d.py:103-223 (operator, direct problem, --periodic 1,

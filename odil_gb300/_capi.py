@@ -61,6 +61,38 @@ class OdilAdvectParams(ctypes.Structure):
     ]
 
 
+class OdilWaveInstance(ctypes.Structure):
+    _fields_ = [
+        ("nt", ctypes.c_int64),
+        ("nx", ctypes.c_int64),
+        ("dt", ctypes.c_double),
+        ("dx", ctypes.c_double),
+        ("c", ctypes.c_double),
+        ("offset", ctypes.c_int64),
+        ("offset_x", ctypes.c_int64),
+        ("offset_t", ctypes.c_int64),
+        ("inv_dt", ctypes.c_double),
+        ("inv_dx2", ctypes.c_double),
+        ("c2", ctypes.c_double),
+        ("dt2", ctypes.c_double),
+        ("lam2", ctypes.c_double),
+    ]
+
+
+class OdilWaveBatch(ctypes.Structure):
+    _fields_ = [
+        ("ninst", ctypes.c_int32),
+        ("max_nx", ctypes.c_int32),
+        ("total_cells", ctypes.c_int64),
+        ("inst", ctypes.c_void_p),
+        ("order", ctypes.c_void_p),
+        ("init_u", ctypes.c_void_p),
+        ("init_ut", ctypes.c_void_p),
+        ("left_u", ctypes.c_void_p),
+        ("right_u", ctypes.c_void_p),
+    ]
+
+
 STENCIL_MAXS = 128
 
 
@@ -99,6 +131,12 @@ SIGNATURES = {
     "odil_wave_update_residual_workspace_bytes": (_I64, [_P]),
     "odil_wave_update_residual_mixed": (_INT, [_P, _P, _P, _P, _P, _P, _P, _I64,
                                                _P]),
+    "odil_wave_batch_setup": (_INT, [_P, ctypes.c_int32, _P]),
+    "odil_wave_batch_workspace_bytes": (_I64, [_P]),
+    "odil_wave_batch_update_residual_mixed": (_INT, [_P, _P, _P, _P, _P, _P]),
+    "odil_wave_batch_march_f32": (_INT, [_P, _P, _P, ctypes.c_int32,
+                                         ctypes.c_int32, ctypes.c_int32,
+                                         ctypes.c_int32, _P, _I64, _P]),
     "odil_advect_workspace_bytes": (_I64, [_P]),
     "odil_advect_residual_f32": (_INT, [_P, _P, _P, _P]),
     "odil_advect_residual_f64": (_INT, [_P, _P, _P, _P]),

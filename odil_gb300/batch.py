@@ -1,0 +1,135 @@
+"""Batched solves of many independent wave instances of uneven sizes.
+
+The reference solves such families as separate processes farmed out by MPI
+(vary_wave.py:7-43).  Here all instances share packed device arrays and one
+mixed-precision Newton solve of the whole batch is a fixed sequence of
+launches -- per epoch one FP64 update/residual over every cell and one
+persistent FP32 forward-substitution launch that pulls instances from a work
+queue -- captured once into a CUDA graph and replayed.
+"""
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _capi, autotune
+from ._capi import call, ptr, stream_handle
+
+
+def _align4(n):
+    return (n + 3) // 4 * 4
+
+
+class WaveBatch:
+    """Packed device state of many wave instances.
+
+    ``instances``: list of dicts with nt, nx, dt, dx, c and the boundary
+    arrays init_u, init_ut [nx], left_u, right_u [nt] (as WaveOperator).
+    """
+
+    def __init__(self, instances, device="cuda"):
+        _capi.load()
+        self.device = torch.device(device)
+        self.n = len(instances)
+        if self.n < 1:
+            raise ValueError("empty batch")
+        descs = (_capi.OdilWaveInstance * self.n)()
+        off = offx = offt = 0
+        self.offsets, self.shapes = [], []
+        bcx_u, bcx_ut, bct_l, bct_r = [], [], [], []
+        for d, inst in zip(descs, instances):
+            nt, nx = int(inst["nt"]), int(inst["nx"])
+            d.nt, d.nx = nt, nx
+            d.dt, d.dx, d.c = float(inst["dt"]), float(inst["dx"]), float(inst["c"])
+            d.offset, d.offset_x, d.offset_t = off, offx, offt
+            self.offsets.append(off)
+            self.shapes.append((nt, nx))
+            off = _align4(off + nt * nx)
+            offx += nx
+            offt += nt
+            bcx_u.append(np.asarray(inst["init_u"], np.float64))
+            bcx_ut.append(np.asarray(inst["init_ut"], np.float64))
+            bct_l.append(np.asarray(inst["left_u"], np.float64))
+            bct_r.append(np.asarray(inst["right_u"], np.float64))
+        self.total = off
+        self.max_nx = max(s[1] for s in self.shapes)
+        dev = self.device
+        raw = bytes(descs)
+        self.desc = torch.frombuffer(bytearray(raw), dtype=torch.uint8).to(dev)
+        self.bc = [torch.as_tensor(np.concatenate(a), device=dev)
+                   for a in (bcx_u, bcx_ut, bct_l, bct_r)]
+        call("odil_wave_batch_setup", ptr(self.desc), self.n, stream_handle())
+        # Largest instances first: the work queue then balances the tail.
+        order = np.argsort([-s[0] * s[1] for s in self.shapes], kind="stable")
+        self.order = torch.as_tensor(order.astype(np.int32), device=dev)
+        b = _capi.OdilWaveBatch()
+        b.ninst, b.max_nx, b.total_cells = self.n, self.max_nx, self.total
+        b.inst, b.order = self.desc.data_ptr(), self.order.data_ptr()
+        b.init_u, b.init_ut, b.left_u, b.right_u = [t.data_ptr() for t in self.bc]
+        self.b = b
+        kw64 = dict(dtype=torch.float64, device=dev)
+        kw32 = dict(dtype=torch.float32, device=dev)
+        self.u = torch.zeros(self.total, **kw64)
+        self.ub = torch.zeros(self.total, **kw64)
+        self.rhs = torch.zeros(self.total, **kw32)
+        self.d = torch.zeros(self.total, **kw32)
+        self.ws = torch.zeros(256, dtype=torch.uint8, device=dev)
+        self.march_cfg = None
+        self.graph = None
+
+    # -- launches -------------------------------------------------------------
+    def update_residual(self, u, d, u_out, rhs):
+        call("odil_wave_batch_update_residual_mixed", ctypes.byref(self.b),
+             ptr(u), ptr(d), ptr(u_out if d is not None else None), ptr(rhs),
+             stream_handle())
+
+    def march(self, rhs, x, cfg=None):
+        cfg = cfg or self.march_cfg or autotune.default_batch_march(self.max_nx)
+        call("odil_wave_batch_march_f32", ctypes.byref(self.b), ptr(rhs), ptr(x),
+             cfg["threads"], cfg["cpt"], cfg["pf"], cfg["blocks_per_sm"],
+             ptr(self.ws), self.ws.numel(), stream_handle())
+
+    def tune(self, cache=True):
+        """Chooses the persistent march's launch shape by timing candidates
+        on this batch (cached per device and batch size class)."""
+        self.update_residual(self.u, None, None, self.rhs)
+        self.march_cfg = autotune.tune_batch_march(self, cache=cache)
+        return self.march_cfg
+
+    def solve_mixed(self, epochs=2):
+        """u <- mixed-precision Newton solution from u = 0 (all instances)."""
+        self.u.zero_()
+        ua, ub = self.u, self.ub
+        self.update_residual(ua, None, None, self.rhs)
+        for _ in range(epochs):
+            self.march(self.rhs, self.d)
+            self.update_residual(ua, self.d, ub, self.rhs)
+            ua, ub = ub, ua
+        if ua is not self.u:
+            self.u.copy_(ua)
+        return self.u
+
+    def capture(self, epochs=2):
+        """Captures solve_mixed into a CUDA graph (replay with .replay())."""
+        if self.march_cfg is None:
+            self.march_cfg = autotune.default_batch_march(self.max_nx)
+        s = torch.cuda.Stream(self.device)
+        s.wait_stream(torch.cuda.current_stream(self.device))
+        with torch.cuda.stream(s):
+            self.solve_mixed(epochs)  # warm-up outside the graph
+        torch.cuda.current_stream(self.device).wait_stream(s)
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, stream=s):
+            self.solve_mixed(epochs)
+        self.graph = g
+        return g
+
+    def replay(self):
+        self.graph.replay()
+        return self.u
+
+    def unpack(self, u=None):
+        u = self.u if u is None else u
+        host = u.cpu().numpy()
+        return [host[o:o + s[0] * s[1]].reshape(s)
+                for o, s in zip(self.offsets, self.shapes)]

@@ -1,0 +1,229 @@
+// Many independent wave instances of uneven sizes solved together (the
+// reference farms such runs out as separate processes, vary_wave.py:7-43).
+// Fields of all instances are packed back to back (each instance starts on a
+// 16-byte boundary); a device array of descriptors gives each instance's
+// grid, wave speed, offsets and derived constants.
+//
+// One mixed-precision Newton epoch for the whole batch is two launches:
+//   * batch_update_residual: FP64 u_out = u + d and rhs = float(-F(u_out))
+//     over every cell of every instance (all SMs; the instance of a cell by
+//     binary search over the start offsets);
+//   * batch_march: a persistent FP32 forward-substitution kernel; each block
+//     takes the next instance from an atomic work queue (instances ordered
+//     largest first) and marches it with the single-instance device code.
+// Both are stream-ordered, allocation-free and capture into a CUDA graph.
+#include "wave_dev.cuh"
+
+namespace odil {
+namespace {
+using namespace wavedev;
+
+// Derived constants of every instance (double and float copies).
+__global__ void batch_setup_kernel(odil_wave_instance* inst, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    odil_wave_instance& d = inst[i];
+    const double inv_dt = 1.0 / d.dt;
+    const double inv_dx2 = 1.0 / (d.dx * d.dx);
+    d.inv_dt = inv_dt;
+    d.inv_dx2 = inv_dx2;
+    d.c2 = d.c * d.c;
+    d.dt2 = d.dt * d.dt;
+    d.lam2 = d.c * d.c * d.dt * d.dt * inv_dx2;
+}
+
+template <typename T>
+__device__ __forceinline__ WaveDev<T> dev_of(const odil_wave_instance& d, const T* init_u,
+                                             const T* init_ut, const T* left_u,
+                                             const T* right_u) {
+    WaveDev<T> g;
+    g.nt = (int)d.nt;
+    g.nx = (int)d.nx;
+    g.inv_dt = (T)d.inv_dt;
+    g.inv_dx2 = (T)d.inv_dx2;
+    g.c2 = (T)d.c2;
+    g.half_dt = (T)(0.5 * d.dt);
+    g.A = (T)(d.inv_dt * d.inv_dt);
+    g.B = (T)(d.c2 * d.inv_dx2);
+    g.dt2 = (T)d.dt2;
+    g.lam2 = (T)d.lam2;
+    g.init_u = init_u ? init_u + d.offset_x : nullptr;
+    g.init_ut = init_ut ? init_ut + d.offset_x : nullptr;
+    g.left_u = left_u ? left_u + d.offset_t : nullptr;
+    g.right_u = right_u ? right_u + d.offset_t : nullptr;
+    return g;
+}
+
+// Instance holding packed cell k (starts sorted ascending), or -1 in padding.
+__device__ __forceinline__ int find_inst(const odil_wave_instance* __restrict__ inst, int n,
+                                         int64_t k) {
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldg(&inst[mid].offset) <= k) lo = mid; else hi = mid - 1;
+    }
+    const int64_t off = __ldg(&inst[lo].offset);
+    const int64_t cells = __ldg(&inst[lo].nt) * __ldg(&inst[lo].nx);
+    return (k >= off && k < off + cells) ? lo : -1;
+}
+
+__global__ void __launch_bounds__(256) batch_update_residual_kernel(
+    odil_wave_batch b, const double* __restrict__ u, const float* __restrict__ d,
+    double* __restrict__ uout, float* __restrict__ rhs) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    const double* iu = (const double*)b.init_u;
+    const double* iut = (const double*)b.init_ut;
+    const double* lu = (const double*)b.left_u;
+    const double* ru = (const double*)b.right_u;
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < b.total_cells;
+         k += stride) {
+        const int q = find_inst(b.inst, b.ninst, k);
+        if (q < 0) {
+            rhs[k] = 0.f;
+            if (d) uout[k] = 0.0;
+            continue;
+        }
+        const odil_wave_instance desc = b.inst[q];
+        const WaveDev<double> g = dev_of<double>(desc, iu, iut, lu, ru);
+        const int64_t local = k - desc.offset;
+        const int i = (int)(local / g.nx);
+        const int j = (int)(local - (int64_t)i * g.nx);
+        const double* ub = u + desc.offset;
+        const float* db = d ? d + desc.offset : nullptr;
+        auto val = [&](int ii, int jj) -> double {
+            const int64_t kk = (int64_t)ii * g.nx + jj;
+            double v = __ldg(ub + kk);
+            if (db) v += (double)__ldg(db + kk);
+            return v;
+        };
+        const double uc = val(i, j);
+        double utm = 0, utmm = 0, uxm = 0, uxp = 0;
+        if (i >= 1) {
+            utm = val(i - 1, j);
+            uxm = val(i - 1, j == 0 ? g.nx - 1 : j - 1);
+            uxp = val(i - 1, j + 1 == g.nx ? 0 : j + 1);
+        }
+        if (i >= 2) utmm = val(i - 2, j);
+        const double f = wave_f(g, i, j, uc, utm, utmm, uxm, uxp);
+        if (d) uout[k] = uc;
+        rhs[k] = (float)(-f);
+    }
+}
+
+template <int CPT, int PF>
+__global__ void __launch_bounds__(1024) batch_march_kernel(odil_wave_batch b,
+                                                           const float* __restrict__ rhs,
+                                                           float* __restrict__ x,
+                                                           unsigned* __restrict__ counter) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ int sh_q;
+    for (;;) {
+        if (threadIdx.x == 0) sh_q = (int)atomicAdd(counter, 1u);
+        __syncthreads();
+        const int q = sh_q;
+        __syncthreads();
+        if (q >= b.ninst) break;
+        const int idx = __ldg(b.order + q);
+        const odil_wave_instance desc = b.inst[idx];
+        const WaveDev<float> g = dev_of<float>(desc, nullptr, nullptr, nullptr, nullptr);
+        const float* bb = rhs + desc.offset;
+        float* xx = x + desc.offset;
+        if (g.nx % CPT == 0) {
+            march_instance<float, CPT, PF, true>(g, bb, xx, smem_raw);
+        } else {
+            march_instance<float, CPT, PF, false>(g, bb, xx, smem_raw);
+        }
+        __syncthreads();
+    }
+}
+
+int check_batch(const odil_wave_batch* b) {
+    if (!b) return ODIL_ERR_ARG;
+    if (b->ninst < 1 || b->total_cells < 1 || b->max_nx < 1 || b->max_nx > 4096)
+        return ODIL_ERR_SHAPE;
+    if (!b->inst || !b->order) return ODIL_ERR_ARG;
+    return ODIL_OK;
+}
+
+inline int sms() {
+    int dev = 0, n = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    return n > 0 ? n : 132;
+}
+
+template <int CPT, int PF>
+int launch_batch_march(const odil_wave_batch* b, const float* rhs, float* x, unsigned* counter,
+                       int threads, int blocks, cudaStream_t st) {
+    if ((int64_t)threads * CPT < b->max_nx) return ODIL_ERR_SHAPE;
+    const size_t smem = (2 + PF) * (size_t)b->max_nx * sizeof(float);
+    if (smem > 200 * 1024) return ODIL_ERR_SHAPE;
+    auto kern = batch_march_kernel<CPT, PF>;
+    // Raise the dynamic shared-memory limit only when it grows, so replays
+    // and graph captures after the first launch issue no attribute calls.
+    static size_t smem_set = 0;
+    if (smem > smem_set) {
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        smem_set = smem;
+    }
+    cudaMemsetAsync(counter, 0, sizeof(unsigned), st);
+    kern<<<blocks, threads, smem, st>>>(*b, rhs, x, counter);
+    return launch_status();
+}
+
+}  // namespace
+}  // namespace odil
+
+using namespace odil;
+
+ODIL_API int odil_wave_batch_setup(odil_wave_instance* inst, int32_t ninst, void* stream) {
+    if (!inst || ninst < 1) return ODIL_ERR_ARG;
+    batch_setup_kernel<<<(ninst + 127) / 128, 128, 0, as_stream(stream)>>>(inst, ninst);
+    return launch_status();
+}
+
+ODIL_API int64_t odil_wave_batch_workspace_bytes(const odil_wave_batch* b) {
+    (void)b;
+    return 256;
+}
+
+ODIL_API int odil_wave_batch_update_residual_mixed(const odil_wave_batch* b, const double* u,
+                                                   const float* d, double* u_out, float* rhs,
+                                                   void* stream) {
+    int st = check_batch(b);
+    if (st) return st;
+    if (!u || !rhs || (d && (!u_out || u_out == u))) return ODIL_ERR_ARG;
+    if (!b->init_u || !b->init_ut || !b->left_u || !b->right_u) return ODIL_ERR_ARG;
+    int64_t blocks = (b->total_cells + 255) / 256;
+    const int64_t cap = (int64_t)sms() * 16;
+    if (blocks > cap) blocks = cap;
+    batch_update_residual_kernel<<<(int)blocks, 256, 0, as_stream(stream)>>>(*b, u, d, u_out,
+                                                                             rhs);
+    return launch_status();
+}
+
+ODIL_API int odil_wave_batch_march_f32(const odil_wave_batch* b, const float* rhs, float* x,
+                                       int32_t threads, int32_t cpt, int32_t pf,
+                                       int32_t blocks_per_sm, void* workspace,
+                                       int64_t workspace_bytes, void* stream) {
+    int st = check_batch(b);
+    if (st) return st;
+    if (!rhs || !x) return ODIL_ERR_ARG;
+    if (!workspace || workspace_bytes < 256) return ODIL_ERR_WORKSPACE;
+    if (threads < 32 || threads > 1024 || threads % 32 || blocks_per_sm < 1 || blocks_per_sm > 32)
+        return ODIL_ERR_SHAPE;
+    int blocks = sms() * blocks_per_sm;
+    if (blocks > b->ninst) blocks = b->ninst;
+    unsigned* counter = reinterpret_cast<unsigned*>(workspace);
+    cudaStream_t s = as_stream(stream);
+    const int key = cpt * 100 + pf;
+    switch (key) {
+        case 108: return launch_batch_march<1, 8>(b, rhs, x, counter, threads, blocks, s);
+        case 116: return launch_batch_march<1, 16>(b, rhs, x, counter, threads, blocks, s);
+        case 208: return launch_batch_march<2, 8>(b, rhs, x, counter, threads, blocks, s);
+        case 216: return launch_batch_march<2, 16>(b, rhs, x, counter, threads, blocks, s);
+        case 408: return launch_batch_march<4, 8>(b, rhs, x, counter, threads, blocks, s);
+        case 416: return launch_batch_march<4, 16>(b, rhs, x, counter, threads, blocks, s);
+        default: return ODIL_ERR_SHAPE;
+    }
+}

@@ -113,10 +113,13 @@ __global__ void __launch_bounds__(VT) axpby_kernel(T* z, const T* x, const T* y,
 
 // ---------------------------------------------------------------------------
 // Multi-dot: D[i*r + j] = sum_e M[i*ld + e] * Q_j[e], i < k, j < r <= 4.
-// Block (i, c) reduces row i over column chunk c; the last block adds the
-// chunk partials in order (deterministic).  Rows of one chunk run on
-// consecutive block ids so the Q chunk is reused from L2.
+// Block (g, c) reduces the MD_G rows g*MD_G ... of M over column chunk c: each
+// thread keeps its slice of the r query vectors in registers (read once per
+// chunk and row group), streams the group's rows (MD_G independent loads in
+// flight), and accumulates MD_G x r partial sums in the working precision.
+// The last block adds the chunk partials in index order (deterministic).
 constexpr int MD_MAXR = 4;
+constexpr int MD_G = 4;
 
 struct QPtrs {
     const void* q[MD_MAXR];
@@ -130,72 +133,77 @@ __global__ void __launch_bounds__(VT) multidot_kernel(const T* __restrict__ M, i
                                                       bool vec) {
     using V = typename Vec<T>::V;
     constexpr int W = Vec<T>::W;
-    const int i = blockIdx.x;       // row
-    const int64_t c = blockIdx.y;   // chunk
+    const int g0 = blockIdx.x * MD_G;   // first row of the group
+    const int64_t c = blockIdx.y;       // chunk
     const int64_t e0 = c * chunk;
     int64_t e1 = e0 + chunk;
     if (e1 > n) e1 = n;
-    const T* row = M + (int64_t)i * ld;
-    // Per-thread partial sums in the working precision (a thread adds at most
-    // chunk / (VT * W) products), FP64 across threads and blocks: the FP64
-    // pipe stays off the streaming loop.
-    T acc[MD_MAXR] = {T(0), T(0), T(0), T(0)};
+    T acc[MD_G][MD_MAXR];
+#pragma unroll
+    for (int g = 0; g < MD_G; ++g)
+#pragma unroll
+        for (int j = 0; j < MD_MAXR; ++j) acc[g][j] = T(0);
     if (vec) {
         const int64_t v0 = e0 / W, v1 = e1 / W;
-        // Four vector elements per thread per step, all loads issued first:
-        // enough bytes in flight per SM to cover the HBM latency.
-        constexpr int U = 4;
-        int64_t e = v0 + threadIdx.x;
-        for (; e + (U - 1) * VT < v1; e += U * VT) {
-            V mv[U], qv[MD_MAXR][U];
-#pragma unroll
-            for (int uu = 0; uu < U; ++uu) mv[uu] = __ldcs(reinterpret_cast<const V*>(row) + e + uu * VT);
+        for (int64_t e = v0 + threadIdx.x; e < v1; e += VT) {
+            V qv[MD_MAXR];
 #pragma unroll
             for (int j = 0; j < MD_MAXR; ++j)
-                if (j < r)
+                if (j < r) qv[j] = __ldg(reinterpret_cast<const V*>(qs.q[j]) + e);
+            V mv[MD_G];
 #pragma unroll
-                    for (int uu = 0; uu < U; ++uu)
-                        qv[j][uu] = __ldg(reinterpret_cast<const V*>(qs.q[j]) + e + uu * VT);
+            for (int g = 0; g < MD_G; ++g)
+                if (g0 + g < k)
+                    mv[g] = __ldcs(reinterpret_cast<const V*>(M + (int64_t)(g0 + g) * ld) + e);
 #pragma unroll
-            for (int uu = 0; uu < U; ++uu) {
-                const T* ms = reinterpret_cast<const T*>(&mv[uu]);
+            for (int g = 0; g < MD_G; ++g) {
+                if (g0 + g < k) {
+                    const T* ms = reinterpret_cast<const T*>(&mv[g]);
 #pragma unroll
-                for (int j = 0; j < MD_MAXR; ++j) {
-                    if (j < r) {
-                        const T* qq = reinterpret_cast<const T*>(&qv[j][uu]);
+                    for (int j = 0; j < MD_MAXR; ++j) {
+                        if (j < r) {
+                            const T* qq = reinterpret_cast<const T*>(&qv[j]);
 #pragma unroll
-                        for (int w = 0; w < W; ++w) acc[j] += ms[w] * qq[w];
+                            for (int w = 0; w < W; ++w) acc[g][j] += ms[w] * qq[w];
+                        }
                     }
                 }
             }
         }
-        for (; e < v1; e += VT) {
-            V mv = __ldcs(reinterpret_cast<const V*>(row) + e);
-            const T* ms = reinterpret_cast<const T*>(&mv);
+        for (int64_t e = v1 * W + threadIdx.x; e < e1; e += VT) {
 #pragma unroll
-            for (int j = 0; j < MD_MAXR; ++j) {
-                if (j < r) {
-                    V qv = __ldg(reinterpret_cast<const V*>(qs.q[j]) + e);
-                    const T* qq = reinterpret_cast<const T*>(&qv);
+            for (int g = 0; g < MD_G; ++g) {
+                if (g0 + g < k) {
+                    const T mval = M[(int64_t)(g0 + g) * ld + e];
 #pragma unroll
-                    for (int w = 0; w < W; ++w) acc[j] += ms[w] * qq[w];
+                    for (int j = 0; j < MD_MAXR; ++j)
+                        if (j < r) acc[g][j] += mval * ((const T*)qs.q[j])[e];
                 }
             }
         }
-        for (int64_t e = v1 * W + threadIdx.x; e < e1; e += VT) {
-            const T mval = row[e];
-            for (int j = 0; j < r; ++j) acc[j] += mval * ((const T*)qs.q[j])[e];
-        }
     } else {
         for (int64_t e = e0 + threadIdx.x; e < e1; e += VT) {
-            const T mval = row[e];
-            for (int j = 0; j < r; ++j) acc[j] += mval * ((const T*)qs.q[j])[e];
+#pragma unroll
+            for (int g = 0; g < MD_G; ++g) {
+                if (g0 + g < k) {
+                    const T mval = M[(int64_t)(g0 + g) * ld + e];
+#pragma unroll
+                    for (int j = 0; j < MD_MAXR; ++j)
+                        if (j < r) acc[g][j] += mval * ((const T*)qs.q[j])[e];
+                }
+            }
         }
     }
     const int64_t nchunk = gridDim.y;
-    for (int j = 0; j < r; ++j) {
-        double s = block_sum((double)acc[j]);
-        if (threadIdx.x == 0) partials[((int64_t)i * r + j) * nchunk + c] = s;
+#pragma unroll
+    for (int g = 0; g < MD_G; ++g) {
+#pragma unroll
+        for (int j = 0; j < MD_MAXR; ++j) {
+            if (g0 + g < k && j < r) {
+                double s = block_sum((double)acc[g][j]);
+                if (threadIdx.x == 0) partials[((int64_t)(g0 + g) * r + j) * nchunk + c] = s;
+            }
+        }
     }
     __shared__ bool is_last;
     if (threadIdx.x == 0) {
@@ -281,7 +289,7 @@ int axpby_impl(T* z, const T* x, const T* y, int64_t n, double a, double b, void
 
 inline int64_t md_chunk(int64_t n) {
     // ~2 waves of blocks per row group; chunks are multiples of 1024 elements.
-    int64_t chunk = 1 << 16;
+    int64_t chunk = 1 << 15;
     if (n < chunk) chunk = ((n + 1023) / 1024) * 1024;
     if (chunk < 1024) chunk = 1024;
     return chunk;
@@ -309,7 +317,7 @@ int multidot_impl(const T* M, int64_t ld, int k, const void* const* q, int r, in
     const int64_t nchunk = (n + chunk - 1) / chunk;
     if (nchunk > 65535) return ODIL_ERR_SHAPE;
     ReduceWs w = reduce_ws(ws);
-    dim3 grid(k, (unsigned)nchunk);
+    dim3 grid((k + MD_G - 1) / MD_G, (unsigned)nchunk);
     multidot_kernel<T><<<grid, VT, 0, as_stream(stream)>>>(M, ld, k, qs, r, n, chunk, w.partials,
                                                            w.counter, out, vec);
     return launch_status();

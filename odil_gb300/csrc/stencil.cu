@@ -150,7 +150,7 @@ __global__ void __launch_bounds__(256) st_apply_t_kernel(StDev A, const T* __res
 // pair_d[q] = index of shift d of the pair list; one thread per (cell, d).
 struct PairList {
     int npair;
-    short ia[MAXS * 4], ib[MAXS * 4], id[MAXS * 4];
+    short ia[MAXS * 32], ib[MAXS * 32], id[MAXS * 32];
 };
 
 template <typename T>
@@ -373,7 +373,7 @@ static int mto_impl(const odil_stencil* A, const odil_stencil* B, odil_stencil* 
         if (a.nw[ax] != b.nw[ax] || a.nw[ax] != c.nw[ax]) return ODIL_ERR_SHAPE;
     if (!ws || ws_bytes < (int64_t)sizeof(PairList)) return ODIL_ERR_WORKSPACE;
     if (!A->coef || !B->coef || !C->coef) return ODIL_ERR_ARG;
-    PairList pl;
+    static PairList pl;  // ~24 KB: keep it off the stack (set-up path, one host thread)
     pl.npair = 0;
     for (int i = 0; i < a.ns; ++i)
         for (int j = 0; j < b.ns; ++j) {
@@ -385,7 +385,7 @@ static int mto_impl(const odil_stencil* A, const odil_stencil* B, odil_stencil* 
                 if (eq) { d = q; break; }
             }
             if (d < 0) return ODIL_ERR_SHAPE;  // C must list every b - a
-            if (pl.npair >= MAXS * 4) return ODIL_ERR_SHAPE;
+            if (pl.npair >= MAXS * 32) return ODIL_ERR_SHAPE;
             pl.ia[pl.npair] = (short)i;
             pl.ib[pl.npair] = (short)j;
             pl.id[pl.npair] = (short)d;

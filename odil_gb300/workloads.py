@@ -127,3 +127,25 @@ class AdvectInstance:
 
     def exact(self):
         return self._exact()
+
+
+# -- batched wave instances ---------------------------------------------------
+def wave_batch_instances(count=512, seed=4, nmin=64, nmax=512, cmin=0.5,
+                         cmax=2.0, nmodes=5):
+    """Seeded uneven batch: side n ~ U{nmin..nmax} (nt = nx = n), wave speed
+    c ~ U[cmin, cmax], 5-mode sine profile with per-instance seed.  Returns
+    the instance dicts of WaveBatch plus each one's exact solution."""
+    rng = np.random.default_rng(seed)
+    sides = rng.integers(nmin, nmax + 1, count)
+    speeds = rng.uniform(cmin, cmax, count)
+    out = []
+    for i, (n, c) in enumerate(zip(sides, speeds)):
+        inst = WaveInstance(int(n), int(n), profile="sine",
+                            seed=seed * 100003 + i, nmodes=nmodes,
+                            c=float(c), device="cpu")
+        op = inst.operator
+        out.append({"nt": int(n), "nx": int(n), "dt": 1.0 / n, "dx": 2.0 / n,
+                    "c": float(c), "init_u": op.init_u, "init_ut": op.init_ut,
+                    "left_u": op.left_u, "right_u": op.right_u,
+                    "exact_u": inst.exact_u, "seed": seed * 100003 + i})
+    return out

@@ -1,0 +1,63 @@
+"""Batched uneven wave instances: per-instance parity with the FP64 oracle,
+CUDA-graph replay, and the autotuned persistent launch."""
+import numpy as np
+import pytest
+import torch
+
+from oracle import wave as W
+
+pytestmark = pytest.mark.gpu
+
+
+def _oracle(inst):
+    s = W.WaveSetup(inst["nt"], inst["nx"], inst["init_u"], inst["init_ut"],
+                    inst["left_u"], inst["right_u"], c=inst["c"])
+    return W.solve_march(s, rounds=2)
+
+
+def _small_batch():
+    from odil_gb300.workloads import wave_batch_instances
+    return wave_batch_instances(count=24, seed=9, nmin=5, nmax=70)
+
+
+def test_batch_matches_oracle_per_instance(cuda):
+    from odil_gb300.batch import WaveBatch
+    insts = _small_batch()
+    assert len({i["nx"] % 4 for i in insts}) > 1  # vector and scalar paths
+    b = WaveBatch(insts, device=cuda)
+    b.solve_mixed(epochs=2)
+    got = b.unpack()
+    for inst, u in zip(insts, got):
+        ref = _oracle(inst)
+        assert W.rel_err(u, ref) <= 1e-8, (inst["nt"], inst["c"])
+
+
+def test_graph_replay_and_autotune(cuda, tmp_path, monkeypatch):
+    monkeypatch.setenv("ODIL_GB300_TUNE_CACHE", str(tmp_path / "tune.json"))
+    from odil_gb300.batch import WaveBatch
+    from odil_gb300 import autotune
+    insts = _small_batch()
+    b = WaveBatch(insts, device=cuda)
+    cfg = b.tune()
+    assert cfg in autotune.candidates_batch_march(b.max_nx)
+    assert (tmp_path / "tune.json").exists()
+    b.solve_mixed()
+    eager = b.u.clone()
+    b.capture()
+    b.u.fill_(123.0)
+    b.replay()
+    assert torch.equal(b.u, eager)
+    b.replay()
+    assert torch.equal(b.u, eager)
+
+
+def test_batch_benchmark_sizes_sample(cuda):
+    """A sample of the 512-instance benchmark batch (sides 64..512, c in
+    [0.5, 2]): every instance reaches rel err <= 1e-5 (here 1e-8)."""
+    from odil_gb300.batch import WaveBatch
+    from odil_gb300.workloads import wave_batch_instances
+    insts = wave_batch_instances(count=512)[:40]
+    b = WaveBatch(insts, device=cuda)
+    b.solve_mixed()
+    for inst, u in zip(insts, b.unpack()):
+        assert W.rel_err(u, _oracle(inst)) <= 1e-8

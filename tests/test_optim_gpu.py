@@ -145,6 +145,7 @@ def test_lbfgs_fp32_wave_1024_runs(cuda):
     assert info.epochs == 30, info
     # The initial-row residual is removed in the first iterations; after that
     # the FP32 loss sits near its rounding floor (kappa(J^T J) ~ 1e12), and
-    # accepted steps stay within the approximate-Wolfe tolerance.
+    # accepted steps stay within the approximate-Wolfe tolerance (1e-6 |f|
+    # per step, so at most 30e-6 over the run).
     assert min(losses) < 0.01 * l0
-    assert losses[-1] <= min(losses) * (1 + 1e-5)
+    assert losses[-1] <= min(losses) * (1 + 30e-6)
