@@ -234,6 +234,47 @@ int odil_dense_apply_f64(int64_t n, const double* Ainv, const float* b,
                          float* x, void* stream);
 
 /* ------------------------------------------------------------------------
+ * Steady Navier-Stokes, lid-driven cavity on an n x n grid of [0, 1]^2.
+ *
+ * Replaces ns_steady.py:142-433 (operator) with its defaults: no-slip walls
+ * and lid u = 1 at y = 1 by quadratic extrapolation (bc 0), deferred-
+ * correction upwind momentum, central pressure gradient, Rhie-Chow
+ * continuity; mu = 1/Re.  Residual terms, in order: fu, fv, fp, then
+ * [imposed u, v] (mask != NULL), [kreg u_xx, u_yy, v_xx, v_yy] (kreg != 0),
+ * [pin_weight * p at cell `pin`] (pin >= 0, the benchmark's pressure pin).
+ * ---------------------------------------------------------------------- */
+typedef struct odil_ns_params {
+    int64_t n;
+    double re;
+    double kreg;
+    const void* mask;   /* [n*n] imposed-point mask (kernel precision) or NULL */
+    const void* u_imp;  /* [n*n] imposed values */
+    const void* v_imp;
+    double imp_coeff;   /* alpha * n^2 / n_imp (ns_steady.py:400) */
+    int64_t pin;        /* flat index of the pinned pressure cell, -1: none */
+    double pin_weight;
+} odil_ns_params;
+
+/* Number of residual terms for these parameters (or a negative status). */
+int odil_ns_num_equations(const odil_ns_params* q);
+/* f[e*n*n + cell] = residual term e at (u, v, p) (frozen = live = state). */
+int odil_ns_residual_f32(const odil_ns_params* q, const float* u,
+                         const float* v, const float* p, float* f,
+                         void* stream);
+int odil_ns_residual_f64(const odil_ns_params* q, const double* u,
+                         const double* v, const double* p, double* f,
+                         void* stream);
+/* Jacobian in stencil form at the state (util_op.py:585-614):
+ * coef[(e*15 + s)*n*n + cell] = d f_e / d (live slot s), s = field*5 + k,
+ * field in (u, v, p), k in (c, x-1, x+1, y-1, y+1). */
+int odil_ns_jacobian_f32(const odil_ns_params* q, const float* u,
+                         const float* v, const float* p, float* coef,
+                         void* stream);
+int odil_ns_jacobian_f64(const odil_ns_params* q, const double* u,
+                         const double* v, const double* p, double* coef,
+                         void* stream);
+
+/* ------------------------------------------------------------------------
  * Operators in stencil form (the reference's SparseOperator,
  * multigrid.py:877-1214): shifts s with one coefficient field C_s each on the
  * output grid,  (A u)[c] = sum_s C_s[c] u[stride*c + s], zero outside the

@@ -93,6 +93,20 @@ class OdilWaveBatch(ctypes.Structure):
     ]
 
 
+class OdilNsParams(ctypes.Structure):
+    _fields_ = [
+        ("n", ctypes.c_int64),
+        ("re", ctypes.c_double),
+        ("kreg", ctypes.c_double),
+        ("mask", ctypes.c_void_p),
+        ("u_imp", ctypes.c_void_p),
+        ("v_imp", ctypes.c_void_p),
+        ("imp_coeff", ctypes.c_double),
+        ("pin", ctypes.c_int64),
+        ("pin_weight", ctypes.c_double),
+    ]
+
+
 STENCIL_MAXS = 128
 
 
@@ -137,6 +151,11 @@ SIGNATURES = {
     "odil_wave_batch_march_f32": (_INT, [_P, _P, _P, ctypes.c_int32,
                                          ctypes.c_int32, ctypes.c_int32,
                                          ctypes.c_int32, _P, _I64, _P]),
+    "odil_ns_num_equations": (_INT, [_P]),
+    "odil_ns_residual_f32": (_INT, [_P, _P, _P, _P, _P, _P]),
+    "odil_ns_residual_f64": (_INT, [_P, _P, _P, _P, _P, _P]),
+    "odil_ns_jacobian_f32": (_INT, [_P, _P, _P, _P, _P, _P]),
+    "odil_ns_jacobian_f64": (_INT, [_P, _P, _P, _P, _P, _P]),
     "odil_advect_workspace_bytes": (_I64, [_P]),
     "odil_advect_residual_f32": (_INT, [_P, _P, _P, _P]),
     "odil_advect_residual_f64": (_INT, [_P, _P, _P, _P]),

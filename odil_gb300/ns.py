@@ -1,0 +1,151 @@
+"""Steady Navier-Stokes lid-driven cavity: the registered, kernel form of
+ns_steady.py:142-433 (operator) with its defaults, forward and inverse
+(imposed points, Laplacian penalty) problems.
+
+Fields (u, v, p) on an (n, n) grid of [0, 1]^2.  The Jacobian at the state is
+computed by a kernel as per-shift coefficient fields (the reference's
+split-shift linearize, util_op.py:585-614) and applied as stencil operators:
+J v and J^T w run through libodil_gb300's stencil kernels.
+"""
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _capi
+from ._capi import call, ptr, stream_handle
+from .stencil import StencilOp
+
+SHIFTS = ((0, 0), (-1, 0), (1, 0), (0, -1), (0, 1))
+FIELDS = ("u", "v", "p")
+
+
+class NsCavityOperator:
+    """Registered operator family "ns_cavity".
+
+    Re: Reynolds number (mu = 1/Re, ns_steady.py:867); mask/u_imp/v_imp:
+    imposed points (ns_steady.py:396-404) with weight alpha; kreg: Laplacian
+    penalty (406-411); pin: (ix, iy) of a cell whose pressure is pinned to 0
+    with weight pin_weight (removes the constant-pressure null space)."""
+    family = "ns_cavity"
+
+    def __init__(self, Re, mask=None, u_imp=None, v_imp=None, alpha=1.0,
+                 kreg=0.0, pin=None, pin_weight=1.0):
+        self.Re = float(Re)
+        self.mask = None if mask is None else np.asarray(mask, np.float64)
+        self.u_imp = None if u_imp is None else np.asarray(u_imp, np.float64)
+        self.v_imp = None if v_imp is None else np.asarray(v_imp, np.float64)
+        self.alpha = float(alpha)
+        self.kreg = float(kreg)
+        self.pin = pin
+        self.pin_weight = float(pin_weight)
+
+    def bind(self, domain):
+        assert domain.ndim == 2 and tuple(domain.fieldnames[:3]) == FIELDS
+        n = domain.shape[0]
+        assert domain.shape == (n, n)
+        return NsKernels(n, self, device=domain.device)
+
+
+class NsKernels:
+    """Device state of one cavity problem."""
+
+    def __init__(self, n, op, device="cuda"):
+        _capi.load()
+        self.n = int(n)
+        self.shape = (self.n, self.n)
+        self.N = self.n * self.n
+        self.op = op
+        self.device = torch.device(device)
+        dev = self.device
+        self._arr = {}
+        for dt in (torch.float32, torch.float64):
+            self._arr[dt] = [None if a is None else
+                             torch.as_tensor(a, dtype=dt, device=dev)
+                             for a in (op.mask, op.u_imp, op.v_imp)]
+        self.params = {dt: self._params(dt) for dt in self._arr}
+        self.neq = _capi.load().odil_ns_num_equations(
+            ctypes.byref(self.params[torch.float64]))
+        if self.neq < 0:
+            raise ValueError("invalid cavity parameters")
+        self.loss_buf = torch.zeros(1, dtype=torch.float64, device=dev)
+
+    def _params(self, dt):
+        q = _capi.OdilNsParams()
+        q.n = self.n
+        q.re = self.op.Re
+        q.kreg = self.op.kreg
+        mask, ui, vi = self._arr[dt]
+        q.mask = None if mask is None else mask.data_ptr()
+        q.u_imp = None if ui is None else ui.data_ptr()
+        q.v_imp = None if vi is None else vi.data_ptr()
+        nimp = 0 if self.op.mask is None else float(np.sum(self.op.mask))
+        q.imp_coeff = self.op.alpha * self.N / nimp if nimp else 0.0
+        q.pin = -1 if self.op.pin is None else \
+            int(self.op.pin[0]) * self.n + int(self.op.pin[1])
+        q.pin_weight = self.op.pin_weight
+        return q
+
+    def _sfx(self, t):
+        if t.dtype not in self.params:
+            raise TypeError("cavity kernels take float32 or float64")
+        return ctypes.byref(self.params[t.dtype]), \
+            "f64" if t.dtype == torch.float64 else "f32"
+
+    def residual(self, u, v, p, out=None):
+        """[neq, n, n] residual terms."""
+        q, sfx = self._sfx(u)
+        out = torch.empty((self.neq, ) + self.shape, dtype=u.dtype,
+                          device=u.device) if out is None else out
+        call("odil_ns_residual_" + sfx, q, ptr(u), ptr(v), ptr(p), ptr(out),
+             stream_handle())
+        return out
+
+    def jacobian(self, u, v, p):
+        """J[e][field]: StencilOp of d f_e / d field at the state."""
+        q, sfx = self._sfx(u)
+        coef = torch.empty((self.neq, 15) + self.shape, dtype=u.dtype,
+                           device=u.device)
+        call("odil_ns_jacobian_" + sfx, q, ptr(u), ptr(v), ptr(p), ptr(coef),
+             stream_handle())
+        return [[StencilOp(SHIFTS, coef[e, 5 * j:5 * j + 5].contiguous(),
+                           self.shape) for j in range(3)]
+                for e in range(self.neq)]
+
+    @staticmethod
+    def jv(J, w):
+        """J w for w = (wu, wv, wp): list of neq fields."""
+        out = []
+        for row in J:
+            acc = None
+            for j, A in enumerate(row):
+                if acc is None:
+                    acc = A.mul_field(w[j])
+                else:
+                    A.mul_field(w[j], out=acc, beta=1.0)
+            out.append(acc)
+        return out
+
+    @staticmethod
+    def jtv(J, r, scale=1.0):
+        """J^T r for r = list of neq fields: (gu, gv, gp)."""
+        out = []
+        for j in range(3):
+            acc = None
+            for e, row in enumerate(J):
+                if acc is None:
+                    acc = row[j].mul_transpose_field(r[e], alpha=scale)
+                else:
+                    row[j].mul_transpose_field(r[e], out=acc, alpha=scale,
+                                               beta=1.0)
+            out.append(acc)
+        return out
+
+    def loss_grad(self, u, v, p):
+        """loss = sum_e mean(f_e^2), grads = (2/N) J^T f (the reference's
+        tape gradient through the live fields, util_op.py:627-654)."""
+        f = self.residual(u, v, p)
+        J = self.jacobian(u, v, p)
+        g = self.jtv(J, list(f), scale=2.0 / self.N)
+        loss = (f.double()**2).mean(dim=(1, 2)).sum()
+        return loss, g

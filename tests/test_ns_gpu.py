@@ -1,0 +1,115 @@
+"""GPU parity of the Navier-Stokes cavity operator against the CPU oracle
+(ns_steady.py:142-433 restated) and the reference's FP64 cavity solutions."""
+import os
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import ns as NS
+
+pytestmark = pytest.mark.gpu
+
+GOLD = np.load(os.path.join(os.path.dirname(__file__), "golden",
+                            "cavity_N128.npz"))
+
+
+def _rel(a, b):
+    return np.abs(np.asarray(a) - b).max() / max(np.abs(b).max(), 1e-300)
+
+
+def _setup(n, variant, rng):
+    kw = {}
+    if variant in ("inverse", "all"):
+        mask = np.zeros((n, n))
+        idx = rng.choice(n * n, max(2, n * n // 10), replace=False)
+        mask.ravel()[idx] = 1
+        kw.update(mask=mask, u_imp=rng.standard_normal((n, n)),
+                  v_imp=rng.standard_normal((n, n)), kreg=1e-4)
+    if variant in ("pin", "all"):
+        kw.update(pin=(n // 2, n // 3), pin_weight=3.0)
+    return kw
+
+
+def _kernels(n, Re, kw, dev):
+    from odil_gb300.ns import NsCavityOperator, NsKernels
+    op = NsCavityOperator(Re, mask=kw.get("mask"), u_imp=kw.get("u_imp"),
+                          v_imp=kw.get("v_imp"), kreg=kw.get("kreg", 0.0),
+                          pin=kw.get("pin"), pin_weight=kw.get("pin_weight", 1))
+    return NsKernels(n, op, device=dev)
+
+
+@pytest.mark.parametrize("n", [4, 9, 16])
+@pytest.mark.parametrize("variant", ["forward", "inverse", "pin", "all"])
+def test_residual_and_jacobian(cuda, n, variant):
+    rng = np.random.default_rng(n)
+    kw = _setup(n, variant, rng)
+    s = NS.NsSetup(n, 400.0, **kw)
+    st = {k: rng.standard_normal((n, n)) for k in "uvp"}
+    k = _kernels(n, 400.0, kw, cuda)
+    t = [torch.as_tensor(st[c], device=cuda) for c in "uvp"]
+    f = k.residual(*t).cpu().numpy()
+    const, coefs = NS.coefficients(s, st)
+    assert f.shape[0] == len(const)
+    for e in range(len(const)):
+        assert _rel(f[e], const[e]) < 1e-12, e
+    J = k.jacobian(*t)
+    for e in range(len(const)):
+        for j, fld in enumerate("uvp"):
+            for si, sh in enumerate(NS.SHIFTS):
+                got = J[e][j].coef[si].cpu().numpy()
+                ref = coefs[e][(fld, sh)]
+                assert np.allclose(got, ref, rtol=1e-12,
+                                   atol=1e-12 * max(1, np.abs(ref).max())), \
+                    (e, fld, sh)
+    # J w and J^T r against the CSR of util_op.py:859-937.
+    _, Jcsr = NS.linearize(s, st)
+    w = [rng.standard_normal((n, n)) for _ in range(3)]
+    jw = k.jv(J, [torch.as_tensor(x, device=cuda) for x in w])
+    ref = Jcsr @ np.concatenate([x.ravel() for x in w])
+    got = np.concatenate([x.cpu().numpy().ravel() for x in jw])
+    assert _rel(got, ref) < 1e-12
+    r = [rng.standard_normal((n, n)) for _ in range(len(const))]
+    jtr = k.jtv(J, [torch.as_tensor(x, device=cuda) for x in r])
+    ref = Jcsr.T @ np.concatenate([x.ravel() for x in r])
+    got = np.concatenate([x.cpu().numpy().ravel() for x in jtr])
+    assert _rel(got, ref) < 1e-12
+    # FP32 path.
+    t32 = [x.float() for x in t]
+    f32 = k.residual(*t32).cpu().numpy()
+    for e in range(len(const)):
+        assert _rel(f32[e], const[e]) < 1e-4
+
+
+def test_loss_grad_against_oracle_autodiff(cuda):
+    n = 12
+    rng = np.random.default_rng(3)
+    kw = _setup(n, "all", rng)
+    s = NS.NsSetup(n, 100.0, **kw)
+    st = {k: rng.standard_normal((n, n)) for k in "uvp"}
+    k = _kernels(n, 100.0, kw, cuda)
+    t = [torch.as_tensor(st[c], device=cuda) for c in "uvp"]
+    loss, g = k.loss_grad(*t)
+    const, coefs = NS.coefficients(s, st)
+    lo = sum(np.mean(c**2) for c in const)
+    assert abs(loss.item() - lo) <= 1e-12 * lo
+    _, Jcsr = NS.linearize(s, st)
+    fo = np.concatenate([c.ravel() for c in const])
+    go = (2.0 / (n * n)) * (Jcsr.T @ fo)
+    got = np.concatenate([x.cpu().numpy().ravel() for x in g])
+    assert _rel(got, go) < 1e-12
+
+
+@pytest.mark.parametrize("Re", [100, 400])
+def test_reference_cavity_solutions_are_roots(cuda, Re):
+    """The reference's FP64 Newton solutions (cavity_N128_Re*.pickle) leave
+    only the residual the reference itself converged to (rms ~1e-6)."""
+    n = 128
+    k = _kernels(n, float(Re), {}, cuda)
+    t = [torch.as_tensor(GOLD["Re%d_%s" % (Re, c)], device=cuda) for c in "uvp"]
+    f = k.residual(*t).cpu().numpy()
+    st = {c: GOLD["Re%d_%s" % (Re, c)] for c in "uvp"}
+    fo = NS.residual(NS.NsSetup(n, Re), st)
+    for e in range(3):
+        assert _rel(f[e], fo[e]) < 1e-9
+        assert np.sqrt(np.mean(f[e]**2)) < 1e-5

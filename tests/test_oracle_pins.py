@@ -94,3 +94,41 @@ def test_lbfgsb_error_table_is_consistent():
         if N in newton and N >= 256:
             assert e >= newton[N] * 0.95
             assert e <= newton[N] * 1.2
+
+
+def test_ns_oracle_reference_solutions():
+    """ns_steady.py restated: the reference's shipped FP64 Newton cavity
+    solutions (N=128, Re=100 and 400) are roots of the restated operator to
+    the level the reference converged them (rms residual ~1e-6 against
+    terms of O(10)); a wrong operator leaves O(1e-1 .. 10) residuals."""
+    from oracle import ns as NS
+    gold = np.load(os.path.join(GOLDEN, "cavity_N128.npz"))
+    for Re in (100, 400):
+        st = {k: gold["Re%d_%s" % (Re, k)] for k in "uvp"}
+        ff = NS.residual(NS.NsSetup(128, Re), st)
+        for f in ff:
+            assert np.sqrt(np.mean(f**2)) < 1e-5
+        # Sensitivity: another Reynolds number is not a root.
+        ff2 = NS.residual(NS.NsSetup(128, 2 * Re), st)
+        assert max(np.sqrt(np.mean(f**2)) for f in ff2) > 1e-3
+
+
+def test_ns_oracle_jacobian_is_affine():
+    """const + J (w - w0) reproduces F(w) for the live part of the operator
+    (the frozen copies held at w0), as the reference's linearize assumes."""
+    from oracle import ns as NS
+    import torch
+    n = 10
+    rng = np.random.default_rng(0)
+    s = NS.NsSetup(n, 400, kreg=1e-4, pin=(3, 4), pin_weight=2.0)
+    w0 = {k: rng.standard_normal((n, n)) for k in "uvp"}
+    w1 = {k: w0[k] + rng.standard_normal((n, n)) for k in "uvp"}
+    const, J = NS.linearize(s, w0)
+    frozen = {k: torch.as_tensor(w0[k]) for k in "uvp"}
+    live = NS._live_from(w1)
+    with torch.no_grad():
+        f1 = [f.numpy() for f in NS.operator(s, live, frozen)]
+    dw = np.concatenate([(w1[k] - w0[k]).ravel() for k in "uvp"])
+    lin = np.concatenate([c.ravel() for c in const]) + J @ dw
+    assert np.allclose(lin, np.concatenate([f.ravel() for f in f1]),
+                       atol=1e-9 * np.abs(lin).max())
