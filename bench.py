@@ -193,21 +193,34 @@ def run_optimizers(problem, inst, dev, with_oracle):
         loss, g = kk.loss_grad(x.reshape(NT, NX), grad=torch.empty_like(grad))
         return loss, g.reshape(-1), [loss]
 
+    inst64 = WaveInstance(NT, NX, profile="sine", seed=SEED, nmodes=NMODES,
+                          c=C, dtype=np.float64, device=dev)
+    k64 = Problem(inst64.operator, inst64.domain).kernels
+
+    def lg64(x, epoch):
+        loss, g = k64.loss_grad(x.reshape(NT, NX))
+        return loss, g.reshape(-1), [loss]
+
     res = {}
     ref = oracle_solution() if with_oracle else None
-    for name in ("lbfgsb", "adam"):
-        opt = make_optimizer(name)
-        x0 = torch.zeros(NT * NX, dtype=torch.float32, device=dev)
+    for name, fn, dt in (("lbfgsb", lg, torch.float32),
+                         ("adam", lg, torch.float32),
+                         ("lbfgsb_fp64", lg64, torch.float64)):
+        opt = make_optimizer(name.replace("_fp64", ""))
+        x0 = torch.zeros(NT * NX, dtype=dt, device=dev)
         torch.cuda.synchronize(dev)
         t0 = time.perf_counter()
-        x, info = opt.run(x0, lg, epochs=OPT_ITERS, lr=1e-3)
+        l0 = (kk if dt == torch.float32 else k64).loss_grad(
+            x0.reshape(NT, NX))[0].item()
+        x, info = opt.run(x0, fn, epochs=OPT_ITERS, lr=1e-3)
         torch.cuda.synchronize(dev)
         wall = time.perf_counter() - t0
         xs = x.double().cpu().numpy().reshape(NT, NX)
-        loss, _ = kk.loss_grad(x.reshape(NT, NX))
+        loss, _ = (kk if dt == torch.float32 else k64).loss_grad(
+            x.reshape(NT, NX))
         ent = {"iterations": int(info.epochs), "evals": int(info.evals),
                "wall_s": wall, "ms_per_iter": 1000 * wall / max(1, info.epochs),
-               "final_loss": float(loss.item()),
+               "initial_loss": l0, "final_loss": float(loss.item()),
                "err_vs_exact_l2": float(np.mean((xs - inst.exact_u)**2)**0.5)}
         if ref is not None:
             ent["rel_err_vs_oracle"] = float(np.linalg.norm(xs - ref) /

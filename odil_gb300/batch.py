@@ -133,3 +133,21 @@ class WaveBatch:
         host = u.cpu().numpy()
         return [host[o:o + s[0] * s[1]].reshape(s)
                 for o, s in zip(self.offsets, self.shapes)]
+
+
+def shard_instances(costs, rank, world):
+    """Indices of the instances rank `rank` of `world` solves.
+
+    Instances are independent (no exchange between them), so the batch
+    shards with no collective on the data path: longest-processing-time
+    first, each instance to the currently lightest rank (deterministic, every
+    rank computes the same assignment)."""
+    if not 0 <= rank < world:
+        raise ValueError("rank %d outside world of %d" % (rank, world))
+    load = [0.0] * world
+    owner = []
+    for i in sorted(range(len(costs)), key=lambda i: (-costs[i], i)):
+        r = min(range(world), key=lambda q: (load[q], q))
+        load[r] += costs[i]
+        owner.append((i, r))
+    return sorted(i for i, r in owner if r == rank)

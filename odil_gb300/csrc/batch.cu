@@ -159,13 +159,7 @@ int launch_batch_march(const odil_wave_batch* b, const float* rhs, float* x, uns
     const size_t smem = (2 + PF) * (size_t)b->max_nx * sizeof(float);
     if (smem > 200 * 1024) return ODIL_ERR_SHAPE;
     auto kern = batch_march_kernel<CPT, PF>;
-    // Raise the dynamic shared-memory limit only when it grows, so replays
-    // and graph captures after the first launch issue no attribute calls.
-    static size_t smem_set = 0;
-    if (smem > smem_set) {
-        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        smem_set = smem;
-    }
+    ensure_dynamic_smem(reinterpret_cast<const void*>(kern), smem);
     cudaMemsetAsync(counter, 0, sizeof(unsigned), st);
     kern<<<blocks, threads, smem, st>>>(*b, rhs, x, counter);
     return launch_status();

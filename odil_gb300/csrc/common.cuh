@@ -18,6 +18,31 @@ inline int launch_status() {
 
 inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
 
+// Raises a kernel's dynamic shared-memory limit the first time a launch needs
+// more than 48 KiB (per kernel, keyed by its address), so later launches --
+// including those recorded into CUDA graphs -- make no attribute calls.
+inline void ensure_dynamic_smem(const void* kern, size_t bytes) {
+    constexpr int kSlots = 64;
+    static const void* keys[kSlots];
+    static size_t vals[kSlots];
+    static int used = 0;
+    if (bytes <= 48 * 1024) return;
+    for (int i = 0; i < used; ++i) {
+        if (keys[i] == kern) {
+            if (vals[i] >= bytes) return;
+            cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+            vals[i] = bytes;
+            return;
+        }
+    }
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (used < kSlots) {
+        keys[used] = kern;
+        vals[used] = bytes;
+        ++used;
+    }
+}
+
 // Periodic wrap of an index that is at most one period outside [0, n).
 __device__ __forceinline__ int wrap1(int i, int n) {
     return i < 0 ? i + n : (i >= n ? i - n : i);

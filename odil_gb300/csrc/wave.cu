@@ -209,11 +209,7 @@ int launch_march_cfg(const WaveDev<T>& g, const T* b, T* x, cudaStream_t st) {
     if (threads > 1024) return ODIL_ERR_SHAPE;
     const size_t smem = (2 + PF) * (size_t)nx * sizeof(T);
     auto go = [&](auto kern) {
-        static size_t smem_set = 0;  // per instantiation: raise only when needed
-        if (smem > smem_set) {
-            cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            smem_set = smem;
-        }
+        ensure_dynamic_smem(reinterpret_cast<const void*>(kern), smem);
         kern<<<1, threads, smem, st>>>(g, b, x);
     };
     if (vec) {

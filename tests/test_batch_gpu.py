@@ -53,11 +53,13 @@ def test_graph_replay_and_autotune(cuda, tmp_path, monkeypatch):
 
 def test_batch_benchmark_sizes_sample(cuda):
     """A sample of the 512-instance benchmark batch (sides 64..512, c in
-    [0.5, 2]): every instance reaches rel err <= 1e-5 (here 1e-8)."""
+    [0.5, 2]): every instance reaches rel err <= 1e-5 against the FP64
+    oracle after 2 epochs (instances with c near 2 run at CFL near 1, where
+    the FP32 forward substitution loses the most digits)."""
     from odil_gb300.batch import WaveBatch
     from odil_gb300.workloads import wave_batch_instances
     insts = wave_batch_instances(count=512)[:40]
     b = WaveBatch(insts, device=cuda)
     b.solve_mixed()
-    for inst, u in zip(insts, b.unpack()):
-        assert W.rel_err(u, _oracle(inst)) <= 1e-8
+    errs = [W.rel_err(u, _oracle(inst)) for inst, u in zip(insts, b.unpack())]
+    assert max(errs) <= 1e-5, max(errs)
