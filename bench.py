@@ -359,8 +359,7 @@ def run_ours(args):
     state = State(fields={"u": u})
 
     def solve_mixed():
-        u.zero_()
-        newton.solve(problem, state, "mixed", MIXED_EPOCHS)
+        newton.solve(problem, state, "mixed", MIXED_EPOCHS, from_zero=True)
 
     def solve_fp64():
         u.zero_()
@@ -378,7 +377,7 @@ def run_ours(args):
     d32 = torch.empty_like(rhs)
     ub = torch.empty_like(u)
     k.update_residual_mixed(u, None, None, rhs)
-    t_march = timed(lambda: k.march(rhs, out=d32), 20, 3)
+    t_march = timed(lambda: k.march_tuned(rhs, d32), 20, 3)
     t_upd = timed(lambda: k.update_residual_mixed(u, d32, ub, rhs), 20, 3)
     r64 = torch.empty_like(u)
     t_march64 = timed(lambda: k.march(r64, out=ub), 5, 2)
@@ -418,8 +417,7 @@ def run_ours(args):
         k.bc32[1].copy_(k.bc64[1])
         k.bc32[2].copy_(k.bc64[2])
         k.bc32[3].copy_(k.bc64[3])
-        u.zero_()
-        newton.solve(problem, state, "mixed", MIXED_EPOCHS)
+        newton.solve(problem, state, "mixed", MIXED_EPOCHS, from_zero=True)
         out_host.copy_(u, non_blocking=True)
 
     t_e2e = timed(e2e_step, args.steps, args.warmup)
@@ -466,6 +464,7 @@ def run_ours(args):
                    "l2": "flushed (256 MiB write) before every timed solve",
                    "parallelism": "replicas" if world > 1 else "single"},
         "gpu_launches": (2 * MIXED_EPOCHS + 1) * args.steps,
+        "march_cfg": getattr(k, "_march_cfg", None),
         "clocks": clk,
         "e2e": {"value": 1000.0 / e2e_ms, "unit": "solves/s",
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
@@ -549,7 +548,7 @@ def run_case(args):
     fn = {
         "loss_grad_big": lambda: kb.loss_grad(ubig, grad=gbig),
         "batch": lambda: wb.solve_mixed(),
-        "march": lambda: k.march(rhs, out=d32),
+        "march": lambda: k.march_tuned(rhs, d32),
         "march64": lambda: k.march(u, out=ub),
         "update_residual": lambda: k.update_residual_mixed(u, d32, ub, rhs),
         "loss_grad": lambda: k.loss_grad(u32, grad=g32),

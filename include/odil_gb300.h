@@ -118,6 +118,16 @@ int odil_wave_update_residual_mixed(const odil_wave_params* p, const double* u,
                                     double* rnorm2, void* workspace,
                                     int64_t workspace_bytes, void* stream);
 
+/* rhs = (float)(-F(0)): the first right-hand side of a mixed Newton solve
+ * from u = 0.  FP64 work only where boundary data enter (rows 0 and 1,
+ * columns 0 and nx-1); all other cells are 0. */
+int odil_wave_initial_rhs_mixed(const odil_wave_params* p, float* rhs,
+                                void* stream);
+/* odil_wave_march_f32 with an explicit launch shape: cpt columns per thread
+ * (1, 2, 4, 8; nx <= 1024 cpt) and pf prefetched rows (8, 16). */
+int odil_wave_march_shape_f32(const odil_wave_params* p, const float* b,
+                              float* x, int32_t cpt, int32_t pf, void* stream);
+
 /* ------------------------------------------------------------------------
  * Batched wave instances of uneven sizes (the reference runs them as
  * separate processes, vary_wave.py:7-43).  Fields of all instances are
@@ -368,6 +378,11 @@ int odil_axpby_f32(float* z, const float* x, const float* y, int64_t n,
                    double a, double b, void* stream);
 int odil_axpby_f64(double* z, const double* x, const double* y, int64_t n,
                    double a, double b, void* stream);
+
+/* out = u + (double)d (n elements): the FP64 update after the last FP32
+ * correction of a mixed-precision Newton solve. */
+int odil_add_f32_to_f64(const double* u, const float* d, double* out,
+                        int64_t n, void* stream);
 
 /* Multi-dot: out[i*r + j] = sum_e M[i*ld + e] * q[j][e] for i < k, j < r
  * (r <= 4), in one pass over M.  FP64 accumulation, deterministic order.

@@ -142,6 +142,10 @@ SIGNATURES = {
     "odil_wave_jtv_f64": (_INT, [_P, _P, _P, _P]),
     "odil_wave_march_f32": (_INT, [_P, _P, _P, _P]),
     "odil_wave_march_f64": (_INT, [_P, _P, _P, _P]),
+    "odil_wave_initial_rhs_mixed": (_INT, [_P, _P, _P]),
+    "odil_wave_march_shape_f32": (_INT, [_P, _P, _P, ctypes.c_int32,
+                                         ctypes.c_int32, _P]),
+    "odil_add_f32_to_f64": (_INT, [_P, _P, _P, _I64, _P]),
     "odil_wave_update_residual_workspace_bytes": (_I64, [_P]),
     "odil_wave_update_residual_mixed": (_INT, [_P, _P, _P, _P, _P, _P, _P, _I64,
                                                _P]),

@@ -105,3 +105,40 @@ def tune_batch_march(batch, cache=True):
                      "tried": [[t, c] for t, c in results]}
         _store(data)
     return best[1]
+
+
+def candidates_march(nx, smem_limit=200 * 1024):
+    out = []
+    for cpt in (1, 2, 4, 8):
+        threads = ((nx + cpt - 1) // cpt + 31) // 32 * 32
+        if threads > 1024 or (cpt > 1 and (nx + cpt - 1) // cpt < 32):
+            continue
+        for pf in (8, 16):
+            if (2 + pf) * nx * 4 <= smem_limit:
+                out.append({"cpt": cpt, "pf": pf})
+    return out
+
+
+def tune_march(kernels, cache=True):
+    """Launch shape of the single-instance FP32 forward substitution."""
+    dev = torch.cuda.get_device_name(kernels.device)
+    key = "wave_march|%s|nx%d|nt%d" % (dev, kernels.nx,
+                                        _pow2_bucket(kernels.nt))
+    data = _load() if cache else {}
+    if key in data:
+        return data[key]["cfg"]
+    b = torch.zeros(kernels.shape, dtype=torch.float32, device=kernels.device)
+    x = torch.empty_like(b)
+    kernels.initial_rhs(b)
+    best = None
+    results = []
+    for cfg in candidates_march(kernels.nx):
+        t = _time(lambda: kernels.march_shape(b, x, cfg["cpt"], cfg["pf"]))
+        results.append((t, cfg))
+        if best is None or t < best[0]:
+            best = (t, cfg)
+    if cache:
+        data[key] = {"cfg": best[1], "ms": best[0],
+                     "tried": [[t, c] for t, c in results]}
+        _store(data)
+    return best[1]

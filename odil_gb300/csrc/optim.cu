@@ -335,6 +335,15 @@ int lincomb_impl(T* out, const T* x, const T* M, int64_t ld, int k, const double
     return launch_status();
 }
 
+// out = u + (double)d: the FP64 update of a mixed-precision step.
+__global__ void __launch_bounds__(VT) add_f32_to_f64_kernel(const double* __restrict__ u,
+                                                            const float* __restrict__ d,
+                                                            double* __restrict__ out, int64_t n) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+        out[i] = __ldcs(u + i) + (double)__ldcs(d + i);
+}
+
 }  // namespace
 }  // namespace odil
 
@@ -379,4 +388,13 @@ ODIL_API int odil_lincomb_f32(float* out, const float* x, const float* M, int64_
 ODIL_API int odil_lincomb_f64(double* out, const double* x, const double* M, int64_t ld, int k,
                               const double* coef, int64_t n, void* stream) {
     return lincomb_impl<double>(out, x, M, ld, k, coef, n, stream);
+}
+
+ODIL_API int odil_add_f32_to_f64(const double* u, const float* d, double* out, int64_t n,
+                                 void* stream) {
+    if (n < 0) return ODIL_ERR_SHAPE;
+    if (n == 0) return ODIL_OK;
+    if (!u || !d || !out) return ODIL_ERR_ARG;
+    add_f32_to_f64_kernel<<<stream_blocks(n, 1), VT, 0, as_stream(stream)>>>(u, d, out, n);
+    return launch_status();
 }

@@ -332,6 +332,26 @@ int loss_grad_impl(const odil_wave_params* p, const T* u, T* grad, double* loss,
     return launch_status();
 }
 
+// rhs = float(-F(0)) for the first mixed Newton epoch from u = 0: the
+// residual of the zero field is nonzero only where boundary data enter (rows
+// 0 and 1, columns 0 and nx-1), so only those cells do FP64 work.
+__global__ void __launch_bounds__(256) wave_initial_rhs_kernel(WaveDev<double> g,
+                                                               float* __restrict__ rhs) {
+    const int nx = g.nx;
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= nx) return;
+    for (int i = blockIdx.y; i < g.nt; i += gridDim.y) {
+        float v = 0.f;
+        if (i <= 1 || j == 0 || j == nx - 1) v = (float)(-wave_f(g, i, j, 0.0, 0.0, 0.0, 0.0, 0.0));
+        rhs[(int64_t)i * nx + j] = v;
+    }
+}
+
+template <int CPT, int PF>
+int launch_march_shape(const WaveDev<float>& g, const float* b, float* x, cudaStream_t st) {
+    return launch_march_cfg<float, CPT, PF>(g, b, x, st);
+}
+
 }  // namespace
 }  // namespace odil
 
@@ -429,4 +449,36 @@ ODIL_API int odil_wave_update_residual_mixed(const odil_wave_params* p, const do
             wave_update_residual_kernel<false, false><<<grid, block, 0, s>>>(g, u, d, u_out, rhs, ws, rnorm2);
     }
     return launch_status();
+}
+
+ODIL_API int odil_wave_initial_rhs_mixed(const odil_wave_params* p, float* rhs, void* stream) {
+    WaveDev<double> g;
+    int st = make_dev<double>(p, &g, true);
+    if (st) return st;
+    if (!rhs) return ODIL_ERR_ARG;
+    dim3 grid, block;
+    grid_rows(g, &grid, &block);
+    wave_initial_rhs_kernel<<<grid, block, 0, as_stream(stream)>>>(g, rhs);
+    return launch_status();
+}
+
+ODIL_API int odil_wave_march_shape_f32(const odil_wave_params* p, const float* b, float* x,
+                                       int32_t cpt, int32_t pf, void* stream) {
+    WaveDev<float> g;
+    int st = make_dev<float>(p, &g, false);
+    if (st) return st;
+    if (!b || !x) return ODIL_ERR_ARG;
+    if ((int64_t)g.nx > 1024 * (int64_t)cpt) return ODIL_ERR_SHAPE;
+    cudaStream_t s = as_stream(stream);
+    switch (cpt * 100 + pf) {
+        case 108: return launch_march_shape<1, 8>(g, b, x, s);
+        case 116: return launch_march_shape<1, 16>(g, b, x, s);
+        case 208: return launch_march_shape<2, 8>(g, b, x, s);
+        case 216: return launch_march_shape<2, 16>(g, b, x, s);
+        case 408: return launch_march_shape<4, 8>(g, b, x, s);
+        case 416: return launch_march_shape<4, 16>(g, b, x, s);
+        case 808: return launch_march_shape<8, 8>(g, b, x, s);
+        case 816: return launch_march_shape<8, 16>(g, b, x, s);
+        default: return ODIL_ERR_SHAPE;
+    }
 }

@@ -15,6 +15,7 @@ precision="mixed"  FP64 residual and update, FP32 solve.  Per epoch: one
 import torch
 
 from . import vec
+from ._capi import call, ptr, stream_handle
 
 
 def _scratch(k, name, dtype):
@@ -27,13 +28,16 @@ def _scratch(k, name, dtype):
     return t
 
 
-def solve(problem, state, precision="mixed", epochs=None, rnorm2=None):
+def solve(problem, state, precision="mixed", epochs=None, rnorm2=None,
+          from_zero=False):
     """Runs ``epochs`` Newton epochs in place on ``state``; returns the field.
 
     Default 2 epochs (as the reference runs Newton on the wave): the second
     epoch refines the first, and the mixed method reaches ~1e-10 against the
     FP64 discrete solution.  ``rnorm2`` (a float64 [1] device tensor), if
     given, receives sum(F(u)^2) of the final state (mixed only).
+    ``from_zero``: start from u = 0 (the first right-hand side then needs
+    FP64 work on the boundary cells only).
     """
     k = problem.kernels
     if k is None:
@@ -54,12 +58,23 @@ def solve(problem, state, precision="mixed", epochs=None, rnorm2=None):
         rhs = _scratch(k, "rhs32", torch.float32)
         d = _scratch(k, "d32", torch.float32)
         ua, ub = u, _scratch(k, "u64", torch.float64)
-        k.update_residual_mixed(ua, None, None, rhs,
-                                rnorm2 if epochs == 0 else None)
+        if from_zero:
+            u.zero_()
+        if from_zero and (epochs > 0 or rnorm2 is None):
+            k.initial_rhs(rhs)
+        else:
+            k.update_residual_mixed(ua, None, None, rhs,
+                                    rnorm2 if epochs == 0 else None)
         for e in range(epochs):
-            k.march(rhs, out=d)
-            k.update_residual_mixed(ua, d, ub, rhs,
-                                    rnorm2 if e == epochs - 1 else None)
+            k.march_tuned(rhs, d)
+            last = e == epochs - 1
+            if last and rnorm2 is None:
+                # After the last correction only the FP64 update is needed.
+                call("odil_add_f32_to_f64", ptr(ua), ptr(d), ptr(ub), ua.numel(),
+                     stream_handle())
+            else:
+                k.update_residual_mixed(ua, d, ub, rhs,
+                                        rnorm2 if last else None)
             ua, ub = ub, ua
         if ua is not u:
             u.copy_(ua)

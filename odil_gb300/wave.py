@@ -174,6 +174,26 @@ class WaveKernels:
         call("odil_wave_march_" + sfx, p, ptr(b), ptr(out), stream_handle())
         return out
 
+    def march_shape(self, b, out, cpt, pf):
+        """FP32 forward substitution with an explicit launch shape."""
+        call("odil_wave_march_shape_f32", ctypes.byref(self.p32), ptr(b),
+             ptr(out), int(cpt), int(pf), stream_handle())
+        return out
+
+    def march_tuned(self, b, out):
+        """FP32 forward substitution with the autotuned launch shape."""
+        if getattr(self, "_march_cfg", None) is None:
+            from . import autotune
+            self._march_cfg = autotune.tune_march(self)
+        cfg = self._march_cfg
+        return self.march_shape(b, out, cfg["cpt"], cfg["pf"])
+
+    def initial_rhs(self, rhs):
+        """rhs = float32(-F(0)) (boundary cells only do FP64 work)."""
+        call("odil_wave_initial_rhs_mixed", ctypes.byref(self.p64), ptr(rhs),
+             stream_handle())
+        return rhs
+
     def update_residual_mixed(self, u, d, u_out, rhs, rnorm2=None):
         """u_out = u + d (d FP32 or None), rhs = float32(-F(u_out)) with the
         residual in FP64; optionally rnorm2[0] = sum(F^2)."""

@@ -111,5 +111,8 @@ def test_reference_cavity_solutions_are_roots(cuda, Re):
     st = {c: GOLD["Re%d_%s" % (Re, c)] for c in "uvp"}
     fo = NS.residual(NS.NsSetup(n, Re), st)
     for e in range(3):
-        assert _rel(f[e], fo[e]) < 1e-9
+        # At a root the residual (~1e-5) is the cancellation of O(1) terms,
+        # so operation-order rounding (~1e-16 of the terms) is ~1e-11 of it
+        # at best and ~1e-9 at the largest cells: bound it by 1e-8.
+        assert _rel(f[e], fo[e]) < 1e-8
         assert np.sqrt(np.mean(f[e]**2)) < 1e-5

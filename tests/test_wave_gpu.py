@@ -145,6 +145,65 @@ def test_march_direct_solve(cuda, shape):
     assert _rel(x32.cpu().numpy(), xo) < 1e-3
 
 
+@pytest.mark.parametrize("shape", [(5, 1), (40, 33), (300, 257), (1100, 1024)])
+def test_march_shapes_agree(cuda, shape):
+    """Every explicit FP32 launch shape gives the same forward substitution
+    (same formula per cell; 1e-5 relative allows for a different FMA
+    contraction between template instances)."""
+    from odil_gb300 import autotune
+    s = _setup(*shape, seed=8, c=0.9)
+    assert shape[0] <= 5 or s.c * s.dt / s.dx < 1  # stable march, finite x
+    k = _kernels(s, cuda)
+    b = torch.as_tensor(np.random.default_rng(9).standard_normal(shape),
+                        dtype=torch.float32, device=cuda)
+    ref = k.march(b)
+    assert torch.isfinite(ref).all()
+    cands = autotune.candidates_march(shape[1])
+    assert cands
+    for cfg in cands:
+        x = torch.full_like(b, float("nan"))
+        k.march_shape(b, x, cfg["cpt"], cfg["pf"])
+        assert _rel(x.cpu().numpy(), ref.cpu().numpy()) < 1e-5, cfg
+
+
+def test_initial_rhs_and_f32_update(cuda):
+    """rhs of u = 0 from the boundary-only kernel equals the general
+    update/residual kernel's; the FP32->FP64 update is exact."""
+    s = _setup(129, 257, seed=2, c=0.9)
+    k = _kernels(s, cuda)
+    z = torch.zeros((129, 257), dtype=torch.float64, device=cuda)
+    r1 = torch.empty((129, 257), dtype=torch.float32, device=cuda)
+    r2 = torch.full_like(r1, float("nan"))
+    k.update_residual_mixed(z, None, None, r1)
+    k.initial_rhs(r2)
+    assert torch.equal(r1, r2)
+    from odil_gb300._capi import call, ptr, stream_handle
+    u = torch.randn(1000, dtype=torch.float64, device=cuda)
+    d = torch.randn(1000, dtype=torch.float32, device=cuda)
+    out = torch.empty_like(u)
+    call("odil_add_f32_to_f64", ptr(u), ptr(d), ptr(out), 1000, stream_handle())
+    assert torch.equal(out, u + d.double())
+
+
+def test_mixed_newton_from_zero(cuda):
+    """The from-zero sequence (boundary-only first rhs, plain final update)
+    gives the same field as the general sequence started at u = 0."""
+    from odil_gb300 import newton
+    from odil_gb300.domain import State
+    from odil_gb300.problem import Problem
+    from odil_gb300.workloads import WaveInstance
+    inst = WaveInstance(256, 256, profile="sine", seed=1, nmodes=16,
+                        device=cuda)
+    prob = Problem(inst.operator, inst.domain)
+    x1 = torch.zeros((256, 256), dtype=torch.float64, device=cuda)
+    rn = torch.zeros(1, dtype=torch.float64, device=cuda)
+    newton.solve(prob, State(fields={"u": x1}), "mixed", epochs=2, rnorm2=rn)
+    x2 = torch.randn((256, 256), dtype=torch.float64, device=cuda)
+    newton.solve(prob, State(fields={"u": x2}), "mixed", epochs=2,
+                 from_zero=True)
+    assert torch.equal(x1, x2)
+
+
 def test_mixed_newton_reaches_oracle(cuda):
     """Mixed precision (FP64 residual, FP32 solve) converges to the FP64
     discrete solution of the 1024^2 benchmark wave to <= 1e-5 (here 1e-9)."""
