@@ -85,6 +85,22 @@ int odil_wave_loss_grad_f64(const odil_wave_params* p, const double* u,
                             double* grad, double* loss, void* workspace,
                             int64_t workspace_bytes, void* stream);
 
+/* Allocation-free odil_wave_loss_grad_f32.  No counterpart in the
+ * reference: it serves callers that cannot allocate device memory (a host
+ * whose memory pool is sealed at start-up, a fixed-budget real-time loop, a
+ * plugin given no allocator).  The reduction scratch is a 256 KiB
+ * file-scope device array held by every GPU that loads the library, so:
+ *   - grids needing more than odil_wave_loss_grad_noalloc_max_blocks()
+ *     reduction blocks (tiles of the fused kernel, so the cell limit
+ *     depends on the shape: 8192 x 8192 fits, 16384 x 16384 does not) are
+ *     rejected with ODIL_ERR_WORKSPACE;
+ *   - all calls share that array: calls that overlap on the GPU race;
+ *   - the first call on each device looks up the array's address; make it
+ *     before any stream capture. */
+int64_t odil_wave_loss_grad_noalloc_max_blocks(void);
+int odil_wave_loss_grad_f32_noalloc(const odil_wave_params* p, const float* u,
+                                    float* grad, double* loss, void* stream);
+
 /* out = J v  (matrix-free; replaces the CSR product of util_op.py:877-896). */
 int odil_wave_jv_f32(const odil_wave_params* p, const float* v, float* out,
                      void* stream);

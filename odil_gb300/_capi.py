@@ -136,6 +136,8 @@ SIGNATURES = {
     "odil_wave_residual_f64": (_INT, [_P, _P, _P, _P]),
     "odil_wave_loss_grad_f32": (_INT, [_P, _P, _P, _P, _P, _I64, _P]),
     "odil_wave_loss_grad_f64": (_INT, [_P, _P, _P, _P, _P, _I64, _P]),
+    "odil_wave_loss_grad_noalloc_max_blocks": (_I64, []),
+    "odil_wave_loss_grad_f32_noalloc": (_INT, [_P, _P, _P, _P, _P]),
     "odil_wave_jv_f32": (_INT, [_P, _P, _P, _P]),
     "odil_wave_jv_f64": (_INT, [_P, _P, _P, _P]),
     "odil_wave_jtv_f32": (_INT, [_P, _P, _P, _P]),

@@ -482,3 +482,77 @@ ODIL_API int odil_wave_march_shape_f32(const odil_wave_params* p, const float* b
         default: return ODIL_ERR_SHAPE;
     }
 }
+
+// ---------------------------------------------------------------------------
+// Allocation-free variant of odil_wave_loss_grad_f32.
+//
+// Some callers cannot allocate device memory at all: a host framework whose
+// memory pool is sized and sealed at start-up, a real-time loop with a fixed
+// memory budget, a plugin whose process hands it no allocator.  For them the reduction scratch of the fused loss lives in
+// this file-scope device array instead of a caller workspace.  Every GPU that
+// loads the library holds these 256 KiB until the process exits.
+//
+// Limits and sharing rules:
+//   * at most kNoAllocMaxBlocks reduction blocks (grid of the fused kernel,
+//     odil_wave_loss_grad_noalloc_max_blocks()); larger grids are rejected
+//     with ODIL_ERR_WORKSPACE before anything is launched;
+//   * every call shares the one array, which keeps the previous call's
+//     partial sums: the counter that must start at zero is cleared on the
+//     stream before each launch, and calls that overlap on the GPU (other
+//     streams, other host threads) race on the array;
+//   * the first call on each device looks up the array's device address with
+//     cudaGetSymbolAddress and caches it; make that first call before any
+//     stream capture.
+constexpr int64_t kNoAllocBytes = 256 * 1024;
+constexpr int64_t kNoAllocMaxBlocks = (kNoAllocBytes - kReduceHeader) / (int64_t)sizeof(double);
+static __device__ __align__(256) unsigned char g_loss_scratch[kNoAllocBytes];
+
+namespace {
+constexpr int kMaxDevices = 64;
+void* g_scratch_ptr[kMaxDevices] = {nullptr};
+
+// Device address of g_loss_scratch on the current device (set-up on first use).
+int scratch_address(void** out) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices)
+        return ODIL_ERR_LAUNCH;
+    if (!g_scratch_ptr[dev]) {
+        void* ptr = nullptr;
+        if (cudaGetSymbolAddress(&ptr, g_loss_scratch) != cudaSuccess || !ptr) {
+            cudaGetLastError();
+            return ODIL_ERR_LAUNCH;
+        }
+        g_scratch_ptr[dev] = ptr;
+    }
+    *out = g_scratch_ptr[dev];
+    return ODIL_OK;
+}
+}  // namespace
+
+ODIL_API int64_t odil_wave_loss_grad_noalloc_max_blocks(void) { return kNoAllocMaxBlocks; }
+
+ODIL_API int odil_wave_loss_grad_f32_noalloc(const odil_wave_params* p, const float* u,
+                                             float* grad, double* loss, void* stream) {
+    WaveDev<float> g;
+    int st = make_dev<float>(p, &g, true);
+    if (st) return st;
+    if (!u || !grad || !loss) return ODIL_ERR_ARG;
+    const dim3 grid = lg_grid(g.nt, g.nx);
+    if (grid.y > 65535) return ODIL_ERR_SHAPE;
+    const int64_t nb = (int64_t)grid.x * grid.y;
+    if (nb > kNoAllocMaxBlocks) return ODIL_ERR_WORKSPACE;
+    void* ws = nullptr;
+    st = scratch_address(&ws);
+    if (st) return st;
+    cudaStream_t s = as_stream(stream);
+    if (cudaMemsetAsync(ws, 0, sizeof(unsigned), s) != cudaSuccess) return ODIL_ERR_LAUNCH;
+    const double n = (double)g.nt * (double)g.nx;
+    if (lg_ty(g.nt, g.nx) == 16) {
+        wave_loss_grad_kernel<float, 16><<<grid, LG_WARPS * 32, 0, s>>>(
+            g, u, grad, reduce_ws(ws), loss, (float)(2.0 / n), 1.0 / n);
+    } else {
+        wave_loss_grad_kernel<float, 32><<<grid, LG_WARPS * 32, 0, s>>>(
+            g, u, grad, reduce_ws(ws), loss, (float)(2.0 / n), 1.0 / n);
+    }
+    return launch_status();
+}
