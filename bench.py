@@ -48,7 +48,7 @@ def parse():
     ap.add_argument("--case", default=None,
                     choices=("march", "march64", "update_residual", "loss_grad",
                              "loss_grad64", "loss_grad_big", "lbfgs_iter",
-                             "adam_iter", "batch"),
+                             "adam_iter", "batch", "ns_newton"),
                     help="run one kernel of the workload --steps times (for "
                     "profiler captures) instead of the benchmark")
     return ap.parse_args()
@@ -231,9 +231,11 @@ def run_optimizers(problem, inst, dev, with_oracle):
 
 def run_batch(dev, with_oracle, steps=5):
     """512 wave instances, sides U{64..512}, c in [0.5, 2], 5-mode profiles:
-    mixed Newton for the whole batch as one CUDA-graph replay (FP64
-    update/residual + persistent FP32 forward substitution, 2 epochs), against
-    the plain FP64 method run instance by instance on the same GPU."""
+    mixed Newton for the whole batch as one CUDA-graph replay (right-hand
+    sides with FP64 only on boundary cells, persistent FP32 forward
+    substitution, 2 epochs, one FP64 write of the solution), against the plain
+    FP64 method run instance by instance on the same GPU.  The packed arrays
+    (about 1.3 GB) are larger than L2, so replays do not flush it."""
     import torch
     from odil_gb300.batch import WaveBatch
     from odil_gb300.workloads import wave_batch_instances
@@ -287,7 +289,8 @@ def run_batch(dev, with_oracle, steps=5):
     out = {"instances": len(insts), "cells": cells,
            "ms_per_batch": ms, "value": len(insts) / (ms / 1000.0),
            "unit": "solves/s", "march_cfg": cfg,
-           "launches_per_batch": 2 * MIXED_EPOCHS + 1 + MIXED_EPOCHS,
+           "launches_per_batch": 2 * MIXED_EPOCHS + 1,
+           "l2": "not flushed: packed arrays larger than L2",
            "plain_fp64_per_instance": {"ms": plain_ms,
                                        "value": len(insts) / (plain_ms / 1e3)},
            "speedup_vs_plain_fp64": plain_ms / ms}
@@ -379,6 +382,8 @@ def run_ours(args):
     k.update_residual_mixed(u, None, None, rhs)
     t_march = timed(lambda: k.march_tuned(rhs, d32), 20, 3)
     t_upd = timed(lambda: k.update_residual_mixed(u, d32, ub, rhs), 20, 3)
+    t_pair = timed(lambda: k.pair_residual(d32, None, rhs), 20, 3)
+    t_init = timed(lambda: k.initial_rhs(rhs), 20, 3)
     r64 = torch.empty_like(u)
     t_march64 = timed(lambda: k.march(r64, out=ub), 5, 2)
     u32 = u.float()
@@ -465,6 +470,7 @@ def run_ours(args):
                    "parallelism": "replicas" if world > 1 else "single"},
         "gpu_launches": (2 * MIXED_EPOCHS + 1) * args.steps,
         "march_cfg": getattr(k, "_march_cfg", None),
+        "march_tune": getattr(k, "march_tune_table", None),
         "clocks": clk,
         "e2e": {"value": 1000.0 / e2e_ms, "unit": "solves/s",
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
@@ -483,6 +489,8 @@ def run_ours(args):
             "march_f32_ms": march_ms,
             "update_residual_mixed_ms": upd_ms,
             "update_residual_mixed_GBs": upd_bytes / (upd_ms * 1e6),
+            "pair_residual_ms": statistics.mean(t_pair),
+            "initial_rhs_ms": statistics.mean(t_init),
             "march_f64_ms": statistics.mean(t_march64),
             "loss_grad_f32_ms": statistics.mean(t_lg),
             "loss_grad_f32_GBs": lg_bytes / (statistics.mean(t_lg) * 1e6),
@@ -507,6 +515,41 @@ def run_ours(args):
     if world > 1:
         dist.barrier()
         dist.destroy_process_group()
+
+
+def run_ns_newton(args):
+    """Forward lid-driven cavity, Re = 400, on an n x n grid (n = 512 unless
+    ODIL_NS_N is set) from rest: Newton with the FP32 block-tridiagonal
+    direct solve and FP64 iterative refinement, until the residual rms is
+    below 1e-10 (at most --steps epochs).  Prints per-epoch times and the
+    residual history as one JSON line."""
+    import torch
+    from odil_gb300.ns import NsCavityOperator, NsKernels, NsDirectNewton
+    dev = torch.device("cuda", 0)
+    n = int(os.environ.get("ODIL_NS_N", "512"))
+    k = NsKernels(n, NsCavityOperator(400.0), device=dev)
+    t = [torch.zeros((n, n), dtype=torch.float64, device=dev) for _ in range(3)]
+    solver = NsDirectNewton(k)
+    times = []
+    rms = None
+    for ep in range(args.steps):
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        rms = solver.step(*t)
+        torch.cuda.synchronize(dev)
+        times.append(time.perf_counter() - t0)
+        if rms <= 1e-10:
+            break
+    f = k.residual(*t)
+    final = float(torch.sqrt((f**2).mean()))
+    print(json.dumps({"case": "ns_newton", "n": n, "Re": 400.0,
+                      "epochs": len(times), "s_per_epoch": times,
+                      "total_s": sum(times), "rms_history":
+                      [st["rms"] for st in solver.stats],
+                      "refine_iters": [st["refine"] for st in solver.stats],
+                      "factor_ms": [st["factor_ms"] for st in solver.stats],
+                      "final_rms": final,
+                      "workspace_GB": solver.ws.numel() / 1e9}))
 
 
 def run_case(args):
@@ -544,7 +587,7 @@ def run_case(args):
         from odil_gb300.batch import WaveBatch
         from odil_gb300.workloads import wave_batch_instances
         wb = WaveBatch(wave_batch_instances(count=512), device=dev)
-        wb.update_residual(wb.u, None, None, wb.rhs)
+        wb.initial_rhs(wb.rhs)
     fn = {
         "loss_grad_big": lambda: kb.loss_grad(ubig, grad=gbig),
         "batch": lambda: wb.solve_mixed(),
@@ -569,7 +612,9 @@ def run_case(args):
 
 def main():
     args = parse()
-    if args.case:
+    if args.case == "ns_newton":
+        run_ns_newton(args)
+    elif args.case:
         run_case(args)
     elif args.impl == "reference":
         run_reference(args)

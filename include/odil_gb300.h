@@ -91,9 +91,10 @@ int odil_wave_loss_grad_f64(const odil_wave_params* p, const double* u,
  * plugin given no allocator).  The reduction scratch is a 256 KiB
  * file-scope device array held by every GPU that loads the library, so:
  *   - grids needing more than odil_wave_loss_grad_noalloc_max_blocks()
- *     reduction blocks (tiles of the fused kernel, so the cell limit
- *     depends on the shape: 8192 x 8192 fits, 16384 x 16384 does not) are
- *     rejected with ODIL_ERR_WORKSPACE;
+ *     reduction blocks are rejected with ODIL_ERR_WORKSPACE.  A block is a
+ *     tile of the fused kernel (64 x 240 cells for large grids whose rows
+ *     are 16-byte aligned, 32 x 120 otherwise), so about 5e8 or 1.2e8
+ *     cells fit: 16384 x 16384 (aligned) does, 65536 x 8192 does not;
  *   - all calls share that array: calls that overlap on the GPU race;
  *   - the first call on each device looks up the array's address; make it
  *     before any stream capture. */
@@ -139,8 +140,19 @@ int odil_wave_update_residual_mixed(const odil_wave_params* p, const double* u,
  * columns 0 and nx-1); all other cells are 0. */
 int odil_wave_initial_rhs_mixed(const odil_wave_params* p, float* rhs,
                                 void* stream);
+/* rhs = (float)(-F(hi + lo)) for a field held as the unevaluated sum of two
+ * FP32 arrays (lo may be NULL): the right-hand side of a mixed Newton epoch
+ * whose iterate is kept as FP32 corrections, without an FP64 state.
+ * Interior cells are evaluated with exact FP32 products and compensated sums
+ * (about 2^-48 of the largest stencil term); boundary cells (rows 0, 1 and
+ * columns 0, nx-1) in FP64.  p's boundary arrays are FP64.  Replaces the
+ * residual evaluation of util_op.py:859-937 inside the Newton loop. */
+int odil_wave_pair_residual_mixed(const odil_wave_params* p, const float* hi,
+                                  const float* lo, float* rhs, void* stream);
 /* odil_wave_march_f32 with an explicit launch shape: cpt columns per thread
- * (1, 2, 4, 8; nx <= 1024 cpt) and pf prefetched rows (8, 16). */
+ * (1, 2, 4, 8) and pf right-hand-side rows prefetched into registers (8,
+ * 16); the block (nx / cpt threads rounded up to 32) may hold at most 1024,
+ * 512 or 256 threads for cpt pf <= 16, <= 32 or more (ODIL_ERR_SHAPE). */
 int odil_wave_march_shape_f32(const odil_wave_params* p, const float* b,
                               float* x, int32_t cpt, int32_t pf, void* stream);
 
@@ -182,6 +194,13 @@ int odil_wave_batch_update_residual_mixed(const odil_wave_batch* b,
                                           const double* u, const float* d,
                                           double* u_out, float* rhs,
                                           void* stream);
+/* Batched odil_wave_initial_rhs_mixed / odil_wave_pair_residual_mixed on
+ * the packed arrays (one block per row task, FP64 only on boundary cells). */
+int odil_wave_batch_initial_rhs_mixed(const odil_wave_batch* b, float* rhs,
+                                      void* stream);
+int odil_wave_batch_pair_residual_mixed(const odil_wave_batch* b,
+                                        const float* hi, const float* lo,
+                                        float* rhs, void* stream);
 /* FP32 forward substitution of every instance in one persistent launch:
  * blocks_per_sm x #SM blocks of `threads` threads take instances from an
  * atomic work queue in `order`; threads * cpt >= max_nx; (cpt, pf) in
@@ -300,6 +319,26 @@ int odil_ns_jacobian_f64(const odil_ns_params* q, const double* u,
                          const double* v, const double* p, double* coef,
                          void* stream);
 
+/* Direct solve of the cavity Newton system (3 equations, forward problem:
+ * no imposed points, no penalty) with the continuity row of cell `pin`
+ * (= i n + j) replaced by p[pin] = value, which makes the square Jacobian
+ * nonsingular.  Replaces the SuperLU solve of linsolver.py:28-45 for this
+ * family.  coef: the [3][15][n][n] FP64 output of odil_ns_jacobian_f64.
+ * The system is block tridiagonal over the first grid axis (blocks of 3n
+ * unknowns); factor computes its FP32 block LU (cuSOLVER dense LU per
+ * block) into the workspace, solve applies it to an FP32 right-hand side
+ * (field-major [3][n][n]) for FP64 iterative refinement by the caller.
+ * Workspace: about 8 (3n)^2 n bytes (9.7 GB at n = 512).  check returns the
+ * number of blocks with a singular pivot (synchronises the stream). */
+int64_t odil_ns_direct_workspace_bytes(int64_t n);
+int odil_ns_direct_factor(int64_t n, const double* coef, int64_t pin,
+                          void* workspace, int64_t workspace_bytes,
+                          void* stream);
+int odil_ns_direct_check(int64_t n, const void* workspace, void* stream);
+int odil_ns_direct_solve(int64_t n, const double* coef, int64_t pin,
+                         void* workspace, int64_t workspace_bytes,
+                         const float* b, float* x, void* stream);
+
 /* ------------------------------------------------------------------------
  * Operators in stencil form (the reference's SparseOperator,
  * multigrid.py:877-1214): shifts s with one coefficient field C_s each on the
@@ -399,6 +438,11 @@ int odil_axpby_f64(double* z, const double* x, const double* y, int64_t n,
  * correction of a mixed-precision Newton solve. */
 int odil_add_f32_to_f64(const double* u, const float* d, double* out,
                         int64_t n, void* stream);
+
+/* out = (double)hi + (double)lo (n elements; lo may be NULL): the FP64
+ * iterate of a mixed Newton solve kept as FP32 corrections. */
+int odil_pair_to_f64(const float* hi, const float* lo, double* out, int64_t n,
+                     void* stream);
 
 /* Multi-dot: out[i*r + j] = sum_e M[i*ld + e] * q[j][e] for i < k, j < r
  * (r <= 4), in one pass over M.  FP64 accumulation, deterministic order.

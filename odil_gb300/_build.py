@@ -79,7 +79,7 @@ def build(force=False, verbose=False, extra_flags=()):
     libdir_cuda = os.path.join(cuda_home(), "lib64")
     tmp = lib + ".tmp"
     cmd = [nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-L" + libdir_cuda,
-           "-Xlinker", "-rpath=" + libdir_cuda, "-lcusparse", "-lcublas"]
+           "-Xlinker", "-rpath=" + libdir_cuda, "-lcusparse", "-lcublas", "-lcusolver"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s\n%s" % (r.stdout, r.stderr))

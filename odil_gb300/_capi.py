@@ -148,6 +148,14 @@ SIGNATURES = {
     "odil_wave_march_shape_f32": (_INT, [_P, _P, _P, ctypes.c_int32,
                                          ctypes.c_int32, _P]),
     "odil_add_f32_to_f64": (_INT, [_P, _P, _P, _I64, _P]),
+    "odil_pair_to_f64": (_INT, [_P, _P, _P, _I64, _P]),
+    "odil_ns_direct_workspace_bytes": (_I64, [_I64]),
+    "odil_ns_direct_factor": (_INT, [_I64, _P, _I64, _P, _I64, _P]),
+    "odil_ns_direct_check": (_INT, [_I64, _P, _P]),
+    "odil_ns_direct_solve": (_INT, [_I64, _P, _I64, _P, _I64, _P, _P, _P]),
+    "odil_wave_pair_residual_mixed": (_INT, [_P, _P, _P, _P, _P]),
+    "odil_wave_batch_initial_rhs_mixed": (_INT, [_P, _P, _P]),
+    "odil_wave_batch_pair_residual_mixed": (_INT, [_P, _P, _P, _P, _P]),
     "odil_wave_update_residual_workspace_bytes": (_I64, [_P]),
     "odil_wave_update_residual_mixed": (_INT, [_P, _P, _P, _P, _P, _P, _P, _I64,
                                                _P]),

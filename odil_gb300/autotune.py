@@ -60,7 +60,7 @@ def candidates_batch_march(max_nx, smem_limit=200 * 1024):
         if threads > 1024:
             continue
         for pf in (8, 16):
-            smem = (2 + pf) * max_nx * 4
+            smem = pf * max_nx * 4 + 512
             if smem > smem_limit:
                 continue
             for bps in (1, 2, 4, 8):
@@ -107,14 +107,20 @@ def tune_batch_march(batch, cache=True):
     return best[1]
 
 
-def candidates_march(nx, smem_limit=200 * 1024):
+def march_max_threads(cpt, pf):
+    """Block limit of the FP32 march (register ring of cpt * pf values)."""
+    b = cpt * pf * 4
+    return 1024 if b <= 64 else (512 if b <= 128 else 256)
+
+
+def candidates_march(nx):
     out = []
     for cpt in (1, 2, 4, 8):
         threads = ((nx + cpt - 1) // cpt + 31) // 32 * 32
-        if threads > 1024 or (cpt > 1 and (nx + cpt - 1) // cpt < 32):
+        if cpt > 1 and (nx + cpt - 1) // cpt < 32:
             continue
         for pf in (8, 16):
-            if (2 + pf) * nx * 4 <= smem_limit:
+            if threads <= march_max_threads(cpt, pf):
                 out.append({"cpt": cpt, "pf": pf})
     return out
 
@@ -126,6 +132,7 @@ def tune_march(kernels, cache=True):
                                         _pow2_bucket(kernels.nt))
     data = _load() if cache else {}
     if key in data:
+        kernels.march_tune_table = data[key].get("tried")
         return data[key]["cfg"]
     b = torch.zeros(kernels.shape, dtype=torch.float32, device=kernels.device)
     x = torch.empty_like(b)
@@ -137,6 +144,7 @@ def tune_march(kernels, cache=True):
         results.append((t, cfg))
         if best is None or t < best[0]:
             best = (t, cfg)
+    kernels.march_tune_table = [[t, c] for t, c in results]
     if cache:
         data[key] = {"cfg": best[1], "ms": best[0],
                      "tried": [[t, c] for t, c in results]}

@@ -3,9 +3,10 @@
 The reference solves such families as separate processes farmed out by MPI
 (vary_wave.py:7-43).  Here all instances share packed device arrays and one
 mixed-precision Newton solve of the whole batch is a fixed sequence of
-launches -- per epoch one FP64 update/residual over every cell and one
-persistent FP32 forward-substitution launch that pulls instances from a work
-queue -- captured once into a CUDA graph and replayed.
+launches -- per epoch one right-hand-side pass over every cell (FP64 only on
+boundary cells) and one persistent FP32 forward-substitution launch that
+pulls instances from a work queue, then one FP64 write of the solution --
+captured once into a CUDA graph and replayed.
 """
 import ctypes
 
@@ -73,6 +74,8 @@ class WaveBatch:
         self.ub = torch.zeros(self.total, **kw64)
         self.rhs = torch.zeros(self.total, **kw32)
         self.d = torch.zeros(self.total, **kw32)
+        self.hi = torch.zeros(self.total, **kw32)
+        self.lo = torch.zeros(self.total, **kw32)
         self.ws = torch.zeros(256, dtype=torch.uint8, device=dev)
         self.march_cfg = None
         self.graph = None
@@ -83,6 +86,14 @@ class WaveBatch:
              ptr(u), ptr(d), ptr(u_out if d is not None else None), ptr(rhs),
              stream_handle())
 
+    def initial_rhs(self, rhs):
+        call("odil_wave_batch_initial_rhs_mixed", ctypes.byref(self.b), ptr(rhs),
+             stream_handle())
+
+    def pair_residual(self, hi, lo, rhs):
+        call("odil_wave_batch_pair_residual_mixed", ctypes.byref(self.b), ptr(hi),
+             ptr(lo), ptr(rhs), stream_handle())
+
     def march(self, rhs, x, cfg=None):
         cfg = cfg or self.march_cfg or autotune.default_batch_march(self.max_nx)
         call("odil_wave_batch_march_f32", ctypes.byref(self.b), ptr(rhs), ptr(x),
@@ -92,21 +103,33 @@ class WaveBatch:
     def tune(self, cache=True):
         """Chooses the persistent march's launch shape by timing candidates
         on this batch (cached per device and batch size class)."""
-        self.update_residual(self.u, None, None, self.rhs)
+        self.initial_rhs(self.rhs)
         self.march_cfg = autotune.tune_batch_march(self, cache=cache)
         return self.march_cfg
 
     def solve_mixed(self, epochs=2):
-        """u <- mixed-precision Newton solution from u = 0 (all instances)."""
-        self.u.zero_()
-        ua, ub = self.u, self.ub
-        self.update_residual(ua, None, None, self.rhs)
-        for _ in range(epochs):
-            self.march(self.rhs, self.d)
-            self.update_residual(ua, self.d, ub, self.rhs)
-            ua, ub = ub, ua
-        if ua is not self.u:
-            self.u.copy_(ua)
+        """u <- mixed-precision Newton solution from u = 0 (all instances).
+
+        The iterate is kept as FP32 corrections hi + lo: the first
+        right-hand side needs FP64 work on boundary cells only, later ones
+        come from the float-pair residual, and one pass writes u in FP64."""
+        if epochs < 1:
+            self.u.zero_()
+            return self.u
+        self.initial_rhs(self.rhs)
+        self.march(self.rhs, self.hi)
+        have_lo = False
+        for _ in range(1, epochs):
+            self.pair_residual(self.hi, self.lo if have_lo else None, self.rhs)
+            if have_lo:
+                self.march(self.rhs, self.d)
+                call("odil_axpby_f32", ptr(self.lo), ptr(self.lo), ptr(self.d),
+                     self.total, 1.0, 1.0, stream_handle())
+            else:
+                self.march(self.rhs, self.lo)
+                have_lo = True
+        call("odil_pair_to_f64", ptr(self.hi), ptr(self.lo if have_lo else None),
+             ptr(self.u), self.total, stream_handle())
         return self.u
 
     def capture(self, epochs=2):

@@ -110,6 +110,57 @@ __global__ void __launch_bounds__(256) batch_update_residual_kernel(
     }
 }
 
+// Instance holding packed row r of the row sequence (row offsets offset_t
+// ascending), by binary search; one search per row task, not per cell.
+__device__ __forceinline__ int find_inst_row(const odil_wave_instance* __restrict__ inst, int n,
+                                             int64_t r) {
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldg(&inst[mid].offset_t) <= r) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+// Row tasks over all instances: block-strided over the rows of the batch,
+// threads over the columns of the row.  KIND 0: rhs = float(-F(0)) (FP64
+// only on boundary cells); KIND 1: rhs = float(-F(hi + lo)) in the float-pair
+// form (wave_dev.cuh), FP64 only on boundary cells.
+template <int KIND>
+__global__ void __launch_bounds__(256) batch_rows_kernel(odil_wave_batch b,
+                                                         const float* __restrict__ hi,
+                                                         const float* __restrict__ lo,
+                                                         float* __restrict__ rhs) {
+    const odil_wave_instance last = b.inst[b.ninst - 1];
+    const int64_t rows = last.offset_t + last.nt;
+    const double* iu = (const double*)b.init_u;
+    const double* iut = (const double*)b.init_ut;
+    const double* lu = (const double*)b.left_u;
+    const double* ru = (const double*)b.right_u;
+    for (int64_t r = blockIdx.x; r < rows; r += gridDim.x) {
+        const int q = find_inst_row(b.inst, b.ninst, r);
+        const odil_wave_instance desc = b.inst[q];
+        const WaveDev<double> g = dev_of<double>(desc, iu, iut, lu, ru);
+        const int i = (int)(r - desc.offset_t);
+        float* rrow = rhs + desc.offset + (int64_t)i * g.nx;
+        if (KIND == 0) {
+            const bool brow = i <= 1;
+            for (int j = threadIdx.x; j < g.nx; j += blockDim.x) {
+                float v = 0.f;
+                if (brow || j == 0 || j == g.nx - 1)
+                    v = (float)(-wave_f(g, i, j, 0.0, 0.0, 0.0, 0.0, 0.0));
+                rrow[j] = v;
+            }
+        } else {
+            const PairCoef k = pair_coef_dev((double)g.A, (double)g.B);
+            const float* h = hi + desc.offset;
+            const float* l = lo ? lo + desc.offset : nullptr;
+            for (int j = threadIdx.x; j < g.nx; j += blockDim.x)
+                rrow[j] = pair_cell_rhs(g, k, h, l, i, j);
+        }
+    }
+}
+
 template <int CPT, int PF>
 __global__ void __launch_bounds__(1024) batch_march_kernel(odil_wave_batch b,
                                                            const float* __restrict__ rhs,
@@ -156,7 +207,7 @@ template <int CPT, int PF>
 int launch_batch_march(const odil_wave_batch* b, const float* rhs, float* x, unsigned* counter,
                        int threads, int blocks, cudaStream_t st) {
     if ((int64_t)threads * CPT < b->max_nx) return ODIL_ERR_SHAPE;
-    const size_t smem = (2 + PF) * (size_t)b->max_nx * sizeof(float);
+    const size_t smem = march_ring_smem_bytes<float>(b->max_nx, PF);
     if (smem > 200 * 1024) return ODIL_ERR_SHAPE;
     auto kern = batch_march_kernel<CPT, PF>;
     ensure_dynamic_smem(reinterpret_cast<const void*>(kern), smem);
@@ -193,6 +244,26 @@ ODIL_API int odil_wave_batch_update_residual_mixed(const odil_wave_batch* b, con
     if (blocks > cap) blocks = cap;
     batch_update_residual_kernel<<<(int)blocks, 256, 0, as_stream(stream)>>>(*b, u, d, u_out,
                                                                              rhs);
+    return launch_status();
+}
+
+ODIL_API int odil_wave_batch_initial_rhs_mixed(const odil_wave_batch* b, float* rhs,
+                                               void* stream) {
+    int st = check_batch(b);
+    if (st) return st;
+    if (!rhs) return ODIL_ERR_ARG;
+    if (!b->init_u || !b->init_ut || !b->left_u || !b->right_u) return ODIL_ERR_ARG;
+    batch_rows_kernel<0><<<sms() * 8, 256, 0, as_stream(stream)>>>(*b, nullptr, nullptr, rhs);
+    return launch_status();
+}
+
+ODIL_API int odil_wave_batch_pair_residual_mixed(const odil_wave_batch* b, const float* hi,
+                                                 const float* lo, float* rhs, void* stream) {
+    int st = check_batch(b);
+    if (st) return st;
+    if (!hi || !rhs || rhs == hi || rhs == lo) return ODIL_ERR_ARG;
+    if (!b->init_u || !b->init_ut || !b->left_u || !b->right_u) return ODIL_ERR_ARG;
+    batch_rows_kernel<1><<<sms() * 8, 256, 0, as_stream(stream)>>>(*b, hi, lo, rhs);
     return launch_status();
 }
 

@@ -43,6 +43,21 @@ inline void ensure_dynamic_smem(const void* kern, size_t bytes) {
     }
 }
 
+// Exact FP32 -> FP64 conversion with integer instructions (normal numbers,
+// zeros, infinities, NaN; subnormal inputs take the hardware conversion).
+__device__ __forceinline__ double f2d_exact(float x) {
+    const unsigned b = __float_as_uint(x);
+    const unsigned e = (b >> 23) & 0xffu;
+    if (e == 0u && (b & 0x7fffffu) != 0u) return (double)x;
+    const unsigned long long sign = (unsigned long long)(b >> 31) << 63;
+    const unsigned long long mant = (unsigned long long)(b & 0x7fffffu) << 29;
+    unsigned long long de;
+    if (e == 0u) de = 0ull;
+    else if (e == 0xffu) de = 0x7ffull;
+    else de = (unsigned long long)(e + (1023u - 127u));
+    return __longlong_as_double((long long)(sign | (de << 52) | mant));
+}
+
 // Periodic wrap of an index that is at most one period outside [0, n).
 __device__ __forceinline__ int wrap1(int i, int n) {
     return i < 0 ? i + n : (i >= n ? i - n : i);
@@ -102,6 +117,32 @@ inline ReduceWs reduce_ws(void* ws) {
     return r;
 }
 
+// Sum of partials[0 .. count) by the whole block in a fixed order (bitwise
+// reproducible for a fixed blockDim): each thread keeps 8 loads in flight, so
+// a single warp finishing thousands of partial sums is not bound by one L2
+// round trip per partial.
+__device__ __forceinline__ double sum_partials(const double* partials, int64_t count) {
+    constexpr int U = 8;
+    double acc[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) acc[u] = 0.0;
+    const int64_t step = (int64_t)blockDim.x * U;
+    for (int64_t k0 = threadIdx.x; k0 < count; k0 += step) {
+        double v[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int64_t k = k0 + (int64_t)u * blockDim.x;
+            v[u] = k < count ? __ldcg(partials + k) : 0.0;
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) acc[u] += v[u];
+    }
+    double s = 0.0;
+#pragma unroll
+    for (int u = 0; u < U; ++u) s += acc[u];
+    return block_sum(s);
+}
+
 // Called by every thread of every block with the thread's partial sum.  Block
 // `bid` of `nblocks` stores its sum; the last block to arrive adds the partial
 // sums in index order (deterministic), writes out[0] = sum * scale and resets
@@ -119,11 +160,39 @@ __device__ __forceinline__ void reduce_finish(double v, int64_t bid, int64_t nbl
     __syncthreads();
     if (is_last) {
         __threadfence();
-        double s = 0.0;
-        for (int64_t k = threadIdx.x; k < nblocks; k += blockDim.x) {
-            s += __ldcg(ws.partials + k);
+        double s = sum_partials(ws.partials, nblocks);
+        if (threadIdx.x == 0) {
+            out[0] = s * scale;
+            *ws.counter = 0u;
         }
-        s = block_sum(s);
+    }
+}
+
+// Two-kernel variant.  The first kernel's blocks store their sums at
+// partials[0 .. first) with reduce_store (no counter); the second kernel's
+// `nblocks` blocks call reduce_finish_after with slot = first + bid, and its
+// last block adds all first + nblocks partial sums in index order.  Kernel
+// order on the stream makes the first kernel's stores visible.
+__device__ __forceinline__ void reduce_store(double v, int64_t slot, ReduceWs ws) {
+    v = block_sum(v);
+    if (threadIdx.x == 0) ws.partials[slot] = v;
+}
+
+__device__ __forceinline__ void reduce_finish_after(double v, int64_t first, int64_t bid,
+                                                    int64_t nblocks, ReduceWs ws, double scale,
+                                                    double* out) {
+    __shared__ bool is_last;
+    v = block_sum(v);
+    if (threadIdx.x == 0) {
+        ws.partials[first + bid] = v;
+        __threadfence();
+        unsigned prev = atomicAdd(ws.counter, 1u);
+        is_last = (prev == (unsigned)(nblocks - 1));
+    }
+    __syncthreads();
+    if (is_last) {
+        __threadfence();
+        double s = sum_partials(ws.partials, first + nblocks);
         if (threadIdx.x == 0) {
             out[0] = s * scale;
             *ws.counter = 0u;

@@ -335,13 +335,27 @@ int lincomb_impl(T* out, const T* x, const T* M, int64_t ld, int k, const double
     return launch_status();
 }
 
+// out = hi + lo in FP64 (lo may be null).  The FP32 -> FP64 conversions use
+// integer instructions; the one FP64 add per element is exact whenever the
+// exponents of hi and lo differ by at most 29.
+__global__ void __launch_bounds__(VT) pair_to_f64_kernel(const float* __restrict__ hi,
+                                                         const float* __restrict__ lo,
+                                                         double* __restrict__ out, int64_t n) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        double v = f2d_exact(__ldcs(hi + i));
+        if (lo) v += f2d_exact(__ldcs(lo + i));
+        out[i] = v;
+    }
+}
+
 // out = u + (double)d: the FP64 update of a mixed-precision step.
 __global__ void __launch_bounds__(VT) add_f32_to_f64_kernel(const double* __restrict__ u,
                                                             const float* __restrict__ d,
                                                             double* __restrict__ out, int64_t n) {
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
-        out[i] = __ldcs(u + i) + (double)__ldcs(d + i);
+        out[i] = __ldcs(u + i) + f2d_exact(__ldcs(d + i));
 }
 
 }  // namespace
@@ -396,5 +410,14 @@ ODIL_API int odil_add_f32_to_f64(const double* u, const float* d, double* out, i
     if (n == 0) return ODIL_OK;
     if (!u || !d || !out) return ODIL_ERR_ARG;
     add_f32_to_f64_kernel<<<stream_blocks(n, 1), VT, 0, as_stream(stream)>>>(u, d, out, n);
+    return launch_status();
+}
+
+ODIL_API int odil_pair_to_f64(const float* hi, const float* lo, double* out, int64_t n,
+                              void* stream) {
+    if (n < 0) return ODIL_ERR_SHAPE;
+    if (n == 0) return ODIL_OK;
+    if (!hi || !out) return ODIL_ERR_ARG;
+    pair_to_f64_kernel<<<stream_blocks(n, 1), VT, 0, as_stream(stream)>>>(hi, lo, out, n);
     return launch_status();
 }

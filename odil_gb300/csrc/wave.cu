@@ -191,6 +191,414 @@ inline dim3 lg_grid(int nt, int nx) {
     return dim3((nx + cols - 1) / cols, (nt + ty - 1) / ty);
 }
 
+// ---------------------------------------------------------------------------
+// Vectorised fused loss + adjoint (nx a multiple of V = 16 / sizeof(T) and
+// 16-byte aligned u and grad).  Same march as above, but lane l of a warp
+// holds the V contiguous columns [c0 - V + V l, c0 + V l): one 16-byte load
+// and one 16-byte store per lane and row, x-neighbours inside the vector from
+// registers and only the two vector ends by shuffles.  Lanes 1..30 produce the
+// 30 V output columns [c0, c0 + 30 V); lanes 0 and 31 are the halo.  Tiles
+// that touch no boundary class evaluate the interior residual (the operation
+// order of wave_f) and the interior gather with constant coefficients and
+// reuse the first time difference of the previous row; the others go through
+// wave_f / wave_gather cell by cell.
+constexpr int LV_WARPS = 2;
+
+template <typename T>
+struct Vec16;
+template <>
+struct Vec16<float> {
+    using type = float4;
+    static constexpr int n = 4;
+};
+template <>
+struct Vec16<double> {
+    using type = double2;
+    static constexpr int n = 2;
+};
+
+template <typename T>
+__device__ __forceinline__ void ld16(T (&v)[Vec16<T>::n], const T* p) {
+    const typename Vec16<T>::type x = __ldg(reinterpret_cast<const typename Vec16<T>::type*>(p));
+    if constexpr (Vec16<T>::n == 4) {
+        v[0] = x.x; v[1] = x.y; v[2] = x.z; v[3] = x.w;
+    } else {
+        v[0] = x.x; v[1] = x.y;
+    }
+}
+
+template <typename T>
+__device__ __forceinline__ void st16(T* p, const T (&v)[Vec16<T>::n]) {
+    typename Vec16<T>::type x;
+    if constexpr (Vec16<T>::n == 4) {
+        x.x = v[0]; x.y = v[1]; x.z = v[2]; x.w = v[3];
+    } else {
+        x.x = v[0]; x.y = v[1];
+    }
+    __stcs(reinterpret_cast<typename Vec16<T>::type*>(p), x);
+}
+
+// Interior residual from the first time differences of rows (i, i-1) and
+// (i-1, i-2): the operation order of wave_f's general branch.
+template <typename T>
+__device__ __forceinline__ T wave_f_int(const WaveDev<T>& g, T u_t_tm, T u_t_tmm, T utm, T uxm,
+                                        T uxp) {
+    const T u_tt = (u_t_tm - u_t_tmm) * g.inv_dt;
+    const T u_xx = (uxm - T(2) * utm + uxp) * g.inv_dx2;
+    return u_tt - g.c2 * u_xx;
+}
+
+// Rows of u in flight per warp: a shared-memory ring filled by cp.async
+// (16 bytes per lane and row), so the prefetch depth costs no registers.
+constexpr int LV_RING = 8;
+
+template <typename T>
+__device__ __forceinline__ void vload_smem(T (&v)[Vec16<T>::n], const T* p) {
+    const typename Vec16<T>::type x = *reinterpret_cast<const typename Vec16<T>::type*>(p);
+    if constexpr (Vec16<T>::n == 4) {
+        v[0] = x.x; v[1] = x.y; v[2] = x.z; v[3] = x.w;
+    } else {
+        v[0] = x.x; v[1] = x.y;
+    }
+}
+
+// One warp's tile: rows [a0, a0 + TY) of the gradient at the lane's columns.
+// Row q of the march (q = 0 .. TY + 3) is u row a0 - 2 + q; rows q >= 2
+// produce residuals, rows q >= 4 the gradient of row q - 4 + a0.
+template <typename T, int TY, bool FAST>
+__device__ __forceinline__ T lg_vec_tile(const WaveDev<T>& g, const T* __restrict__ u,
+                                         T* __restrict__ grad, int a0, int c0, int lane,
+                                         T gscale, T* ring, T* bcs) {
+    constexpr int V = Vec16<T>::n;
+    constexpr int R = LV_RING;
+    constexpr int NQ = TY + 4;
+    static_assert((R & (R - 1)) == 0, "ring length is a power of two");
+    const int nt = g.nt, nx = g.nx;
+    const int cl = c0 - V + V * lane;           // first column of this lane
+    const bool col_ok = cl >= 0 && cl < nx;     // nx % V == 0: all V or none
+    const bool out_lane = lane >= 1 && lane <= 30 && col_ok;
+    const T A = g.A, B = g.B;
+    const T ctm_int = T(-2) * A + B * T(2);
+    T* my = ring + lane * V;                    // this lane's slot column
+    const T* src = u + (int64_t)(a0 - 2) * nx + cl;
+    auto issue = [&](int q) {
+        if (q < NQ) {
+            const int r = a0 - 2 + q;
+            T* to = my + (q & (R - 1)) * (32 * V);
+            if (FAST || (r >= 0 && r < nt && col_ok)) {
+                cp_async_n(to, src + (int64_t)q * nx, 16);
+            } else {
+#pragma unroll
+                for (int e = 0; e < V; ++e) to[e] = T(0);
+            }
+        }
+        cp_async_commit();
+    };
+    T u1[V], u2[V], f1[V], f2[V], ut1[V];
+#pragma unroll
+    for (int e = 0; e < V; ++e) u1[e] = u2[e] = f1[e] = f2[e] = ut1[e] = T(0);
+    T lsum = T(0);
+    // Boundary tiles: the boundary data of the tile's rows and columns are
+    // staged once (left/right values per row in shared memory, initial values
+    // per column in registers), so no dependent global load sits in the march.
+    T iu[V], iut[V];
+#pragma unroll
+    for (int e = 0; e < V; ++e) iu[e] = iut[e] = T(0);
+    if (!FAST) {
+        for (int q = lane; q < NQ; q += 32) {
+            const int r = a0 - 2 + q;
+            const bool ok = r >= 1 && r <= nt;
+            bcs[q] = ok ? opt_ld(g.left_u, r - 1) : T(0);
+            bcs[NQ + q] = ok ? opt_ld(g.right_u, r - 1) : T(0);
+        }
+        if (col_ok && a0 <= 3) {
+#pragma unroll
+            for (int e = 0; e < V; ++e) {
+                iu[e] = opt_ld(g.init_u, cl + e);
+                iut[e] = opt_ld(g.init_ut, cl + e);
+            }
+        }
+        __syncwarp();
+    }
+    // Residuals of row q into f0 (q >= 2); advances u1, u2, ut1.
+    auto residual_row = [&](int q, const T (&u0)[V], T (&f0)[V]) {
+        const int r = a0 - 2 + q;
+        const T lm = __shfl_up_sync(0xffffffffu, u1[V - 1], 1);
+        const T rp = __shfl_down_sync(0xffffffffu, u1[0], 1);
+        if (FAST) {
+            T ut0[V];
+#pragma unroll
+            for (int e = 0; e < V; ++e) ut0[e] = (u0[e] - u1[e]) * g.inv_dt;
+#pragma unroll
+            for (int e = 0; e < V; ++e) {
+                const T um = e == 0 ? lm : u1[e - 1];
+                const T up = e == V - 1 ? rp : u1[e + 1];
+                f0[e] = wave_f_int(g, ut0[e], ut1[e], u1[e], um, up);
+                ut1[e] = ut0[e];
+            }
+        } else {
+#pragma unroll
+            for (int e = 0; e < V; ++e) {
+                const T um = e == 0 ? lm : u1[e - 1];
+                const T up = e == V - 1 ? rp : u1[e + 1];
+                const T lb = bcs[q], rb = bcs[NQ + q];
+                const T a = iu[e], b = iut[e];
+                f0[e] = (col_ok && r >= 0 && r < nt)
+                            ? wave_f_with(
+                                  g, r, cl + e, u0[e], u1[e], u2[e], um, up,
+                                  [&](int) { return a; }, [&](int) { return b; },
+                                  [&](int) { return lb; }, [&](int) { return rb; })
+                            : T(0);
+            }
+        }
+#pragma unroll
+        for (int e = 0; e < V; ++e) {
+            u2[e] = u1[e];
+            u1[e] = u0[e];
+        }
+    };
+#pragma unroll
+    for (int q = 0; q < R - 1; ++q) issue(q);
+    // Rows q = 0..3: no gradient yet.
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        issue(q + R - 1);
+        cp_async_wait<R - 1>();
+        T u0[V];
+        vload_smem<T>(u0, my + q * (32 * V));
+        if (q == 0 && FAST) {
+#pragma unroll
+            for (int e = 0; e < V; ++e) {
+                u2[e] = u1[e];
+                u1[e] = u0[e];
+            }
+        } else if (q == 1 && FAST) {
+#pragma unroll
+            for (int e = 0; e < V; ++e) {
+                ut1[e] = (u0[e] - u1[e]) * g.inv_dt;
+                u2[e] = u1[e];
+                u1[e] = u0[e];
+            }
+        } else if (q < 2) {
+            T f0[V];
+            residual_row(q, u0, f0);  // rows before the tile: f unused
+        } else {
+            T f0[V];
+            residual_row(q, u0, f0);
+#pragma unroll
+            for (int e = 0; e < V; ++e) {
+                f2[e] = f1[e];
+                f1[e] = f0[e];
+            }
+        }
+    }
+    // Rows q = 4 .. TY + 3: residual of row q, gradient of row a = r - 2.
+    // Unrolled by 4 only: a whole ring turn of this body overflows the
+    // instruction cache.
+    T* gout = grad + (int64_t)a0 * nx + cl;
+#pragma unroll 4
+    for (int q = 4; q < NQ; ++q) {
+        {
+            issue(q + R - 1);
+            cp_async_wait<R - 1>();
+            T u0[V], f0[V];
+            vload_smem<T>(u0, my + (q & (R - 1)) * (32 * V));
+            residual_row(q, u0, f0);
+            const T fl = __shfl_up_sync(0xffffffffu, f1[V - 1], 1);
+            const T fr = __shfl_down_sync(0xffffffffu, f1[0], 1);
+            const int a = a0 - 4 + q;
+            if (out_lane && (FAST || a < nt)) {
+                T gv[V];
+#pragma unroll
+                for (int e = 0; e < V; ++e) {
+                    const T fm = e == 0 ? fl : f1[e - 1];
+                    const T fp = e == V - 1 ? fr : f1[e + 1];
+                    T sg;
+                    if (FAST) {
+                        sg = A * f2[e];
+                        sg += ctm_int * f1[e];
+                        sg -= B * (fp + fm);
+                        sg += A * f0[e];
+                    } else {
+                        sg = wave_gather(g, a, cl + e, f2[e], f1[e], f0[e], fp, fm);
+                    }
+                    gv[e] = sg * gscale;
+                    lsum += f2[e] * f2[e];
+                }
+                st16<T>(gout, gv);
+            }
+            gout += nx;
+#pragma unroll
+            for (int e = 0; e < V; ++e) {
+                f2[e] = f1[e];
+                f1[e] = f0[e];
+            }
+        }
+    }
+    cp_async_wait<0>();
+    return lsum;
+}
+
+// Tile geometry of the vectorised loss: warp tiles (strip sw, row tile ty)
+// cover columns [30 V sw, 30 V (sw + 1)) and rows [TY ty, TY (ty + 1)).  The
+// tiles with 1 <= sw <= sw_hi and 1 <= ty <= ty_hi touch no boundary class
+// (interior kernel); the rest of the grid goes to the edge kernel in tiles of
+// LV_EDGE_TY rows, so that its short marches run in parallel.
+constexpr int LV_EDGE_TY = 16;
+
+struct LvGeom {
+    int nsw;           // strips across
+    int sw_hi, ty_hi;  // last interior strip / interior row tile (0: none)
+    int nte;           // edge row tiles down
+    int lo, hi;        // edge row tiles [lo, hi] lie beside the interior
+    int64_t n_int_blocks, n_edge;
+    dim3 int_grid;
+};
+
+template <typename T>
+LvGeom lv_geom(int nt, int nx, int ty) {
+    constexpr int V = Vec16<T>::n;
+    LvGeom q;
+    q.nsw = (nx + 30 * V - 1) / (30 * V);
+    q.sw_hi = nx >= 31 * V ? (nx - 31 * V) / (30 * V) : 0;
+    q.ty_hi = nt >= ty + 2 ? (nt - ty - 2) / ty : 0;
+    if (q.sw_hi < 1 || q.ty_hi < 1) q.sw_hi = q.ty_hi = 0;
+    q.int_grid = dim3((q.sw_hi + LV_WARPS - 1) / LV_WARPS, q.ty_hi);
+    q.n_int_blocks = (int64_t)q.int_grid.x * q.int_grid.y;
+    q.nte = (nt + LV_EDGE_TY - 1) / LV_EDGE_TY;
+    const int per = ty / LV_EDGE_TY;
+    if (q.ty_hi > 0) {
+        q.lo = per;
+        q.hi = (q.ty_hi + 1) * per - 1;
+    } else {
+        q.lo = q.nte;
+        q.hi = q.nte - 1;
+    }
+    q.n_edge = (int64_t)q.nsw * q.nte - (int64_t)(q.hi - q.lo + 1) * q.sw_hi;
+    return q;
+}
+
+// Interior tiles only: constant coefficients, no boundary branches, at most
+// 64 registers so that 8 warps per scheduler hide the load latency.
+template <typename T, int TY>
+__global__ void __launch_bounds__(LV_WARPS * 32, 16) wave_loss_grad_int_kernel(
+    WaveDev<T> g, const T* __restrict__ u, T* __restrict__ grad, ReduceWs ws, int sw_hi,
+    T gscale) {
+    constexpr int V = Vec16<T>::n;
+    __shared__ __align__(16) T ring_all[LV_WARPS][LV_RING][32 * V];
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    const int sw = 1 + blockIdx.x * LV_WARPS + warp;
+    T lsum = T(0);
+    if (sw <= sw_hi) {
+        lsum = lg_vec_tile<T, TY, true>(g, u, grad, (1 + blockIdx.y) * TY, sw * (30 * V), lane,
+                                        gscale, &ring_all[warp][0][0], nullptr);
+    }
+    reduce_store((double)lsum, (int64_t)blockIdx.y * gridDim.x + blockIdx.x, ws);
+}
+
+// The remaining (boundary) tiles, LV_EDGE_TY rows each, one warp per block,
+// through the general class functions; its last block finishes the loss over
+// both kernels' partial sums.
+template <typename T>
+__global__ void __launch_bounds__(32) wave_loss_grad_edge_kernel(
+    WaveDev<T> g, const T* __restrict__ u, T* __restrict__ grad, ReduceWs ws, LvGeom q,
+    double* loss, T gscale, double lscale) {
+    constexpr int V = Vec16<T>::n;
+    __shared__ __align__(16) T ring[LV_RING][32 * V];
+    __shared__ T bcs[2 * (LV_EDGE_TY + 4)];
+    const int64_t b = blockIdx.x;
+    // Rows [0, lo) and (hi, nte) are whole; rows [lo, hi] hold strip 0 and
+    // the strips past sw_hi.
+    const int64_t nfull = (int64_t)(q.nte - (q.hi - q.lo + 1)) * q.nsw;
+    int sw, ty;
+    if (b < nfull) {
+        const int r = (int)(b / q.nsw);
+        sw = (int)(b - (int64_t)r * q.nsw);
+        ty = r < q.lo ? r : q.hi + 1 + (r - q.lo);
+    } else {
+        const int m = q.nsw - q.sw_hi;
+        const int64_t k = b - nfull;
+        ty = q.lo + (int)(k / m);
+        const int c = (int)(k - (int64_t)(ty - q.lo) * m);
+        sw = c == 0 ? 0 : q.sw_hi + c;
+    }
+    const T lsum = lg_vec_tile<T, LV_EDGE_TY, false>(g, u, grad, ty * LV_EDGE_TY, sw * (30 * V),
+                                                     threadIdx.x, gscale, &ring[0][0], bcs);
+    reduce_finish_after((double)lsum, q.n_int_blocks, b, q.n_edge, ws, lscale, loss);
+}
+
+// Launch plan of the fused loss + adjoint: the vectorised kernels when the
+// rows allow 16-byte accesses, else the one-column-per-lane kernel.
+struct LgPlan {
+    dim3 grid;      // one-column-per-lane kernel
+    int ty;
+    bool vec;
+    LvGeom geom;    // vectorised kernels
+    int64_t blocks; // reduction partials
+};
+
+template <typename T>
+LgPlan lg_plan(int nt, int nx, const void* u, const void* grad) {
+    constexpr int V = Vec16<T>::n;
+    LgPlan pl;
+    pl.vec = (nx % V == 0) &&
+             ((reinterpret_cast<uintptr_t>(u) | reinterpret_cast<uintptr_t>(grad)) % 16 == 0);
+    if (pl.vec) {
+        const int64_t cells = (int64_t)nt * nx;
+        pl.ty = cells >= (16 << 20) ? 64 : (cells >= (4 << 20) ? 32 : 16);
+        pl.geom = lv_geom<T>(nt, nx, pl.ty);
+        pl.grid = dim3(1, pl.geom.nte);
+        pl.blocks = pl.geom.n_int_blocks + pl.geom.n_edge;
+    } else {
+        pl.ty = lg_ty(nt, nx);
+        pl.grid = lg_grid(nt, nx);
+        pl.blocks = (int64_t)pl.grid.x * pl.grid.y;
+    }
+    return pl;
+}
+
+// Reduction blocks a caller workspace must cover for either kernel.
+template <typename T>
+int64_t lg_max_blocks(int nt, int nx) {
+    const LgPlan a = lg_plan<T>(nt, nx, nullptr, nullptr);
+    const dim3 b = lg_grid(nt, nx);
+    const int64_t nb = (int64_t)b.x * b.y;
+    return a.blocks > nb ? a.blocks : nb;
+}
+
+template <typename T, int TY>
+void lv_launch(const LgPlan& pl, const WaveDev<T>& g, const T* u, T* grad, ReduceWs ws,
+               double* loss, T gs, double ls, cudaStream_t s) {
+    if (pl.geom.n_int_blocks > 0) {
+        wave_loss_grad_int_kernel<T, TY><<<pl.geom.int_grid, LV_WARPS * 32, 0, s>>>(
+            g, u, grad, ws, pl.geom.sw_hi, gs);
+    }
+    wave_loss_grad_edge_kernel<T><<<(unsigned)pl.geom.n_edge, 32, 0, s>>>(
+        g, u, grad, ws, pl.geom, loss, gs, ls);
+}
+
+template <typename T>
+void lg_launch(const LgPlan& pl, const WaveDev<T>& g, const T* u, T* grad, ReduceWs ws,
+               double* loss, cudaStream_t s) {
+    const double n = (double)g.nt * (double)g.nx;
+    const T gs = (T)(2.0 / n);
+    const double ls = 1.0 / n;
+    if (pl.vec) {
+        if (pl.ty == 16) {
+            lv_launch<T, 16>(pl, g, u, grad, ws, loss, gs, ls, s);
+        } else if (pl.ty == 32) {
+            lv_launch<T, 32>(pl, g, u, grad, ws, loss, gs, ls, s);
+        } else {
+            lv_launch<T, 64>(pl, g, u, grad, ws, loss, gs, ls, s);
+        }
+    } else if (pl.ty == 16) {
+        wave_loss_grad_kernel<T, 16><<<pl.grid, LG_WARPS * 32, 0, s>>>(g, u, grad, ws, loss, gs, ls);
+    } else {
+        wave_loss_grad_kernel<T, 32><<<pl.grid, LG_WARPS * 32, 0, s>>>(g, u, grad, ws, loss, gs, ls);
+    }
+}
+
 // Columns per thread for a row of nx cells (at most 1024 threads).
 inline int march_cpt(int nx) {
     if (nx <= 128) return 1;
@@ -206,8 +614,8 @@ int launch_march_cfg(const WaveDev<T>& g, const T* b, T* x, cudaStream_t st) {
                       (CPT * sizeof(T))) == 0;
     int threads = (nx + CPT - 1) / CPT;
     threads = ((threads + 31) / 32) * 32;
-    if (threads > 1024) return ODIL_ERR_SHAPE;
-    const size_t smem = (2 + PF) * (size_t)nx * sizeof(T);
+    if (threads > march_max_threads<T, CPT, PF>()) return ODIL_ERR_SHAPE;
+    const size_t smem = march_smem_bytes<T>(nx, PF);
     auto go = [&](auto kern) {
         ensure_dynamic_smem(reinterpret_cast<const void*>(kern), smem);
         kern<<<1, threads, smem, st>>>(g, b, x);
@@ -224,8 +632,16 @@ template <typename T>
 int launch_march(const WaveDev<T>& g, const T* b, T* x, cudaStream_t st) {
     const int nx = g.nx;
     if (nx > 2048) return ODIL_ERR_SHAPE;
-    // Ring depth: 16 rows when it fits in shared memory, else 8.
-    const bool deep = (2 + 16) * (size_t)nx * sizeof(T) <= 200 * 1024;
+    if constexpr (march_reg<T>()) {
+        // Register ring: 8 rows ahead.
+        switch (march_cpt(nx)) {
+            case 1: return launch_march_cfg<T, 1, 8>(g, b, x, st);
+            case 2: return launch_march_cfg<T, 2, 8>(g, b, x, st);
+            default: return launch_march_cfg<T, 4, 8>(g, b, x, st);
+        }
+    }
+    // Shared-memory ring: 16 rows when it fits, else 8.
+    const bool deep = march_smem_bytes<T>(nx, 16) <= 200 * 1024;
     switch (march_cpt(nx)) {
         case 1: return deep ? launch_march_cfg<T, 1, 16>(g, b, x, st)
                             : launch_march_cfg<T, 1, 8>(g, b, x, st);
@@ -317,18 +733,11 @@ int loss_grad_impl(const odil_wave_params* p, const T* u, T* grad, double* loss,
     int st = make_dev<T>(p, &g, true);
     if (st) return st;
     if (!u || !grad || !loss) return ODIL_ERR_ARG;
-    const dim3 grid = lg_grid(g.nt, g.nx);
-    if (grid.y > 65535) return ODIL_ERR_SHAPE;
-    const int64_t nb = (int64_t)grid.x * grid.y;
+    const LgPlan pl = lg_plan<T>(g.nt, g.nx, u, grad);
+    if (pl.grid.y > 65535) return ODIL_ERR_SHAPE;
+    const int64_t nb = pl.blocks;
     if (!ws || ws_bytes < reduce_ws_bytes(nb)) return ODIL_ERR_WORKSPACE;
-    const double n = (double)g.nt * (double)g.nx;
-    if (lg_ty(g.nt, g.nx) == 16) {
-        wave_loss_grad_kernel<T, 16><<<grid, LG_WARPS * 32, 0, as_stream(stream)>>>(
-            g, u, grad, reduce_ws(ws), loss, (T)(2.0 / n), 1.0 / n);
-    } else {
-        wave_loss_grad_kernel<T, 32><<<grid, LG_WARPS * 32, 0, as_stream(stream)>>>(
-            g, u, grad, reduce_ws(ws), loss, (T)(2.0 / n), 1.0 / n);
-    }
+    lg_launch<T>(pl, g, u, grad, reduce_ws(ws), loss, as_stream(stream));
     return launch_status();
 }
 
@@ -347,6 +756,19 @@ __global__ void __launch_bounds__(256) wave_initial_rhs_kernel(WaveDev<double> g
     }
 }
 
+// rhs = float(-F(hi + lo)) for a field held as two FP32 arrays (lo may be
+// null): the right-hand side of a mixed Newton epoch without an FP64 state.
+__global__ void __launch_bounds__(256) wave_pair_residual_kernel(WaveDev<double> g, PairCoef k,
+                                                                 const float* __restrict__ hi,
+                                                                 const float* __restrict__ lo,
+                                                                 float* __restrict__ rhs) {
+    const int nx = g.nx;
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= nx) return;
+    for (int i = blockIdx.y; i < g.nt; i += gridDim.y)
+        rhs[(int64_t)i * nx + j] = pair_cell_rhs(g, k, hi, lo, i, j);
+}
+
 template <int CPT, int PF>
 int launch_march_shape(const WaveDev<float>& g, const float* b, float* x, cudaStream_t st) {
     return launch_march_cfg<float, CPT, PF>(g, b, x, st);
@@ -359,8 +781,9 @@ using namespace odil;
 
 ODIL_API int64_t odil_wave_workspace_bytes(const odil_wave_params* p) {
     if (!p || p->nt < 1 || p->nx < 1) return 0;
-    const dim3 grid = lg_grid((int)p->nt, (int)p->nx);
-    return reduce_ws_bytes((int64_t)grid.x * grid.y);
+    const int64_t b64 = lg_max_blocks<double>((int)p->nt, (int)p->nx);
+    const int64_t b32 = lg_max_blocks<float>((int)p->nt, (int)p->nx);
+    return reduce_ws_bytes(b64 > b32 ? b64 : b32);
 }
 
 ODIL_API int odil_wave_residual_f32(const odil_wave_params* p, const float* u, float* f,
@@ -462,6 +885,20 @@ ODIL_API int odil_wave_initial_rhs_mixed(const odil_wave_params* p, float* rhs, 
     return launch_status();
 }
 
+ODIL_API int odil_wave_pair_residual_mixed(const odil_wave_params* p, const float* hi,
+                                           const float* lo, float* rhs, void* stream) {
+    WaveDev<double> g;
+    int st = make_dev<double>(p, &g, true);
+    if (st) return st;
+    if (!hi || !rhs || rhs == hi || rhs == lo) return ODIL_ERR_ARG;
+    if (!g.init_u || !g.init_ut || !g.left_u || !g.right_u) return ODIL_ERR_ARG;
+    const PairCoef k = pair_coef((double)g.A, (double)g.B);
+    dim3 grid, block;
+    grid_rows(g, &grid, &block);
+    wave_pair_residual_kernel<<<grid, block, 0, as_stream(stream)>>>(g, k, hi, lo, rhs);
+    return launch_status();
+}
+
 ODIL_API int odil_wave_march_shape_f32(const odil_wave_params* p, const float* b, float* x,
                                        int32_t cpt, int32_t pf, void* stream) {
     WaveDev<float> g;
@@ -537,22 +974,15 @@ ODIL_API int odil_wave_loss_grad_f32_noalloc(const odil_wave_params* p, const fl
     int st = make_dev<float>(p, &g, true);
     if (st) return st;
     if (!u || !grad || !loss) return ODIL_ERR_ARG;
-    const dim3 grid = lg_grid(g.nt, g.nx);
-    if (grid.y > 65535) return ODIL_ERR_SHAPE;
-    const int64_t nb = (int64_t)grid.x * grid.y;
+    const LgPlan pl = lg_plan<float>(g.nt, g.nx, u, grad);
+    if (pl.grid.y > 65535) return ODIL_ERR_SHAPE;
+    const int64_t nb = pl.blocks;
     if (nb > kNoAllocMaxBlocks) return ODIL_ERR_WORKSPACE;
     void* ws = nullptr;
     st = scratch_address(&ws);
     if (st) return st;
     cudaStream_t s = as_stream(stream);
     if (cudaMemsetAsync(ws, 0, sizeof(unsigned), s) != cudaSuccess) return ODIL_ERR_LAUNCH;
-    const double n = (double)g.nt * (double)g.nx;
-    if (lg_ty(g.nt, g.nx) == 16) {
-        wave_loss_grad_kernel<float, 16><<<grid, LG_WARPS * 32, 0, s>>>(
-            g, u, grad, reduce_ws(ws), loss, (float)(2.0 / n), 1.0 / n);
-    } else {
-        wave_loss_grad_kernel<float, 32><<<grid, LG_WARPS * 32, 0, s>>>(
-            g, u, grad, reduce_ws(ws), loss, (float)(2.0 / n), 1.0 / n);
-    }
+    lg_launch<float>(pl, g, u, grad, reduce_ws(ws), loss, s);
     return launch_status();
 }

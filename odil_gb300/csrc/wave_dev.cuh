@@ -55,20 +55,32 @@ __device__ __forceinline__ T opt_ld(const T* p, int k) {
 }
 
 // Residual of cell (i, j) from its five stencil values, in the operation order
-// of wave.py:106-118.
-template <typename T>
-__device__ __forceinline__ T wave_f(const WaveDev<T>& g, int i, int j, T u, T utm, T utmm,
-                                    T uxm, T uxp) {
+// of wave.py:106-118.  The boundary data come from the callables init_u(j),
+// init_ut(j), left(i-1), right(i-1) (called only where they enter).
+template <typename T, typename IU, typename IUT, typename LB, typename RB>
+__device__ __forceinline__ T wave_f_with(const WaveDev<T>& g, int i, int j, T u, T utm, T utmm,
+                                         T uxm, T uxp, IU init_u, IUT init_ut, LB left,
+                                         RB right) {
     if (i == 0) {
-        return u - (opt_ld(g.init_u, j) + g.half_dt * opt_ld(g.init_ut, j));
+        return u - (init_u(j) + g.half_dt * init_ut(j));
     }
-    if (j == 0) uxm = (uxp - T(6) * utm + T(8) * opt_ld(g.left_u, i - 1)) / T(3);
-    if (j == g.nx - 1) uxp = (uxm - T(6) * utm + T(8) * opt_ld(g.right_u, i - 1)) / T(3);
+    if (j == 0) uxm = (uxp - T(6) * utm + T(8) * left(i - 1)) / T(3);
+    if (j == g.nx - 1) uxp = (uxm - T(6) * utm + T(8) * right(i - 1)) / T(3);
     const T u_t_tm = (u - utm) * g.inv_dt;
-    const T u_t_tmm = (i == 1) ? opt_ld(g.init_ut, j) : (utm - utmm) * g.inv_dt;
+    const T u_t_tmm = (i == 1) ? init_ut(j) : (utm - utmm) * g.inv_dt;
     const T u_tt = (u_t_tm - u_t_tmm) * g.inv_dt;
     const T u_xx = (uxm - T(2) * utm + uxp) * g.inv_dx2;
     return u_tt - g.c2 * u_xx;
+}
+
+// wave_f_with reading the boundary data from global memory.
+template <typename T>
+__device__ __forceinline__ T wave_f(const WaveDev<T>& g, int i, int j, T u, T utm, T utmm,
+                                    T uxm, T uxp) {
+    return wave_f_with(
+        g, i, j, u, utm, utmm, uxm, uxp, [&](int k) { return opt_ld(g.init_u, k); },
+        [&](int k) { return opt_ld(g.init_ut, k); }, [&](int k) { return opt_ld(g.left_u, k); },
+        [&](int k) { return opt_ld(g.right_u, k); });
 }
 
 // Column-class factors of d(u_xx_raw)/d(slot) (see the header comment).
@@ -109,18 +121,134 @@ __device__ __forceinline__ T wave_gather(const WaveDev<T>& g, int a, int b, T f_
 
 
 // ---------------------------------------------------------------------------
+// Accurate residual of a field held as an unevaluated sum of two FP32 arrays,
+// hi + lo, without FP64 arithmetic at interior cells.  In the interior (i >= 2,
+// 0 < j < nx-1) the residual of wave_f equals
+//   F = A (u0 + u2) + C u1 - B (um + up),  C = 2B - 2A,
+// (u0, u1, u2 = rows i, i-1, i-2 at column j; um, up = row i-1 at j -+ 1).
+// Each coefficient is split into FP32 hi + lo parts; every product of a hi
+// coefficient with a hi value is formed exactly (p + e, e by FMA) and the p are
+// summed with Knuth's two-sum, so the only roundings are those of the small
+// correction terms: the result carries about 2^-48 of the largest term, the
+// accuracy a mixed-precision Newton step needs of its right-hand side (GB300's
+// FP64 pipe, ~1/64 of FP32, would otherwise bound the step).  Boundary cells
+// (rows 0, 1 and columns 0, nx-1) use wave_f in FP64.
+struct PairCoef {
+    float ah, al, ch, cl, bh, bl;  // A, C, -B as hi + lo
+};
+
+inline void split_f64(double x, float* hi, float* lo) {
+    *hi = (float)x;
+    *lo = (float)(x - (double)*hi);
+}
+
+inline PairCoef pair_coef(double A, double B) {
+    PairCoef k;
+    split_f64(A, &k.ah, &k.al);
+    split_f64(2.0 * B - 2.0 * A, &k.ch, &k.cl);
+    split_f64(-B, &k.bh, &k.bl);
+    return k;
+}
+
+__device__ __forceinline__ PairCoef pair_coef_dev(double A, double B) {
+    PairCoef k;
+    const double C = 2.0 * B - 2.0 * A;
+    k.ah = __double2float_rn(A);
+    k.al = __double2float_rn(A - (double)k.ah);
+    k.ch = __double2float_rn(C);
+    k.cl = __double2float_rn(C - (double)k.ch);
+    k.bh = __double2float_rn(-B);
+    k.bl = __double2float_rn(-B - (double)k.bh);
+    return k;
+}
+
+// s + c += (ch + cl) * (v + w): exact hi product, two-sum into s, the
+// rounding errors and small products into c.  Explicit _rn intrinsics keep
+// the compiler from contracting the two-sum into an FMA.
+__device__ __forceinline__ void pair_acc(float ch, float cl, float v, float w, float& s,
+                                         float& c) {
+    const float p = __fmul_rn(ch, v);
+    const float e = __fmaf_rn(ch, v, -p);
+    const float t = __fadd_rn(s, p);
+    const float bp = __fsub_rn(t, s);
+    const float err = __fadd_rn(__fsub_rn(s, __fsub_rn(t, bp)), __fsub_rn(p, bp));
+    s = t;
+    c = __fadd_rn(c, __fadd_rn(err, e));
+    c = __fmaf_rn(cl, v, c);
+    c = __fmaf_rn(ch, w, c);
+}
+
+// -F(hi + lo) at interior cell (i, j) rounded to FP32.  lo may be null.
+__device__ __forceinline__ float pair_interior_rhs(const PairCoef& k, const float* __restrict__ hi,
+                                                   const float* __restrict__ lo, int64_t c0,
+                                                   int nx) {
+    const int64_t c1 = c0 - nx, c2 = c0 - 2 * (int64_t)nx;
+    const float v0 = __ldg(hi + c0), v2 = __ldg(hi + c2), v1 = __ldg(hi + c1);
+    const float vm = __ldg(hi + c1 - 1), vp = __ldg(hi + c1 + 1);
+    float w0 = 0.f, w2 = 0.f, w1 = 0.f, wm = 0.f, wp = 0.f;
+    if (lo) {
+        w0 = __ldg(lo + c0);
+        w2 = __ldg(lo + c2);
+        w1 = __ldg(lo + c1);
+        wm = __ldg(lo + c1 - 1);
+        wp = __ldg(lo + c1 + 1);
+    }
+    float s = 0.f, c = 0.f;
+    pair_acc(k.ah, k.al, v0, w0, s, c);
+    pair_acc(k.ah, k.al, v2, w2, s, c);
+    pair_acc(k.ch, k.cl, v1, w1, s, c);
+    pair_acc(k.bh, k.bl, vm, wm, s, c);
+    pair_acc(k.bh, k.bl, vp, wp, s, c);
+    return -__fadd_rn(s, c);
+}
+
+// -F(hi + lo) at any cell: the float-pair form inside, FP64 wave_f on the
+// boundary rows and columns.
+__device__ __forceinline__ float pair_cell_rhs(const WaveDev<double>& g, const PairCoef& k,
+                                               const float* __restrict__ hi,
+                                               const float* __restrict__ lo, int i, int j) {
+    const int nx = g.nx;
+    const int64_t c0 = (int64_t)i * nx + j;
+    if (i >= 2 && j >= 1 && j + 1 < nx) return pair_interior_rhs(k, hi, lo, c0, nx);
+    auto val = [&](int ii, int jj) -> double {
+        const int64_t kk = (int64_t)ii * nx + jj;
+        double v = (double)__ldg(hi + kk);
+        if (lo) v += (double)__ldg(lo + kk);
+        return v;
+    };
+    const double uc = val(i, j);
+    double utm = 0, utmm = 0, uxm = 0, uxp = 0;
+    if (i >= 1) {
+        utm = val(i - 1, j);
+        uxm = val(i - 1, j == 0 ? nx - 1 : j - 1);
+        uxp = val(i - 1, j + 1 == nx ? 0 : j + 1);
+    }
+    if (i >= 2) utmm = val(i - 2, j);
+    return (float)(-wave_f(g, i, j, uc, utm, utmm, uxm, uxp));
+}
+
+// ---------------------------------------------------------------------------
 // Forward substitution J x = b, one block marching the rows (the rows are a
 // dependency chain; the parallelism is across x).  Thread t owns the CPT
-// contiguous columns [CPT t, CPT t + CPT).  Row i-1 lives in a double buffer in
-// shared memory for the x-neighbours at the ends of a thread's run; rows i-1
-// and i-2 of the own columns stay in registers.  Right-hand-side rows stream
-// into a PF-row shared-memory ring with cp.async (one CPT-wide copy per thread
-// and row, PF-1 rows ahead of the march), so the HBM latency is off the
-// dependency chain.  Each thread copies and later reads only its own columns,
-// so cp.async.wait_group alone orders the ring; one __syncthreads per row
-// publishes the new row to the neighbours.  The row loop is unrolled by PF so
+// contiguous columns [CPT t, CPT t + CPT); rows i-1 and i-2 of its columns stay
+// in registers.  The x-neighbours of row i-1 at the ends of a thread's run come
+// from the adjacent lanes by warp shuffles; only the two end values of each
+// warp go through shared memory (a two-row-parity buffer), so one
+// __syncthreads per row orders them and the shared-memory pipe carries a few
+// words per warp and row.  Right-hand-side rows stream into a PF-row
+// shared-memory ring with cp.async (one CPT-wide copy per thread and row, PF-1
+// rows ahead of the march), so the HBM latency is off the dependency chain;
+// each thread copies and later reads only its own columns, so
+// cp.async.wait_group alone orders the ring.  The row loop is unrolled by PF so
 // ring slots are compile-time constants.  No FP64 arithmetic in the FP32
 // instance: GB300's FP64 pipe would bound the chain.
+//
+// At the two ends of a row the periodic neighbour (column nx-1 left of column
+// 0, column 0 right of column nx-1) has coefficient zero (k_xm(0) = k_xp(nx-1)
+// = 0), so the march uses 0 there; for nx = 1 the right neighbour is the cell
+// itself, with k_xp = 4/9.
+constexpr int kMarchMaxWarps = 32;
+
 __device__ __forceinline__ void cp_async_n(void* smem, const void* gmem, int bytes) {
     const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
     if (bytes == 16) {
@@ -145,12 +273,39 @@ struct Chunk {
 // VEC: the thread's CPT columns are contiguous and 16/8/4-byte aligned in
 // global memory (nx % CPT == 0 and aligned pointers), so the ring copy and the
 // solution store are single vector accesses.
-template <typename T, int CPT, int PF, bool VEC>
+// REG: the right-hand-side rows are prefetched into registers (PF rows of
+// the thread's CPT values, loads in flight until first use) instead of the
+// shared-memory ring, which takes the ring's write and read off the L1 pipe
+// and its read off the row-to-row dependency chain; the shared memory then
+// holds only the edge words.
+template <typename T, int CPT>
+__device__ __forceinline__ void ld_run(T (&out)[CPT], const T* __restrict__ p) {
+    constexpr int bytes = CPT * (int)sizeof(T);
+    if constexpr (bytes % 16 == 0) {
+#pragma unroll
+        for (int o = 0; o < bytes / 16; ++o) {
+            const float4 v = __ldg(reinterpret_cast<const float4*>(p) + o);
+            memcpy(reinterpret_cast<char*>(out) + 16 * o, &v, 16);
+        }
+    } else if constexpr (bytes == 8) {
+        const float2 v = __ldg(reinterpret_cast<const float2*>(p));
+        memcpy(out, &v, 8);
+    } else {
+#pragma unroll
+        for (int c = 0; c < CPT; ++c) out[c] = __ldg(p + c);
+    }
+}
+
+template <typename T, int CPT, int PF, bool VEC, bool REG = false>
 __device__ __forceinline__ void march_instance(const WaveDev<T>& g, const T* __restrict__ b,
                                                T* __restrict__ x, unsigned char* smem_raw) {
     const int nx = g.nx, nt = g.nt;
-    T* buf = reinterpret_cast<T*>(smem_raw);  // [2][nx] rows i-1 / i
-    T* ring = buf + 2 * nx;                   // [PF][nx] right-hand sides
+    T* ring = reinterpret_cast<T*>(smem_raw);  // [PF][nx] right-hand sides (ring mode)
+    T* edge = REG ? ring : ring + PF * nx;     // [2 parity][2 end][kMarchMaxWarps]
+    T pre[REG ? PF : 1][CPT];                  // register ring (REG mode)
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    const int nwarp = (blockDim.x + 31) >> 5;
     const int j0 = threadIdx.x * CPT;
     const bool active = j0 < nx;
     T kxm[CPT], ktm[CPT], kxp[CPT], d1[CPT], d2[CPT];
@@ -164,28 +319,53 @@ __device__ __forceinline__ void march_instance(const WaveDev<T>& g, const T* __r
         d1[c] = T(0);
         d2[c] = T(0);
     }
-    const int jl = j0 == 0 ? nx - 1 : j0 - 1;       // left neighbour of the run
-    const int jr = j0 + CPT >= nx ? (j0 + CPT) % nx : j0 + CPT;  // right neighbour
+    // Edge slots this thread reads (every lane of a warp reads the same word,
+    // a broadcast) and whether the value there is a real neighbour.
+    const int wl = warp > 0 ? warp - 1 : 0;
+    const int wr = warp + 1 < nwarp ? warp + 1 : warp;
+    const bool use_l = lane == 0, use_r = lane == 31;
+    const T mask_l = warp > 0 ? T(1) : T(0);
+    const T mask_r = warp + 1 < nwarp ? T(1) : T(0);
+    const bool self_r = nx == 1;
+    // Both parities start at 0: row 0 scales its neighbours by 0, which must
+    // not meet a stale non-finite word.
+    for (int e = threadIdx.x; e < 4 * kMarchMaxWarps; e += blockDim.x) edge[e] = T(0);
+    __syncthreads();
+    const T* src = b + j0;  // next right-hand-side row to prefetch
+    T* dst = x + j0;        // solution row being written
     auto issue = [&](int row, int slot) {
+        if constexpr (REG) {
+            if (active && row < nt) {
+                if constexpr (VEC) {
+                    ld_run<T, CPT>(pre[slot], src);
+                } else {
+#pragma unroll
+                    for (int c = 0; c < CPT; ++c)
+                        pre[slot][c] = j0 + c < nx ? __ldg(src + c) : T(0);
+                }
+            }
+            src += nx;
+            return;
+        }
         if (active && row < nt) {
-            const T* src = b + (int64_t)row * nx + j0;
-            T* dst = ring + slot * nx + j0;
+            T* to = ring + slot * nx + j0;
             if constexpr (VEC) {
                 constexpr int bytes = CPT * (int)sizeof(T);
                 if constexpr (bytes <= 16) {
-                    cp_async_n(dst, src, bytes);
+                    cp_async_n(to, src, bytes);
                 } else {
 #pragma unroll
                     for (int off = 0; off < bytes; off += 16)
-                        cp_async_n(reinterpret_cast<char*>(dst) + off,
+                        cp_async_n(reinterpret_cast<char*>(to) + off,
                                    reinterpret_cast<const char*>(src) + off, 16);
                 }
             } else {
 #pragma unroll
                 for (int c = 0; c < CPT; ++c)
-                    if (j0 + c < nx) cp_async_n(dst + c, src + c, (int)sizeof(T));
+                    if (j0 + c < nx) cp_async_n(to + c, src + c, (int)sizeof(T));
             }
         }
+        src += nx;
         cp_async_commit();
     };
 #pragma unroll
@@ -196,63 +376,107 @@ __device__ __forceinline__ void march_instance(const WaveDev<T>& g, const T* __r
             const int i = i0 + s;
             if (i >= nt) break;
             issue(i + PF - 1, (s + PF - 1) % PF);
-            cp_async_wait<PF - 1>();  // this thread's copy of row i has landed
-            const T* rrow = ring + s * nx;
-            T* cur = buf + (i & 1) * nx;
-            const T* prv = buf + ((i & 1) ^ 1) * nx;
+            // Row 0 of J is the identity; row 1 has no u[i-2] term.
+            const T c_rhs = i == 0 ? T(1) : g.dt2;
+            const T c_d1 = i == 1 ? T(1) : T(2);
+            const T c_lam = i == 0 ? T(0) : g.lam2;
+            // x-neighbours of row i-1 at the ends of this thread's run.
+            const T* eprv = edge + ((i & 1) ^ 1) * 2 * kMarchMaxWarps;
+            const T el = eprv[kMarchMaxWarps + wl] * mask_l;
+            const T er = eprv[wr] * mask_r;
+            const T sl = __shfl_up_sync(0xffffffffu, d1[CPT - 1], 1);
+            const T sr = __shfl_down_sync(0xffffffffu, d1[0], 1);
+            const T left = use_l ? el : sl;
+            const T right = self_r ? d1[0] : (use_r ? er : sr);
+            // Threads past the row end read nothing (their columns lie
+            // outside the ring) and carry zeros.
+            Chunk<T, CPT> rhs;
+            if constexpr (REG) {
+#pragma unroll
+                for (int c = 0; c < CPT; ++c) rhs.v[c] = active ? pre[s][c] : T(0);
+            } else if constexpr (VEC) {
+                cp_async_wait<PF - 1>();  // this thread's copy of row i has landed
+                const T* rrow = ring + s * nx + j0;
+                if (active) {
+                    rhs = *reinterpret_cast<const Chunk<T, CPT>*>(rrow);
+                } else {
+#pragma unroll
+                    for (int c = 0; c < CPT; ++c) rhs.v[c] = T(0);
+                }
+            } else {
+                cp_async_wait<PF - 1>();
+                const T* rrow = ring + s * nx + j0;
+#pragma unroll
+                for (int c = 0; c < CPT; ++c) rhs.v[c] = j0 + c < nx ? rrow[c] : T(0);
+            }
+            Chunk<T, CPT> out;
+#pragma unroll
+            for (int c = 0; c < CPT; ++c) {
+                const T xm = c == 0 ? left : d1[c - 1];
+                const T xp = c == CPT - 1 ? right : d1[c + 1];
+                const T tprev = c_d1 * d1[c] - d2[c];
+                out.v[c] = c_rhs * rhs.v[c] + tprev +
+                           c_lam * (kxm[c] * xm - ktm[c] * d1[c] + kxp[c] * xp);
+            }
             if (active) {
-                Chunk<T, CPT> rhs;
                 if constexpr (VEC) {
-                    rhs = *reinterpret_cast<const Chunk<T, CPT>*>(rrow + j0);
-                } else {
-#pragma unroll
-                    for (int c = 0; c < CPT; ++c) rhs.v[c] = j0 + c < nx ? rrow[j0 + c] : T(0);
-                }
-                Chunk<T, CPT> out;
-                if (i == 0) {
-#pragma unroll
-                    for (int c = 0; c < CPT; ++c) out.v[c] = rhs.v[c];
-                } else {
-                    const T left = prv[jl];
-                    const T right = prv[jr];
-#pragma unroll
-                    for (int c = 0; c < CPT; ++c) {
-                        const T xm = c == 0 ? left : d1[c - 1];
-                        const T xp = c == CPT - 1 ? right : d1[c + 1];
-                        const T tprev = (i == 1) ? d1[c] : T(2) * d1[c] - d2[c];
-                        out.v[c] = g.dt2 * rhs.v[c] + tprev +
-                                   g.lam2 * (kxm[c] * xm - ktm[c] * d1[c] + kxp[c] * xp);
-                    }
-                }
-                if constexpr (VEC) {
-                    *reinterpret_cast<Chunk<T, CPT>*>(x + (int64_t)i * nx + j0) = out;
-                    *reinterpret_cast<Chunk<T, CPT>*>(cur + j0) = out;
+                    *reinterpret_cast<Chunk<T, CPT>*>(dst) = out;
                 } else {
 #pragma unroll
                     for (int c = 0; c < CPT; ++c) {
-                        if (j0 + c < nx) {
-                            x[(int64_t)i * nx + j0 + c] = out.v[c];
-                            cur[j0 + c] = out.v[c];
-                        }
+                        if (j0 + c < nx) dst[c] = out.v[c];
                     }
                 }
+            }
 #pragma unroll
-                for (int c = 0; c < CPT; ++c) {
-                    d2[c] = d1[c];
-                    d1[c] = out.v[c];
-                }
+            for (int c = 0; c < CPT; ++c)
+                if (j0 + c >= nx) out.v[c] = T(0);  // columns past the row end
+            dst += nx;
+            T* ecur = edge + (i & 1) * 2 * kMarchMaxWarps;
+            if (use_l) ecur[warp] = out.v[0];
+            if (use_r) ecur[kMarchMaxWarps + warp] = out.v[CPT - 1];
+#pragma unroll
+            for (int c = 0; c < CPT; ++c) {
+                d2[c] = d1[c];
+                d1[c] = out.v[c];
             }
             __syncthreads();
         }
     }
-    cp_async_wait<0>();
+    if constexpr (!REG) cp_async_wait<0>();
+}
+
+// Largest block of a march with CPT columns per thread and PF prefetched
+// rows: the register ring of the FP32 march needs CPT PF registers on top of
+// the rest; the shared-memory ring of the FP64 march needs none, but runs of
+// 32 bytes or more need more than the 64 registers a 1024-thread block leaves.
+template <typename T>
+__host__ __device__ constexpr bool march_reg() { return sizeof(T) == 4; }
+
+template <typename T, int CPT, int PF>
+__host__ __device__ constexpr int march_max_threads() {
+    return march_reg<T>() ? (CPT * PF * (int)sizeof(T) <= 64
+                                 ? 1024
+                                 : (CPT * PF * (int)sizeof(T) <= 128 ? 512 : 256))
+                          : (CPT * sizeof(T) >= 32 ? 512 : 1024);
+}
+
+// Shared memory of a march with the ring (REG false) / of wave_march_kernel.
+template <typename T>
+inline size_t march_ring_smem_bytes(int nx, int pf) {
+    return (size_t)pf * nx * sizeof(T) + 4 * kMarchMaxWarps * sizeof(T);
+}
+
+template <typename T>
+inline size_t march_smem_bytes(int nx, int pf) {
+    return march_reg<T>() ? 4 * kMarchMaxWarps * sizeof(T) : march_ring_smem_bytes<T>(nx, pf);
 }
 
 template <typename T, int CPT, int PF, bool VEC>
-__global__ void __launch_bounds__(1024) wave_march_kernel(WaveDev<T> g, const T* __restrict__ b,
-                                                          T* __restrict__ x) {
+__global__ void __launch_bounds__(march_max_threads<T, CPT, PF>()) wave_march_kernel(
+    WaveDev<T> g, const T* __restrict__ b, T* __restrict__ x) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    march_instance<T, CPT, PF, VEC>(g, b, x, smem_raw);
+    march_instance<T, CPT, PF, VEC, march_reg<T>()>(g, b, x, smem_raw);
 }
 
 

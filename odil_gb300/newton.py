@@ -11,6 +11,11 @@ precision="fp64"   plain method: FP64 residual, FP64 solve, FP64 update.
 precision="mixed"  FP64 residual and update, FP32 solve.  Per epoch: one
                    fully parallel FP64 kernel (u += d, r = F(u), rhs = -r as
                    FP32) and one FP32 forward substitution (d = J^{-1} rhs).
+                   From u = 0 the iterate is instead kept as FP32 corrections
+                   hi + lo: the first right-hand side needs FP64 work on the
+                   boundary cells only, later ones come from the float-pair
+                   residual (exact FP32 products, compensated sums), and one
+                   final pass writes u = hi + lo in FP64.
 """
 import torch
 
@@ -57,14 +62,14 @@ def solve(problem, state, precision="mixed", epochs=None, rnorm2=None,
     if precision == "mixed":
         rhs = _scratch(k, "rhs32", torch.float32)
         d = _scratch(k, "d32", torch.float32)
+        if from_zero and epochs > 0:
+            _solve_pairs(k, u, rhs, d, epochs, rnorm2)
+            return u
         ua, ub = u, _scratch(k, "u64", torch.float64)
         if from_zero:
             u.zero_()
-        if from_zero and (epochs > 0 or rnorm2 is None):
-            k.initial_rhs(rhs)
-        else:
-            k.update_residual_mixed(ua, None, None, rhs,
-                                    rnorm2 if epochs == 0 else None)
+        k.update_residual_mixed(ua, None, None, rhs,
+                                rnorm2 if epochs == 0 else None)
         for e in range(epochs):
             k.march_tuned(rhs, d)
             last = e == epochs - 1
@@ -87,3 +92,24 @@ def solve(problem, state, precision="mixed", epochs=None, rnorm2=None,
     else:
         raise ValueError("Unknown precision=" + precision)
     return u
+
+
+def _solve_pairs(k, u, rhs, d, epochs, rnorm2):
+    """Mixed Newton from u = 0 with the iterate kept as FP32 hi + lo."""
+    hi = _scratch(k, "hi32", torch.float32)
+    lo = _scratch(k, "lo32", torch.float32)
+    k.initial_rhs(rhs)
+    k.march_tuned(rhs, hi)
+    have_lo = False
+    for _ in range(1, epochs):
+        k.pair_residual(hi, lo if have_lo else None, rhs)
+        if have_lo:
+            k.march_tuned(rhs, d)
+            vec.axpby(lo, 1.0, lo, 1.0, d)
+        else:
+            k.march_tuned(rhs, lo)
+            have_lo = True
+    call("odil_pair_to_f64", ptr(hi), ptr(lo if have_lo else None), ptr(u),
+         u.numel(), stream_handle())
+    if rnorm2 is not None:
+        k.update_residual_mixed(u, None, None, rhs, rnorm2)

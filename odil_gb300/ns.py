@@ -149,3 +149,105 @@ class NsKernels:
         g = self.jtv(J, list(f), scale=2.0 / self.N)
         loss = (f.double()**2).mean(dim=(1, 2)).sum()
         return loss, g
+
+
+class NsDirectNewton:
+    """Newton for the forward cavity problem with a direct GPU solve.
+
+    The reference solves each Newton step's normal equations with SuperLU
+    (util.py:242-268, linsolver.py:28-45).  Here the square Jacobian, with the
+    continuity row of the pinned cell replaced by p[pin] = 0, is factored in
+    FP32 as a block-tridiagonal LU (odil_ns_direct_factor) and each step
+    J d = -F is solved by FP64 iterative refinement: the FP32 factors give a
+    correction, the FP64 stencil J d gives the new residual of the linear
+    system, until it falls below `rtol` of -F.  The pressure is fixed at the
+    pinned cell; the reference leaves the constant free, so compare pressures
+    up to a constant.  Forward problem only (neq = 3)."""
+
+    def __init__(self, kernels, pin=(0, 0)):
+        if kernels.neq != 3:
+            raise ValueError("direct Newton needs the forward problem "
+                             "(no imposed points, penalty or pin term)")
+        self.k = kernels
+        self.n = kernels.n
+        self.pin = int(pin[0]) * self.n + int(pin[1])
+        lib = _capi.load()
+        nb = lib.odil_ns_direct_workspace_bytes(self.n)
+        if nb <= 0:
+            raise ValueError("cavity side %d outside the direct solver's range"
+                             % self.n)
+        dev = kernels.device
+        self.ws = torch.empty(nb, dtype=torch.uint8, device=dev)
+        self.coef = torch.empty((3, 15, self.n, self.n), dtype=torch.float64,
+                                device=dev)
+        self.b32 = torch.empty((3, self.n, self.n), dtype=torch.float32,
+                               device=dev)
+        self.x32 = torch.empty_like(self.b32)
+        self.stats = []
+
+    def _pinned(self, r, p_field):
+        i, j = divmod(self.pin, self.n)
+        r[2, i, j] = p_field[i, j]
+        return r
+
+    def factor(self, u, v, p):
+        k = self.k
+        q = ctypes.byref(k.params[torch.float64])
+        call("odil_ns_jacobian_f64", q, ptr(u), ptr(v), ptr(p), ptr(self.coef),
+             stream_handle())
+        call("odil_ns_direct_factor", self.n, ptr(self.coef), self.pin,
+             ptr(self.ws), self.ws.numel(), stream_handle())
+
+    def solve32(self, b):
+        self.b32.copy_(b)
+        call("odil_ns_direct_solve", self.n, ptr(self.coef), self.pin,
+             ptr(self.ws), self.ws.numel(), ptr(self.b32), ptr(self.x32),
+             stream_handle())
+        return self.x32
+
+    def apply(self, d):
+        """J' d in FP64 (stencil products; pinned row = d_p[pin])."""
+        J = [[StencilOp(SHIFTS, self.coef[e, 5 * f:5 * f + 5], self.k.shape)
+              for f in range(3)] for e in range(3)]
+        out = torch.stack(self.k.jv(J, [d[0], d[1], d[2]]))
+        return self._pinned(out, d[2])
+
+    def step(self, u, v, p, refine=8, rtol=1e-13):
+        """One Newton step in place; returns the FP64 residual rms before it."""
+        f = self.k.residual(u, v, p)
+        rms = float(torch.sqrt((f**2).mean()))
+        r = self._pinned(f.clone(), p)
+        st = torch.cuda.current_stream(self.k.device)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        self.factor(u, v, p)
+        e1.record(st)
+        d = torch.zeros_like(r)
+        res = -r
+        rn0 = float(torch.linalg.vector_norm(res))
+        it = 0
+        for it in range(1, refine + 1):
+            d += self.solve32(res).double()
+            res = -r - self.apply(d)
+            if float(torch.linalg.vector_norm(res)) <= rtol * rn0:
+                break
+        self.stats.append({"rms": rms, "refine": it,
+                           "lin_rel": float(torch.linalg.vector_norm(res)) /
+                           max(rn0, 1e-300),
+                           "factor_ms": e0.elapsed_time(e1)})
+        u += d[0]
+        v += d[1]
+        p += d[2]
+        return rms
+
+    def solve(self, u, v, p, epochs=50, tol=1e-10, callback=None):
+        """Newton epochs until the residual rms is below `tol`."""
+        for ep in range(epochs):
+            rms = self.step(u, v, p)
+            if callback is not None:
+                callback(ep, rms)
+            if rms <= tol:
+                break
+        f = self.k.residual(u, v, p)
+        return float(torch.sqrt((f**2).mean()))

@@ -194,6 +194,12 @@ class WaveKernels:
              stream_handle())
         return rhs
 
+    def pair_residual(self, hi, lo, rhs):
+        """rhs = float32(-F(hi + lo)) for FP32 arrays hi, lo (lo may be None)."""
+        call("odil_wave_pair_residual_mixed", ctypes.byref(self.p64), ptr(hi),
+             ptr(lo), ptr(rhs), stream_handle())
+        return rhs
+
     def update_residual_mixed(self, u, d, u_out, rhs, rnorm2=None):
         """u_out = u + d (d FP32 or None), rhs = float32(-F(u_out)) with the
         residual in FP64; optionally rnorm2[0] = sum(F^2)."""

@@ -270,3 +270,28 @@ def newton(s, state, epochs=1):
         for i, k in enumerate(FIELDS):
             st[k] = st[k] + d[i * n * n:(i + 1) * n * n].reshape(s.shape)
     return st
+
+
+def newton_pinned(s, state, epochs=1, pin=(0, 0)):
+    """Newton on the square system with the continuity row of cell `pin`
+    replaced by p[pin] = 0 (the forward problem's constant-pressure null
+    space removed), each step solved directly (scipy spsolve).  Same fixed
+    point as newton() up to the pressure constant."""
+    st = {k: np.array(state[k], np.float64) for k in FIELDS}
+    n = s.n
+    N = n * n
+    pidx = pin[0] * n + pin[1]
+    for _ in range(epochs):
+        const, J = linearize(s, st)
+        if len(const) != 3:
+            raise ValueError("forward problem only")
+        r = np.concatenate([c.ravel() for c in const])
+        J = J.tolil()
+        row = 2 * N + pidx
+        J.rows[row] = [2 * N + pidx]
+        J.data[row] = [1.0]
+        r[row] = st["p"].ravel()[pidx]
+        d = scipy.sparse.linalg.spsolve(J.tocsc(), -r)
+        for i, k in enumerate(FIELDS):
+            st[k] = st[k] + d[i * N:(i + 1) * N].reshape(s.shape)
+    return st

@@ -63,3 +63,43 @@ def test_batch_benchmark_sizes_sample(cuda):
     b.solve_mixed()
     errs = [W.rel_err(u, _oracle(inst)) for inst, u in zip(insts, b.unpack())]
     assert max(errs) <= 1e-5, max(errs)
+
+
+def test_batch_rhs_kernels_match_single_instance(cuda):
+    """The batched right-hand-side kernels (initial, float-pair) give, per
+    instance, what the single-instance kernels give."""
+    from odil_gb300.batch import WaveBatch
+    from odil_gb300.wave import WaveKernels
+    insts = _small_batch()
+    b = WaveBatch(insts, device=cuda)
+    rng = np.random.default_rng(3)
+    hi = torch.as_tensor(rng.standard_normal(b.total), dtype=torch.float32,
+                         device=cuda)
+    lo = torch.as_tensor(1e-7 * rng.standard_normal(b.total),
+                         dtype=torch.float32, device=cuda)
+    r0 = torch.zeros(b.total, dtype=torch.float32, device=cuda)
+    r1 = torch.zeros_like(r0)
+    b.initial_rhs(r0)
+    b.pair_residual(hi, lo, r1)
+    for inst, off, (nt, nx) in zip(insts, b.offsets, b.shapes):
+        k = WaveKernels(nt, nx, inst["dt"], inst["dx"], inst["c"],
+                        inst["init_u"], inst["init_ut"], inst["left_u"],
+                        inst["right_u"], device=cuda)
+        sl = slice(off, off + nt * nx)
+        e0 = torch.empty((nt, nx), dtype=torch.float32, device=cuda)
+        k.initial_rhs(e0)
+        assert torch.equal(r0[sl].view(nt, nx), e0)
+        e1 = torch.empty_like(e0)
+        k.pair_residual(hi[sl].view(nt, nx).contiguous(),
+                        lo[sl].view(nt, nx).contiguous(), e1)
+        assert torch.equal(r1[sl].view(nt, nx), e1)
+
+
+def test_batch_three_epochs(cuda):
+    """Three epochs (the third correction accumulates into lo)."""
+    from odil_gb300.batch import WaveBatch
+    insts = _small_batch()
+    b = WaveBatch(insts, device=cuda)
+    b.solve_mixed(epochs=3)
+    for inst, u in zip(insts, b.unpack()):
+        assert W.rel_err(u, _oracle(inst)) <= 1e-10, (inst["nt"], inst["c"])

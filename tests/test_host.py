@@ -102,3 +102,50 @@ def test_unknown_names_raise_value_error():
         make_optimizer("sgd")
     with pytest.raises(ValueError):
         linsolver.solve(None, torch.zeros(1), linsolver="nope")
+
+
+def test_history_csv_rows_backfill_and_errors(tmp_path):
+    """History (util_history.py:7-108): rows, zero back-fill of a late
+    column, warm-up, the header fixed at the first write, pickle round trip."""
+    from odil_gb300.history import History
+    path = tmp_path / "train.csv"
+    h = History(str(path), warmup=1)
+    h.append("epoch", 0)
+    h.append("loss", 1.5)
+    h.write()  # count 1 <= warmup: nothing written yet
+    assert path.read_text() == ""
+    h.append("epoch", 1)
+    h.append("loss", 0.25)
+    h.write()
+    assert path.read_text() == "epoch,loss\n0,1.5\n1,0.25\n"
+    h.append("epoch", 2)
+    h.append("loss", None)  # repeats the kind of the last value as zero
+    h.write()
+    assert path.read_text().splitlines()[-1] == "2,0.0"
+    h.append("epoch", 3)
+    h.append("loss", 0.125)
+    h.append("err", 1e-3)  # new column: back-filled, but the header is fixed
+    assert h.get("err") == [0.0, 0.0, 0.0, 1e-3]
+    with pytest.raises(RuntimeError, match="Unexpected keys"):
+        h.write()
+    h.close()
+    h2 = History()
+    h2.append("a", 1)
+    h2.append("b", 2.0)
+    h2.commit()
+    h2.append("a", 2)
+    with pytest.raises(RuntimeError, match="Missing values for columns: b,"):
+        h2.commit()
+    with pytest.raises(TypeError):
+        h2.append("a", [1])
+    pk = tmp_path / "hist.pickle"
+    h3 = History()
+    h3.append_dict({"x": 1, "y": 0.5})
+    h3.commit()
+    h3.save(str(pk))
+    out = tmp_path / "re.csv"
+    h4 = History(str(out))
+    h4.load(str(pk))
+    h4.close()
+    assert out.read_text() == "x,y\n1,0.5\n"
+    assert h4.count == 1 and h4.get("y") == [0.5]

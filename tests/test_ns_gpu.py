@@ -116,3 +116,43 @@ def test_reference_cavity_solutions_are_roots(cuda, Re):
         # at best and ~1e-9 at the largest cells: bound it by 1e-8.
         assert _rel(f[e], fo[e]) < 1e-8
         assert np.sqrt(np.mean(f[e]**2)) < 1e-5
+
+
+def test_direct_newton_step_matches_oracle(cuda):
+    """One pinned Newton step from a seeded state: the FP32 block LU with FP64
+    refinement gives the oracle's direct-solve update (spsolve) to 1e-9 of
+    the fields (the refinement stops at 1e-13 of the linear residual;
+    cond(J) ~ 1e4 here)."""
+    from odil_gb300.ns import NsDirectNewton
+    n = 24
+    rng = np.random.default_rng(2)
+    st = {c: 0.1 * rng.standard_normal((n, n)) for c in "uvp"}
+    ref = NS.newton_pinned(NS.NsSetup(n, 400.0), st, epochs=1, pin=(3, 5))
+    k = _kernels(n, 400.0, {}, cuda)
+    t = [torch.as_tensor(st[c], device=cuda).clone() for c in "uvp"]
+    solver = NsDirectNewton(k, pin=(3, 5))
+    solver.step(*t)
+    assert solver.stats[-1]["lin_rel"] <= 1e-13
+    scale = max(np.abs(ref[c]).max() for c in "uvp")
+    for c, x in zip("uvp", t):
+        assert np.abs(x.cpu().numpy() - ref[c]).max() <= 1e-9 * scale, c
+
+
+def test_direct_newton_reaches_reference_cavity(cuda):
+    """Forward cavity at N = 128, Re = 400 from rest: the GPU Newton reaches
+    the reference's own FP64 Newton solution (cavity_N128_Re400.pickle, which
+    the reference converged to a residual rms ~1e-6) to 1e-5 in u, v and in
+    p up to its free constant."""
+    from odil_gb300.ns import NsDirectNewton
+    n = 128
+    k = _kernels(n, 400.0, {}, cuda)
+    t = [torch.zeros((n, n), dtype=torch.float64, device=cuda)
+         for _ in range(3)]
+    solver = NsDirectNewton(k)
+    rms = solver.solve(*t, epochs=60, tol=1e-11)
+    assert rms <= 1e-10, solver.stats[-3:]
+    for c, x in zip("uv", t[:2]):
+        ref = GOLD["Re400_" + c]
+        assert np.abs(x.cpu().numpy() - ref).max() <= 1e-5 * np.abs(ref).max()
+    dp = t[2].cpu().numpy() - GOLD["Re400_p"]
+    assert np.abs(dp - dp.mean()).max() <= 1e-5 * np.abs(GOLD["Re400_p"]).max()

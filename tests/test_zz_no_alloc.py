@@ -63,11 +63,11 @@ def test_noalloc_rejects_oversized_grids(cuda):
     lib = _capi.load()
     maxb = lib.odil_wave_loss_grad_noalloc_max_blocks()
     assert maxb > 10000
-    n = 16384  # needs more reduction blocks than the limit
-    p, keep = _params(n, n, cuda, 0)
+    nt, nx = 65536, 8192  # needs more reduction blocks than the limit
+    p, keep = _params(nt, nx, cuda, 0)
     # Full-size buffers, so that the call would stay in bounds even if the
     # size check were missing.
-    u = torch.zeros((n, n), dtype=torch.float32, device=cuda)
+    u = torch.zeros((nt, nx), dtype=torch.float32, device=cuda)
     g = torch.zeros_like(u)
     loss = torch.zeros(1, dtype=torch.float64, device=cuda)
     stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
