@@ -170,6 +170,8 @@ typedef struct odil_wave_instance {
     int64_t offset_t;  /* first entry in packed left_u / right_u */
     /* Derived constants, filled on the device by odil_wave_batch_setup. */
     double inv_dt, inv_dx2, c2, dt2, lam2;
+    double a, b, half_dt;  /* 1/dt^2, c^2/dx^2, dt/2 */
+    float ah, al, ch, cl, bh, bl;  /* A, 2B - 2A, -B as FP32 hi + lo */
 } odil_wave_instance;
 
 typedef struct odil_wave_batch {

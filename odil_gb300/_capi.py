@@ -76,6 +76,15 @@ class OdilWaveInstance(ctypes.Structure):
         ("c2", ctypes.c_double),
         ("dt2", ctypes.c_double),
         ("lam2", ctypes.c_double),
+        ("a", ctypes.c_double),
+        ("b", ctypes.c_double),
+        ("half_dt", ctypes.c_double),
+        ("ah", ctypes.c_float),
+        ("al", ctypes.c_float),
+        ("ch", ctypes.c_float),
+        ("cl", ctypes.c_float),
+        ("bh", ctypes.c_float),
+        ("bl", ctypes.c_float),
     ]
 
 

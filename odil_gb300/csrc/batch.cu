@@ -30,6 +30,16 @@ __global__ void batch_setup_kernel(odil_wave_instance* inst, int n) {
     d.c2 = d.c * d.c;
     d.dt2 = d.dt * d.dt;
     d.lam2 = d.c * d.c * d.dt * d.dt * inv_dx2;
+    d.a = inv_dt * inv_dt;
+    d.b = d.c2 * inv_dx2;
+    d.half_dt = 0.5 * d.dt;
+    const PairCoef k = pair_coef_dev(d.a, d.b);
+    d.ah = k.ah;
+    d.al = k.al;
+    d.ch = k.ch;
+    d.cl = k.cl;
+    d.bh = k.bh;
+    d.bl = k.bl;
 }
 
 template <typename T>
@@ -39,12 +49,14 @@ __device__ __forceinline__ WaveDev<T> dev_of(const odil_wave_instance& d, const 
     WaveDev<T> g;
     g.nt = (int)d.nt;
     g.nx = (int)d.nx;
+    // Copies of constants computed once by batch_setup_kernel (no FP64
+    // arithmetic per block or row).
     g.inv_dt = (T)d.inv_dt;
     g.inv_dx2 = (T)d.inv_dx2;
     g.c2 = (T)d.c2;
-    g.half_dt = (T)(0.5 * d.dt);
-    g.A = (T)(d.inv_dt * d.inv_dt);
-    g.B = (T)(d.c2 * d.inv_dx2);
+    g.half_dt = (T)d.half_dt;
+    g.A = (T)d.a;
+    g.B = (T)d.b;
     g.dt2 = (T)d.dt2;
     g.lam2 = (T)d.lam2;
     g.init_u = init_u ? init_u + d.offset_x : nullptr;
@@ -152,7 +164,13 @@ __global__ void __launch_bounds__(256) batch_rows_kernel(odil_wave_batch b,
                 rrow[j] = v;
             }
         } else {
-            const PairCoef k = pair_coef_dev((double)g.A, (double)g.B);
+            PairCoef k;
+            k.ah = desc.ah;
+            k.al = desc.al;
+            k.ch = desc.ch;
+            k.cl = desc.cl;
+            k.bh = desc.bh;
+            k.bl = desc.bl;
             const float* h = hi + desc.offset;
             const float* l = lo ? lo + desc.offset : nullptr;
             for (int j = threadIdx.x; j < g.nx; j += blockDim.x)
@@ -253,7 +271,7 @@ ODIL_API int odil_wave_batch_initial_rhs_mixed(const odil_wave_batch* b, float* 
     if (st) return st;
     if (!rhs) return ODIL_ERR_ARG;
     if (!b->init_u || !b->init_ut || !b->left_u || !b->right_u) return ODIL_ERR_ARG;
-    batch_rows_kernel<0><<<sms() * 8, 256, 0, as_stream(stream)>>>(*b, nullptr, nullptr, rhs);
+    batch_rows_kernel<0><<<sms() * 32, 256, 0, as_stream(stream)>>>(*b, nullptr, nullptr, rhs);
     return launch_status();
 }
 
@@ -263,7 +281,7 @@ ODIL_API int odil_wave_batch_pair_residual_mixed(const odil_wave_batch* b, const
     if (st) return st;
     if (!hi || !rhs || rhs == hi || rhs == lo) return ODIL_ERR_ARG;
     if (!b->init_u || !b->init_ut || !b->left_u || !b->right_u) return ODIL_ERR_ARG;
-    batch_rows_kernel<1><<<sms() * 8, 256, 0, as_stream(stream)>>>(*b, hi, lo, rhs);
+    batch_rows_kernel<1><<<sms() * 32, 256, 0, as_stream(stream)>>>(*b, hi, lo, rhs);
     return launch_status();
 }
 

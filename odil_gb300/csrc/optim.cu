@@ -145,16 +145,18 @@ __global__ void __launch_bounds__(VT) multidot_kernel(const T* __restrict__ M, i
         for (int j = 0; j < MD_MAXR; ++j) acc[g][j] = T(0);
     if (vec) {
         const int64_t v0 = e0 / W, v1 = e1 / W;
-        for (int64_t e = v0 + threadIdx.x; e < v1; e += VT) {
-            V qv[MD_MAXR];
+        // Two elements per thread and step, all their loads issued before the
+        // multiply-adds: 8 row loads in flight per thread.
+        auto load = [&](int64_t e, V (&qv)[MD_MAXR], V (&mv)[MD_G]) {
 #pragma unroll
             for (int j = 0; j < MD_MAXR; ++j)
                 if (j < r) qv[j] = __ldg(reinterpret_cast<const V*>(qs.q[j]) + e);
-            V mv[MD_G];
 #pragma unroll
             for (int g = 0; g < MD_G; ++g)
                 if (g0 + g < k)
                     mv[g] = __ldcs(reinterpret_cast<const V*>(M + (int64_t)(g0 + g) * ld) + e);
+        };
+        auto madd = [&](const V (&qv)[MD_MAXR], const V (&mv)[MD_G]) {
 #pragma unroll
             for (int g = 0; g < MD_G; ++g) {
                 if (g0 + g < k) {
@@ -169,6 +171,14 @@ __global__ void __launch_bounds__(VT) multidot_kernel(const T* __restrict__ M, i
                     }
                 }
             }
+        };
+        for (int64_t e = v0 + threadIdx.x; e < v1; e += 2 * VT) {
+            V qa[MD_MAXR], ma[MD_G], qb[MD_MAXR], mb[MD_G];
+            const bool two = e + VT < v1;
+            load(e, qa, ma);
+            if (two) load(e + VT, qb, mb);
+            madd(qa, ma);
+            if (two) madd(qb, mb);
         }
         for (int64_t e = v1 * W + threadIdx.x; e < e1; e += VT) {
 #pragma unroll

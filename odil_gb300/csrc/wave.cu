@@ -528,6 +528,56 @@ __global__ void __launch_bounds__(32) wave_loss_grad_edge_kernel(
     reduce_finish_after((double)lsum, q.n_int_blocks, b, q.n_edge, ws, lscale, loss);
 }
 
+// Both tile kinds in one launch: the first blocks take the boundary tiles
+// (two per block, one per warp), the rest the interior tiles, so the slow
+// boundary marches run beside the interior ones instead of after them.  The
+// register cap of the interior path applies to the whole kernel; the
+// boundary path is rare enough that its spills do not matter.
+template <typename T, int TY>
+__global__ void __launch_bounds__(LV_WARPS * 32, 16) wave_loss_grad_all_kernel(
+    WaveDev<T> g, const T* __restrict__ u, T* __restrict__ grad, ReduceWs ws, LvGeom q,
+    double* loss, T gscale, double lscale) {
+    static_assert(LV_WARPS == 2, "two boundary tiles per block");
+    constexpr int V = Vec16<T>::n;
+    __shared__ __align__(16) T ring_all[LV_WARPS][LV_RING][32 * V];
+    __shared__ T bcs_all[LV_WARPS][2 * (LV_EDGE_TY + 4)];
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    const int64_t neb = (q.n_edge + 1) / 2;  // boundary blocks
+    const int64_t b = blockIdx.x;
+    T lsum = T(0);
+    if (b < neb) {
+        const int64_t t = 2 * b + warp;
+        if (t < q.n_edge) {
+            const int64_t nfull = (int64_t)(q.nte - (q.hi - q.lo + 1)) * q.nsw;
+            int sw, ty;
+            if (t < nfull) {
+                const int r = (int)(t / q.nsw);
+                sw = (int)(t - (int64_t)r * q.nsw);
+                ty = r < q.lo ? r : q.hi + 1 + (r - q.lo);
+            } else {
+                const int m = q.nsw - q.sw_hi;
+                const int64_t k = t - nfull;
+                ty = q.lo + (int)(k / m);
+                const int c = (int)(k - (int64_t)(ty - q.lo) * m);
+                sw = c == 0 ? 0 : q.sw_hi + c;
+            }
+            lsum = lg_vec_tile<T, LV_EDGE_TY, false>(g, u, grad, ty * LV_EDGE_TY, sw * (30 * V),
+                                                     lane, gscale, &ring_all[warp][0][0],
+                                                     &bcs_all[warp][0]);
+        }
+    } else {
+        const int64_t ib = b - neb;
+        const int bx = (int)(ib % q.int_grid.x), by = (int)(ib / q.int_grid.x);
+        const int sw = 1 + bx * LV_WARPS + warp;
+        if (sw <= q.sw_hi) {
+            lsum = lg_vec_tile<T, TY, true>(g, u, grad, (1 + by) * TY, sw * (30 * V), lane,
+                                            gscale, &ring_all[warp][0][0], nullptr);
+        }
+    }
+    reduce_finish((double)lsum, b, (int64_t)gridDim.x, ws, lscale, loss);
+}
+
 // Launch plan of the fused loss + adjoint: the vectorised kernels when the
 // rows allow 16-byte accesses, else the one-column-per-lane kernel.
 struct LgPlan {
@@ -549,7 +599,7 @@ LgPlan lg_plan(int nt, int nx, const void* u, const void* grad) {
         pl.ty = cells >= (16 << 20) ? 64 : (cells >= (4 << 20) ? 32 : 16);
         pl.geom = lv_geom<T>(nt, nx, pl.ty);
         pl.grid = dim3(1, pl.geom.nte);
-        pl.blocks = pl.geom.n_int_blocks + pl.geom.n_edge;
+        pl.blocks = pl.geom.n_int_blocks + (pl.geom.n_edge + 1) / 2;
     } else {
         pl.ty = lg_ty(nt, nx);
         pl.grid = lg_grid(nt, nx);
@@ -570,11 +620,7 @@ int64_t lg_max_blocks(int nt, int nx) {
 template <typename T, int TY>
 void lv_launch(const LgPlan& pl, const WaveDev<T>& g, const T* u, T* grad, ReduceWs ws,
                double* loss, T gs, double ls, cudaStream_t s) {
-    if (pl.geom.n_int_blocks > 0) {
-        wave_loss_grad_int_kernel<T, TY><<<pl.geom.int_grid, LV_WARPS * 32, 0, s>>>(
-            g, u, grad, ws, pl.geom.sw_hi, gs);
-    }
-    wave_loss_grad_edge_kernel<T><<<(unsigned)pl.geom.n_edge, 32, 0, s>>>(
+    wave_loss_grad_all_kernel<T, TY><<<(unsigned)pl.blocks, LV_WARPS * 32, 0, s>>>(
         g, u, grad, ws, pl.geom, loss, gs, ls);
 }
 

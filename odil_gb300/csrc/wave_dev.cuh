@@ -299,6 +299,7 @@ __device__ __forceinline__ void ld_run(T (&out)[CPT], const T* __restrict__ p) {
 template <typename T, int CPT, int PF, bool VEC, bool REG = false>
 __device__ __forceinline__ void march_instance(const WaveDev<T>& g, const T* __restrict__ b,
                                                T* __restrict__ x, unsigned char* smem_raw) {
+    static_assert(PF % 2 == 0, "row parity follows the ring slot");
     const int nx = g.nx, nt = g.nt;
     T* ring = reinterpret_cast<T*>(smem_raw);  // [PF][nx] right-hand sides (ring mode)
     T* edge = REG ? ring : ring + PF * nx;     // [2 parity][2 end][kMarchMaxWarps]
@@ -321,12 +322,14 @@ __device__ __forceinline__ void march_instance(const WaveDev<T>& g, const T* __r
     }
     // Edge slots this thread reads (every lane of a warp reads the same word,
     // a broadcast) and whether the value there is a real neighbour.
+    // The first warp's left word and the last warp's right word are the
+    // warp's own ends: finite values that meet k_xm(0) = 0 / k_xp(nx-1) = 0.
     const int wl = warp > 0 ? warp - 1 : 0;
     const int wr = warp + 1 < nwarp ? warp + 1 : warp;
     const bool use_l = lane == 0, use_r = lane == 31;
-    const T mask_l = warp > 0 ? T(1) : T(0);
-    const T mask_r = warp + 1 < nwarp ? T(1) : T(0);
     const bool self_r = nx == 1;
+    // Every thread's run lies inside the row (no columns past its end).
+    const bool full = (int64_t)nwarp * 32 * CPT == nx;
     // Both parities start at 0: row 0 scales its neighbours by 0, which must
     // not meet a stale non-finite word.
     for (int e = threadIdx.x; e < 4 * kMarchMaxWarps; e += blockDim.x) edge[e] = T(0);
@@ -381,9 +384,9 @@ __device__ __forceinline__ void march_instance(const WaveDev<T>& g, const T* __r
             const T c_d1 = i == 1 ? T(1) : T(2);
             const T c_lam = i == 0 ? T(0) : g.lam2;
             // x-neighbours of row i-1 at the ends of this thread's run.
-            const T* eprv = edge + ((i & 1) ^ 1) * 2 * kMarchMaxWarps;
-            const T el = eprv[kMarchMaxWarps + wl] * mask_l;
-            const T er = eprv[wr] * mask_r;
+            const T* eprv = edge + ((s & 1) ^ 1) * 2 * kMarchMaxWarps;  // PF is even
+            const T el = eprv[kMarchMaxWarps + wl];
+            const T er = eprv[wr];
             const T sl = __shfl_up_sync(0xffffffffu, d1[CPT - 1], 1);
             const T sr = __shfl_down_sync(0xffffffffu, d1[0], 1);
             const T left = use_l ? el : sl;
@@ -428,11 +431,13 @@ __device__ __forceinline__ void march_instance(const WaveDev<T>& g, const T* __r
                     }
                 }
             }
+            if (!full) {
 #pragma unroll
-            for (int c = 0; c < CPT; ++c)
-                if (j0 + c >= nx) out.v[c] = T(0);  // columns past the row end
+                for (int c = 0; c < CPT; ++c)
+                    if (j0 + c >= nx) out.v[c] = T(0);  // columns past the row end
+            }
             dst += nx;
-            T* ecur = edge + (i & 1) * 2 * kMarchMaxWarps;
+            T* ecur = edge + (s & 1) * 2 * kMarchMaxWarps;
             if (use_l) ecur[warp] = out.v[0];
             if (use_r) ecur[kMarchMaxWarps + warp] = out.v[CPT - 1];
 #pragma unroll

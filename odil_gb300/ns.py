@@ -157,12 +157,18 @@ class NsDirectNewton:
     The reference solves each Newton step's normal equations with SuperLU
     (util.py:242-268, linsolver.py:28-45).  Here the square Jacobian, with the
     continuity row of the pinned cell replaced by p[pin] = 0, is factored in
-    FP32 as a block-tridiagonal LU (odil_ns_direct_factor) and each step
-    J d = -F is solved by FP64 iterative refinement: the FP32 factors give a
-    correction, the FP64 stencil J d gives the new residual of the linear
-    system, until it falls below `rtol` of -F.  The pressure is fixed at the
-    pinned cell; the reference leaves the constant free, so compare pressures
-    up to a constant.  Forward problem only (neq = 3)."""
+    FP32 as a block-tridiagonal LU (odil_ns_direct_factor), and each step
+    J d = -F is solved by iterative refinement: the FP32 factors give a
+    correction, the FP64 stencil J d (current Jacobian) the new residual of
+    the linear system.  The factors are reused across epochs while the
+    refinement still contracts fast (the Jacobian changes slowly near the
+    solution); a step that needs more than `max_refine` // 2 corrections
+    triggers a new factorisation for the next one.  Each linear system is
+    solved to `rtol` of its right-hand side: the outer iteration converges
+    linearly anyway (the Jacobian leaves out the frozen second-order upwind
+    part, as the reference's does), so an inexact step costs no epochs.  The
+    pressure is fixed at the pinned cell; the reference leaves the constant
+    free, so compare pressures up to a constant.  Forward problem only."""
 
     def __init__(self, kernels, pin=(0, 0)):
         if kernels.neq != 3:
@@ -178,11 +184,13 @@ class NsDirectNewton:
                              % self.n)
         dev = kernels.device
         self.ws = torch.empty(nb, dtype=torch.uint8, device=dev)
-        self.coef = torch.empty((3, 15, self.n, self.n), dtype=torch.float64,
-                                device=dev)
+        shape = (3, 15, self.n, self.n)
+        self.coef = torch.empty(shape, dtype=torch.float64, device=dev)
+        self.coef_fac = torch.empty(shape, dtype=torch.float64, device=dev)
         self.b32 = torch.empty((3, self.n, self.n), dtype=torch.float32,
                                device=dev)
         self.x32 = torch.empty_like(self.b32)
+        self.factored = False
         self.stats = []
 
     def _pinned(self, r, p_field):
@@ -190,61 +198,90 @@ class NsDirectNewton:
         r[2, i, j] = p_field[i, j]
         return r
 
-    def factor(self, u, v, p):
-        k = self.k
-        q = ctypes.byref(k.params[torch.float64])
+    def jacobian(self, u, v, p):
+        q = ctypes.byref(self.k.params[torch.float64])
         call("odil_ns_jacobian_f64", q, ptr(u), ptr(v), ptr(p), ptr(self.coef),
              stream_handle())
-        call("odil_ns_direct_factor", self.n, ptr(self.coef), self.pin,
+
+    def factor(self):
+        """Factors the current Jacobian (call jacobian() first)."""
+        self.coef_fac.copy_(self.coef)
+        call("odil_ns_direct_factor", self.n, ptr(self.coef_fac), self.pin,
              ptr(self.ws), self.ws.numel(), stream_handle())
+        self.factored = True
 
     def solve32(self, b):
         self.b32.copy_(b)
-        call("odil_ns_direct_solve", self.n, ptr(self.coef), self.pin,
+        call("odil_ns_direct_solve", self.n, ptr(self.coef_fac), self.pin,
              ptr(self.ws), self.ws.numel(), ptr(self.b32), ptr(self.x32),
              stream_handle())
         return self.x32
 
     def apply(self, d):
-        """J' d in FP64 (stencil products; pinned row = d_p[pin])."""
+        """J' d in FP64 with the current Jacobian (pinned row = d_p[pin])."""
         J = [[StencilOp(SHIFTS, self.coef[e, 5 * f:5 * f + 5], self.k.shape)
               for f in range(3)] for e in range(3)]
         out = torch.stack(self.k.jv(J, [d[0], d[1], d[2]]))
         return self._pinned(out, d[2])
 
-    def step(self, u, v, p, refine=8, rtol=1e-13):
-        """One Newton step in place; returns the FP64 residual rms before it."""
-        f = self.k.residual(u, v, p)
-        rms = float(torch.sqrt((f**2).mean()))
-        r = self._pinned(f.clone(), p)
-        st = torch.cuda.current_stream(self.k.device)
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record(st)
-        self.factor(u, v, p)
-        e1.record(st)
+    def _refine(self, r, max_refine, rtol):
+        """d with J' d ~= -r by refinement on the current factors; stops at
+        `rtol`, after `max_refine` corrections, or when a correction fails to
+        halve the residual (stale factors)."""
         d = torch.zeros_like(r)
         res = -r
         rn0 = float(torch.linalg.vector_norm(res))
-        it = 0
-        for it in range(1, refine + 1):
-            d += self.solve32(res).double()
-            res = -r - self.apply(d)
-            if float(torch.linalg.vector_norm(res)) <= rtol * rn0:
+        rn, it, ok = rn0, 0, True
+        for it in range(1, max_refine + 1):
+            d_new = d + self.solve32(res).double()
+            res_new = -r - self.apply(d_new)
+            rn_new = float(torch.linalg.vector_norm(res_new))
+            if not rn_new < 0.5 * rn:  # no contraction (or NaN): keep d
+                ok = False
                 break
-        self.stats.append({"rms": rms, "refine": it,
-                           "lin_rel": float(torch.linalg.vector_norm(res)) /
-                           max(rn0, 1e-300),
+            d, res, rn = d_new, res_new, rn_new
+            if rn <= rtol * rn0:
+                break
+        return d, rn, rn0, it, ok and rn <= rtol * rn0
+
+    def step(self, u, v, p, refactor=None, max_refine=8, rtol=1e-13):
+        """One Newton step in place; returns the FP64 residual rms before it.
+        refactor: True / False, or None to factor when the factors are stale
+        (and again within the step if refinement on the old ones stalls)."""
+        f = self.k.residual(u, v, p)
+        rms = float(torch.sqrt((f**2).mean()))
+        r = self._pinned(f.clone(), p)
+        self.jacobian(u, v, p)
+        st = torch.cuda.current_stream(self.k.device)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        did = False
+        e0.record(st)
+        if refactor or not self.factored or (
+                refactor is None and getattr(self, "_stale", True)):
+            self.factor()
+            did = True
+        e1.record(st)
+        d, rn, rn0, it, ok = self._refine(r, max_refine, rtol)
+        if not ok and not did and refactor is None:
+            self.factor()
+            did = True
+            d, rn, rn0, it, ok = self._refine(r, max_refine, rtol)
+        self._stale = not ok or it > max_refine // 2
+        self.stats.append({"rms": rms, "refine": it, "factored": did,
+                           "lin_rel": rn / max(rn0, 1e-300),
                            "factor_ms": e0.elapsed_time(e1)})
         u += d[0]
         v += d[1]
         p += d[2]
         return rms
 
-    def solve(self, u, v, p, epochs=50, tol=1e-10, callback=None):
-        """Newton epochs until the residual rms is below `tol`."""
+    def solve(self, u, v, p, epochs=60, tol=1e-10, rtol=1e-4, callback=None):
+        """Inexact Newton epochs (each linear system to `rtol`) until the
+        residual rms is below `tol`; returns the final rms."""
+        self._stale = True
         for ep in range(epochs):
-            rms = self.step(u, v, p)
+            rms = self.step(u, v, p, rtol=rtol)
             if callback is not None:
                 callback(ep, rms)
             if rms <= tol:
