@@ -184,6 +184,15 @@ typedef struct odil_wave_batch {
     const void* init_ut;
     const void* left_u;
     const void* right_u;
+    const int32_t* row_inst;         /* device [total_rows]: instance of each
+                                        packed time row (rows of instance q
+                                        start at inst[q].offset_t) */
+    int64_t total_rows;
+    const int64_t* bnd_off;          /* device [ninst]: first boundary cell of
+                                        each instance in the boundary-cell
+                                        sequence (rows 0, 1, then columns 0
+                                        and nx-1 of rows 2..) */
+    int64_t total_bnd;
 } odil_wave_batch;
 
 /* Fills the derived constants of a device descriptor array. */

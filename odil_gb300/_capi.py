@@ -99,6 +99,10 @@ class OdilWaveBatch(ctypes.Structure):
         ("init_ut", ctypes.c_void_p),
         ("left_u", ctypes.c_void_p),
         ("right_u", ctypes.c_void_p),
+        ("row_inst", ctypes.c_void_p),
+        ("total_rows", ctypes.c_int64),
+        ("bnd_off", ctypes.c_void_p),
+        ("total_bnd", ctypes.c_int64),
     ]
 
 

@@ -67,6 +67,16 @@ class WaveBatch:
         b.ninst, b.max_nx, b.total_cells = self.n, self.max_nx, self.total
         b.inst, b.order = self.desc.data_ptr(), self.order.data_ptr()
         b.init_u, b.init_ut, b.left_u, b.right_u = [t.data_ptr() for t in self.bc]
+        nts = np.array([sh[0] for sh in self.shapes], np.int64)
+        self.row_inst = torch.as_tensor(
+            np.repeat(np.arange(self.n, dtype=np.int32), nts), device=dev)
+        b.row_inst, b.total_rows = self.row_inst.data_ptr(), int(nts.sum())
+        nbnd = np.array([min(nt, 2) * nx + max(nt - 2, 0) * min(nx, 2)
+                         for nt, nx in self.shapes], np.int64)
+        self.bnd_off = torch.as_tensor(
+            np.concatenate([[0], np.cumsum(nbnd)[:-1]]).astype(np.int64),
+            device=dev)
+        b.bnd_off, b.total_bnd = self.bnd_off.data_ptr(), int(nbnd.sum())
         self.b = b
         kw64 = dict(dtype=torch.float64, device=dev)
         kw32 = dict(dtype=torch.float32, device=dev)

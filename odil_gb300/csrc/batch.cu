@@ -122,61 +122,84 @@ __global__ void __launch_bounds__(256) batch_update_residual_kernel(
     }
 }
 
-// Instance holding packed row r of the row sequence (row offsets offset_t
-// ascending), by binary search; one search per row task, not per cell.
-__device__ __forceinline__ int find_inst_row(const odil_wave_instance* __restrict__ inst, int n,
-                                             int64_t r) {
-    int lo = 0, hi = n - 1;
-    while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (__ldg(&inst[mid].offset_t) <= r) lo = mid; else hi = mid - 1;
-    }
-    return lo;
-}
 
-// Row tasks over all instances: block-strided over the rows of the batch,
-// threads over the columns of the row.  KIND 0: rhs = float(-F(0)) (FP64
-// only on boundary cells); KIND 1: rhs = float(-F(hi + lo)) in the float-pair
-// form (wave_dev.cuh), FP64 only on boundary cells.
+// Interior cells of all instances, one warp per packed time row (the row's
+// instance from the row table), lanes over the columns 1 .. nx-2 of rows
+// >= 2.  KIND 0: rhs = 0 there (F(0) vanishes inside); KIND 1: rhs =
+// float(-F(hi + lo)) in the float-pair form (wave_dev.cuh).  No FP64.
 template <int KIND>
 __global__ void __launch_bounds__(256) batch_rows_kernel(odil_wave_batch b,
                                                          const float* __restrict__ hi,
                                                          const float* __restrict__ lo,
                                                          float* __restrict__ rhs) {
-    const odil_wave_instance last = b.inst[b.ninst - 1];
-    const int64_t rows = last.offset_t + last.nt;
-    const double* iu = (const double*)b.init_u;
-    const double* iut = (const double*)b.init_ut;
-    const double* lu = (const double*)b.left_u;
-    const double* ru = (const double*)b.right_u;
-    for (int64_t r = blockIdx.x; r < rows; r += gridDim.x) {
-        const int q = find_inst_row(b.inst, b.ninst, r);
-        const odil_wave_instance desc = b.inst[q];
-        const WaveDev<double> g = dev_of<double>(desc, iu, iut, lu, ru);
-        const int i = (int)(r - desc.offset_t);
-        float* rrow = rhs + desc.offset + (int64_t)i * g.nx;
-        if (KIND == 0) {
-            const bool brow = i <= 1;
-            for (int j = threadIdx.x; j < g.nx; j += blockDim.x) {
-                float v = 0.f;
-                if (brow || j == 0 || j == g.nx - 1)
-                    v = (float)(-wave_f(g, i, j, 0.0, 0.0, 0.0, 0.0, 0.0));
-                rrow[j] = v;
-            }
-        } else {
-            PairCoef k;
-            k.ah = desc.ah;
-            k.al = desc.al;
-            k.ch = desc.ch;
-            k.cl = desc.cl;
-            k.bh = desc.bh;
-            k.bl = desc.bl;
-            const float* h = hi + desc.offset;
-            const float* l = lo ? lo + desc.offset : nullptr;
-            for (int j = threadIdx.x; j < g.nx; j += blockDim.x)
-                rrow[j] = pair_cell_rhs(g, k, h, l, i, j);
-        }
+    const int lane = threadIdx.x & 31;
+    const int64_t r = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (r >= b.total_rows) return;
+    const odil_wave_instance& d = b.inst[__ldg(b.row_inst + r)];
+    const int i = (int)(r - d.offset_t);
+    const int nx = (int)d.nx;
+    if (i < 2) return;
+    const int64_t off = d.offset;
+    float* rrow = rhs + off + (int64_t)i * nx;
+    if (KIND == 0) {
+        for (int j = 1 + lane; j < nx - 1; j += 32) rrow[j] = 0.f;
+    } else {
+        PairCoef k;
+        k.ah = d.ah;
+        k.al = d.al;
+        k.ch = d.ch;
+        k.cl = d.cl;
+        k.bh = d.bh;
+        k.bl = d.bl;
+        const float* h = hi + off;
+        const float* l = lo ? lo + off : nullptr;
+        for (int j = 1 + lane; j < nx - 1; j += 32)
+            rrow[j] = pair_interior_rhs(k, h, l, (int64_t)i * nx + j, nx);
     }
+}
+
+// Boundary cells of all instances, one thread per cell (full warps): the
+// instance by binary search over the boundary offsets, the cell by
+// bnd_cell, the value in FP64.
+template <int KIND>
+__global__ void __launch_bounds__(256) batch_bnd_kernel(odil_wave_batch b,
+                                                        const float* __restrict__ hi,
+                                                        const float* __restrict__ lo,
+                                                        float* __restrict__ rhs) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= b.total_bnd) return;
+    int a = 0, z = b.ninst - 1;
+    while (a < z) {
+        const int mid = (a + z + 1) >> 1;
+        if (__ldg(b.bnd_off + mid) <= t) a = mid; else z = mid - 1;
+    }
+    const odil_wave_instance desc = b.inst[a];
+    const WaveDev<double> g =
+        dev_of<double>(desc, (const double*)b.init_u, (const double*)b.init_ut,
+                       (const double*)b.left_u, (const double*)b.right_u);
+    int i, j;
+    bnd_cell(t - __ldg(b.bnd_off + a), g.nt, g.nx, &i, &j);
+    PairCoef k;
+    k.ah = desc.ah;
+    k.al = desc.al;
+    k.ch = desc.ch;
+    k.cl = desc.cl;
+    k.bh = desc.bh;
+    k.bl = desc.bl;
+    const int64_t off = desc.offset;
+    rhs[off + (int64_t)i * g.nx + j] =
+        bnd_cell_rhs<KIND>(g, k, hi ? hi + off : nullptr, lo ? lo + off : nullptr, i, j);
+}
+
+template <int KIND>
+int launch_rhs(const odil_wave_batch* b, const float* hi, const float* lo, float* rhs,
+               cudaStream_t s) {
+    if (!b->row_inst || b->total_rows < 1 || !b->bnd_off || b->total_bnd < 1)
+        return ODIL_ERR_ARG;
+    batch_rows_kernel<KIND><<<(unsigned)((b->total_rows + 7) / 8), 256, 0, s>>>(*b, hi, lo, rhs);
+    batch_bnd_kernel<KIND><<<(unsigned)((b->total_bnd + 255) / 256), 256, 0, s>>>(*b, hi, lo,
+                                                                                rhs);
+    return launch_status();
 }
 
 template <int CPT, int PF>
@@ -271,8 +294,7 @@ ODIL_API int odil_wave_batch_initial_rhs_mixed(const odil_wave_batch* b, float* 
     if (st) return st;
     if (!rhs) return ODIL_ERR_ARG;
     if (!b->init_u || !b->init_ut || !b->left_u || !b->right_u) return ODIL_ERR_ARG;
-    batch_rows_kernel<0><<<sms() * 32, 256, 0, as_stream(stream)>>>(*b, nullptr, nullptr, rhs);
-    return launch_status();
+    return launch_rhs<0>(b, nullptr, nullptr, rhs, as_stream(stream));
 }
 
 ODIL_API int odil_wave_batch_pair_residual_mixed(const odil_wave_batch* b, const float* hi,
@@ -281,8 +303,7 @@ ODIL_API int odil_wave_batch_pair_residual_mixed(const odil_wave_batch* b, const
     if (st) return st;
     if (!hi || !rhs || rhs == hi || rhs == lo) return ODIL_ERR_ARG;
     if (!b->init_u || !b->init_ut || !b->left_u || !b->right_u) return ODIL_ERR_ARG;
-    batch_rows_kernel<1><<<sms() * 32, 256, 0, as_stream(stream)>>>(*b, hi, lo, rhs);
-    return launch_status();
+    return launch_rhs<1>(b, hi, lo, rhs, as_stream(stream));
 }
 
 ODIL_API int odil_wave_batch_march_f32(const odil_wave_batch* b, const float* rhs, float* x,

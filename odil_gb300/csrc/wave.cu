@@ -787,32 +787,35 @@ int loss_grad_impl(const odil_wave_params* p, const T* u, T* grad, double* loss,
     return launch_status();
 }
 
-// rhs = float(-F(0)) for the first mixed Newton epoch from u = 0: the
-// residual of the zero field is nonzero only where boundary data enter (rows
-// 0 and 1, columns 0 and nx-1), so only those cells do FP64 work.
-__global__ void __launch_bounds__(256) wave_initial_rhs_kernel(WaveDev<double> g,
-                                                               float* __restrict__ rhs) {
-    const int nx = g.nx;
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= nx) return;
-    for (int i = blockIdx.y; i < g.nt; i += gridDim.y) {
-        float v = 0.f;
-        if (i <= 1 || j == 0 || j == nx - 1) v = (float)(-wave_f(g, i, j, 0.0, 0.0, 0.0, 0.0, 0.0));
-        rhs[(int64_t)i * nx + j] = v;
-    }
-}
-
-// rhs = float(-F(hi + lo)) for a field held as two FP32 arrays (lo may be
-// null): the right-hand side of a mixed Newton epoch without an FP64 state.
-__global__ void __launch_bounds__(256) wave_pair_residual_kernel(WaveDev<double> g, PairCoef k,
+// Right-hand sides of the mixed Newton from zero.  Interior cells (rows >= 2,
+// columns 1 .. nx-2) and boundary cells are separate launches: the interior
+// one has no FP64 instruction, and the boundary one packs the boundary cells
+// into full warps, so its FP64 work is not replicated across idle lanes.
+//   initial:  rhs = float(-F(0)), 0 inside (a memset) and FP64 on the boundary;
+//   pair:     rhs = float(-F(hi + lo)), float-pair inside.
+__global__ void __launch_bounds__(256) wave_pair_interior_kernel(int nt, int nx, PairCoef k,
                                                                  const float* __restrict__ hi,
                                                                  const float* __restrict__ lo,
                                                                  float* __restrict__ rhs) {
-    const int nx = g.nx;
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= nx) return;
-    for (int i = blockIdx.y; i < g.nt; i += gridDim.y)
-        rhs[(int64_t)i * nx + j] = pair_cell_rhs(g, k, hi, lo, i, j);
+    const int j = 1 + blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= nx - 1) return;
+    for (int i = 2 + blockIdx.y; i < nt; i += gridDim.y) {
+        const int64_t c0 = (int64_t)i * nx + j;
+        rhs[c0] = pair_interior_rhs(k, hi, lo, c0, nx);
+    }
+}
+
+template <int KIND>
+__global__ void __launch_bounds__(256) wave_bnd_rhs_kernel(WaveDev<double> g, PairCoef k,
+                                                           const float* __restrict__ hi,
+                                                           const float* __restrict__ lo,
+                                                           float* __restrict__ rhs,
+                                                           int64_t count) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= count) return;
+    int i, j;
+    bnd_cell(t, g.nt, g.nx, &i, &j);
+    rhs[(int64_t)i * g.nx + j] = bnd_cell_rhs<KIND>(g, k, hi, lo, i, j);
 }
 
 template <int CPT, int PF>
@@ -925,9 +928,13 @@ ODIL_API int odil_wave_initial_rhs_mixed(const odil_wave_params* p, float* rhs, 
     int st = make_dev<double>(p, &g, true);
     if (st) return st;
     if (!rhs) return ODIL_ERR_ARG;
-    dim3 grid, block;
-    grid_rows(g, &grid, &block);
-    wave_initial_rhs_kernel<<<grid, block, 0, as_stream(stream)>>>(g, rhs);
+    cudaStream_t s = as_stream(stream);
+    if (cudaMemsetAsync(rhs, 0, (size_t)g.nt * g.nx * sizeof(float), s) != cudaSuccess)
+        return ODIL_ERR_LAUNCH;
+    const int64_t nb = bnd_count(g.nt, g.nx);
+    const PairCoef k{};
+    wave_bnd_rhs_kernel<0><<<(unsigned)((nb + 255) / 256), 256, 0, s>>>(g, k, nullptr, nullptr,
+                                                                       rhs, nb);
     return launch_status();
 }
 
@@ -939,9 +946,15 @@ ODIL_API int odil_wave_pair_residual_mixed(const odil_wave_params* p, const floa
     if (!hi || !rhs || rhs == hi || rhs == lo) return ODIL_ERR_ARG;
     if (!g.init_u || !g.init_ut || !g.left_u || !g.right_u) return ODIL_ERR_ARG;
     const PairCoef k = pair_coef((double)g.A, (double)g.B);
-    dim3 grid, block;
-    grid_rows(g, &grid, &block);
-    wave_pair_residual_kernel<<<grid, block, 0, as_stream(stream)>>>(g, k, hi, lo, rhs);
+    cudaStream_t s = as_stream(stream);
+    if (g.nt > 2 && g.nx > 2) {
+        const int bx = 256;
+        const int gy = g.nt - 2 < 65535 ? g.nt - 2 : 65535;
+        wave_pair_interior_kernel<<<dim3((g.nx - 2 + bx - 1) / bx, gy), bx, 0, s>>>(
+            g.nt, g.nx, k, hi, lo, rhs);
+    }
+    const int64_t nb = bnd_count(g.nt, g.nx);
+    wave_bnd_rhs_kernel<1><<<(unsigned)((nb + 255) / 256), 256, 0, s>>>(g, k, hi, lo, rhs, nb);
     return launch_status();
 }
 

@@ -227,6 +227,37 @@ __device__ __forceinline__ float pair_cell_rhs(const WaveDev<double>& g, const P
     return (float)(-wave_f(g, i, j, uc, utm, utmm, uxm, uxp));
 }
 
+// -F(hi + lo) (KIND 1) or -F(0) (KIND 0) at a boundary cell (row 0 or 1,
+// column 0 or nx-1) in FP64.
+template <int KIND>
+__device__ __forceinline__ float bnd_cell_rhs(const WaveDev<double>& g, const PairCoef& k,
+                                              const float* __restrict__ hi,
+                                              const float* __restrict__ lo, int i, int j) {
+    if (KIND == 0) return (float)(-wave_f(g, i, j, 0.0, 0.0, 0.0, 0.0, 0.0));
+    return pair_cell_rhs(g, k, hi, lo, i, j);
+}
+
+// Boundary cells of an nt x nx grid: rows 0 and 1 (all columns), then columns
+// 0 and nx-1 of rows 2.. .  Count and the cell of index t.
+__host__ __device__ __forceinline__ int64_t bnd_count(int nt, int nx) {
+    const int r = nt < 2 ? nt : 2;
+    const int c = nx < 2 ? nx : 2;
+    return (int64_t)r * nx + (int64_t)(nt > 2 ? nt - 2 : 0) * c;
+}
+__device__ __forceinline__ void bnd_cell(int64_t t, int nt, int nx, int* i, int* j) {
+    const int r = nt < 2 ? nt : 2;
+    const int64_t head = (int64_t)r * nx;
+    if (t < head) {
+        *i = (int)(t / nx);
+        *j = (int)(t - (int64_t)*i * nx);
+    } else {
+        const int c = nx < 2 ? nx : 2;
+        const int64_t u = t - head;
+        *i = 2 + (int)(u / c);
+        *j = (u % c) == 0 ? 0 : nx - 1;
+    }
+}
+
 // ---------------------------------------------------------------------------
 // Forward substitution J x = b, one block marching the rows (the rows are a
 // dependency chain; the parallelism is across x).  Thread t owns the CPT
