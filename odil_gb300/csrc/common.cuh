@@ -58,6 +58,37 @@ __device__ __forceinline__ double f2d_exact(float x) {
     return __longlong_as_double((long long)(sign | (de << 52) | mant));
 }
 
+// (double)h + (double)l, exactly when the sum fits in a double, with integer
+// instructions only in the common case: both normal, exponents at most 28
+// apart, so the aligned integer sum has at most 53 significant bits and is
+// exact.  Other cases (zeros, subnormals, wide gaps) take the FP64 add, which
+// is exact or correctly rounded the same way.
+__device__ __forceinline__ double pair_sum_exact(float h, float l) {
+    unsigned bh = __float_as_uint(h), bl = __float_as_uint(l);
+    unsigned eh = (bh >> 23) & 0xffu, el = (bl >> 23) & 0xffu;
+    if (eh < el) {
+        const unsigned t = bh; bh = bl; bl = t;
+        const unsigned te = eh; eh = el; el = te;
+    }
+    const unsigned d = eh - el;
+    if (el == 0u || eh == 0xffu || d > 28u) return f2d_exact(h) + f2d_exact(l);
+    const long long mh = (long long)((bh & 0x7fffffu) | 0x800000u);
+    const long long ml = (long long)((bl & 0x7fffffu) | 0x800000u);
+    long long M = mh << d;
+    M = ((bh ^ bl) >> 31) ? M - ml : M + ml;  // magnitude of |big| -+ |small|
+    if (M == 0) return 0.0;
+    unsigned long long sign = (unsigned long long)(bh >> 31) << 63;
+    if (M < 0) {  // equal exponents, |small| > |big|: the small one's sign
+        M = -M;
+        sign ^= 1ull << 63;
+    }
+    const int p = 63 - __clzll(M);  // top bit, p <= 52
+    const unsigned long long mant =
+        ((unsigned long long)M << (52 - p)) & ((1ull << 52) - 1ull);
+    const unsigned long long ex = (unsigned long long)(p + (int)el - 150 + 1023);
+    return __longlong_as_double((long long)(sign | (ex << 52) | mant));
+}
+
 // Periodic wrap of an index that is at most one period outside [0, n).
 __device__ __forceinline__ int wrap1(int i, int n) {
     return i < 0 ? i + n : (i >= n ? i - n : i);

@@ -345,9 +345,9 @@ int lincomb_impl(T* out, const T* x, const T* M, int64_t ld, int k, const double
     return launch_status();
 }
 
-// out = hi + lo in FP64 (lo may be null).  The FP32 -> FP64 conversions use
-// integer instructions; the one FP64 add per element is exact whenever the
-// exponents of hi and lo differ by at most 29.
+// out = hi + lo in FP64 (lo may be null), exactly (the sum of two floats
+// with exponents at most 28 apart fits in a double): integer instructions
+// only in that common case, the FP64 add otherwise.
 __global__ void __launch_bounds__(VT) pair_to_f64_kernel(const float* __restrict__ hi,
                                                          const float* __restrict__ lo,
                                                          double* __restrict__ out, int64_t n,
@@ -360,10 +360,17 @@ __global__ void __launch_bounds__(VT) pair_to_f64_kernel(const float* __restrict
             float4 l = make_float4(0.f, 0.f, 0.f, 0.f);
             if (lo) l = __ldcs(reinterpret_cast<const float4*>(lo) + v);
             double2 a, c;
-            a.x = f2d_exact(h.x) + f2d_exact(l.x);
-            a.y = f2d_exact(h.y) + f2d_exact(l.y);
-            c.x = f2d_exact(h.z) + f2d_exact(l.z);
-            c.y = f2d_exact(h.w) + f2d_exact(l.w);
+            if (lo) {
+                a.x = pair_sum_exact(h.x, l.x);
+                a.y = pair_sum_exact(h.y, l.y);
+                c.x = pair_sum_exact(h.z, l.z);
+                c.y = pair_sum_exact(h.w, l.w);
+            } else {
+                a.x = f2d_exact(h.x);
+                a.y = f2d_exact(h.y);
+                c.x = f2d_exact(h.z);
+                c.y = f2d_exact(h.w);
+            }
             __stcs(reinterpret_cast<double2*>(out) + 2 * v, a);
             __stcs(reinterpret_cast<double2*>(out) + 2 * v + 1, c);
         }

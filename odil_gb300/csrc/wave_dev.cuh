@@ -5,6 +5,8 @@
 // reference (wave.py:67-122).
 #pragma once
 
+#include <type_traits>
+
 #include "common.cuh"
 
 namespace odil {
@@ -404,79 +406,90 @@ __device__ __forceinline__ void march_instance(const WaveDev<T>& g, const T* __r
     };
 #pragma unroll
     for (int s = 0; s < PF - 1; ++s) issue(s, s);
-    for (int i0 = 0; i0 < nt; i0 += PF) {
+    // One row; GEN: the general step (rows 0 and 1 of J, rows past nt,
+    // threads past the row end); the middle blocks of PF rows, where none of
+    // these can occur, use the check-free step.
+    auto row = [&](auto gen_tag, int i, int s) {
+        constexpr bool GEN = decltype(gen_tag)::value;
+        issue(i + PF - 1, (s + PF - 1) % PF);
+        // Row 0 of J is the identity; row 1 has no u[i-2] term.
+        const T c_rhs = GEN ? (i == 0 ? T(1) : g.dt2) : g.dt2;
+        const T c_d1 = GEN ? (i == 1 ? T(1) : T(2)) : T(2);
+        const T c_lam = GEN ? (i == 0 ? T(0) : g.lam2) : g.lam2;
+        // x-neighbours of row i-1 at the ends of this thread's run.
+        const T* eprv = edge + ((s & 1) ^ 1) * 2 * kMarchMaxWarps;  // PF is even
+        const T el = eprv[kMarchMaxWarps + wl];
+        const T er = eprv[wr];
+        const T sl = __shfl_up_sync(0xffffffffu, d1[CPT - 1], 1);
+        const T sr = __shfl_down_sync(0xffffffffu, d1[0], 1);
+        const T left = use_l ? el : sl;
+        const T right = self_r ? d1[0] : (use_r ? er : sr);
+        // Threads past the row end read nothing (their columns lie outside
+        // the ring) and carry zeros.
+        Chunk<T, CPT> rhs;
+        if constexpr (REG) {
 #pragma unroll
-        for (int s = 0; s < PF; ++s) {
-            const int i = i0 + s;
-            if (i >= nt) break;
-            issue(i + PF - 1, (s + PF - 1) % PF);
-            // Row 0 of J is the identity; row 1 has no u[i-2] term.
-            const T c_rhs = i == 0 ? T(1) : g.dt2;
-            const T c_d1 = i == 1 ? T(1) : T(2);
-            const T c_lam = i == 0 ? T(0) : g.lam2;
-            // x-neighbours of row i-1 at the ends of this thread's run.
-            const T* eprv = edge + ((s & 1) ^ 1) * 2 * kMarchMaxWarps;  // PF is even
-            const T el = eprv[kMarchMaxWarps + wl];
-            const T er = eprv[wr];
-            const T sl = __shfl_up_sync(0xffffffffu, d1[CPT - 1], 1);
-            const T sr = __shfl_down_sync(0xffffffffu, d1[0], 1);
-            const T left = use_l ? el : sl;
-            const T right = self_r ? d1[0] : (use_r ? er : sr);
-            // Threads past the row end read nothing (their columns lie
-            // outside the ring) and carry zeros.
-            Chunk<T, CPT> rhs;
-            if constexpr (REG) {
-#pragma unroll
-                for (int c = 0; c < CPT; ++c) rhs.v[c] = active ? pre[s][c] : T(0);
-            } else if constexpr (VEC) {
-                cp_async_wait<PF - 1>();  // this thread's copy of row i has landed
-                const T* rrow = ring + s * nx + j0;
-                if (active) {
-                    rhs = *reinterpret_cast<const Chunk<T, CPT>*>(rrow);
-                } else {
-#pragma unroll
-                    for (int c = 0; c < CPT; ++c) rhs.v[c] = T(0);
-                }
+            for (int c = 0; c < CPT; ++c) rhs.v[c] = (!GEN || active) ? pre[s][c] : T(0);
+        } else if constexpr (VEC) {
+            cp_async_wait<PF - 1>();  // this thread's copy of row i has landed
+            const T* rrow = ring + s * nx + j0;
+            if (!GEN || active) {
+                rhs = *reinterpret_cast<const Chunk<T, CPT>*>(rrow);
             } else {
-                cp_async_wait<PF - 1>();
-                const T* rrow = ring + s * nx + j0;
 #pragma unroll
-                for (int c = 0; c < CPT; ++c) rhs.v[c] = j0 + c < nx ? rrow[c] : T(0);
+                for (int c = 0; c < CPT; ++c) rhs.v[c] = T(0);
             }
-            Chunk<T, CPT> out;
+        } else {
+            cp_async_wait<PF - 1>();
+            const T* rrow = ring + s * nx + j0;
 #pragma unroll
-            for (int c = 0; c < CPT; ++c) {
-                const T xm = c == 0 ? left : d1[c - 1];
-                const T xp = c == CPT - 1 ? right : d1[c + 1];
-                const T tprev = c_d1 * d1[c] - d2[c];
-                out.v[c] = c_rhs * rhs.v[c] + tprev +
-                           c_lam * (kxm[c] * xm - ktm[c] * d1[c] + kxp[c] * xp);
-            }
-            if (active) {
-                if constexpr (VEC) {
-                    *reinterpret_cast<Chunk<T, CPT>*>(dst) = out;
-                } else {
+            for (int c = 0; c < CPT; ++c) rhs.v[c] = j0 + c < nx ? rrow[c] : T(0);
+        }
+        Chunk<T, CPT> out;
 #pragma unroll
-                    for (int c = 0; c < CPT; ++c) {
-                        if (j0 + c < nx) dst[c] = out.v[c];
-                    }
+        for (int c = 0; c < CPT; ++c) {
+            const T xm = c == 0 ? left : d1[c - 1];
+            const T xp = c == CPT - 1 ? right : d1[c + 1];
+            const T tprev = c_d1 * d1[c] - d2[c];
+            out.v[c] = c_rhs * rhs.v[c] + tprev +
+                       c_lam * (kxm[c] * xm - ktm[c] * d1[c] + kxp[c] * xp);
+        }
+        if (!GEN || active) {
+            if constexpr (VEC) {
+                *reinterpret_cast<Chunk<T, CPT>*>(dst) = out;
+            } else {
+#pragma unroll
+                for (int c = 0; c < CPT; ++c) {
+                    if (j0 + c < nx) dst[c] = out.v[c];
                 }
             }
-            if (!full) {
+        }
+        if (GEN || !VEC) {
 #pragma unroll
-                for (int c = 0; c < CPT; ++c)
-                    if (j0 + c >= nx) out.v[c] = T(0);  // columns past the row end
-            }
-            dst += nx;
-            T* ecur = edge + (s & 1) * 2 * kMarchMaxWarps;
-            if (use_l) ecur[warp] = out.v[0];
-            if (use_r) ecur[kMarchMaxWarps + warp] = out.v[CPT - 1];
+            for (int c = 0; c < CPT; ++c)
+                if (j0 + c >= nx) out.v[c] = T(0);  // columns past the row end
+        }
+        dst += nx;
+        T* ecur = edge + (s & 1) * 2 * kMarchMaxWarps;
+        if (use_l) ecur[warp] = out.v[0];
+        if (use_r) ecur[kMarchMaxWarps + warp] = out.v[CPT - 1];
 #pragma unroll
-            for (int c = 0; c < CPT; ++c) {
-                d2[c] = d1[c];
-                d1[c] = out.v[c];
+        for (int c = 0; c < CPT; ++c) {
+            d2[c] = d1[c];
+            d1[c] = out.v[c];
+        }
+        __syncthreads();
+    };
+    for (int i0 = 0; i0 < nt; i0 += PF) {
+        if (i0 == 0 || i0 + PF > nt || !full) {
+#pragma unroll
+            for (int s = 0; s < PF; ++s) {
+                if (i0 + s >= nt) break;
+                row(std::true_type{}, i0 + s, s);
             }
-            __syncthreads();
+        } else {
+#pragma unroll
+            for (int s = 0; s < PF; ++s) row(std::false_type{}, i0 + s, s);
         }
     }
     if constexpr (!REG) cp_async_wait<0>();

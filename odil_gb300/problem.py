@@ -113,6 +113,17 @@ class Jacobian:
     def solve(self, rhs):
         return self.kernels.march(rhs.reshape(self.kernels.shape)).reshape(-1)
 
+    def to_csr(self):
+        """J as a device CSR matrix in the reference's layout (what
+        util_op.py:859-937 assembles), for callers that want the explicit
+        matrix; the registered family must expose per-slot coefficients."""
+        if not hasattr(self.kernels, "coefficients"):
+            raise NotImplementedError("this family has no coefficient fields")
+        from .stencil import StencilOp
+        coef = self.kernels.coefficients()
+        return StencilOp(self.kernels.SLOT_SHIFTS, coef,
+                         self.kernels.shape).to_csr()
+
 
 class Problem:
     """util_op.py:566-973."""

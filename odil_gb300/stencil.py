@@ -70,6 +70,34 @@ class StencilOp:
     def ref(self):
         return ctypes.byref(self._s)
 
+    def to_csr(self):
+        """The operator as a device CSR matrix (torch.sparse_csr_tensor) in
+        the reference's column convention (util_op.py:877-896): entry
+        (c, c + shift) with the neighbour index wrapped periodically on every
+        axis, zero coefficients dropped.  Stride 1 only."""
+        if self.stride != 1:
+            raise ValueError("to_csr supports stride 1")
+        dev = self.coef.device
+        n = 1
+        for v in self.nw:
+            n *= v
+        idx = torch.arange(n, device=dev).reshape(self.nw)
+        rows, cols, vals = [], [], []
+        for k, sh in enumerate(self.shifts):
+            col = torch.roll(idx, tuple(-v for v in sh), tuple(range(self.dim)))
+            c = self.coef[k].reshape(-1)
+            keep = c != 0
+            rows.append(idx.reshape(-1)[keep])
+            cols.append(col.reshape(-1)[keep])
+            vals.append(c[keep])
+        r = torch.cat(rows)
+        c = torch.cat(cols)
+        v = torch.cat(vals)
+        order = torch.argsort(r * n + c)
+        coo = torch.sparse_coo_tensor(torch.stack([r[order], c[order]]), v[order],
+                                      (n, n)).coalesce()
+        return coo.to_sparse_csr()
+
     def mul_field(self, u, out=None, alpha=1.0, beta=0.0):
         out = torch.empty(self.nwh, dtype=u.dtype, device=u.device) \
             if out is None else out

@@ -194,6 +194,39 @@ class WaveKernels:
              stream_handle())
         return rhs
 
+    # Shifts (t, x) of the Jacobian's five slots (see wave.cu).
+    SLOT_SHIFTS = ((0, 0), (-1, 0), (-2, 0), (-1, -1), (-1, 1))
+
+    def coefficients(self, dtype=torch.float64):
+        """[5, nt, nx] per-slot coefficient fields of J (the reference's
+        split-shift Jacobian, util_op.py:585-614), from the column-class
+        factors the kernels use."""
+        nt, nx = self.nt, self.nx
+        dev = self.device
+        A = 1.0 / self.dt**2
+        B = self.c**2 / self.dx**2
+        j = torch.arange(nx, device=dev)
+        if nx == 1:
+            ktm = torch.full((nx, ), 20.0 / 3.0, device=dev, dtype=dtype)
+            kxm = torch.zeros(nx, device=dev, dtype=dtype)
+            kxp = torch.full((nx, ), 4.0 / 9.0, device=dev, dtype=dtype)
+        else:
+            edge = (j == 0) | (j == nx - 1)
+            ktm = torch.where(edge, 4.0, 2.0).to(dtype)
+            kxm = torch.where(j == 0, 0.0,
+                              torch.where(j == nx - 1, 4.0 / 3.0, 1.0)).to(dtype)
+            kxp = torch.where(j == nx - 1, 0.0,
+                              torch.where(j == 0, 4.0 / 3.0, 1.0)).to(dtype)
+        i = torch.arange(nt, device=dev)[:, None]
+        one = torch.ones((nt, nx), device=dev, dtype=dtype)
+        cu = torch.where(i == 0, 1.0, A) * one
+        ctm = torch.where(i == 0, 0.0,
+                          torch.where(i == 1, -A, -2.0 * A) + B * ktm[None, :])
+        ctmm = torch.where(i >= 2, A, 0.0) * one
+        cxm = torch.where(i == 0, 0.0, -B * kxm[None, :]) * one
+        cxp = torch.where(i == 0, 0.0, -B * kxp[None, :]) * one
+        return torch.stack([cu, ctm * one, ctmm, cxm, cxp]).to(dtype)
+
     def pair_residual(self, hi, lo, rhs):
         """rhs = float32(-F(hi + lo)) for FP32 arrays hi, lo (lo may be None)."""
         call("odil_wave_pair_residual_mixed", ctypes.byref(self.p64), ptr(hi),

@@ -149,3 +149,20 @@ def test_history_csv_rows_backfill_and_errors(tmp_path):
     h4.close()
     assert out.read_text() == "x,y\n1,0.5\n"
     assert h4.count == 1 and h4.get("y") == [0.5]
+
+
+@pytest.mark.parametrize("shape", [(12, 9), (1, 4), (3, 1), (7, 2)])
+def test_stencil_to_csr_reference_layout(shape):
+    """StencilOp.to_csr() with the oracle's per-shift coefficients gives the
+    CSR matrix the reference assembles (util_op.py:877-896), exactly."""
+    from odil_gb300.stencil import StencilOp
+    from odil_gb300.wave import WaveKernels
+    rng = np.random.default_rng(0)
+    s = W.WaveSetup(*shape, rng.standard_normal(shape[1]),
+                    rng.standard_normal(shape[1]), rng.standard_normal(shape[0]),
+                    rng.standard_normal(shape[0]), c=1.3)
+    co = W.slot_coefficients(s)
+    coef = torch.as_tensor(np.stack([co[sh] for sh in WaveKernels.SLOT_SHIFTS]))
+    J = StencilOp(WaveKernels.SLOT_SHIFTS, coef, shape).to_csr().to_dense()
+    _, Jo = W.linearize(s, np.zeros(shape))
+    assert np.array_equal(J.numpy(), Jo.toarray())

@@ -237,6 +237,27 @@ def test_mixed_newton_from_zero(cuda):
         assert W.rel_err(xh, y.cpu().numpy()) <= tol
 
 
+def test_pair_to_f64_exact(cuda):
+    """u = hi + lo is written exactly (equal to the FP64 sum of the two
+    floats), over wide exponent gaps, cancellations, zeros and both signs."""
+    from odil_gb300._capi import call, ptr, stream_handle
+    g = torch.Generator().manual_seed(5)
+    n = 1 << 20
+    h = torch.randn(n, generator=g, dtype=torch.float64) * \
+        10.0**torch.randint(-6, 6, (n, ), generator=g)
+    l = h * torch.randn(n, generator=g, dtype=torch.float64) * \
+        10.0**(-torch.randint(0, 14, (n, ), generator=g).double())
+    l[::7] = -h[::7] * (1 + 1e-7 * torch.randn(len(h[::7]), generator=g,
+                                                   dtype=torch.float64))
+    l[::11] = 0.0
+    h32, l32 = h.float().to(cuda), l.float().to(cuda)
+    out = torch.empty(n, dtype=torch.float64, device=cuda)
+    for lo in (l32, None):
+        call("odil_pair_to_f64", ptr(h32), ptr(lo), ptr(out), n, stream_handle())
+        ref = h32.double() + (lo.double() if lo is not None else 0.0)
+        assert torch.equal(out, ref)
+
+
 def test_pair_residual_accuracy(cuda):
     """float(-F(hi + lo)) from FP32 arrays agrees with the FP64 residual of
     hi + lo to ~2^-46 of the largest stencil term, also where F cancels to
@@ -320,6 +341,19 @@ def test_generic_operator_matches_fused(cuda):
     l2, g2, _, _ = generic.eval_loss_grad(st)
     assert abs(l1.item() - l2.item()) <= 1e-12 * l2.item()
     assert _rel(g1["u"].cpu().numpy(), g2["u"].cpu().numpy()) < 1e-12
+
+
+@pytest.mark.parametrize("shape", [(1, 4), (3, 1), (12, 9), (7, 2)])
+def test_jacobian_csr_matches_reference_layout(cuda, shape):
+    """Jacobian.to_csr() equals the CSR matrix the reference assembles
+    (util_op.py:859-937, restated by the oracle), entry by entry."""
+    from odil_gb300.problem import Jacobian
+    s = _setup(*shape, seed=3)
+    k = _kernels(s, cuda)
+    J = Jacobian(k, k.shape).to_csr().to_dense().cpu().numpy()
+    _, Jo = W.linearize(s, np.zeros(shape))
+    Jo = Jo.toarray()
+    assert np.abs(J - Jo).max() <= 1e-12 * np.abs(Jo).max()
 
 
 def test_autograd_function_backward(cuda):
