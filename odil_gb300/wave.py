@@ -200,32 +200,32 @@ class WaveKernels:
     def coefficients(self, dtype=torch.float64):
         """[5, nt, nx] per-slot coefficient fields of J (the reference's
         split-shift Jacobian, util_op.py:585-614), from the column-class
-        factors the kernels use."""
+        factors the kernels use (computed in FP64)."""
         nt, nx = self.nt, self.nx
-        dev = self.device
+        kw = dict(device=self.device, dtype=torch.float64)
         A = 1.0 / self.dt**2
         B = self.c**2 / self.dx**2
-        j = torch.arange(nx, device=dev)
+        ktm = torch.full((nx, ), 2.0, **kw)
+        kxm = torch.ones(nx, **kw)
+        kxp = torch.ones(nx, **kw)
         if nx == 1:
-            ktm = torch.full((nx, ), 20.0 / 3.0, device=dev, dtype=dtype)
-            kxm = torch.zeros(nx, device=dev, dtype=dtype)
-            kxp = torch.full((nx, ), 4.0 / 9.0, device=dev, dtype=dtype)
+            ktm[0], kxm[0], kxp[0] = 20.0 / 3.0, 0.0, 4.0 / 9.0
         else:
-            edge = (j == 0) | (j == nx - 1)
-            ktm = torch.where(edge, 4.0, 2.0).to(dtype)
-            kxm = torch.where(j == 0, 0.0,
-                              torch.where(j == nx - 1, 4.0 / 3.0, 1.0)).to(dtype)
-            kxp = torch.where(j == nx - 1, 0.0,
-                              torch.where(j == 0, 4.0 / 3.0, 1.0)).to(dtype)
-        i = torch.arange(nt, device=dev)[:, None]
-        one = torch.ones((nt, nx), device=dev, dtype=dtype)
-        cu = torch.where(i == 0, 1.0, A) * one
-        ctm = torch.where(i == 0, 0.0,
-                          torch.where(i == 1, -A, -2.0 * A) + B * ktm[None, :])
-        ctmm = torch.where(i >= 2, A, 0.0) * one
-        cxm = torch.where(i == 0, 0.0, -B * kxm[None, :]) * one
-        cxp = torch.where(i == 0, 0.0, -B * kxp[None, :]) * one
-        return torch.stack([cu, ctm * one, ctmm, cxm, cxp]).to(dtype)
+            ktm[0] = ktm[-1] = 4.0
+            kxm[0], kxm[-1] = 0.0, 4.0 / 3.0
+            kxp[0], kxp[-1] = 4.0 / 3.0, 0.0
+        cu = torch.full((nt, nx), A, **kw)
+        ctm = (-2.0 * A + B * ktm)[None, :].repeat(nt, 1)
+        ctmm = torch.full((nt, nx), A, **kw)
+        cxm = (-B * kxm)[None, :].repeat(nt, 1)
+        cxp = (-B * kxp)[None, :].repeat(nt, 1)
+        cu[0] = 1.0
+        for c in (ctm, ctmm, cxm, cxp):
+            c[0] = 0.0
+        ctmm[:2] = 0.0
+        if nt > 1:
+            ctm[1] = -A + B * ktm
+        return torch.stack([cu, ctm, ctmm, cxm, cxp]).to(dtype)
 
     def pair_residual(self, hi, lo, rhs):
         """rhs = float32(-F(hi + lo)) for FP32 arrays hi, lo (lo may be None)."""

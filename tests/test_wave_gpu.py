@@ -237,6 +237,39 @@ def test_mixed_newton_from_zero(cuda):
         assert W.rel_err(xh, y.cpu().numpy()) <= tol
 
 
+def test_captured_solve_replays_with_new_inputs(cuda):
+    """newton.CapturedSolve: a replay equals the eager solve, and refilling
+    the captured input buffers (new boundary data) changes the result as an
+    eager solve with that data would."""
+    from odil_gb300 import newton
+    from odil_gb300.domain import State
+    from odil_gb300.problem import Problem
+    from odil_gb300.workloads import WaveInstance
+    n = 128
+    inst = WaveInstance(n, n, profile="sine", seed=1, nmodes=8, device=cuda)
+    prob = Problem(inst.operator, inst.domain)
+    k = prob.kernels
+    u = torch.zeros((n, n), dtype=torch.float64, device=cuda)
+    st = State(fields={"u": u})
+    host = [k.bc64[i].cpu().pin_memory() for i in range(4)]
+    out = torch.empty((n, n), dtype=torch.float64).pin_memory()
+    cap = newton.CapturedSolve(prob, st, "mixed", 2,
+                               inputs=list(zip(host, k.bc64)),
+                               outputs=[(u, out)])
+    for scale in (1.0, -0.5):
+        for h in host:
+            h.mul_(scale)
+        cap()
+        torch.cuda.synchronize()
+        got = out.clone()
+        ref = torch.zeros_like(u)
+        for h, d in zip(host, k.bc64):
+            d.copy_(h)
+        newton.solve(prob, State(fields={"u": ref}), "mixed", 2,
+                     from_zero=True)
+        assert torch.equal(got, ref.cpu())
+
+
 def test_pair_to_f64_exact(cuda):
     """u = hi + lo is written exactly (equal to the FP64 sum of the two
     floats), over wide exponent gaps, cancellations, zeros and both signs."""
