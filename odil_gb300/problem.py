@@ -225,6 +225,44 @@ class Problem:
                  for n, g in zip(names, gg)}
         return loss.detach(), grads, {}, [l.detach() for l in loss_split]
 
+    def eval_diag(self, state, epoch=0, nsmp=10, generator=None):
+        """util_op.py:675-731: stochastic estimate of the diagonal of
+        sum_k J_k^T J_k / N_k as the mean over `nsmp` samples of g^2, with
+        g = sum_k J_k^T z_k / sqrt(N_k) and z_k ~ N(0, 1) per residual cell.
+        Registered families form J^T z with their adjoint kernel; generic
+        operators by autograd.  Returns the packed diagonal."""
+        self.init_missing(state)
+        self._check_device(state)
+        names = self.domain.fieldnames
+        acc = None
+        for _ in range(nsmp):
+            if self.kernels is not None:
+                k = self.kernels
+                u = state.fields[names[0]]
+                z = torch.randn(k.shape, dtype=u.dtype, device=u.device,
+                                generator=generator)
+                z /= float(z.numel())**0.5
+                g = k.jtv(z).reshape(-1)
+            else:
+                fields = {n: v.detach().requires_grad_(True)
+                          for n, v in state.fields.items()}
+                ff = self._generic(fields, epoch)
+                lossn = 0
+                for f in ff:
+                    if isinstance(f, Problem.Raw):
+                        lossn = lossn + f.value
+                    else:
+                        z = torch.randn(f.shape, dtype=f.dtype,
+                                        device=f.device, generator=generator)
+                        lossn = lossn + (f * z).sum() / float(f.numel())**0.5
+                gg = torch.autograd.grad(lossn, [fields[n] for n in names],
+                                         allow_unused=True)
+                g = torch.cat([(x if x is not None else
+                                torch.zeros_like(fields[n])).reshape(-1)
+                               for n, x in zip(names, gg)])
+            acc = g * g if acc is None else acc + g * g
+        return acc / nsmp
+
     def loss(self, u):
         """Differentiable loss of the packed state (torch.autograd.Function
         over the fused adjoint for registered families)."""

@@ -108,10 +108,52 @@ def optimize_opt(args, optname, problem, state, callback=None, **kwargs):
     return packed, info
 
 
+def optimize_jacobi(args, problem, state, callback=None):
+    """util.py:320-362: gradient steps preconditioned by a running estimate
+    of diag(sum_k J_k^T J_k / N_k) (Problem.eval_diag): nsmp0 samples
+    before the first epoch, nsmp1 more per epoch with weight jac_factor;
+    step -lr/2 g / (diag + jac_epsilon)."""
+    opt = optimizer_mod.Optimizer(name='jacobi', displayname='Jacobi')
+    problem.init_missing(state)
+    packed = problem.pack_state(state)
+    dhistory = defaultdict(list)
+    nsmp0 = getattr(args, "jac_nsmp0", 50)
+    nsmp1 = getattr(args, "jac_nsmp1", 1)
+    factor = getattr(args, "jac_factor", 1.0)
+    epsilon = getattr(args, "jac_epsilon", 1e-8)
+    lr = getattr(args, "lr", 1e-3)
+    epoch_start = getattr(args, "epoch_start", 0)
+    diag = problem.eval_diag(state, epoch=epoch_start, nsmp=nsmp0)
+    ntotal = nsmp0
+    for epoch in range(epoch_start, args.epochs + 1):
+        s = problem.unpack_state(packed)
+        problem.domain.assign_active_state(state, s)
+        loss, grads, _, loss_split = problem.eval_loss_grad(state, epoch=epoch)
+        diag1 = problem.eval_diag(state, epoch=epoch, nsmp=nsmp1)
+        diag = (diag * ntotal + diag1 * nsmp1 * factor) / \
+            (ntotal + nsmp1 * factor)
+        ntotal += nsmp1
+        g = problem.pack_fields(grads)
+        dpacked = -(g / (diag + epsilon)) * (lr * 0.5)
+        opt.last_loss = loss
+        opt.last_residual = [v**0.5 if v >= 0 else v for v in loss_split]
+        if callback:
+            callback(packed, epoch, dhistory=dhistory, opt=opt)
+        if epoch == args.epochs:
+            break
+        opt.evals += 1
+        packed += dpacked
+    s = problem.unpack_state(packed)
+    problem.domain.assign_active_state(state, s)
+    return packed
+
+
 def optimize(args, optname, problem, state, callback=None, **kwargs):
     """util.py:365-370."""
     if optname == 'newton':
         return optimize_newton(args, problem, state, callback)
+    if optname == 'jacobi':
+        return optimize_jacobi(args, problem, state, callback)
     return optimize_opt(args, optname, problem, state, callback, **kwargs)
 
 
@@ -133,3 +175,11 @@ def add_arguments(parser):
     parser.add_argument('--adam_beta_2', type=float, default=None)
     parser.add_argument('--outdir', type=str, default='.',
                         help="Output directory")
+    parser.add_argument('--jac_nsmp0', type=int, default=50,
+                        help="Jacobi: samples for the initial diagonal")
+    parser.add_argument('--jac_nsmp1', type=int, default=1,
+                        help="Jacobi: samples per epoch")
+    parser.add_argument('--jac_factor', type=float, default=1,
+                        help="Jacobi: weight of the new samples")
+    parser.add_argument('--jac_epsilon', type=float, default=1e-8,
+                        help="Jacobi: added to the diagonal")

@@ -152,3 +152,40 @@ def test_lbfgs_wave_1024(cuda):
             assert losses[-1] < l0
         else:
             assert losses[-1] <= l0 * (1 + 30e-6)
+
+
+def test_eval_diag_and_jacobi_optimizer(cuda):
+    """Problem.eval_diag (util_op.py:675-731) estimates diag(J^T J)/N: with
+    many samples it matches the exact diagonal from the oracle's CSR
+    Jacobian, for the fused adjoint and for the op-by-op generic operator;
+    the Jacobi optimizer (util.py:320-362) then lowers the loss."""
+    import argparse
+    from oracle import wave as W
+    from odil_gb300 import util
+    from odil_gb300.domain import State
+    from odil_gb300.problem import Problem
+    from odil_gb300.workloads import WaveInstance
+    nt, nx = 16, 12
+    inst = WaveInstance(nt, nx, profile="sine", seed=2, nmodes=3, device=cuda)
+    s = W.WaveSetup(nt, nx, inst.operator.init_u, inst.operator.init_ut,
+                    inst.operator.left_u, inst.operator.right_u,
+                    c=inst.operator.c)
+    _, J = W.linearize(s, np.zeros((nt, nx)))
+    exact = np.asarray(J.multiply(J).sum(axis=0)).ravel() / (nt * nx)
+    fused = Problem(inst.operator, inst.domain)
+    generic = Problem(lambda mod, ctx: inst.operator(mod, ctx), inst.domain)
+    for prob in (fused, generic):
+        st = State(fields={"u": torch.zeros((nt, nx), dtype=torch.float64,
+                                            device=cuda)})
+        g = torch.Generator(device=cuda)
+        g.manual_seed(0)
+        d = prob.eval_diag(st, nsmp=4000, generator=g).cpu().numpy()
+        assert np.median(np.abs(d / exact - 1)) < 0.05
+    st = State(fields={"u": torch.zeros((nt, nx), dtype=torch.float64,
+                                        device=cuda)})
+    args = argparse.Namespace(epochs=300, lr=0.5, jac_nsmp0=50, jac_nsmp1=1,
+                              jac_factor=1.0, jac_epsilon=1e-8)
+    losses = []
+    util.optimize_jacobi(args, fused, st,
+                         lambda p, e, **kw: losses.append(float(kw["opt"].last_loss)))
+    assert losses[-1] < 0.2 * losses[0]
