@@ -62,7 +62,8 @@ def parse():
     ap.add_argument("--case", default=None,
                     choices=("march", "march64", "update_residual", "loss_grad",
                              "loss_grad64", "loss_grad_big", "lbfgs_iter",
-                             "adam_iter", "batch", "ns_newton", "advect"),
+                             "adam_iter", "batch", "ns_newton", "advect",
+                             "ns_inverse"),
                     help="run one kernel of the workload --steps times (for "
                     "profiler captures) instead of the benchmark")
     return ap.parse_args()
@@ -306,7 +307,9 @@ def run_batch(dev, with_oracle, steps=5):
     out = {"instances": len(insts), "cells": cells,
            "ms_per_batch": ms, "value": len(insts) / (ms / 1000.0),
            "unit": "solves/s", "march_cfg": cfg,
-           "launches_per_batch": 2 * BATCH_EPOCHS + 1,
+           # kernels: rhs (interior + boundary), march, then per further
+           # epoch rhs (2) + march, and the FP64 write.
+           "launches_per_batch": 3 * BATCH_EPOCHS + 1,
            "epochs": BATCH_EPOCHS, "plain_fp64_epochs": BATCH_FP64_EPOCHS,
            "l2": "not flushed: packed arrays larger than L2",
            "plain_fp64_per_instance": {"ms": plain_ms,
@@ -501,7 +504,9 @@ def run_ours(args):
                              "substitution), %d epochs" % MIXED_EPOCHS,
                    "l2": "flushed (256 MiB write) before every timed solve",
                    "parallelism": "replicas" if world > 1 else "single"},
-        "gpu_launches": (2 * MIXED_EPOCHS + 1) * args.steps,
+        # kernels per solve: boundary rhs (the interior is a memset), march,
+        # per further epoch pair rhs (interior + boundary) + march, FP64 write.
+        "gpu_launches": (3 * MIXED_EPOCHS) * args.steps,
         "march_cfg": getattr(k, "_march_cfg", None),
         "march_tune": getattr(k, "march_tune_table", None),
         "clocks": clk,
@@ -616,6 +621,50 @@ def run_ns_newton(args):
                       "workspace_GB": solver.ws.numel() / 1e9}))
 
 
+def run_ns_inverse(args):
+    """Inverse lid-driven cavity (Re = 400, n x n, n = 512 unless ODIL_NS_N
+    is set): 256 seeded interior points of the forward solution with
+    Gaussian noise (sigma 0.01) imposed, Laplacian penalty 1e-4; Gauss-Newton
+    from rest with PCG on the normal equations (block-LU preconditioner) for
+    --steps epochs.  Prints per-epoch times, CG iterations, the loss history
+    and the reconstruction error against the forward solution."""
+    import torch
+    from odil_gb300.ns import (NsCavityOperator, NsKernels, NsDirectNewton,
+                               NsGaussNewton)
+    dev = torch.device("cuda", 0)
+    n = int(os.environ.get("ODIL_NS_N", "512"))
+    fk = NsKernels(n, NsCavityOperator(400.0), device=dev)
+    fw = [torch.zeros((n, n), dtype=torch.float64, device=dev) for _ in range(3)]
+    NsDirectNewton(fk).solve(*fw, epochs=60, tol=1e-10)
+    rng = np.random.default_rng(SEED)
+    mask = np.zeros((n, n))
+    mask.ravel()[rng.choice(n * n, 256, replace=False)] = 1.0
+    uimp = fw[0].cpu().numpy() + 0.01 * rng.standard_normal((n, n))
+    vimp = fw[1].cpu().numpy() + 0.01 * rng.standard_normal((n, n))
+    k = NsKernels(n, NsCavityOperator(400.0, mask=mask, u_imp=uimp,
+                                      v_imp=vimp, kreg=1e-4), device=dev)
+    t = [torch.zeros((n, n), dtype=torch.float64, device=dev) for _ in range(3)]
+    gn = NsGaussNewton(k)
+    times = []
+    for ep in range(args.steps):
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        gn.step(*t, rtol=1e-3)
+        torch.cuda.synchronize(dev)
+        times.append(time.perf_counter() - t0)
+    f = k.residual(*t)
+    loss = float((f**2).mean(dim=(1, 2)).sum())
+    err = [float(torch.linalg.vector_norm(a - b) / torch.linalg.vector_norm(b))
+           for a, b in zip(t[:2], fw[:2])]
+    print(json.dumps({"case": "ns_inverse", "n": n, "Re": 400.0,
+                      "imposed": 256, "noise": 0.01, "kreg": 1e-4,
+                      "epochs": len(times), "s_per_epoch": times,
+                      "cg_iters": [st["cg"] for st in gn.stats],
+                      "loss_history": [st["loss"] for st in gn.stats],
+                      "final_loss": loss,
+                      "rel_err_uv_vs_forward": err}))
+
+
 def run_advect(args):
     """2D advection on an n^3 (t, x, y) grid (n = 256 unless ODIL_ADV_N is
     set), 8 seeded periodic blobs: mixed Newton (FP64 residual, FP32
@@ -716,6 +765,8 @@ def main():
         run_ns_newton(args)
     elif args.case == "advect":
         run_advect(args)
+    elif args.case == "ns_inverse":
+        run_ns_inverse(args)
     elif args.case:
         run_case(args)
     elif args.impl == "reference":

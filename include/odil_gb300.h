@@ -349,6 +349,11 @@ int odil_ns_direct_check(int64_t n, const void* workspace, void* stream);
 int odil_ns_direct_solve(int64_t n, const double* coef, int64_t pin,
                          void* workspace, int64_t workspace_bytes,
                          const float* b, float* x, void* stream);
+/* The transposed solve J'^T x = b with the same factors (the preconditioner
+ * (J'^T J')^-1 of the inverse problem's normal equations needs both). */
+int odil_ns_direct_solve_t(int64_t n, const double* coef, int64_t pin,
+                           void* workspace, int64_t workspace_bytes,
+                           const float* b, float* x, void* stream);
 
 /* ------------------------------------------------------------------------
  * Operators in stencil form (the reference's SparseOperator,

@@ -192,6 +192,37 @@ __global__ void nd_scatter(int n, const float* __restrict__ y, float* __restrict
     x[(int64_t)f * N + k * n + j] = y[i];
 }
 
+// y (block-major) from b (field-major).
+__global__ void nd_gather(int n, const float* __restrict__ b, float* __restrict__ y) {
+    const int64_t N = (int64_t)n * n;
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= 3 * N) return;
+    const int64_t k = i / (3 * n);
+    const int r = (int)(i - k * 3 * n);
+    const int f = r / n, j = r - f * n;
+    y[i] = b[(int64_t)f * N + k * n + j];
+}
+
+// t = y_k - L_{k+1}^T x_{k+1}: (L^T x)[(f, j)] = sum_e L[(e, j), (f, j)] x[(e, j)]
+// with L_{k+1}[(e, j), (f, j)] the slot-1 coefficient at cell (k+1, j) (zero
+// on the pinned row).
+__global__ void nd_rhs_t(const double* __restrict__ coef, int n, int k1, int pin_k, int pin_j,
+                         const float* __restrict__ yk, const float* __restrict__ x1,
+                         float* __restrict__ t) {
+    const int m = 3 * n;
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= m) return;
+    const int f = r / n, j = r - f * n;
+    const int64_t N = (int64_t)n * n;
+    float v = yk[r];
+#pragma unroll
+    for (int e = 0; e < 3; ++e) {
+        if (e == 2 && k1 == pin_k && j == pin_j) continue;
+        v -= cf(coef, N, n, e, f, 1, k1, j) * x1[e * n + j];
+    }
+    t[r] = v;
+}
+
 int check(int64_t n, int64_t pin) {
     if (n < 2 || n > 4096) return ODIL_ERR_SHAPE;
     if (pin < 0 || pin >= n * n) return ODIL_ERR_ARG;
@@ -328,6 +359,63 @@ ODIL_API int odil_ns_direct_solve(int64_t n, const double* coef, int64_t pin, vo
             return ODIL_ERR_LAUNCH;
     }
     const int64_t tot = 3 * (int64_t)n * n;
+    nd_scatter<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(nn, y, x);
+    return launch_status();
+}
+
+// Transposed solve J'^T x = b with the same factors: J' = Lt Ut with Lt block
+// lower bidiagonal (diagonal S_k, subdiagonal L_k) and Ut block upper
+// bidiagonal (identity diagonal, superdiagonal W_k = S_k^-1 U_k), so
+// Ut^T y = b:  y_k = b_k - W_{k-1}^T y_{k-1};
+// Lt^T x = y:  x_k = S_k^-T (y_k - L_{k+1}^T x_{k+1}).
+// Transposed GEMVs on the stored S_k^-1 and W_k.
+ODIL_API int odil_ns_direct_solve_t(int64_t n, const double* coef, int64_t pin, void* ws,
+                                    int64_t ws_bytes, const float* b, float* x, void* stream) {
+    int st = check(n, pin);
+    if (st) return st;
+    if (!coef || !ws || !b || !x) return ODIL_ERR_ARG;
+    int64_t lwork = 0;
+    if ((st = lwork_of(n, &lwork))) return st;
+    const NdLayout q = nd_layout(n, lwork);
+    if (ws_bytes < q.total) return ODIL_ERR_WORKSPACE;
+    cudaStream_t s = as_stream(stream);
+    cusolverDnHandle_t sol;
+    cublasHandle_t blas;
+    if ((st = handles(s, &sol, &blas))) return st;
+    char* base = reinterpret_cast<char*>(ws);
+    const float* INV = reinterpret_cast<const float*>(base + q.off_lu);
+    const float* W = reinterpret_cast<const float*>(base + q.off_w);
+    float* y = reinterpret_cast<float*>(base + q.off_y);
+    float* t = reinterpret_cast<float*>(base + q.off_t);
+    const int m = (int)q.m, nn = (int)n;
+    const int pk = (int)(pin / n), pj = (int)(pin % n);
+    const int64_t mm = (int64_t)m * m;
+    const int tb = 128, rb = (m + tb - 1) / tb;
+    const float minus1 = -1.f, one = 1.f, zero = 0.f;
+    if (cublasSetPointerMode(blas, CUBLAS_POINTER_MODE_HOST) != CUBLAS_STATUS_SUCCESS)
+        return ODIL_ERR_LAUNCH;
+    const int64_t tot = 3 * (int64_t)n * n;
+    nd_gather<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(nn, b, y);
+    for (int k = 1; k < nn; ++k) {
+        if (cublasSgemv(blas, CUBLAS_OP_T, m, m, &minus1, W + (k - 1) * mm, m,
+                        y + (int64_t)(k - 1) * m, 1, &one, y + (int64_t)k * m, 1) !=
+            CUBLAS_STATUS_SUCCESS)
+            return ODIL_ERR_LAUNCH;
+    }
+    // x overwrites y block by block from the last one (x_{k+1} is read
+    // before block k is overwritten).
+    for (int k = nn - 1; k >= 0; --k) {
+        float* yk = y + (int64_t)k * m;
+        if (k + 1 < nn) {
+            nd_rhs_t<<<rb, tb, 0, s>>>(coef, nn, k + 1, pk, pj, yk, yk + m, t);
+        } else if (cudaMemcpyAsync(t, yk, m * sizeof(float), cudaMemcpyDeviceToDevice, s) !=
+                   cudaSuccess) {
+            return ODIL_ERR_LAUNCH;
+        }
+        if (cublasSgemv(blas, CUBLAS_OP_T, m, m, &one, INV + k * mm, m, t, 1, &zero, yk, 1) !=
+            CUBLAS_STATUS_SUCCESS)
+            return ODIL_ERR_LAUNCH;
+    }
     nd_scatter<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(nn, y, x);
     return launch_status();
 }

@@ -288,3 +288,103 @@ class NsDirectNewton:
                 break
         f = self.k.residual(u, v, p)
         return float(torch.sqrt((f**2).mean()))
+
+
+class NsGaussNewton:
+    """Gauss-Newton for the cavity with imposed points and/or the Laplacian
+    penalty (the inverse problem, ns_steady.py:396-411), whose Jacobian J
+    stacks more residual terms than unknowns.  The reference solves each
+    step's normal equations J^T J d = -J^T f with SuperLU (linsolver.py:
+    35-45).  Here they are solved by preconditioned CG in FP64 (J^T J v by
+    stencil products), with the preconditioner (J3'^T J3')^-1 applied by the
+    FP32 block-tridiagonal factors of the forward Jacobian J3' (the three
+    flow equations, continuity row of the pinned cell replaced): one
+    transposed and one forward block solve per iteration.  The pressure
+    constant is the null space of J^T J; CG stays in its complement since
+    J^T f is orthogonal to it.  Each system is solved to `rtol`."""
+
+    def __init__(self, kernels, pin=(0, 0)):
+        if kernels.neq <= 3:
+            raise ValueError("use NsDirectNewton for the forward problem")
+        self.k = kernels
+        self.n = kernels.n
+        self.pin = int(pin[0]) * self.n + int(pin[1])
+        lib = _capi.load()
+        nb = lib.odil_ns_direct_workspace_bytes(self.n)
+        if nb <= 0:
+            raise ValueError("cavity side %d outside the direct solver's range"
+                             % self.n)
+        dev = kernels.device
+        self.ws = torch.empty(nb, dtype=torch.uint8, device=dev)
+        self.coef = torch.empty((kernels.neq, 15, self.n, self.n),
+                                dtype=torch.float64, device=dev)
+        self.b32 = torch.empty((3, self.n, self.n), dtype=torch.float32,
+                               device=dev)
+        self.x32 = torch.empty_like(self.b32)
+        self.y32 = torch.empty_like(self.b32)
+        self.stats = []
+
+    def _J(self):
+        return [[StencilOp(SHIFTS, self.coef[e, 5 * f:5 * f + 5], self.k.shape)
+                 for f in range(3)] for e in range(self.k.neq)]
+
+    def _prec(self, r):
+        """(J3'^T J3')^-1 r in FP32 by the block factors."""
+        self.b32.copy_(r)
+        args = (self.n, ptr(self.coef), self.pin, ptr(self.ws), self.ws.numel())
+        call("odil_ns_direct_solve_t", *args, ptr(self.b32), ptr(self.y32),
+             stream_handle())
+        call("odil_ns_direct_solve", *args, ptr(self.y32), ptr(self.x32),
+             stream_handle())
+        return self.x32.double()
+
+    def step(self, u, v, p, rtol=1e-3, maxit=2000):
+        """One Gauss-Newton step in place; returns the loss sum_e mean f_e^2
+        before it and records the CG iterations."""
+        k = self.k
+        f = k.residual(u, v, p)
+        loss = float((f**2).mean(dim=(1, 2)).sum())
+        q = ctypes.byref(k.params[torch.float64])
+        call("odil_ns_jacobian_f64", q, ptr(u), ptr(v), ptr(p), ptr(self.coef),
+             stream_handle())
+        call("odil_ns_direct_factor", self.n, ptr(self.coef), self.pin,
+             ptr(self.ws), self.ws.numel(), stream_handle())
+        J = self._J()
+
+        def normal(w):
+            return torch.stack(k.jtv(J, k.jv(J, [w[0], w[1], w[2]])))
+
+        b = -torch.stack(k.jtv(J, list(f)))
+        x = torch.zeros_like(b)
+        r = b.clone()
+        z = self._prec(r)
+        pdir = z.clone()
+        rz = float((r * z).sum())
+        nb = float(torch.linalg.vector_norm(b))
+        it = 0
+        for it in range(1, maxit + 1):
+            ap = normal(pdir)
+            alpha = rz / float((pdir * ap).sum())
+            x += alpha * pdir
+            r -= alpha * ap
+            if float(torch.linalg.vector_norm(r)) <= rtol * nb:
+                break
+            z = self._prec(r)
+            rz_new = float((r * z).sum())
+            pdir = z + (rz_new / rz) * pdir
+            rz = rz_new
+        self.stats.append({"loss": loss, "cg": it,
+                           "lin_rel": float(torch.linalg.vector_norm(r)) /
+                           max(nb, 1e-300)})
+        u += x[0]
+        v += x[1]
+        p += x[2]
+        return loss
+
+    def solve(self, u, v, p, epochs=30, rtol=1e-3, callback=None):
+        for ep in range(epochs):
+            loss = self.step(u, v, p, rtol=rtol)
+            if callback is not None:
+                callback(ep, loss)
+        f = self.k.residual(u, v, p)
+        return float((f**2).mean(dim=(1, 2)).sum())

@@ -156,3 +156,29 @@ def test_direct_newton_reaches_reference_cavity(cuda):
         assert np.abs(x.cpu().numpy() - ref).max() <= 1e-5 * np.abs(ref).max()
     dp = t[2].cpu().numpy() - GOLD["Re400_p"]
     assert np.abs(dp - dp.mean()).max() <= 1e-5 * np.abs(GOLD["Re400_p"]).max()
+
+
+def test_gauss_newton_inverse_step_matches_oracle(cuda):
+    """One Gauss-Newton step of the inverse cavity (imposed points, Laplacian
+    penalty): PCG on the normal equations with the block-LU preconditioner
+    gives the oracle's normal-equation update (SuperLU, as the reference) in
+    u, v, and in p up to the pressure constant (the null space of J^T J)."""
+    from odil_gb300.ns import NsGaussNewton
+    n = 24
+    rng = np.random.default_rng(5)
+    kw = _setup(n, "inverse", rng)
+    st = {c: 0.05 * rng.standard_normal((n, n)) for c in "uvp"}
+    s = NS.NsSetup(n, 400.0, mask=kw["mask"], u_imp=kw["u_imp"],
+                   v_imp=kw["v_imp"], alpha=1.0, kreg=kw["kreg"])
+    ref = NS.newton(s, st, epochs=1)
+    k = _kernels(n, 400.0, kw, cuda)
+    t = [torch.as_tensor(st[c], device=cuda).clone() for c in "uvp"]
+    gn = NsGaussNewton(k, pin=(3, 5))
+    gn.step(*t, rtol=1e-11)
+    assert gn.stats[-1]["cg"] < 300
+    for c, x in zip("uv", t[:2]):
+        d = x.cpu().numpy() - ref[c]
+        assert np.abs(d).max() <= 1e-6 * np.abs(ref[c] - st[c]).max(), c
+    dp = (t[2].cpu().numpy() - st["p"]) - (ref["p"] - st["p"])
+    scale = np.abs(ref["p"] - st["p"] - (ref["p"] - st["p"]).mean()).max()
+    assert np.abs(dp - dp.mean()).max() <= 1e-6 * scale

@@ -181,11 +181,27 @@ def test_eval_diag_and_jacobi_optimizer(cuda):
         g.manual_seed(0)
         d = prob.eval_diag(st, nsmp=4000, generator=g).cpu().numpy()
         assert np.median(np.abs(d / exact - 1)) < 0.05
-    st = State(fields={"u": torch.zeros((nt, nx), dtype=torch.float64,
-                                        device=cuda)})
-    args = argparse.Namespace(epochs=300, lr=0.5, jac_nsmp0=50, jac_nsmp1=1,
+    # One epoch is the reference's update: packed -= lr/2 g / (diag + eps)
+    # with diag the running mean of nsmp0 then nsmp1 samples.
+    args = argparse.Namespace(epochs=1, lr=0.5, jac_nsmp0=50, jac_nsmp1=1,
                               jac_factor=1.0, jac_epsilon=1e-8)
+    u0 = torch.as_tensor(np.random.default_rng(1).standard_normal((nt, nx)),
+                         device=cuda)
+    st = State(fields={"u": u0.clone()})
+    torch.manual_seed(7)
+    packed = util.optimize_jacobi(args, fused, st)
+    torch.manual_seed(7)
+    st0 = State(fields={"u": u0.clone()})
+    d0 = fused.eval_diag(st0, nsmp=50)
+    _, grads, _, _ = fused.eval_loss_grad(st0)
+    d1 = fused.eval_diag(st0, nsmp=1)
+    diag = (d0 * 50 + d1) / 51
+    expect = u0.reshape(-1) - grads["u"].reshape(-1) / (diag + 1e-8) * 0.25
+    assert torch.allclose(packed, expect, rtol=1e-12, atol=0)
+    # Many epochs lower the loss.
+    args.epochs = 200
+    st = State(fields={"u": u0.clone()})
     losses = []
     util.optimize_jacobi(args, fused, st,
                          lambda p, e, **kw: losses.append(float(kw["opt"].last_loss)))
-    assert losses[-1] < 0.2 * losses[0]
+    assert np.isfinite(losses).all() and losses[-1] < 0.5 * losses[0]
