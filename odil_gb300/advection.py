@@ -179,9 +179,9 @@ class AdvectKernels:
                         device=self.device)
         call("odil_advect_dense", ctypes.byref(last.params), ptr(A),
              stream_handle())
-        # The coarsest operator is tiny (<= 1024 cells): invert it once here.
-        last.Ainv = torch.as_tensor(np.linalg.inv(A.cpu().numpy()),
-                                    device=self.device)
+        # The coarsest operator is tiny (<= 1024 cells): invert it once here
+        # (on the device, cuSOLVER through torch.linalg).
+        last.Ainv = torch.linalg.inv(A)
         self._mg = dict(levels=levels, omega=omega, pre=pre, post=post)
         return self._mg
 
@@ -225,6 +225,28 @@ class AdvectKernels:
                                                   device=self.device)
         return t
 
+    def _vcycle_graphs(self, p, ph, s, sh):
+        """The two V-cycles of a BiCGStab iteration (p -> ph, s -> sh) as
+        CUDA graphs, captured once: a V-cycle is ~40 launches, most of them
+        on small coarse levels, so replaying them saves the per-launch host
+        cost."""
+        g = self._scratch.get("vc_graphs")
+        if g is not None:
+            return g
+        self.vcycle(p, ph)  # builds the hierarchy, warms up
+        torch.cuda.synchronize(self.device)
+        side = torch.cuda.Stream(self.device)
+        side.wait_stream(torch.cuda.current_stream(self.device))
+        g = []
+        for src, dst in ((p, ph), (s, sh)):
+            graph = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(graph, stream=side):
+                self.vcycle(src, dst)
+            g.append(graph)
+        torch.cuda.current_stream(self.device).wait_stream(side)
+        self._scratch["vc_graphs"] = g
+        return g
+
     def bicgstab(self, b, x, tol=1e-6, maxit=100):
         """Right-preconditioned BiCGStab on J x = b in FP32 (x overwritten,
         zero initial guess); returns the iteration count."""
@@ -235,6 +257,7 @@ class AdvectKernels:
         r, rh, p, v, ph, s, sh, t = [self._buf(k) for k in
                                      ("r", "rh", "p", "v", "ph", "s", "sh",
                                       "t")]
+        vc = self._vcycle_graphs(p, ph, s, sh)
         fl = lambda a: a.reshape(-1)
         x.zero_()
         r.copy_(b)
@@ -252,7 +275,7 @@ class AdvectKernels:
             # p = r + beta (p - w v)
             vec.axpby(p, 1.0, p, -w, v)
             vec.axpby(p, 1.0, r, beta, p)
-            self.vcycle(p, ph)
+            vc[0].replay()  # ph = V(p)
             self.jv(ph, out=v)
             alpha = rho / md(fl(rh), 1, [fl(v)])[0, 0].item()
             vec.axpby(s, 1.0, r, -alpha, v)
@@ -260,7 +283,7 @@ class AdvectKernels:
             if ns <= tol * nb:
                 vec.axpby(x, 1.0, x, alpha, ph)
                 return it + 1
-            self.vcycle(s, sh)
+            vc[1].replay()  # sh = V(s)
             self.jv(sh, out=t)
             tt = md(fl(t), 1, [fl(t), fl(s)])
             tt_ts = tt[0].cpu().numpy()

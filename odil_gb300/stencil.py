@@ -296,7 +296,7 @@ class MultigridOp:
         nw = self.nnw[level]
         n = int(np.prod(nw))
         N = n * self.nvar
-        M = np.zeros((N, N))
+        M = torch.zeros((N, N), dtype=torch.float64, device=self.device)
         for j in range(self.nvar):
             for k in range(n):
                 e = torch.zeros(n, dtype=self.dtype, device=self.device)
@@ -304,8 +304,10 @@ class MultigridOp:
                 for i in range(self.nvar):
                     if A[i][j] is not None:
                         col = A[i][j].mul_field(e.reshape(nw)).reshape(-1)
-                        M[i * n:(i + 1) * n, j * n + k] = col.double().cpu().numpy()
-        inv = torch.as_tensor(np.linalg.pinv(M), device=self.device)
+                        M[i * n:(i + 1) * n, j * n + k] = col.double()
+        # Pseudo-inverse on the device (the coarsest matrix may be singular,
+        # as the reference's spsolve tolerates).
+        inv = torch.linalg.pinv(M)
         self._coarse_inv[level] = inv
         return inv
 
