@@ -349,6 +349,16 @@ int odil_ns_direct_check(int64_t n, const void* workspace, void* stream);
 int odil_ns_direct_solve(int64_t n, const double* coef, int64_t pin,
                          void* workspace, int64_t workspace_bytes,
                          const float* b, float* x, void* stream);
+/* Explicit inverse of a small dense FP64 matrix (n <= 4096) by cuSOLVER LU
+ * with partial pivoting.  Ainv comes out in the layout A goes in (row- or
+ * column-major): the inverse of the transpose is the transpose of the
+ * inverse.  ODIL_ERR_NONFINITE for an exactly singular matrix; synchronises
+ * the stream. */
+int64_t odil_dense_inverse_workspace_bytes(int64_t n);
+int odil_dense_inverse_f64(int64_t n, const double* A, double* Ainv,
+                           void* workspace, int64_t workspace_bytes,
+                           void* stream);
+
 /* The transposed solve J'^T x = b with the same factors (the preconditioner
  * (J'^T J')^-1 of the inverse problem's normal equations needs both). */
 int odil_ns_direct_solve_t(int64_t n, const double* coef, int64_t pin,

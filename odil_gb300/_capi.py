@@ -167,6 +167,8 @@ SIGNATURES = {
     "odil_ns_direct_check": (_INT, [_I64, _P, _P]),
     "odil_ns_direct_solve": (_INT, [_I64, _P, _I64, _P, _I64, _P, _P, _P]),
     "odil_ns_direct_solve_t": (_INT, [_I64, _P, _I64, _P, _I64, _P, _P, _P]),
+    "odil_dense_inverse_workspace_bytes": (_I64, [_I64]),
+    "odil_dense_inverse_f64": (_INT, [_I64, _P, _P, _P, _I64, _P]),
     "odil_wave_pair_residual_mixed": (_INT, [_P, _P, _P, _P, _P]),
     "odil_wave_batch_initial_rhs_mixed": (_INT, [_P, _P, _P]),
     "odil_wave_batch_pair_residual_mixed": (_INT, [_P, _P, _P, _P, _P]),

@@ -179,9 +179,14 @@ class AdvectKernels:
                         device=self.device)
         call("odil_advect_dense", ctypes.byref(last.params), ptr(A),
              stream_handle())
-        # The coarsest operator is tiny (<= 1024 cells): invert it once here
-        # (on the device, cuSOLVER through torch.linalg).
-        last.Ainv = torch.linalg.inv(A)
+        # The coarsest operator is tiny (<= 1024 cells): invert it once here,
+        # on the device (cuSOLVER LU in libodil_gb300).
+        lib = _capi.load()
+        nb = lib.odil_dense_inverse_workspace_bytes(last.n)
+        ws = torch.empty(max(nb, 256), dtype=torch.uint8, device=self.device)
+        last.Ainv = torch.empty_like(A)
+        call("odil_dense_inverse_f64", last.n, ptr(A), ptr(last.Ainv), ptr(ws),
+             ws.numel(), stream_handle())
         self._mg = dict(levels=levels, omega=omega, pre=pre, post=post)
         return self._mg
 

@@ -419,3 +419,62 @@ ODIL_API int odil_ns_direct_solve_t(int64_t n, const double* coef, int64_t pin, 
     nd_scatter<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(nn, y, x);
     return launch_status();
 }
+
+// Explicit inverse of a small dense FP64 matrix (column-major n x n; the
+// coarsest multigrid operators, n <= 1024): cuSOLVER LU with partial
+// pivoting and a solve against the identity.  Returns ODIL_ERR_NONFINITE when
+// a pivot is exactly zero (synchronises the stream to read it).
+__global__ void nd_identity64(int n, double* __restrict__ A) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r < n) A[r + (int64_t)r * n] = 1.0;
+}
+
+ODIL_API int64_t odil_dense_inverse_workspace_bytes(int64_t n) {
+    if (n < 1 || n > 4096) return -1;
+    cusolverDnHandle_t sol;
+    cublasHandle_t blas;
+    if (handles(nullptr, &sol, &blas)) return -1;
+    int lw = 0;
+    if (cusolverDnDgetrf_bufferSize(sol, (int)n, (int)n, nullptr, (int)n, &lw) !=
+        CUSOLVER_STATUS_SUCCESS)
+        return -1;
+    return al256(n * n * (int64_t)sizeof(double)) + al256(n * (int64_t)sizeof(int)) + 256 +
+           al256((int64_t)lw * (int64_t)sizeof(double));
+}
+
+ODIL_API int odil_dense_inverse_f64(int64_t n, const double* A, double* Ainv, void* ws,
+                                    int64_t ws_bytes, void* stream) {
+    if (n < 1 || n > 4096) return ODIL_ERR_SHAPE;
+    if (!A || !Ainv || !ws) return ODIL_ERR_ARG;
+    const int64_t need = odil_dense_inverse_workspace_bytes(n);
+    if (need < 0) return ODIL_ERR_LAUNCH;
+    if (ws_bytes < need) return ODIL_ERR_WORKSPACE;
+    cudaStream_t s = as_stream(stream);
+    cusolverDnHandle_t sol;
+    cublasHandle_t blas;
+    int st = handles(s, &sol, &blas);
+    if (st) return st;
+    char* base = reinterpret_cast<char*>(ws);
+    double* LU = reinterpret_cast<double*>(base);
+    int* piv = reinterpret_cast<int*>(base + al256(n * n * (int64_t)sizeof(double)));
+    int* info = reinterpret_cast<int*>(reinterpret_cast<char*>(piv) +
+                                       al256(n * (int64_t)sizeof(int)));
+    double* work = reinterpret_cast<double*>(reinterpret_cast<char*>(info) + 256);
+    const int m = (int)n;
+    if (cudaMemcpyAsync(LU, A, n * n * sizeof(double), cudaMemcpyDeviceToDevice, s) !=
+            cudaSuccess ||
+        cudaMemsetAsync(Ainv, 0, n * n * sizeof(double), s) != cudaSuccess)
+        return ODIL_ERR_LAUNCH;
+    nd_identity64<<<(m + 127) / 128, 128, 0, s>>>(m, Ainv);
+    if (cusolverDnDgetrf(sol, m, m, LU, m, work, piv, info) != CUSOLVER_STATUS_SUCCESS)
+        return ODIL_ERR_LAUNCH;
+    int h = 0;
+    if (cudaMemcpyAsync(&h, info, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess)
+        return ODIL_ERR_LAUNCH;
+    if (h != 0) return ODIL_ERR_NONFINITE;
+    if (cusolverDnDgetrs(sol, CUBLAS_OP_N, m, m, LU, m, piv, Ainv, m, info + 1) !=
+        CUSOLVER_STATUS_SUCCESS)
+        return ODIL_ERR_LAUNCH;
+    return launch_status();
+}

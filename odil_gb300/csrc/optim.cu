@@ -236,6 +236,111 @@ __global__ void __launch_bounds__(VT) multidot_kernel(const T* __restrict__ M, i
     if (threadIdx.x == 0) *counter = 0u;
 }
 
+// Vector path of the multi-dot with the number of vectors R fixed at compile
+// time: rows past k in the last group are loaded from row k-1 (valid memory)
+// and dropped at the end, so the loop body has no predicate and all 2 (G + R)
+// 16-byte loads of two elements per thread are issued before the
+// multiply-adds.  Same partial layout and finish as multidot_kernel.
+template <typename T, int R>
+__global__ void __launch_bounds__(VT, 3) multidot_vec_kernel(
+    const T* __restrict__ M, int64_t ld, int k, QPtrs qs, int64_t n, int64_t chunk,
+    double* __restrict__ partials, unsigned* counter, double* __restrict__ out) {
+    using V = typename Vec<T>::V;
+    constexpr int W = Vec<T>::W;
+    const int g0 = blockIdx.x * MD_G;
+    const int64_t c = blockIdx.y;
+    const int64_t e0 = c * chunk;
+    int64_t e1 = e0 + chunk;
+    if (e1 > n) e1 = n;
+    const V* rows[MD_G];
+#pragma unroll
+    for (int g = 0; g < MD_G; ++g) {
+        const int row = g0 + g < k ? g0 + g : k - 1;
+        rows[g] = reinterpret_cast<const V*>(M + (int64_t)row * ld);
+    }
+    const V* qv[R];
+#pragma unroll
+    for (int j = 0; j < R; ++j) qv[j] = reinterpret_cast<const V*>(qs.q[j]);
+    T acc[MD_G][R];
+#pragma unroll
+    for (int g = 0; g < MD_G; ++g)
+#pragma unroll
+        for (int j = 0; j < R; ++j) acc[g][j] = T(0);
+    auto madd = [&](const V (&q)[R], const V (&m)[MD_G]) {
+#pragma unroll
+        for (int g = 0; g < MD_G; ++g) {
+            const T* ms = reinterpret_cast<const T*>(&m[g]);
+#pragma unroll
+            for (int j = 0; j < R; ++j) {
+                const T* qq = reinterpret_cast<const T*>(&q[j]);
+#pragma unroll
+                for (int w = 0; w < W; ++w) acc[g][j] += ms[w] * qq[w];
+            }
+        }
+    };
+    const int64_t v0 = e0 / W, v1 = e1 / W;
+    int64_t e = v0 + threadIdx.x;
+    for (; e + VT < v1; e += 2 * VT) {
+        V qa[R], ma[MD_G], qb[R], mb[MD_G];
+#pragma unroll
+        for (int j = 0; j < R; ++j) {
+            qa[j] = __ldg(qv[j] + e);
+            qb[j] = __ldg(qv[j] + e + VT);
+        }
+#pragma unroll
+        for (int g = 0; g < MD_G; ++g) {
+            ma[g] = __ldcs(rows[g] + e);
+            mb[g] = __ldcs(rows[g] + e + VT);
+        }
+        madd(qa, ma);
+        madd(qb, mb);
+    }
+    if (e < v1) {
+        V qa[R], ma[MD_G];
+#pragma unroll
+        for (int j = 0; j < R; ++j) qa[j] = __ldg(qv[j] + e);
+#pragma unroll
+        for (int g = 0; g < MD_G; ++g) ma[g] = __ldcs(rows[g] + e);
+        madd(qa, ma);
+    }
+    for (int64_t t = v1 * W + threadIdx.x; t < e1; t += VT) {  // scalar tail
+#pragma unroll
+        for (int g = 0; g < MD_G; ++g) {
+            const T mval = reinterpret_cast<const T*>(rows[g])[t];
+#pragma unroll
+            for (int j = 0; j < R; ++j) acc[g][j] += mval * ((const T*)qs.q[j])[t];
+        }
+    }
+    const int64_t nchunk = gridDim.y;
+#pragma unroll
+    for (int g = 0; g < MD_G; ++g) {
+#pragma unroll
+        for (int j = 0; j < R; ++j) {
+            const double sum = block_sum((double)acc[g][j]);
+            if (g0 + g < k && threadIdx.x == 0)
+                partials[((int64_t)(g0 + g) * R + j) * nchunk + c] = sum;
+        }
+    }
+    __shared__ bool is_last;
+    if (threadIdx.x == 0) {
+        __threadfence();
+        unsigned prev = atomicAdd(counter, 1u);
+        is_last = (prev == (unsigned)((int64_t)gridDim.x * gridDim.y - 1));
+    }
+    __syncthreads();
+    if (!is_last) return;
+    __threadfence();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = VT / 32;
+    for (int o = warp; o < k * R; o += nw) {
+        double sum = 0.0;
+        for (int64_t q = lane; q < nchunk; q += 32) sum += __ldcg(partials + (int64_t)o * nchunk + q);
+        sum = warp_sum(sum);
+        if (lane == 0) out[o] = sum;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) *counter = 0u;
+}
+
 // out = c0 * x + sum_i coef[i] * M_i  (coef, c0 read from device memory).
 template <typename T>
 __global__ void __launch_bounds__(VT) lincomb_kernel(T* __restrict__ out, const T* __restrict__ x,
@@ -328,8 +433,29 @@ int multidot_impl(const T* M, int64_t ld, int k, const void* const* q, int r, in
     if (nchunk > 65535) return ODIL_ERR_SHAPE;
     ReduceWs w = reduce_ws(ws);
     dim3 grid((k + MD_G - 1) / MD_G, (unsigned)nchunk);
-    multidot_kernel<T><<<grid, VT, 0, as_stream(stream)>>>(M, ld, k, qs, r, n, chunk, w.partials,
-                                                           w.counter, out, vec);
+    cudaStream_t st = as_stream(stream);
+    if (vec) {
+        switch (r) {
+            case 1:
+                multidot_vec_kernel<T, 1><<<grid, VT, 0, st>>>(M, ld, k, qs, n, chunk, w.partials,
+                                                                w.counter, out);
+                return launch_status();
+            case 2:
+                multidot_vec_kernel<T, 2><<<grid, VT, 0, st>>>(M, ld, k, qs, n, chunk, w.partials,
+                                                                w.counter, out);
+                return launch_status();
+            case 3:
+                multidot_vec_kernel<T, 3><<<grid, VT, 0, st>>>(M, ld, k, qs, n, chunk, w.partials,
+                                                                w.counter, out);
+                return launch_status();
+            default:
+                multidot_vec_kernel<T, 4><<<grid, VT, 0, st>>>(M, ld, k, qs, n, chunk, w.partials,
+                                                                w.counter, out);
+                return launch_status();
+        }
+    }
+    multidot_kernel<T><<<grid, VT, 0, st>>>(M, ld, k, qs, r, n, chunk, w.partials, w.counter, out,
+                                            vec);
     return launch_status();
 }
 
