@@ -19,6 +19,7 @@ struct AdvDev {
     int nt, nx, ny;
     T inv_dt, inv_dx, inv_dy, ax, ay;
     T D;                      // diagonal: 1/dt + |ax|/dx + |ay|/dy
+    T inv_D;                  // 1/D (the Jacobi sweep multiplies)
     bool axpos, aypos;
     const T* p_init;          // [nx * ny] or null (zero)
 };
@@ -39,6 +40,7 @@ int make_adv(const odil_advect_params* p, AdvDev<T>* g, bool with_init) {
     g->ax = (T)p->ax;
     g->ay = (T)p->ay;
     g->D = (T)(1.0 / p->dt + fabs(p->ax) / p->dx + fabs(p->ay) / p->dy);
+    g->inv_D = (T)(1.0 / (1.0 / p->dt + fabs(p->ax) / p->dx + fabs(p->ay) / p->dy));
     g->axpos = p->ax > 0;
     g->aypos = p->ay > 0;
     g->p_init = with_init ? (const T*)p->p_init : nullptr;
@@ -226,13 +228,13 @@ __global__ void __launch_bounds__(256) adv_jacobi_kernel(AdvDev<float> g, const 
     if (!cell_of(g, &c)) return;
     const float bb = __ldg(b + c.k);
     if (!x) {
-        xout[c.k] = omega * bb / g.D;
+        xout[c.k] = omega * bb * g.inv_D;
         return;
     }
     float center;
     const float jx = adv_eval<float, float>(g, c, x, nullptr, &center);
     const float r = bb - jx;
-    if (xout) xout[c.k] = center + omega * r / g.D;
+    if (xout) xout[c.k] = center + omega * r * g.inv_D;
     if (r_out) r_out[c.k] = r;
 }
 
@@ -264,7 +266,7 @@ __device__ __forceinline__ W4 fw_axis(int c, int nf, bool periodic) {
 
 __global__ void __launch_bounds__(256) adv_restrict_kernel(const float* __restrict__ r, int nt,
                                                            int nx, int ny, float* __restrict__ rc) {
-    const int ntc = nt / 2, nxc = nx / 2, nyc = ny / 2;
+    const int nxc = nx / 2, nyc = ny / 2;
     const int yc = blockIdx.x * blockDim.x + threadIdx.x;
     const int xc = blockIdx.y, tc = blockIdx.z;
     if (yc >= nyc) return;
@@ -301,28 +303,38 @@ __device__ __forceinline__ void lin_axis(int f, int nc, bool periodic, int* i0, 
     *w1 = 0.25f;
 }
 
+// One thread per coarse y index c: fine y = 2c and 2c+1 share the coarse
+// values c-1, c, c+1 of the four (t, x) coarse rows, so a thread loads 12
+// coarse values for two fine cells and updates them with one 8-byte access.
 __global__ void __launch_bounds__(256) adv_prolong_add_kernel(const float* __restrict__ e, int nt,
                                                               int nx, int ny, float* __restrict__ x) {
     const int ntc = nt / 2, nxc = nx / 2, nyc = ny / 2;
-    const int y = blockIdx.x * blockDim.x + threadIdx.x;
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;  // coarse y
     const int xx = blockIdx.y, t = blockIdx.z;
-    if (y >= ny) return;
-    int ti[2], xi[2], yi[2];
-    float tw[2], xw[2], yw[2];
+    if (c >= nyc) return;
+    int ti[2], xi[2];
+    float tw[2], xw[2];
     lin_axis(t, ntc, false, &ti[0], &ti[1], &tw[0], &tw[1]);
     lin_axis(xx, nxc, true, &xi[0], &xi[1], &xw[0], &xw[1]);
-    lin_axis(y, nyc, true, &yi[0], &yi[1], &yw[0], &yw[1]);
-    float s = 0.f;
+    const int cm = c == 0 ? nyc - 1 : c - 1;
+    const int cp = c + 1 == nyc ? 0 : c + 1;
+    float s0 = 0.f, s1 = 0.f;
 #pragma unroll
-    for (int a = 0; a < 2; ++a)
+    for (int a = 0; a < 2; ++a) {
 #pragma unroll
-        for (int b = 0; b < 2; ++b)
-#pragma unroll
-            for (int c = 0; c < 2; ++c)
-                s += tw[a] * xw[b] * yw[c] *
-                     __ldg(e + ((int64_t)ti[a] * nxc + xi[b]) * nyc + yi[c]);
-    const int64_t k = ((int64_t)t * nx + xx) * ny + y;
-    x[k] += s;
+        for (int b = 0; b < 2; ++b) {
+            const float* row = e + ((int64_t)ti[a] * nxc + xi[b]) * nyc;
+            const float w = tw[a] * xw[b];
+            const float ec = __ldg(row + c);
+            s0 += w * (0.75f * ec + 0.25f * __ldg(row + cm));
+            s1 += w * (0.75f * ec + 0.25f * __ldg(row + cp));
+        }
+    }
+    float2* dst = reinterpret_cast<float2*>(x + ((int64_t)t * nx + xx) * ny + 2 * c);
+    float2 v = *dst;
+    v.x += s0;
+    v.y += s1;
+    *dst = v;
 }
 
 // Dense FP64 coarsest solve x = Ainv b (Ainv: the explicit inverse of the
@@ -512,7 +524,7 @@ ODIL_API int odil_advect_mg_prolong_add(int64_t nt, int64_t nx, int64_t ny, cons
         return ODIL_ERR_SHAPE;
     if (!e || !x) return ODIL_ERR_ARG;
     dim3 grid, block;
-    adv_launch_dims((int)nt, (int)nx, (int)ny, &grid, &block);
+    adv_launch_dims((int)nt, (int)nx, (int)ny / 2, &grid, &block);  // coarse y per thread
     adv_prolong_add_kernel<<<grid, block, 0, as_stream(stream)>>>(e, (int)nt, (int)nx, (int)ny, x);
     return launch_status();
 }

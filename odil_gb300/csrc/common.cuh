@@ -199,36 +199,4 @@ __device__ __forceinline__ void reduce_finish(double v, int64_t bid, int64_t nbl
     }
 }
 
-// Two-kernel variant.  The first kernel's blocks store their sums at
-// partials[0 .. first) with reduce_store (no counter); the second kernel's
-// `nblocks` blocks call reduce_finish_after with slot = first + bid, and its
-// last block adds all first + nblocks partial sums in index order.  Kernel
-// order on the stream makes the first kernel's stores visible.
-__device__ __forceinline__ void reduce_store(double v, int64_t slot, ReduceWs ws) {
-    v = block_sum(v);
-    if (threadIdx.x == 0) ws.partials[slot] = v;
-}
-
-__device__ __forceinline__ void reduce_finish_after(double v, int64_t first, int64_t bid,
-                                                    int64_t nblocks, ReduceWs ws, double scale,
-                                                    double* out) {
-    __shared__ bool is_last;
-    v = block_sum(v);
-    if (threadIdx.x == 0) {
-        ws.partials[first + bid] = v;
-        __threadfence();
-        unsigned prev = atomicAdd(ws.counter, 1u);
-        is_last = (prev == (unsigned)(nblocks - 1));
-    }
-    __syncthreads();
-    if (is_last) {
-        __threadfence();
-        double s = sum_partials(ws.partials, first + nblocks);
-        if (threadIdx.x == 0) {
-            out[0] = s * scale;
-            *ws.counter = 0u;
-        }
-    }
-}
-
 }  // namespace odil

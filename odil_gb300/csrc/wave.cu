@@ -478,56 +478,6 @@ LvGeom lv_geom(int nt, int nx, int ty) {
     return q;
 }
 
-// Interior tiles only: constant coefficients, no boundary branches, at most
-// 64 registers so that 8 warps per scheduler hide the load latency.
-template <typename T, int TY>
-__global__ void __launch_bounds__(LV_WARPS * 32, 16) wave_loss_grad_int_kernel(
-    WaveDev<T> g, const T* __restrict__ u, T* __restrict__ grad, ReduceWs ws, int sw_hi,
-    T gscale) {
-    constexpr int V = Vec16<T>::n;
-    __shared__ __align__(16) T ring_all[LV_WARPS][LV_RING][32 * V];
-    const int lane = threadIdx.x & 31;
-    const int warp = threadIdx.x >> 5;
-    const int sw = 1 + blockIdx.x * LV_WARPS + warp;
-    T lsum = T(0);
-    if (sw <= sw_hi) {
-        lsum = lg_vec_tile<T, TY, true>(g, u, grad, (1 + blockIdx.y) * TY, sw * (30 * V), lane,
-                                        gscale, &ring_all[warp][0][0], nullptr);
-    }
-    reduce_store((double)lsum, (int64_t)blockIdx.y * gridDim.x + blockIdx.x, ws);
-}
-
-// The remaining (boundary) tiles, LV_EDGE_TY rows each, one warp per block,
-// through the general class functions; its last block finishes the loss over
-// both kernels' partial sums.
-template <typename T>
-__global__ void __launch_bounds__(32) wave_loss_grad_edge_kernel(
-    WaveDev<T> g, const T* __restrict__ u, T* __restrict__ grad, ReduceWs ws, LvGeom q,
-    double* loss, T gscale, double lscale) {
-    constexpr int V = Vec16<T>::n;
-    __shared__ __align__(16) T ring[LV_RING][32 * V];
-    __shared__ T bcs[2 * (LV_EDGE_TY + 4)];
-    const int64_t b = blockIdx.x;
-    // Rows [0, lo) and (hi, nte) are whole; rows [lo, hi] hold strip 0 and
-    // the strips past sw_hi.
-    const int64_t nfull = (int64_t)(q.nte - (q.hi - q.lo + 1)) * q.nsw;
-    int sw, ty;
-    if (b < nfull) {
-        const int r = (int)(b / q.nsw);
-        sw = (int)(b - (int64_t)r * q.nsw);
-        ty = r < q.lo ? r : q.hi + 1 + (r - q.lo);
-    } else {
-        const int m = q.nsw - q.sw_hi;
-        const int64_t k = b - nfull;
-        ty = q.lo + (int)(k / m);
-        const int c = (int)(k - (int64_t)(ty - q.lo) * m);
-        sw = c == 0 ? 0 : q.sw_hi + c;
-    }
-    const T lsum = lg_vec_tile<T, LV_EDGE_TY, false>(g, u, grad, ty * LV_EDGE_TY, sw * (30 * V),
-                                                     threadIdx.x, gscale, &ring[0][0], bcs);
-    reduce_finish_after((double)lsum, q.n_int_blocks, b, q.n_edge, ws, lscale, loss);
-}
-
 // Both tile kinds in one launch: the first blocks take the boundary tiles
 // (two per block, one per warp), the rest the interior tiles, so the slow
 // boundary marches run beside the interior ones instead of after them.  The
