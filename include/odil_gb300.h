@@ -470,8 +470,29 @@ int odil_add_f32_to_f64(const double* u, const float* d, double* out,
 int odil_pair_to_f64(const float* hi, const float* lo, double* out, int64_t n,
                      void* stream);
 
+/* BiCGStab with device-side scalars (the advection inner solve).  sc is an
+ * FP64 [4] array: rho, alpha, omega, beta (start: 1, 1, 1, 0).  scalars:
+ * phase 0: rho' = dots[0] = <r^, r>, beta = (rho'/rho)(alpha/omega),
+ * rho = rho'; phase 1: alpha = rho / dots[0] (= <r^, v>); phase 2: omega =
+ * dots[1] / dots[0] (= <t, s> / <t, t>).  Updates (n % 4 == 0, 16-byte
+ * aligned FP32 vectors): p = r + beta (p - omega v); s = r - alpha v;
+ * x += alpha ph (+ omega sh), r = s - omega t when with_s. */
+int odil_bicgstab_scalars(const double* dots, double* sc, int32_t phase,
+                          void* stream);
+int odil_bicgstab_update_p(float* p, const float* r, const float* v,
+                           const double* sc, int64_t n, void* stream);
+int odil_bicgstab_update_s(float* s, const float* r, const float* v,
+                           const double* sc, int64_t n, void* stream);
+int odil_bicgstab_update_xr(float* x, float* r, const float* ph,
+                            const float* sh, const float* s, const float* t,
+                            const double* sc, int64_t n, int32_t with_s,
+                            void* stream);
+
 /* Multi-dot: out[i*r + j] = sum_e M[i*ld + e] * q[j][e] for i < k, j < r
- * (r <= 4), in one pass over M.  FP64 accumulation, deterministic order.
+ * (r <= 4), in one pass over M.  Each thread sums its share of a chunk in
+ * the input type (about n * ceil(k/4) / (1824 * 256) products, at least 16), the
+ * rest is added in FP64; deterministic order.  The workspace size serves
+ * every call with at most k rows and r vectors.
  * This and odil_lincomb_* are the two streaming passes of the compact L-BFGS
  * direction that replaces scipy's fmin_l_bfgs_b (optimizer.py:61-99):
  * [S; Y] . g (plus the new correction pair's products), then

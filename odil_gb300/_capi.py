@@ -162,6 +162,11 @@ SIGNATURES = {
                                          ctypes.c_int32, _P]),
     "odil_add_f32_to_f64": (_INT, [_P, _P, _P, _I64, _P]),
     "odil_pair_to_f64": (_INT, [_P, _P, _P, _I64, _P]),
+    "odil_bicgstab_scalars": (_INT, [_P, _P, ctypes.c_int32, _P]),
+    "odil_bicgstab_update_p": (_INT, [_P, _P, _P, _P, _I64, _P]),
+    "odil_bicgstab_update_s": (_INT, [_P, _P, _P, _P, _I64, _P]),
+    "odil_bicgstab_update_xr": (_INT, [_P, _P, _P, _P, _P, _P, _P, _I64,
+                                       ctypes.c_int32, _P]),
     "odil_ns_direct_workspace_bytes": (_I64, [_I64]),
     "odil_ns_direct_factor": (_INT, [_I64, _P, _I64, _P, _I64, _P]),
     "odil_ns_direct_check": (_INT, [_I64, _P, _P]),

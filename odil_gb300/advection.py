@@ -254,7 +254,9 @@ class AdvectKernels:
 
     def bicgstab(self, b, x, tol=1e-6, maxit=100):
         """Right-preconditioned BiCGStab on J x = b in FP32 (x overwritten,
-        zero initial guess); returns the iteration count."""
+        zero initial guess); returns the iteration count.  The step scalars
+        stay on the device (odil_bicgstab_*); the host reads the two residual
+        norms it tests per iteration."""
         md = self._scratch.get("md")
         if md is None:
             md = self._scratch["md"] = vec.MultiDot(self.n, 2, 2,
@@ -263,6 +265,55 @@ class AdvectKernels:
                                      ("r", "rh", "p", "v", "ph", "s", "sh",
                                       "t")]
         vc = self._vcycle_graphs(p, ph, s, sh)
+        fl = lambda a: a.reshape(-1)
+        if self.n % 4:
+            return self._bicgstab_host(b, x, tol, maxit, md, vc)
+        sc = self._scratch.get("bicg_sc")
+        if sc is None:
+            sc = self._scratch["bicg_sc"] = torch.empty(4, dtype=torch.float64,
+                                                        device=self.device)
+        st = stream_handle()
+        n = self.n
+        x.zero_()
+        r.copy_(b)
+        rh.copy_(b)
+        p.zero_()
+        v.zero_()
+        sc.fill_(1.0)  # rho, alpha, omega = 1; beta (sc[3]) is set before use
+        nb = md(fl(b), 1, [fl(b)])[0, 0].item()**0.5
+        if nb == 0:
+            return 0
+        for it in range(maxit):
+            dots = md(fl(rh), 1, [fl(r)])
+            call("odil_bicgstab_scalars", ptr(dots), ptr(sc), 0, st)
+            call("odil_bicgstab_update_p", ptr(p), ptr(r), ptr(v), ptr(sc), n, st)
+            vc[0].replay()  # ph = V(p)
+            self.jv(ph, out=v)
+            dots = md(fl(rh), 1, [fl(v)])
+            call("odil_bicgstab_scalars", ptr(dots), ptr(sc), 1, st)
+            call("odil_bicgstab_update_s", ptr(s), ptr(r), ptr(v), ptr(sc), n, st)
+            ns = md(fl(s), 1, [fl(s)])[0, 0].item()**0.5
+            if ns <= tol * nb:
+                call("odil_bicgstab_update_xr", ptr(x), None, ptr(ph), None, None,
+                     None, ptr(sc), n, 0, st)
+                return it + 1
+            vc[1].replay()  # sh = V(s)
+            self.jv(sh, out=t)
+            dots = md(fl(t), 1, [fl(t), fl(s)])
+            call("odil_bicgstab_scalars", ptr(dots), ptr(sc), 2, st)
+            call("odil_bicgstab_update_xr", ptr(x), ptr(r), ptr(ph), ptr(sh), ptr(s),
+                 ptr(t), ptr(sc), n, 1, st)
+            nr = md(fl(r), 1, [fl(r)])[0, 0].item()**0.5
+            if nr <= tol * nb:
+                return it + 1
+        return maxit
+
+    def _bicgstab_host(self, b, x, tol, maxit, md, vc):
+        """The same iteration with host scalars (cell counts not divisible
+        by 4)."""
+        r, rh, p, v, ph, s, sh, t = [self._buf(k) for k in
+                                     ("r", "rh", "p", "v", "ph", "s", "sh",
+                                      "t")]
         fl = lambda a: a.reshape(-1)
         x.zero_()
         r.copy_(b)
@@ -277,10 +328,9 @@ class AdvectKernels:
             rho1 = md(fl(rh), 1, [fl(r)])[0, 0].item()
             beta = (rho1 / rho) * (alpha / w)
             rho = rho1
-            # p = r + beta (p - w v)
             vec.axpby(p, 1.0, p, -w, v)
             vec.axpby(p, 1.0, r, beta, p)
-            vc[0].replay()  # ph = V(p)
+            vc[0].replay()
             self.jv(ph, out=v)
             alpha = rho / md(fl(rh), 1, [fl(v)])[0, 0].item()
             vec.axpby(s, 1.0, r, -alpha, v)
@@ -288,7 +338,7 @@ class AdvectKernels:
             if ns <= tol * nb:
                 vec.axpby(x, 1.0, x, alpha, ph)
                 return it + 1
-            vc[1].replay()  # sh = V(s)
+            vc[1].replay()
             self.jv(sh, out=t)
             tt = md(fl(t), 1, [fl(t), fl(s)])
             tt_ts = tt[0].cpu().numpy()

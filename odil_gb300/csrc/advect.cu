@@ -9,6 +9,8 @@
 // levels rediscretise it with doubled steps): damped Jacobi, residual,
 // full-weighting restriction (the transpose of trilinear prolongation / 8),
 // trilinear prolongation-add, and a dense FP64 coarsest-level solve.
+#include <initializer_list>
+
 #include "common.cuh"
 
 namespace odil {
@@ -378,12 +380,146 @@ __global__ void adv_dense_kernel(AdvDev<double> g, double* __restrict__ A) {
     }
 }
 
+// ---------------------------------------------------------------------------
+// FP32 fast path (ny a multiple of 4, 16-byte aligned arrays): a thread owns 4
+// consecutive y cells of one (t, x) row, loads each stencil row with one
+// 16-byte access, takes the upwind y-neighbour of its first (or last) cell
+// from the adjacent lane by a shuffle, and only the warp's end lanes load a
+// word across the lane boundary (with the periodic wrap).  Same residual
+// formula and operation order as adv_f.
+struct Row4 {
+    int i, x, y0;  // cell (i, x, y0 .. y0+3)
+    int64_t k;     // packed index of (i, x, y0)
+    bool ok;
+};
+
+__device__ __forceinline__ Row4 row4_of(const AdvDev<float>& g) {
+    Row4 c;
+    c.y0 = 4 * (blockIdx.x * blockDim.x + threadIdx.x);
+    c.x = blockIdx.y * blockDim.y + threadIdx.y;
+    c.i = blockIdx.z;
+    c.k = ((int64_t)c.i * g.nx + c.x) * g.ny + c.y0;
+    c.ok = c.y0 < g.ny && c.x < g.nx;
+    return c;
+}
+
+__device__ __forceinline__ float4 ld4(const float* p, int64_t k) {
+    return __ldg(reinterpret_cast<const float4*>(p + k));
+}
+
+// Residuals (init: with p_init on row 0; else the linear part J v) of the 4
+// cells; also returns the centre values.  All lanes must call it (shuffles).
+__device__ __forceinline__ void adv_eval4(const AdvDev<float>& g, const Row4& c,
+                                          const float* __restrict__ u, float (&f)[4],
+                                          float4* centre) {
+    const int nx = g.nx, ny = g.ny;
+    const int lane = threadIdx.x & 31;
+    float4 P = make_float4(0.f, 0.f, 0.f, 0.f), PT = P, PX = P;
+    if (c.ok) {
+        P = ld4(u, c.k);
+        if (c.i == 0) {
+            if (g.p_init) PT = ld4(g.p_init, (int64_t)c.x * ny + c.y0);
+        } else {
+            PT = ld4(u, c.k - (int64_t)nx * ny);
+        }
+        const int xn = g.axpos ? (c.x == 0 ? nx - 1 : c.x - 1) : (c.x + 1 == nx ? 0 : c.x + 1);
+        PX = ld4(u, c.k + (int64_t)(xn - c.x) * ny);
+    }
+    *centre = P;
+    // y-neighbour outside the thread's 4 cells.
+    const int64_t rowk = c.k - c.y0;
+    float yo;
+    if (g.aypos) {
+        yo = __shfl_up_sync(0xffffffffu, P.w, 1);
+        if (c.ok && (lane == 0 || c.y0 == 0))
+            yo = __ldg(u + rowk + (c.y0 == 0 ? ny - 1 : c.y0 - 1));
+    } else {
+        yo = __shfl_down_sync(0xffffffffu, P.x, 1);
+        if (c.ok && (lane == 31 || c.y0 + 4 >= ny))
+            yo = __ldg(u + rowk + (c.y0 + 4 >= ny ? 0 : c.y0 + 4));
+    }
+    const float p[4] = {P.x, P.y, P.z, P.w};
+    const float pt[4] = {PT.x, PT.y, PT.z, PT.w};
+    const float px[4] = {PX.x, PX.y, PX.z, PX.w};
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+        const float ym = e == 0 ? yo : p[e - 1];
+        const float yp = e == 3 ? yo : p[e + 1];
+        f[e] = adv_f(g, p[e], pt[e], px[e], px[e], ym, yp);
+    }
+}
+
+__global__ void __launch_bounds__(256) adv_residual4_kernel(AdvDev<float> g,
+                                                            const float* __restrict__ u,
+                                                            float* __restrict__ f) {
+    const Row4 c = row4_of(g);
+    float r[4];
+    float4 centre;
+    adv_eval4(g, c, u, r, &centre);
+    if (c.ok) *reinterpret_cast<float4*>(f + c.k) = make_float4(r[0], r[1], r[2], r[3]);
+}
+
+// Damped Jacobi (adv_jacobi_kernel's arithmetic, same rounding) on 4 cells
+// per thread.
+__global__ void __launch_bounds__(256) adv_jacobi4_kernel(AdvDev<float> g,
+                                                          const float* __restrict__ x,
+                                                          const float* __restrict__ b,
+                                                          float* __restrict__ xout, float omega,
+                                                          float* __restrict__ r_out) {
+    const Row4 c = row4_of(g);
+    const float iD = g.inv_D;
+    if (!x) {
+        if (!c.ok) return;
+        const float4 B = ld4(b, c.k);
+        *reinterpret_cast<float4*>(xout + c.k) = make_float4(
+            omega * B.x * iD, omega * B.y * iD, omega * B.z * iD, omega * B.w * iD);
+        return;
+    }
+    float jx[4];
+    float4 P;
+    adv_eval4(g, c, x, jx, &P);
+    if (!c.ok) return;
+    const float4 B = ld4(b, c.k);
+    const float r0 = B.x - jx[0], r1 = B.y - jx[1], r2 = B.z - jx[2], r3 = B.w - jx[3];
+    if (xout)
+        *reinterpret_cast<float4*>(xout + c.k) =
+            make_float4(P.x + omega * r0 * iD, P.y + omega * r1 * iD, P.z + omega * r2 * iD,
+                        P.w + omega * r3 * iD);
+    if (r_out) *reinterpret_cast<float4*>(r_out + c.k) = make_float4(r0, r1, r2, r3);
+}
+
+inline bool adv_vec4(const AdvDev<float>& g, std::initializer_list<const void*> ptrs) {
+    if (g.ny % 4) return false;
+    for (const void* q : ptrs)
+        if (q && (reinterpret_cast<uintptr_t>(q) & 15u)) return false;
+    return true;
+}
+
+// Blocks of about 256 threads: whole warps along y (a warp never spans two x
+// rows, so its shuffles stay in one row), then as many x rows as fit.
+inline void adv_launch_dims4(int nt, int nx, int ny, dim3* grid, dim3* block) {
+    const int per = ny / 4;
+    const int bx = per >= 256 ? 256 : ((per + 31) / 32) * 32;
+    int by = 256 / bx;
+    if (by > nx) by = nx;
+    *block = dim3(bx, by);
+    *grid = dim3((per + bx - 1) / bx, (nx + by - 1) / by, nt);
+}
+
 template <typename T>
 int residual_impl(const odil_advect_params* p, const T* u, T* f, void* stream, bool init) {
     AdvDev<T> g;
     int st = make_adv<T>(p, &g, init);
     if (st) return st;
     if (!u || !f) return ODIL_ERR_ARG;
+    if constexpr (sizeof(T) == 4) {
+        if (adv_vec4(g, {u, f, g.p_init})) {
+            dim3 grid, block;
+            adv_launch_dims4(g.nt, g.nx, g.ny, &grid, &block);
+            adv_residual4_kernel<<<grid, block, 0, as_stream(stream)>>>(g, u, f);
+            return launch_status();
+        }
+    }
     dim3 grid, block;
     adv_launch_dims(g.nt, g.nx, g.ny, &grid, &block);
     adv_residual_kernel<T><<<grid, block, 0, as_stream(stream)>>>(g, u, f);
@@ -504,6 +640,11 @@ ODIL_API int odil_advect_mg_jacobi(const odil_advect_params* p, const float* x, 
     if (st) return st;
     if (!b || (!x_out && !r_out) || (x && x == x_out) || (!x && r_out)) return ODIL_ERR_ARG;
     dim3 grid, block;
+    if (adv_vec4(g, {x, b, x_out, r_out})) {
+        adv_launch_dims4(g.nt, g.nx, g.ny, &grid, &block);
+        adv_jacobi4_kernel<<<grid, block, 0, as_stream(stream)>>>(g, x, b, x_out, omega, r_out);
+        return launch_status();
+    }
     adv_launch_dims(g.nt, g.nx, g.ny, &grid, &block);
     adv_jacobi_kernel<<<grid, block, 0, as_stream(stream)>>>(g, x, b, x_out, omega, r_out);
     return launch_status();

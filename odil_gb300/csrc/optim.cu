@@ -224,15 +224,11 @@ __global__ void __launch_bounds__(VT) multidot_kernel(const T* __restrict__ M, i
     __syncthreads();
     if (!is_last) return;
     __threadfence();
-    // One warp per (row, column) output, chunk partials added in order.
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = VT / 32;
-    for (int o = warp; o < k * r; o += nw) {
-        double s = 0.0;
-        for (int64_t q = lane; q < nchunk; q += 32) s += __ldcg(partials + (int64_t)o * nchunk + q);
-        s = warp_sum(s);
-        if (lane == 0) out[o] = s;
+    // Each output's chunk partials summed by the whole block in a fixed order.
+    for (int o = 0; o < k * r; ++o) {
+        const double s = sum_partials(partials + (int64_t)o * nchunk, nchunk);
+        if (threadIdx.x == 0) out[o] = s;
     }
-    __syncthreads();
     if (threadIdx.x == 0) *counter = 0u;
 }
 
@@ -241,34 +237,34 @@ __global__ void __launch_bounds__(VT) multidot_kernel(const T* __restrict__ M, i
 // and dropped at the end, so the loop body has no predicate and all 2 (G + R)
 // 16-byte loads of two elements per thread are issued before the
 // multiply-adds.  Same partial layout and finish as multidot_kernel.
-template <typename T, int R>
+template <typename T, int R, int G>
 __global__ void __launch_bounds__(VT, 3) multidot_vec_kernel(
     const T* __restrict__ M, int64_t ld, int k, QPtrs qs, int64_t n, int64_t chunk,
     double* __restrict__ partials, unsigned* counter, double* __restrict__ out) {
     using V = typename Vec<T>::V;
     constexpr int W = Vec<T>::W;
-    const int g0 = blockIdx.x * MD_G;
+    const int g0 = blockIdx.x * G;
     const int64_t c = blockIdx.y;
     const int64_t e0 = c * chunk;
     int64_t e1 = e0 + chunk;
     if (e1 > n) e1 = n;
-    const V* rows[MD_G];
+    const V* rows[G];
 #pragma unroll
-    for (int g = 0; g < MD_G; ++g) {
+    for (int g = 0; g < G; ++g) {
         const int row = g0 + g < k ? g0 + g : k - 1;
         rows[g] = reinterpret_cast<const V*>(M + (int64_t)row * ld);
     }
     const V* qv[R];
 #pragma unroll
     for (int j = 0; j < R; ++j) qv[j] = reinterpret_cast<const V*>(qs.q[j]);
-    T acc[MD_G][R];
+    T acc[G][R];
 #pragma unroll
-    for (int g = 0; g < MD_G; ++g)
+    for (int g = 0; g < G; ++g)
 #pragma unroll
         for (int j = 0; j < R; ++j) acc[g][j] = T(0);
-    auto madd = [&](const V (&q)[R], const V (&m)[MD_G]) {
+    auto madd = [&](const V (&q)[R], const V (&m)[G]) {
 #pragma unroll
-        for (int g = 0; g < MD_G; ++g) {
+        for (int g = 0; g < G; ++g) {
             const T* ms = reinterpret_cast<const T*>(&m[g]);
 #pragma unroll
             for (int j = 0; j < R; ++j) {
@@ -278,34 +274,34 @@ __global__ void __launch_bounds__(VT, 3) multidot_vec_kernel(
             }
         }
     };
+    // U steps of 16-byte loads per thread issued before their multiply-adds
+    // (more steps when the loads per step are few).
+    constexpr int U = (R + G) <= 3 ? 4 : 2;
     const int64_t v0 = e0 / W, v1 = e1 / W;
     int64_t e = v0 + threadIdx.x;
-    for (; e + VT < v1; e += 2 * VT) {
-        V qa[R], ma[MD_G], qb[R], mb[MD_G];
+    for (; e + (U - 1) * VT < v1; e += U * VT) {
+        V q[U][R], m[U][G];
 #pragma unroll
-        for (int j = 0; j < R; ++j) {
-            qa[j] = __ldg(qv[j] + e);
-            qb[j] = __ldg(qv[j] + e + VT);
+        for (int u = 0; u < U; ++u) {
+#pragma unroll
+            for (int j = 0; j < R; ++j) q[u][j] = __ldg(qv[j] + e + u * VT);
+#pragma unroll
+            for (int g = 0; g < G; ++g) m[u][g] = __ldcs(rows[g] + e + u * VT);
         }
 #pragma unroll
-        for (int g = 0; g < MD_G; ++g) {
-            ma[g] = __ldcs(rows[g] + e);
-            mb[g] = __ldcs(rows[g] + e + VT);
-        }
-        madd(qa, ma);
-        madd(qb, mb);
+        for (int u = 0; u < U; ++u) madd(q[u], m[u]);
     }
-    if (e < v1) {
-        V qa[R], ma[MD_G];
+    for (; e < v1; e += VT) {
+        V qa[R], ma[G];
 #pragma unroll
         for (int j = 0; j < R; ++j) qa[j] = __ldg(qv[j] + e);
 #pragma unroll
-        for (int g = 0; g < MD_G; ++g) ma[g] = __ldcs(rows[g] + e);
+        for (int g = 0; g < G; ++g) ma[g] = __ldcs(rows[g] + e);
         madd(qa, ma);
     }
     for (int64_t t = v1 * W + threadIdx.x; t < e1; t += VT) {  // scalar tail
 #pragma unroll
-        for (int g = 0; g < MD_G; ++g) {
+        for (int g = 0; g < G; ++g) {
             const T mval = reinterpret_cast<const T*>(rows[g])[t];
 #pragma unroll
             for (int j = 0; j < R; ++j) acc[g][j] += mval * ((const T*)qs.q[j])[t];
@@ -313,7 +309,7 @@ __global__ void __launch_bounds__(VT, 3) multidot_vec_kernel(
     }
     const int64_t nchunk = gridDim.y;
 #pragma unroll
-    for (int g = 0; g < MD_G; ++g) {
+    for (int g = 0; g < G; ++g) {
 #pragma unroll
         for (int j = 0; j < R; ++j) {
             const double sum = block_sum((double)acc[g][j]);
@@ -330,14 +326,12 @@ __global__ void __launch_bounds__(VT, 3) multidot_vec_kernel(
     __syncthreads();
     if (!is_last) return;
     __threadfence();
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = VT / 32;
-    for (int o = warp; o < k * R; o += nw) {
-        double sum = 0.0;
-        for (int64_t q = lane; q < nchunk; q += 32) sum += __ldcg(partials + (int64_t)o * nchunk + q);
-        sum = warp_sum(sum);
-        if (lane == 0) out[o] = sum;
+    // Each output's chunk partials summed by the whole block, 8 loads in
+    // flight per thread (fixed order: deterministic).
+    for (int o = 0; o < k * R; ++o) {
+        const double sum = sum_partials(partials + (int64_t)o * nchunk, nchunk);
+        if (threadIdx.x == 0) out[o] = sum;
     }
-    __syncthreads();
     if (threadIdx.x == 0) *counter = 0u;
 }
 
@@ -402,17 +396,61 @@ int axpby_impl(T* z, const T* x, const T* y, int64_t n, double a, double b, void
     return launch_status();
 }
 
-inline int64_t md_chunk(int64_t n) {
-    // ~2 waves of blocks per row group; chunks are multiples of 1024 elements.
-    int64_t chunk = 1 << 15;
-    if (n < chunk) chunk = ((n + 1023) / 1024) * 1024;
-    if (chunk < 1024) chunk = 1024;
+// Chunk length: about kMdBlocks blocks in all (152 SMs x 3 resident blocks x
+// 4 waves, so the last wave is nearly full), chunks a multiple of 1024
+// elements and at least 4096.
+constexpr int64_t kMdBlocks = 152 * 3 * 4;
+
+inline int64_t md_chunk(int64_t n, int k) {
+    const int64_t groups = (k + MD_G - 1) / MD_G;
+    int64_t per = kMdBlocks / groups;
+    if (per < 1) per = 1;
+    int64_t chunk = ((n + per - 1) / per + 1023) / 1024 * 1024;
+    if (chunk < 4096) chunk = 4096;
     return chunk;
 }
 
-inline int64_t md_ws_bytes(int64_t n, int k, int r) {
-    const int64_t nchunk = (n + md_chunk(n) - 1) / md_chunk(n);
+// Workspace one call with k rows and r vectors needs.
+inline int64_t md_ws_need(int64_t n, int k, int r) {
+    const int64_t nchunk = (n + md_chunk(n, k) - 1) / md_chunk(n, k);
     return kReduceHeader + (int64_t)k * r * nchunk * (int64_t)sizeof(double);
+}
+
+// Workspace that serves every call with at most k rows and r vectors (fewer
+// rows can mean more chunks, so the need is not monotone in k; its maximum
+// sits at a row count that fills its last group).
+inline int64_t md_ws_bytes(int64_t n, int k, int r) {
+    int64_t most = 0;
+    for (int64_t groups = 1; (groups - 1) * MD_G < k; ++groups) {
+        const int rows = (int)(groups * MD_G < k ? groups * MD_G : k);
+        const int64_t need = md_ws_need(n, rows, r);
+        if (need > most) most = need;
+    }
+    return most;
+}
+
+template <typename T, int G>
+int md_vec_launch(dim3 grid, cudaStream_t st, const T* M, int64_t ld, int k, QPtrs qs, int r,
+                  int64_t n, int64_t chunk, ReduceWs w, double* out) {
+    switch (r) {
+        case 1:
+            multidot_vec_kernel<T, 1, G><<<grid, VT, 0, st>>>(M, ld, k, qs, n, chunk, w.partials,
+                                                               w.counter, out);
+            break;
+        case 2:
+            multidot_vec_kernel<T, 2, G><<<grid, VT, 0, st>>>(M, ld, k, qs, n, chunk, w.partials,
+                                                               w.counter, out);
+            break;
+        case 3:
+            multidot_vec_kernel<T, 3, G><<<grid, VT, 0, st>>>(M, ld, k, qs, n, chunk, w.partials,
+                                                               w.counter, out);
+            break;
+        default:
+            multidot_vec_kernel<T, 4, G><<<grid, VT, 0, st>>>(M, ld, k, qs, n, chunk, w.partials,
+                                                               w.counter, out);
+            break;
+    }
+    return launch_status();
 }
 
 template <typename T>
@@ -420,7 +458,7 @@ int multidot_impl(const T* M, int64_t ld, int k, const void* const* q, int r, in
                   double* out, void* ws, int64_t ws_bytes, void* stream) {
     if (k < 1 || r < 1 || r > MD_MAXR || n < 1 || ld < n || k > 65535) return ODIL_ERR_SHAPE;
     if (!M || !q || !out) return ODIL_ERR_ARG;
-    if (!ws || ws_bytes < md_ws_bytes(n, k, r)) return ODIL_ERR_WORKSPACE;
+    if (!ws || ws_bytes < md_ws_need(n, k, r)) return ODIL_ERR_WORKSPACE;
     QPtrs qs = {};
     bool vec = aligned16(M) && ((ld * (int64_t)sizeof(T)) % 16 == 0);
     for (int j = 0; j < r; ++j) {
@@ -428,31 +466,17 @@ int multidot_impl(const T* M, int64_t ld, int k, const void* const* q, int r, in
         qs.q[j] = q[j];
         vec = vec && aligned16(q[j]);
     }
-    const int64_t chunk = md_chunk(n);
+    const int64_t chunk = md_chunk(n, k);
     const int64_t nchunk = (n + chunk - 1) / chunk;
     if (nchunk > 65535) return ODIL_ERR_SHAPE;
     ReduceWs w = reduce_ws(ws);
     dim3 grid((k + MD_G - 1) / MD_G, (unsigned)nchunk);
     cudaStream_t st = as_stream(stream);
     if (vec) {
-        switch (r) {
-            case 1:
-                multidot_vec_kernel<T, 1><<<grid, VT, 0, st>>>(M, ld, k, qs, n, chunk, w.partials,
-                                                                w.counter, out);
-                return launch_status();
-            case 2:
-                multidot_vec_kernel<T, 2><<<grid, VT, 0, st>>>(M, ld, k, qs, n, chunk, w.partials,
-                                                                w.counter, out);
-                return launch_status();
-            case 3:
-                multidot_vec_kernel<T, 3><<<grid, VT, 0, st>>>(M, ld, k, qs, n, chunk, w.partials,
-                                                                w.counter, out);
-                return launch_status();
-            default:
-                multidot_vec_kernel<T, 4><<<grid, VT, 0, st>>>(M, ld, k, qs, n, chunk, w.partials,
-                                                                w.counter, out);
-                return launch_status();
-        }
+        // Row groups of G = min(k, 4) rows (k = 3 loads row 2 twice).
+        if (k == 1) return md_vec_launch<T, 1>(grid, st, M, ld, k, qs, r, n, chunk, w, out);
+        if (k == 2) return md_vec_launch<T, 2>(grid, st, M, ld, k, qs, r, n, chunk, w, out);
+        return md_vec_launch<T, MD_G>(grid, st, M, ld, k, qs, r, n, chunk, w, out);
     }
     multidot_kernel<T><<<grid, VT, 0, st>>>(M, ld, k, qs, r, n, chunk, w.partials, w.counter, out,
                                             vec);

@@ -67,6 +67,28 @@ def test_multidot_lincomb_axpby(cuda, dtype, n):
     assert np.allclose(z.double().cpu().numpy(), ref, rtol=tol, atol=tol)
 
 
+@pytest.mark.parametrize("dtype", [torch.float32, torch.float64])
+@pytest.mark.parametrize("k", [1, 2, 3, 6])
+@pytest.mark.parametrize("n", [4100, 3000004])
+def test_multidot_row_groups(cuda, dtype, k, n):
+    """Every row-group width of the vector multi-dot (k = 1, 2, >= 3) and
+    every vector count, with many chunks, against an FP64 product."""
+    from odil_gb300 import vec
+    rng = np.random.default_rng(k + n)
+    M = torch.as_tensor(rng.standard_normal((k, n)), dtype=dtype, device=cuda)
+    qs = [torch.as_tensor(rng.standard_normal(n), dtype=dtype, device=cuda)
+          for _ in range(4)]
+    md = vec.MultiDot(n, k + 3, 4, device=cuda)  # sized for more rows
+    Mn = M.double().cpu().numpy()
+    for r in (1, 2, 3, 4):
+        out = md(M.reshape(-1), k, qs[:r]).cpu().numpy()
+        ref = Mn @ np.stack([q.double().cpu().numpy() for q in qs[:r]], 1)
+        tol = 1e-5 if dtype == torch.float32 else 1e-12
+        assert np.allclose(out, ref, rtol=tol, atol=tol * np.sqrt(n)), r
+        again = md(M.reshape(-1), k, qs[:r]).cpu().numpy()
+        assert np.array_equal(out, again)
+
+
 def _wave_problem(n, cuda, profile="sine", seed=3, nmodes=5, dtype=np.float64):
     from odil_gb300.workloads import WaveInstance
     from odil_gb300.problem import Problem
