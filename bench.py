@@ -319,7 +319,7 @@ def run_batch(dev, with_oracle, steps=5):
             u.zero_()
             for _ in range(BATCH_FP64_EPOCHS):
                 k.residual(u, out=r)
-                k.march(r, out=d)
+                k.march_tuned(r, d)
                 vec.axpby(u, 1.0, u, -1.0, d)
 
     plain()
@@ -451,7 +451,7 @@ def run_ours(args):
     t_pair = timed(lambda: k.pair_residual(d32, None, rhs), 20, 3)
     t_init = timed(lambda: k.initial_rhs(rhs), 20, 3)
     r64 = torch.empty_like(u)
-    t_march64 = timed(lambda: k.march(r64, out=ub), 5, 2)
+    t_march64 = timed(lambda: k.march_tuned(r64, ub), 5, 2)
     u32 = u.float()
     g32 = torch.empty_like(u32)
     t_lg = timed(lambda: k.loss_grad(u32, grad=g32), 20, 3)
@@ -535,7 +535,8 @@ def run_ours(args):
         # kernels per solve: boundary rhs (the interior is a memset), march,
         # per further epoch pair rhs (interior + boundary) + march, FP64 write.
         "gpu_launches": (3 * MIXED_EPOCHS) * args.steps,
-        "march_cfg": getattr(k, "_march_cfg", None),
+        "march_cfg": {str(dt): c for dt, c in
+                      getattr(k, "_march_cfgs", {}).items()},
         "march_tune": getattr(k, "march_tune_table", None),
         "clocks": clk,
         "e2e": {"value": 1000.0 / e2e_ms, "unit": "solves/s",
@@ -546,7 +547,8 @@ def run_ours(args):
         "plain_fp64": {"value": 1000.0 / fp64_ms, "unit": "solves/s",
                        "epochs": FP64_EPOCHS,
                        "speedup_mixed_over_fp64": fp64_ms / (total_ms / args.steps)},
-        "roofline": {"kernel": "wave_march_kernel<float>",
+        "roofline": {"kernel": march_kernel_name(
+                         getattr(k, "_march_cfgs", {}).get(torch.float32)),
                      "bound": "hbm", "achieved": march_bytes / (march_ms * 1e6),
                      "peak": hbm, "unit": "GB/s",
                      "frac": march_bytes / (march_ms * 1e6) / hbm,
@@ -557,8 +559,9 @@ def run_ours(args):
                      "traffic": MARCH_NCU_DRAM_BYTES,
                      "traffic_unit": "bytes per launch (ncu)",
                      "peak_source": peak_src,
-                     "note": "latency-bound: one block marches 1024 dependent "
-                             "rows (algorithmic bytes 8 per cell)"},
+                     "note": "latency-bound: 1024 dependent rows marched by "
+                             "column tiles over one thread-block cluster "
+                             "(algorithmic bytes 8 per cell)"},
         "roofline_loss_grad_8192sq": {
             "kernel": "wave_loss_grad_all_kernel<float, 64>", "bound": "hbm",
             "achieved": 8 * BIG * BIG / (statistics.mean(t_lg_big) * 1e6),
@@ -769,7 +772,7 @@ def run_case(args):
         "loss_grad_big": lambda: kb.loss_grad(ubig, grad=gbig),
         "batch": lambda: wb.solve_mixed(),
         "march": lambda: k.march_tuned(rhs, d32),
-        "march64": lambda: k.march(u, out=ub),
+        "march64": lambda: k.march_tuned(u, ub),
         "update_residual": lambda: k.update_residual_mixed(u, d32, ub, rhs),
         "loss_grad": lambda: k.loss_grad(u32, grad=g32),
         "loss_grad64": lambda: k.loss_grad(u, grad=g64),
@@ -785,6 +788,16 @@ def run_case(args):
     torch.cuda.synchronize(dev)
     print(json.dumps({"case": args.case, "launch_groups": args.warmup +
                       args.steps}))
+
+
+def march_kernel_name(cfg):
+    """Kernel name of an FP32 march launch shape (as ncu lists it)."""
+    if not cfg:
+        return "wave_march_kernel<float>"
+    if cfg.get("kind") == "tiled":
+        return "wave_march_tiled_kernel<float, %d, %d, %d, 1, %d>" % (
+            cfg["cpt"], cfg["halo"], cfg["pf"], cfg.get("exchange", 0))
+    return "wave_march_kernel<float, %d, %d, 1>" % (cfg["cpt"], cfg["pf"])
 
 
 def main():

@@ -156,6 +156,39 @@ int odil_wave_pair_residual_mixed(const odil_wave_params* p, const float* hi,
 int odil_wave_march_shape_f32(const odil_wave_params* p, const float* b,
                               float* x, int32_t cpt, int32_t pf, void* stream);
 
+/* odil_wave_march_* spread over one thread-block cluster: each warp owns
+ * 32 cpt - 2 halo columns and marches them with `halo` extra columns on each
+ * side for `halo` rows between halo exchanges (the halo columns are
+ * recomputed, then refreshed from the neighbours), with pf right-hand-side
+ * rows in flight per thread.  Same arithmetic per cell as the single-block
+ * march.  exchange 0: cluster barrier, then the halo is reloaded from the
+ * stored solution; (cpt, halo, pf) in (4, 32, 16), (4, 48, 16), (8, 96, 16).
+ * exchange 1: the neighbours push their edge columns into the warp's shared
+ * memory (st.async, mbarrier wait bounded at 1 s; a warp whose wait gives up
+ * writes NaN from then on and counts the failure); (cpt, halo, pf) in
+ * (2, 16, 16), (4, 8, 8), (4, 16, 16), (4, 24, 8), (4, 32, 16), (8, 32, 16),
+ * (8, 64, 16).  FP64: cpt pf <= 64.  warps = tiles per block, 1..4; the
+ * cluster (ceil(nx / (32 cpt - 2 halo)) / warps blocks) must hold at most 16
+ * blocks and fit on the device; nx >= 2.  ODIL_ERR_SHAPE otherwise. */
+int odil_wave_march_tiled_f32(const odil_wave_params* p, const float* b,
+                              float* x, int32_t cpt, int32_t halo, int32_t pf,
+                              int32_t warps, int32_t exchange, void* stream);
+int odil_wave_march_tiled_f64(const odil_wave_params* p, const double* b,
+                              double* x, int32_t cpt, int32_t halo, int32_t pf,
+                              int32_t warps, int32_t exchange, void* stream);
+/* Test hook of the bounded halo wait: odil_wave_march_tiled_f32 with
+ * exchange 1 whose every wait expects `missing_bytes` (1..65536) more than
+ * ever arrive, so each wait gives up after its limit. */
+int odil_wave_march_tiled_planted_wait_f32(const odil_wave_params* p,
+                                           const float* b, float* x,
+                                           int32_t cpt, int32_t halo,
+                                           int32_t pf, int32_t warps,
+                                           int32_t missing_bytes,
+                                           void* stream);
+/* Number of halo waits that gave up since the last reset (synchronises the
+ * device). */
+int odil_wave_march_tiled_wait_failures(int64_t* count, int32_t reset);
+
 /* ------------------------------------------------------------------------
  * Batched wave instances of uneven sizes (the reference runs them as
  * separate processes, vary_wave.py:7-43).  Fields of all instances are

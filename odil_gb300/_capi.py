@@ -12,6 +12,7 @@ import torch
 from . import _build
 
 ODIL_OK = 0
+ODIL_ERR_SHAPE = -1
 _STATUS = {
     -1: "ODIL_ERR_SHAPE",
     -2: "ODIL_ERR_DTYPE",
@@ -160,6 +161,13 @@ SIGNATURES = {
     "odil_wave_initial_rhs_mixed": (_INT, [_P, _P, _P]),
     "odil_wave_march_shape_f32": (_INT, [_P, _P, _P, ctypes.c_int32,
                                          ctypes.c_int32, _P]),
+    "odil_wave_march_tiled_f32": (_INT, [_P, _P, _P] + [ctypes.c_int32] * 5
+                                  + [_P]),
+    "odil_wave_march_tiled_f64": (_INT, [_P, _P, _P] + [ctypes.c_int32] * 5
+                                  + [_P]),
+    "odil_wave_march_tiled_planted_wait_f32": (_INT, [_P, _P, _P]
+                                               + [ctypes.c_int32] * 5 + [_P]),
+    "odil_wave_march_tiled_wait_failures": (_INT, [_P, ctypes.c_int32]),
     "odil_add_f32_to_f64": (_INT, [_P, _P, _P, _I64, _P]),
     "odil_pair_to_f64": (_INT, [_P, _P, _P, _I64, _P]),
     "odil_bicgstab_scalars": (_INT, [_P, _P, ctypes.c_int32, _P]),

@@ -11,6 +11,8 @@ import statistics
 
 import torch
 
+from ._capi import ODIL_ERR_SHAPE, OdilError
+
 
 def _cache_path():
     return os.environ.get(
@@ -113,38 +115,70 @@ def march_max_threads(cpt, pf):
     return 1024 if b <= 64 else (512 if b <= 128 else 256)
 
 
-def candidates_march(nx):
+# (cpt, halo, pf, exchange) of the cluster-tiled march (exchange 0: cluster
+# barrier and reload from global memory; 1: pushes into the neighbours'
+# shared memory).
+TILED_SHAPES = ((4, 32, 16, 0), (4, 48, 16, 0), (8, 96, 16, 0),
+                (2, 16, 16, 1), (4, 8, 8, 1), (4, 16, 16, 1), (4, 24, 8, 1),
+                (4, 32, 16, 1), (8, 32, 16, 1), (8, 64, 16, 1))
+
+
+def candidates_march(nx, dtype=torch.float32):
+    """Single-block shapes (FP32; the FP64 entry point's own shape) and
+    cluster-tiled shapes with at most 16 blocks."""
     out = []
-    for cpt in (1, 2, 4, 8):
-        threads = ((nx + cpt - 1) // cpt + 31) // 32 * 32
-        if cpt > 1 and (nx + cpt - 1) // cpt < 32:
-            continue
-        for pf in (8, 16):
-            if threads <= march_max_threads(cpt, pf):
-                out.append({"cpt": cpt, "pf": pf})
+    if dtype == torch.float32:
+        for cpt in (1, 2, 4, 8):
+            threads = ((nx + cpt - 1) // cpt + 31) // 32 * 32
+            if cpt > 1 and (nx + cpt - 1) // cpt < 32:
+                continue
+            for pf in (8, 16):
+                if threads <= march_max_threads(cpt, pf):
+                    out.append({"kind": "block", "cpt": cpt, "pf": pf})
+    elif nx <= 2048:
+        out.append({"kind": "default"})
+    if nx >= 2:
+        for cpt, halo, pf, exch in TILED_SHAPES:
+            if dtype == torch.float64 and cpt * pf > 64:
+                continue  # register ring too large for FP64
+            tiles = -(-nx // (32 * cpt - 2 * halo))
+            for warps in (1, 2, 4):
+                if (warps > 1 and warps > tiles) or -(-tiles // warps) > 16:
+                    continue
+                out.append({"kind": "tiled", "cpt": cpt, "halo": halo,
+                            "pf": pf, "warps": warps, "exchange": exch})
     return out
 
 
-def tune_march(kernels, cache=True):
-    """Launch shape of the single-instance FP32 forward substitution."""
+def tune_march(kernels, cache=True, dtype=torch.float32):
+    """Launch shape of the single-instance forward substitution."""
     dev = torch.cuda.get_device_name(kernels.device)
-    key = "wave_march|%s|nx%d|nt%d" % (dev, kernels.nx,
-                                        _pow2_bucket(kernels.nt))
+    key = "wave_march4|%s|%s|nx%d|nt%d" % (dev, str(dtype), kernels.nx,
+                                           _pow2_bucket(kernels.nt))
     data = _load() if cache else {}
+    table = kernels.__dict__.setdefault("march_tune_table", {})
     if key in data:
-        kernels.march_tune_table = data[key].get("tried")
+        table[str(dtype)] = data[key].get("tried")
         return data[key]["cfg"]
-    b = torch.zeros(kernels.shape, dtype=torch.float32, device=kernels.device)
+    b = torch.zeros(kernels.shape, dtype=dtype, device=kernels.device)
     x = torch.empty_like(b)
-    kernels.initial_rhs(b)
+    if dtype == torch.float32:
+        kernels.initial_rhs(b)
+    else:
+        b.normal_(generator=torch.Generator(kernels.device).manual_seed(0))
     best = None
     results = []
-    for cfg in candidates_march(kernels.nx):
-        t = _time(lambda: kernels.march_shape(b, x, cfg["cpt"], cfg["pf"]))
+    for cfg in candidates_march(kernels.nx, dtype):
+        try:
+            t = _time(lambda: kernels.march_shape(b, x, cfg))
+        except OdilError as e:
+            if e.status != ODIL_ERR_SHAPE:
+                raise
+            continue  # e.g. a cluster that does not fit on this device
         results.append((t, cfg))
         if best is None or t < best[0]:
             best = (t, cfg)
-    kernels.march_tune_table = [[t, c] for t, c in results]
+    table[str(dtype)] = [[t, c] for t, c in results]
     if cache:
         data[key] = {"cfg": best[1], "ms": best[0],
                      "tried": [[t, c] for t, c in results]}

@@ -87,7 +87,7 @@ def solve(problem, state, precision="mixed", epochs=None, rnorm2=None,
         r = _scratch(k, "r64", torch.float64)
         for _ in range(epochs):
             k.residual(u, out=r)
-            d = k.march(r, out=_scratch(k, "d64", torch.float64))
+            d = k.march_tuned(r, _scratch(k, "d64", torch.float64))
             vec.axpby(u, 1.0, u, -1.0, d)  # J d = F(u)  ->  u -= d
     else:
         raise ValueError("Unknown precision=" + precision)

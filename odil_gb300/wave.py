@@ -174,19 +174,40 @@ class WaveKernels:
         call("odil_wave_march_" + sfx, p, ptr(b), ptr(out), stream_handle())
         return out
 
-    def march_shape(self, b, out, cpt, pf):
-        """FP32 forward substitution with an explicit launch shape."""
-        call("odil_wave_march_shape_f32", ctypes.byref(self.p32), ptr(b),
-             ptr(out), int(cpt), int(pf), stream_handle())
+    def march_shape(self, b, out, cpt, pf=None):
+        """Forward substitution with an explicit launch shape: `cpt` is a
+        shape dict or, with `pf`, the block shape's column count.  Shapes:
+        {"kind": "block", "cpt", "pf"}: one thread block (FP32 only);
+        {"kind": "tiled", "cpt", "halo", "pf", "warps", "exchange"}: column
+        tiles over a thread-block cluster; {"kind": "default"}: the plain
+        entry point's own choice."""
+        cfg = cpt if isinstance(cpt, dict) else {"kind": "block", "cpt": cpt,
+                                                 "pf": pf}
+        kind = cfg.get("kind", "block")
+        p, sfx = self._pp(b)
+        if kind == "tiled":
+            call("odil_wave_march_tiled_" + sfx, p, ptr(b), ptr(out),
+                 int(cfg["cpt"]), int(cfg["halo"]), int(cfg["pf"]),
+                 int(cfg["warps"]), int(cfg.get("exchange", 0)),
+                 stream_handle())
+        elif kind == "default":
+            call("odil_wave_march_" + sfx, p, ptr(b), ptr(out),
+                 stream_handle())
+        else:
+            if sfx != "f32":
+                raise ValueError("explicit block shapes are FP32 only")
+            call("odil_wave_march_shape_f32", p, ptr(b), ptr(out),
+                 int(cfg["cpt"]), int(cfg["pf"]), stream_handle())
         return out
 
     def march_tuned(self, b, out):
-        """FP32 forward substitution with the autotuned launch shape."""
-        if getattr(self, "_march_cfg", None) is None:
+        """Forward substitution with the autotuned launch shape for b's
+        precision (FP32 or FP64)."""
+        tuned = self.__dict__.setdefault("_march_cfgs", {})
+        if b.dtype not in tuned:
             from . import autotune
-            self._march_cfg = autotune.tune_march(self)
-        cfg = self._march_cfg
-        return self.march_shape(b, out, cfg["cpt"], cfg["pf"])
+            tuned[b.dtype] = autotune.tune_march(self, dtype=b.dtype)
+        return self.march_shape(b, out, tuned[b.dtype])
 
     def initial_rhs(self, rhs):
         """rhs = float32(-F(0)) (boundary cells only do FP64 work)."""

@@ -170,9 +170,11 @@ def test_march_direct_solve(cuda, shape):
 
 @pytest.mark.parametrize("shape", [(5, 1), (40, 33), (300, 257), (1100, 1024)])
 def test_march_shapes_agree(cuda, shape):
-    """Every explicit FP32 launch shape gives the same forward substitution
-    (same formula per cell; 1e-5 relative allows for a different FMA
-    contraction between template instances)."""
+    """Every explicit FP32 launch shape (single block or cluster-tiled)
+    gives the same forward substitution (same formula per cell; 1e-5
+    relative allows for a different FMA contraction between template
+    instances) and is as accurate as the single-block march against the
+    FP64 solve."""
     from odil_gb300 import autotune
     s = _setup(*shape, seed=8, c=0.9)
     assert shape[0] <= 5 or s.c * s.dt / s.dx < 1  # stable march, finite x
@@ -183,10 +185,48 @@ def test_march_shapes_agree(cuda, shape):
     assert torch.isfinite(ref).all()
     cands = autotune.candidates_march(shape[1])
     assert cands
+    if shape[1] >= 2:
+        assert any(c["kind"] == "tiled" for c in cands)
+    exact = k.march(b.double()).cpu().numpy()
+    ref_err = _rel(ref.cpu().numpy(), exact)
     for cfg in cands:
         x = torch.full_like(b, float("nan"))
-        k.march_shape(b, x, cfg["cpt"], cfg["pf"])
+        k.march_shape(b, x, cfg)
         assert _rel(x.cpu().numpy(), ref.cpu().numpy()) < 1e-5, cfg
+        err = _rel(x.cpu().numpy(), exact)
+        assert err <= max(1.5 * ref_err, 1e-6), (cfg, err, ref_err)
+    # FP64: the cluster-tiled shapes against the single-block march.
+    b64 = b.double()
+    ref64 = k.march(b64).cpu().numpy()
+    for cfg in autotune.candidates_march(shape[1], torch.float64):
+        x = torch.full_like(b64, float("nan"))
+        k.march_shape(b64, x, cfg)
+        assert _rel(x.cpu().numpy(), ref64) < 1e-12, cfg
+
+
+@pytest.mark.parametrize("shape", [(3, 2), (40, 70), (130, 96), (2000, 3000)])
+def test_march_tiled_matches_oracle(cuda, shape):
+    """Cluster-tiled forward substitution against the FP64 oracle, including
+    rows that are not a multiple of the halo depth, a window wider than the
+    row, and a row too wide for the single-block march."""
+    from odil_gb300 import autotune
+    s = _setup(*shape, seed=4, c=0.9)
+    assert shape[0] <= 3 or s.c * s.dt / s.dx < 1
+    k = _kernels(s, cuda)
+    b = np.random.default_rng(5).standard_normal(shape)
+    xo = W.march(s, b)
+    for dtype, tol in ((torch.float64, 1e-10), (torch.float32, 1e-3)):
+        bt = torch.as_tensor(b, dtype=dtype, device=cuda)
+        cands = [c for c in autotune.candidates_march(shape[1], dtype)
+                 if c["kind"] == "tiled"]
+        assert cands
+        for cfg in cands:
+            x = torch.full_like(bt, float("nan"))
+            k.march_shape(bt, x, cfg)
+            assert _rel(x.cpu().numpy(), xo) < tol, (dtype, cfg)
+        x = torch.full_like(bt, float("nan"))
+        k.march_tuned(bt, x)
+        assert _rel(x.cpu().numpy(), xo) < tol
 
 
 def test_initial_rhs_and_f32_update(cuda):
@@ -414,3 +454,35 @@ def test_errors_are_loud(cuda):
     k2 = _kernels(s2, cuda)
     with pytest.raises(OdilError):
         k2.march(torch.zeros((4, 4096), dtype=torch.float64, device=cuda))
+
+
+def test_march_tiled_wait_gives_up(cuda):
+    """The bounded halo wait of the shared-memory exchange: a planted wait
+    for bytes that never arrive gives up (about a second), the warps write
+    NaN instead of hanging, the failure is counted, and the next regular
+    launch on the same context is correct again."""
+    import ctypes
+    from odil_gb300._capi import call, ptr, stream_handle
+    s = _setup(256, 256, seed=4, c=0.9)
+    assert s.c * s.dt / s.dx < 1
+    k = _kernels(s, cuda)
+    b = torch.as_tensor(np.random.default_rng(5).standard_normal(s.shape),
+                        dtype=torch.float32, device=cuda)
+    n = ctypes.c_int64(0)
+    call("odil_wave_march_tiled_wait_failures", ctypes.byref(n), 1)
+    x = torch.zeros_like(b)
+    call("odil_wave_march_tiled_planted_wait_f32", ctypes.byref(k.p32),
+         ptr(b), ptr(x), 4, 16, 16, 1, 16, stream_handle())
+    torch.cuda.synchronize(cuda)
+    call("odil_wave_march_tiled_wait_failures", ctypes.byref(n), 1)
+    assert n.value >= 1
+    assert torch.isnan(x[16:]).any()
+    cfg = {"kind": "tiled", "cpt": 4, "halo": 16, "pf": 16, "warps": 1,
+           "exchange": 1}
+    y = torch.full_like(b, float("nan"))
+    k.march_shape(b, y, cfg)
+    ref = k.march(b)
+    assert torch.isfinite(ref).all()
+    assert _rel(y.cpu().numpy(), ref.cpu().numpy()) < 1e-4
+    call("odil_wave_march_tiled_wait_failures", ctypes.byref(n), 0)
+    assert n.value == 0
