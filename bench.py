@@ -410,16 +410,27 @@ def run_ours(args):
     u = torch.zeros((NT, NX), dtype=torch.float64, device=dev)
     state = State(fields={"u": u})
 
-    def solve_mixed():
-        newton.solve(problem, state, "mixed", MIXED_EPOCHS, from_zero=True)
+    # Each timed solve is one replay of the solve's launch sequence captured
+    # in a CUDA graph (newton.CapturedSolve), so host launch overhead stays
+    # out of the device time; both methods are timed the same way.
+    solve_mixed = newton.CapturedSolve(problem, state, "mixed", MIXED_EPOCHS)
+    solve_fp64 = newton.CapturedSolve(problem, state, "fp64", FP64_EPOCHS)
 
-    def solve_fp64():
-        u.zero_()
-        newton.solve(problem, state, "fp64", FP64_EPOCHS)
-
+    # The timed steps take milliseconds, shorter than nvidia-smi's 200 ms
+    # sampling period, so the sampler starts before an untimed ~0.6 s run of
+    # the same solve loop (extra warm-up at the same load) and stops after
+    # the timed steps: its samples are the clocks under this workload.
     clocks = Clocks(local)
+    t_end = time.perf_counter() + 0.6
+    while time.perf_counter() < t_end:
+        for _ in range(50):
+            flush.zero_()
+            solve_mixed()
+        torch.cuda.synchronize(dev)
     t_mixed = timed(solve_mixed, args.steps, args.warmup)
     clk = clocks.stop()
+    clk["sampled"] = ("during a 0.6 s untimed run of the same solve loop "
+                      "right before the timed steps, and the timed steps")
     u_mixed = u.cpu().numpy()
     t_fp64 = timed(solve_fp64, max(3, args.steps // 2), max(3, args.warmup))
     u_fp64 = u.cpu().numpy()
@@ -429,15 +440,11 @@ def run_ours(args):
     sweep = {"mixed": {}, "fp64": {}}
     sweep_u = {"mixed": {}, "fp64": {}}
     for ep in (1, 2, 3):
-        t = timed(lambda: newton.solve(problem, state, "mixed", ep,
-                                       from_zero=True), 5, 3)
+        t = timed(newton.CapturedSolve(problem, state, "mixed", ep), 5, 3)
         sweep["mixed"][ep] = {"ms": statistics.mean(t)}
         sweep_u["mixed"][ep] = u.cpu().numpy()
     for ep in (1, 2):
-        def f64(ep=ep):
-            u.zero_()
-            newton.solve(problem, state, "fp64", ep)
-        t = timed(f64, 3, 2)
+        t = timed(newton.CapturedSolve(problem, state, "fp64", ep), 3, 2)
         sweep["fp64"][ep] = {"ms": statistics.mean(t)}
         sweep_u["fp64"][ep] = u.cpu().numpy()
 
@@ -482,11 +489,12 @@ def run_ours(args):
     d2h = out_host.numel() * 8
 
     # newton.CapturedSolve: new boundary data H2D (and its FP32 copies),
-    # the solve, the solution D2H, replayed as one CUDA graph per step.
+    # the solve, the solution D2H into pinned host memory, replayed as one
+    # CUDA graph per step.
     cap = newton.CapturedSolve(
         problem, state, "mixed", MIXED_EPOCHS,
         inputs=list(zip(bc_host, k.bc64)) + list(zip(k.bc64, k.bc32)),
-        outputs=[(u, out_host)])
+        host_out=out_host)
     t_e2e = timed(cap, args.steps, args.warmup)
     if rank == 0 and not args.no_cpu_baseline:
         e2e_u = out_host.numpy().copy()
@@ -531,6 +539,8 @@ def run_ours(args):
                    "method": "newton mixed (FP64 residual, FP32 forward "
                              "substitution), %d epochs" % MIXED_EPOCHS,
                    "l2": "flushed (256 MiB write) before every timed solve",
+                   "timing": "one CUDA graph replay per solve "
+                             "(newton.CapturedSolve), CUDA events",
                    "parallelism": "replicas" if world > 1 else "single"},
         # kernels per solve: boundary rhs (the interior is a memset), march,
         # per further epoch pair rhs (interior + boundary) + march, FP64 write.
@@ -542,8 +552,8 @@ def run_ours(args):
         "e2e": {"value": 1000.0 / e2e_ms, "unit": "solves/s",
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "api": "odil_gb300.newton.CapturedSolve (boundary H2D, mixed "
-                       "Newton solve, solution D2H; one graph replay per "
-                       "step)"},
+                       "Newton solve, FP64 solution D2H into pinned host "
+                       "memory; one graph replay per step)"},
         "plain_fp64": {"value": 1000.0 / fp64_ms, "unit": "solves/s",
                        "epochs": FP64_EPOCHS,
                        "speedup_mixed_over_fp64": fp64_ms / (total_ms / args.steps)},

@@ -486,3 +486,33 @@ def test_march_tiled_wait_gives_up(cuda):
     assert _rel(y.cpu().numpy(), ref.cpu().numpy()) < 1e-4
     call("odil_wave_march_tiled_wait_failures", ctypes.byref(n), 0)
     assert n.value == 0
+
+
+def test_solve_host_out(cuda):
+    """host_out receives the FP64 solution (a copy into pinned host memory)
+    equal to the device state bit for bit, also when replayed from a
+    graph; a host tensor that is not pinned is rejected."""
+    from odil_gb300 import newton
+    from odil_gb300.domain import State
+    from odil_gb300.problem import Problem
+    from odil_gb300.workloads import WaveInstance
+    inst = WaveInstance(256, 256, profile="sine", seed=2, nmodes=5,
+                        device=cuda)
+    prob = Problem(inst.operator, inst.domain)
+    u = torch.zeros((256, 256), dtype=torch.float64, device=cuda)
+    st = State(fields={"u": u})
+    host = torch.full((256, 256), float("nan"), dtype=torch.float64).pin_memory()
+    for prec, ep in (("mixed", 1), ("mixed", 2), ("fp64", 1)):
+        host.fill_(float("nan"))
+        newton.solve(prob, st, prec, ep, from_zero=True, host_out=host)
+        torch.cuda.synchronize(cuda)
+        assert torch.equal(host, u.cpu()), (prec, ep)
+    host.fill_(float("nan"))
+    cap = newton.CapturedSolve(prob, st, "mixed", 1, host_out=host)
+    host.fill_(float("nan"))
+    cap()
+    torch.cuda.synchronize(cuda)
+    assert torch.equal(host, u.cpu())
+    with pytest.raises(ValueError):
+        newton.solve(prob, st, "mixed", 1, from_zero=True,
+                     host_out=torch.zeros((256, 256), dtype=torch.float64))
