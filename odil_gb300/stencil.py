@@ -134,6 +134,116 @@ class StencilOp:
         return StencilOp(self.shifts, self.coef.to(dtype), self.nw,
                          self.stride, self.periodic)
 
+    # -- constructors and coefficient-field algebra (multigrid.py:923-1216);
+    # torch ops on the coefficient fields, on the fields' device.
+    @staticmethod
+    def eye(nw, stride=1, periodic=None, dtype=torch.float64, device="cuda"):
+        """Identity (multigrid.py:923-927), restricted by `stride`."""
+        nw = tuple(int(n) for n in nw)
+        per = tuple(bool(p) for p in (periodic or (False, ) * len(nw)))
+        nwh = tuple((n // 2) if (p and stride == 2) else (n - 1) // stride + 1
+                    for n, p in zip(nw, per))
+        return StencilOp([(0, ) * len(nw)],
+                         torch.ones((1, ) + nwh, dtype=dtype, device=device),
+                         nw, stride, per)
+
+    @staticmethod
+    def from_diag(c, nw, stride=1, periodic=None):
+        """diag(c) (the reference's static `SparseOperator.diag`,
+        multigrid.py:929-933); `c` has the output grid's shape."""
+        nw = tuple(int(n) for n in nw)
+        return StencilOp([(0, ) * len(nw)], c.reshape((1, ) + tuple(c.shape)),
+                         nw, stride, periodic)
+
+    @staticmethod
+    def apply_stride(u, stride):
+        """u[::stride, ...] (multigrid.py:935-940)."""
+        return u[(slice(None, None, int(stride)), ) * u.dim()]
+
+    @staticmethod
+    def apply_shift(u, dw, periodic=None):
+        """The field u[i + dw] (multigrid.py:942-947): zero where i + dw is
+        outside the grid, wrapped on periodic axes."""
+        dw = tuple(int(v) for v in dw)
+        periodic = periodic or (False, ) * u.dim()
+        res = u
+        for ax, (s, p) in enumerate(zip(dw, periodic)):
+            if s == 0:
+                continue
+            if p:
+                res = torch.roll(res, -s, ax)
+                continue
+            out = torch.zeros_like(res)
+            n = res.shape[ax]
+            if abs(s) < n:
+                src = [slice(None)] * res.dim()
+                dst = [slice(None)] * res.dim()
+                if s > 0:
+                    src[ax], dst[ax] = slice(s, n), slice(0, n - s)
+                else:
+                    src[ax], dst[ax] = slice(0, n + s), slice(-s, n)
+                out[tuple(dst)] = res[tuple(src)]
+            res = out
+        return res
+
+    def _with(self, shifts, coef):
+        return StencilOp(shifts, coef, self.nw, self.stride, self.periodic)
+
+    def eliminate_zeros(self):
+        """Drops the shifts whose coefficients are all zero, in place
+        (multigrid.py:949-956)."""
+        keep = [i for i in range(len(self.shifts))
+                if bool(torch.any(self.coef[i] != 0))]
+        self.shifts = [self.shifts[i] for i in keep]
+        self.coef = self.coef[keep].contiguous() if keep else \
+            self.coef[:0].contiguous()
+        self._s = self._struct()
+        return self
+
+    def mul_self_transpose(self):
+        """A^T A (multigrid.py:1073-1074)."""
+        return self.mul_transpose_op(self)
+
+    def mul_op(self, other):
+        """A B: not provided by the reference either (multigrid.py:1076-1093
+        raises before its body)."""
+        raise NotImplementedError
+
+    def mul_elementwise(self, other):
+        """Hadamard product on the common shifts (multigrid.py:1095-1136)."""
+        if self.nw != other.nw or self.stride != other.stride:
+            raise ValueError("grid sizes or strides differ")
+        common = [s for s in self.shifts if s in other.shifts]
+        common = sorted(common, key=_serialize)
+        coef = torch.stack([self.coef[self.shifts.index(s)] *
+                            other.coef[other.shifts.index(s)]
+                            for s in common]) if common else \
+            self.coef[:0].clone()
+        return self._with(common, coef)
+
+    def add_elementwise(self, other):
+        """A + B (multigrid.py:1138-1184)."""
+        if self.nw != other.nw or self.stride != other.stride:
+            raise ValueError("grid sizes or strides differ")
+        return self.add(other)
+
+    def shift_left(self, shift):
+        """The operator whose output is shifted: (A' u)[i] = (A u)[i + shift]
+        (multigrid.py:1186-1201)."""
+        shift = tuple(int(v) for v in shift)
+        shifts = [tuple(a + self.stride * b for a, b in zip(dw, shift))
+                  for dw in self.shifts]
+        coef = torch.stack([self.apply_shift(c, shift, self.periodic)
+                            for c in self.coef]) if self.shifts else self.coef
+        return self._with(shifts, coef)
+
+    def shift_right(self, shift):
+        """The operator applied to a shifted input: (A' u)[i] = sum_dw
+        c_dw[i] u[stride i + dw + shift] (multigrid.py:1203-1215)."""
+        shift = tuple(int(v) for v in shift)
+        shifts = [tuple(a + b for a, b in zip(dw, shift)) for dw in self.shifts]
+        return self._with(shifts, self.coef.clone())
+
     def add(self, other):
         """Elementwise sum (multigrid.py:1153-1196)."""
         shifts = sorted(set(self.shifts) | set(other.shifts))
@@ -144,6 +254,12 @@ class StencilOp:
         for s, c in zip(other.shifts, other.coef):
             coef[shifts.index(s)] += c
         return StencilOp(shifts, coef, self.nw, self.stride, self.periodic)
+
+
+def _serialize(dw, bits=3):
+    """Sort key of a shift, the reference's StencilDict.serialize
+    (multigrid.py:684-687)."""
+    return sum((i + 2**bits) << ((1 + bits) * n) for n, i in enumerate(dw))
 
 
 def _shifts(dim, r):

@@ -166,3 +166,84 @@ def test_stencil_to_csr_reference_layout(shape):
     J = StencilOp(WaveKernels.SLOT_SHIFTS, coef, shape).to_csr().to_dense()
     _, Jo = W.linearize(s, np.zeros(shape))
     assert np.array_equal(J.numpy(), Jo.toarray())
+
+
+def _dense_of(op):
+    """Dense matrix of a StencilOp from its definition: output cell i, input
+    cell stride*i + dw, dropped outside the grid on non-periodic axes and
+    wrapped on periodic ones."""
+    import itertools
+    nw, nwh = op.nw, op.nwh
+    M = np.zeros((int(np.prod(nwh)), int(np.prod(nw))))
+    coef = op.coef.double().cpu().numpy()
+    for k, dw in enumerate(op.shifts):
+        for i in itertools.product(*[range(n) for n in nwh]):
+            j = []
+            for a in range(len(nw)):
+                v = op.stride * i[a] + dw[a]
+                if op.periodic[a]:
+                    v %= nw[a]
+                elif not 0 <= v < nw[a]:
+                    break
+                j.append(v)
+            else:
+                M[np.ravel_multi_index(i, nwh),
+                  np.ravel_multi_index(tuple(j), nw)] += coef[(k, ) + i]
+    return M
+
+
+@pytest.mark.parametrize("periodic", [(False, False), (True, False)])
+def test_stencil_coefficient_algebra(periodic):
+    """The SparseOperator algebra of multigrid.py:923-1216 on coefficient
+    fields (torch ops, checked here on CPU tensors against dense matrices
+    built from the operator definition)."""
+    import torch
+    from odil_gb300.stencil import StencilOp
+    rng = np.random.default_rng(1)
+    nw = (6, 5)
+    sh_a = [(0, 0), (-1, 0), (1, 0), (0, 1), (1, -1)]
+    sh_b = [(0, 0), (0, 1), (2, 0)]
+    A = StencilOp(sh_a, torch.as_tensor(rng.standard_normal((5, ) + nw)), nw,
+                  periodic=periodic)
+    B = StencilOp(sh_b, torch.as_tensor(rng.standard_normal((3, ) + nw)), nw,
+                  periodic=periodic)
+    dA, dB = _dense_of(A), _dense_of(B)
+    n = int(np.prod(nw))
+    u = rng.standard_normal(nw)
+    I = StencilOp.eye(nw, periodic=periodic, device="cpu")
+    assert np.array_equal(_dense_of(I), np.eye(n))
+    I2 = StencilOp.eye(nw, stride=2, device="cpu")
+    assert np.array_equal(_dense_of(I2) @ u.ravel(), u[::2, ::2].ravel())
+    c = torch.as_tensor(rng.standard_normal(nw))
+    assert np.allclose(_dense_of(StencilOp.from_diag(c, nw)),
+                       np.diag(c.numpy().ravel()))
+    assert np.allclose(_dense_of(A.add_elementwise(B)), dA + dB)
+    if not any(periodic):
+        # Shifts that alias under the periodic wrap would merge entries.
+        assert np.allclose(_dense_of(A.mul_elementwise(B)), dA * dB)
+    assert A.mul_elementwise(B).shifts == [(0, 0), (0, 1)]
+    # shift_left: the output shifted, (A' u)[i] = (A u)[i + s].
+    for s in [(1, 0), (-1, 2), (0, -1)]:
+        Au = (dA @ u.ravel()).reshape(nw)
+        ref = StencilOp.apply_shift(torch.as_tensor(Au), s, periodic).numpy()
+        got = (_dense_of(A.shift_left(s)) @ u.ravel()).reshape(nw)
+        assert np.allclose(got, ref), s
+    # shift_right: the input shifted, (A' u)[i] = sum c_dw[i] u[i + dw + s].
+    for s in [(1, 0), (0, -2)]:
+        Ar = A.shift_right(s)
+        assert Ar.shifts == [(a + s[0], b + s[1]) for a, b in sh_a]
+        assert torch.equal(Ar.coef, A.coef)
+    # eliminate_zeros drops the all-zero shifts in place.
+    coef = A.coef.clone()
+    coef[2] = 0
+    Z = StencilOp(sh_a, coef, nw, periodic=periodic).eliminate_zeros()
+    assert Z.shifts == [s for k, s in enumerate(sh_a) if k != 2]
+    assert np.allclose(_dense_of(Z), _dense_of(StencilOp(sh_a, coef, nw,
+                                                         periodic=periodic)))
+    with pytest.raises(NotImplementedError):
+        A.mul_op(B)
+    # apply_stride / apply_shift conventions (u[::s], u[i + dw]).
+    ut = torch.as_tensor(u)
+    assert torch.equal(StencilOp.apply_stride(ut, 2), ut[::2, ::2])
+    sh = StencilOp.apply_shift(ut, (1, -1)).numpy()
+    assert sh[0, 1] == u[1, 0] and sh[0, 0] == 0 and sh[-1, 2] == 0

@@ -142,3 +142,40 @@ def test_multigrid_poisson(cuda, dtype):
         uo = mgo.step(uo, f.double().cpu().numpy(), smo, ndirect=3)
     if dtype == torch.float64:
         assert np.allclose(u[0].cpu().numpy(), uo, atol=1e-10)
+
+
+def test_coefficient_algebra_applies_on_device(cuda):
+    """Operators built by the coefficient algebra (shift_left/right,
+    mul_elementwise, add_elementwise, eye, from_diag, mul_self_transpose)
+    applied by the device kernel equal the products they stand for."""
+    from odil_gb300.stencil import StencilOp
+    rng = np.random.default_rng(3)
+    nw = (7, 6)
+    n = int(np.prod(nw))
+    sh = [(0, 0), (-1, 0), (1, 0), (0, 1), (1, -1)]
+    A = StencilOp(sh, torch.as_tensor(rng.standard_normal((5, ) + nw),
+                                      device=cuda), nw)
+    B = StencilOp([(0, 0), (0, 1)], torch.as_tensor(
+        rng.standard_normal((2, ) + nw), device=cuda), nw)
+    dA, dB = _dense(A, nw, cuda), _dense(B, nw, cuda)
+    u = torch.as_tensor(rng.standard_normal(nw), device=cuda)
+    un = u.cpu().numpy().ravel()
+    for s in [(1, 0), (-1, 2)]:
+        Au = torch.as_tensor((dA @ un).reshape(nw))
+        ref = StencilOp.apply_shift(Au, s).numpy()
+        got = A.shift_left(s).mul_field(u).cpu().numpy()
+        assert np.allclose(got, ref, atol=1e-13), s
+        got = A.shift_right(s).mul_field(u).cpu().numpy()
+        ref = sum(A.coef[k].cpu().numpy() * StencilOp.apply_shift(
+            u, tuple(a + b for a, b in zip(dw, s))).cpu().numpy()
+            for k, dw in enumerate(sh))
+        assert np.allclose(got, ref, atol=1e-13), s
+    assert np.allclose(_dense(A.add_elementwise(B), nw, cuda), dA + dB)
+    assert np.allclose(_dense(A.mul_elementwise(B), nw, cuda), dA * dB)
+    assert np.allclose(_dense(StencilOp.eye(nw, dtype=torch.float64,
+                                            device=cuda), nw, cuda), np.eye(n))
+    c = torch.as_tensor(rng.standard_normal(nw), device=cuda)
+    assert np.allclose(_dense(StencilOp.from_diag(c, nw), nw, cuda),
+                       np.diag(c.cpu().numpy().ravel()))
+    assert np.allclose(_dense(A.mul_self_transpose(), nw, cuda), dA.T @ dA,
+                       atol=1e-12)
