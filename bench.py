@@ -63,7 +63,7 @@ def parse():
                     choices=("march", "march64", "update_residual", "loss_grad",
                              "loss_grad64", "loss_grad_big", "lbfgs_iter",
                              "adam_iter", "batch", "ns_newton", "advect",
-                             "ns_inverse"),
+                             "ns_inverse", "generic"),
                     help="run one kernel of the workload --steps times (for "
                     "profiler captures) instead of the benchmark")
     return ap.parse_args()
@@ -800,6 +800,50 @@ def run_case(args):
                       args.steps}))
 
 
+def run_generic(args):
+    """The wave operator written as a generic ``operator(mod, ctx)`` on the
+    1024^2 grid: loss + gradient through the stencil compiler's kernels,
+    through the op-by-op torch path, and through the registered family's
+    fused kernel (FP64; CUDA events around --steps calls each)."""
+    import torch
+    from odil_gb300.domain import State
+    from odil_gb300.problem import Problem
+    from odil_gb300.workloads import WaveInstance
+    dev = torch.device("cuda", 0)
+    inst = WaveInstance(NT, NX, profile="sine", seed=SEED, nmodes=NMODES, c=C,
+                        device=dev)
+
+    def op(mod, ctx):
+        return inst.operator(mod, ctx)
+
+    st = State(fields={"u": torch.randn((NT, NX), dtype=torch.float64,
+                                        device=dev)})
+    paths = {"compiled": Problem(op, inst.domain),
+             "torch_op_by_op": Problem(op, inst.domain, jit=False),
+             "fused_family": Problem(inst.operator, inst.domain)}
+    out = {"case": "generic", "grid": [NT, NX], "dtype": "f64"}
+    ref = None
+    for name, pr in paths.items():
+        for _ in range(max(3, args.warmup)):
+            pr.eval_loss_grad(st)
+        torch.cuda.synchronize(dev)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(args.steps):
+            loss, g, _, _ = pr.eval_loss_grad(st)
+        e1.record()
+        e1.synchronize()
+        ms = e0.elapsed_time(e1) / args.steps
+        if ref is None:
+            ref = (loss.item(), g["u"])
+        out[name] = {"ms_per_loss_grad": ms,
+                     "loss_rel_diff": abs(loss.item() - ref[0]) / ref[0],
+                     "grad_max_rel_diff": float(
+                         (g["u"] - ref[1]).abs().max() / ref[1].abs().max())}
+    print(json.dumps(out))
+
+
 def march_kernel_name(cfg):
     """Kernel name of an FP32 march launch shape (as ncu lists it)."""
     if not cfg:
@@ -818,6 +862,8 @@ def main():
         run_advect(args)
     elif args.case == "ns_inverse":
         run_ns_inverse(args)
+    elif args.case == "generic":
+        run_generic(args)
     elif args.case:
         run_case(args)
     elif args.impl == "reference":

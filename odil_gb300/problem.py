@@ -12,6 +12,8 @@ Two routes:
     (``mod`` is the tf-style namespace of ``odil_gb300.mod``).
 Both run on the GPU; CPU tensors are rejected.
 """
+import os
+
 import numpy as np
 import torch
 
@@ -95,6 +97,24 @@ class FusedLoss(torch.autograd.Function):
         return grad * gout.to(grad.dtype), None
 
 
+class JitLoss(torch.autograd.Function):
+    """loss = sum_k mean(f_k^2) of a compiled generic operator on the packed
+    state, with the gradient from its fused adjoint kernel."""
+
+    @staticmethod
+    def forward(ctx, u, problem):
+        fields = {k: v.contiguous() for k, v in
+                  problem.unpack_fields(u.detach()).items()}
+        loss, grads, _ = problem.jit.loss_grad(fields)
+        ctx.save_for_backward(problem.pack_fields(grads))
+        return loss.to(u.dtype).reshape(()).clone()
+
+    @staticmethod
+    def backward(ctx, gout):
+        grad, = ctx.saved_tensors
+        return grad * gout.to(grad.dtype), None
+
+
 class Jacobian:
     """Matrix-free Jacobian of a registered family (the stencil form of the
     CSR matrix util_op.py:859-937 assembles).  ``matvec``/``rmatvec`` act on
@@ -134,7 +154,11 @@ class Problem:
         def __init__(self, value):
             self.value = value
 
-    def __init__(self, operator, domain, extra=None):
+    def __init__(self, operator, domain, extra=None, jit=None):
+        """jit: compile an unregistered operator to CUDA kernels (the stencil
+        compiler of ``odil_gb300.jit``).  None means yes unless the
+        environment sets ODIL_GB300_JIT=0; operators it cannot trace run op
+        by op on CUDA tensors."""
         self.domain = domain
         self.operator = operator
         self.extra = extra
@@ -142,6 +166,15 @@ class Problem:
             else None
         self.mod = TorchMod(device=domain.device,
                             dtype=_torch_dtype(domain.dtype))
+        self.jit = None
+        if jit is None:
+            jit = os.environ.get("ODIL_GB300_JIT", "1") != "0"
+        if self.kernels is None and jit:
+            from .jit import JitOperator, JitUnsupported
+            try:
+                self.jit = JitOperator(operator, domain, extra)
+            except JitUnsupported:
+                self.jit = None
 
     # -- state handling (util_op.py:733-857) --------------------------------
     @property
@@ -197,6 +230,8 @@ class Problem:
         if self.kernels is not None:
             u = state.fields[self.domain.fieldnames[0]]
             return [self.kernels.residual(u)]
+        if self.jit is not None:
+            return self.jit.residual(state.fields)
         with torch.no_grad():
             ff = self._generic(state.fields, epoch)
         return [f.value if isinstance(f, Problem.Raw) else f for f in ff]
@@ -211,6 +246,9 @@ class Problem:
             loss, grad = self.kernels.loss_grad(u)
             loss = loss.reshape(()).clone()
             return loss, {names[0]: grad}, {}, [loss]
+        if self.jit is not None:
+            loss, grads, split = self.jit.loss_grad(state.fields)
+            return loss, grads, {}, split
         fields = {k: v.detach().requires_grad_(True)
                   for k, v in state.fields.items()}
         ff = self._generic(fields, epoch)
@@ -268,6 +306,8 @@ class Problem:
         over the fused adjoint for registered families)."""
         if self.kernels is not None:
             return FusedLoss.apply(u.reshape(self.kernels.shape), self.kernels)
+        if self.jit is not None:
+            return JitLoss.apply(u, self)
         fields = self.unpack_fields(u)
         ff = self._generic(fields, 0)
         return sum(torch.mean(f.value) if isinstance(f, Problem.Raw) else
