@@ -10,12 +10,14 @@ subexpressions are shared).  From them this module writes one CUDA source
 with
 
   * a residual kernel: f_k at every cell, one thread per cell;
-  * a fused loss + gradient kernel: loss = sum_k mean(f_k^2) and
-    grad_u[c] = sum_k (2/N_k) sum_s f_k(c - s) * df_k/du[. + s](c - s), the
-    adjoint written as a gather: each thread re-evaluates the terms (and
-    their symbolic derivatives) at the cells whose stencil reads its own
-    cell, so the residuals are never stored (the form util_op.py:627-654
-    gets from the TF tape);
+  * loss + gradient in two passes: loss = sum_k mean(f_k^2) and
+    grad_u[c] = sum_k (2/N_k) sum_s f_k(c - s) * df_k/du[. + s](c - s) (what
+    util_op.py:627-654 gets from the TF tape).  Pass 1 evaluates every term
+    and its symbolic derivatives once per cell and stores the products
+    (2/N_k) f_k df_k/du(. + s), one grid per read, plus the per-block loss
+    partials; pass 2 gathers them at the shifted cells.  Storing the products
+    costs a few bytes per read and cell; re-evaluating each term at every
+    read offset instead costs FP64 arithmetic, the scarce resource on GB300;
 
 compiles it with nvcc for sm_103a into an in-tree shared library (cached by a
 hash of the source) and launches it through ctypes.  Shifts wrap
@@ -667,11 +669,13 @@ typedef @T@ T;
 #define NF @NF@
 #define NE @NE@
 #define NK @NK@
+#define NC @NC@
 struct Args {
     const T* f[NF > 0 ? NF : 1];
     const T* e[NE > 0 ? NE : 1];
     T* out[NK];
     T* grad[NF > 0 ? NF : 1];
+    T* contrib[NC > 0 ? NC : 1];
     double* partial;
     int n[3];
     long long es[NE > 0 ? NE : 1][3];
@@ -742,36 +746,31 @@ def generate(g, terms, fields, dtype):
     for k in range(nk):
         src.append("    a.out[%d][c] = term%d(a, %s);" % (k, k, idx))
     src.append("}")
-    # loss + gradient kernel
-    src.append("__global__ void __launch_bounds__(256) loss_grad_kernel(Args a) {")
+    # loss + gradient in two passes.  Pass 1 (contrib_kernel): every term
+    # and its derivatives once per cell; contribution q of read (field j,
+    # offset s) is C_q[c] = (2/N) f_k(c) df_k/du_j(c + s)(c), and the loss
+    # partials.  Pass 2 (gather_kernel): grad_j[c] = sum_q C_q[c - s_q].
+    reads_flat = []  # (term, m, field index, shift)
+    for k, rd in enumerate(term_reads):
+        for m, (name, sh) in enumerate(rd):
+            reads_flat.append((k, m, fields.index(name), sh))
+    src.append("__global__ void __launch_bounds__(256) contrib_kernel(Args a) {")
     src.append(_cell_decode(ndim))
     src.append("    double lk[NK];")
-    if fields:
-        src.append("    T gr[NF];")
-        src.append("    for (int q = 0; q < NF; ++q) gr[q] = T(0);")
+    q = 0
     for k, rd in enumerate(term_reads):
         src.append("    {")
-        src.append("        const T f = term%d(a, %s);" % (k, idx))
+        src.append("        T d[%d];" % max(1, len(rd)))
+        src.append("        const T f = term%d_d(a, %s, d);" % (k, idx))
         src.append("        lk[%d] = live ? (double)f * (double)f : 0.0;" % k)
-        by_shift = {}
-        for m, (name, sh) in enumerate(rd):
-            by_shift.setdefault(sh, []).append((m, fields.index(name)))
-        for sh, uses in sorted(by_shift.items()):
-            # the cell whose read at offset `sh` is this cell: c - sh
-            cell = ", ".join("wrap(i%d - (%d), a.n[%d])" % (d, sh[d], d)
-                             for d in range(ndim))
-            src.append("        {")
-            src.append("            T d[%d];" % max(1, len(rd)))
-            src.append("            const T fs = term%d_d(a, %s, d);" % (k, cell))
-            for m, fi in uses:
-                src.append("            gr[%d] += T(a.scale[%d]) * fs * d[%d];"
-                           % (fi, k, m))
-            src.append("        }")
+        src.append("        const T sf = T(a.scale[%d]) * f;" % k)
+        src.append("        if (live) {")
+        for m in range(len(rd)):
+            src.append("            a.contrib[%d][c] = sf * d[%d];" % (q, m))
+            q += 1
+        src.append("        }")
         src.append("    }")
-    if fields:
-        src.append("    if (live) {")
-        src.append("        for (int q = 0; q < NF; ++q) a.grad[q][c] = gr[q];")
-        src.append("    }")
+    src[0] = src[0].replace("@NC@", str(len(reads_flat)))
     src.append(r"""    __shared__ double red[NK][8];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     for (int k = 0; k < NK; ++k) {
@@ -786,13 +785,31 @@ def generate(g, terms, fields, dtype):
         a.partial[(long long)blockIdx.x * NK + threadIdx.x] = s;
     }
 }
-static int launch_status() { return cudaGetLastError() == cudaSuccess ? 0 : -4; }
+""")
+    src.append("__global__ void __launch_bounds__(256) gather_kernel(Args a) {")
+    src.append(_cell_decode(ndim))
+    src.append("    if (!live) return;")
+    for fi in range(len(fields)):
+        terms_j = [(qq, sh) for qq, (_, _, fj, sh) in enumerate(reads_flat)
+                   if fj == fi]
+        src.append("    {")
+        src.append("        T gsum = T(0);")
+        for qq, sh in terms_j:
+            cell = ", ".join("wrap(i%d - (%d), a.n[%d])" % (d, sh[d], d)
+                             for d in range(ndim))
+            src.append("        gsum += a.contrib[%d][lin(a, %s)];" % (qq, cell))
+        src.append("        a.grad[%d][c] = gsum;" % fi)
+        src.append("    }")
+    src.append("}")
+    src.append(r"""static int launch_status() { return cudaGetLastError() == cudaSuccess ? 0 : -4; }
 extern "C" __attribute__((visibility("default"))) int odil_jit_residual(const Args* a, long long ncell, void* stream) {
     residual_kernel<<<(unsigned)((ncell + 255) / 256), 256, 0, (cudaStream_t)stream>>>(*a);
     return launch_status();
 }
 extern "C" __attribute__((visibility("default"))) int odil_jit_loss_grad(const Args* a, long long ncell, void* stream) {
-    loss_grad_kernel<<<(unsigned)((ncell + 255) / 256), 256, 0, (cudaStream_t)stream>>>(*a);
+    const unsigned nb = (unsigned)((ncell + 255) / 256);
+    contrib_kernel<<<nb, 256, 0, (cudaStream_t)stream>>>(*a);
+    gather_kernel<<<nb, 256, 0, (cudaStream_t)stream>>>(*a);
     return launch_status();
 }
 """)
@@ -852,12 +869,15 @@ class JitOperator:
         self._lib = None
         self._ext = None
         nf, ne, nk = len(self.fields), len(self.graph.ext), len(self.terms)
+        self.ncontrib = sum(len(rd) for rd in self.term_reads)
+        nc = self.ncontrib
 
         class Args(ctypes.Structure):
             _fields_ = [("f", ctypes.c_void_p * max(1, nf)),
                         ("e", ctypes.c_void_p * max(1, ne)),
                         ("out", ctypes.c_void_p * nk),
                         ("grad", ctypes.c_void_p * max(1, nf)),
+                        ("contrib", ctypes.c_void_p * max(1, nc)),
                         ("partial", ctypes.c_void_p),
                         ("n", ctypes.c_int * 3),
                         ("es", (ctypes.c_longlong * 3) * max(1, ne)),
@@ -938,6 +958,11 @@ class JitOperator:
             a.out[k] = dummy.data_ptr()
         for i, name in enumerate(self.fields):
             a.grad[i] = grads[name].data_ptr()
+        # Pass-1 contributions, one grid per (term, read): scratch.
+        contrib = torch.empty((max(1, self.ncontrib), ) + self.graph.shape,
+                              dtype=self.dtype, device=dev)
+        for q in range(self.ncontrib):
+            a.contrib[q] = contrib[q].data_ptr()
         a.partial = partial.data_ptr()
         st = self.lib().odil_jit_loss_grad(ctypes.byref(a), n, stream_handle())
         if st != ODIL_OK:
