@@ -801,7 +801,26 @@ def generate(g, terms, fields, dtype):
         src.append("        a.grad[%d][c] = gsum;" % fi)
         src.append("    }")
     src.append("}")
+    # Jacobian coefficient fields: coef_q[c] = df_k(c)/du_j(c + s_q), the
+    # per-shift form of util_op.py:585-614.
+    src.append("__global__ void __launch_bounds__(256) jacobian_kernel(Args a) {")
+    src.append(_cell_decode(ndim))
+    src.append("    if (!live) return;")
+    q = 0
+    for k, rd in enumerate(term_reads):
+        src.append("    {")
+        src.append("        T d[%d];" % max(1, len(rd)))
+        src.append("        (void)term%d_d(a, %s, d);" % (k, idx))
+        for m in range(len(rd)):
+            src.append("        a.contrib[%d][c] = d[%d];" % (q, m))
+            q += 1
+        src.append("    }")
+    src.append("}")
     src.append(r"""static int launch_status() { return cudaGetLastError() == cudaSuccess ? 0 : -4; }
+extern "C" __attribute__((visibility("default"))) int odil_jit_jacobian(const Args* a, long long ncell, void* stream) {
+    jacobian_kernel<<<(unsigned)((ncell + 255) / 256), 256, 0, (cudaStream_t)stream>>>(*a);
+    return launch_status();
+}
 extern "C" __attribute__((visibility("default"))) int odil_jit_residual(const Args* a, long long ncell, void* stream) {
     residual_kernel<<<(unsigned)((ncell + 255) / 256), 256, 0, (cudaStream_t)stream>>>(*a);
     return launch_status();
@@ -888,7 +907,8 @@ class JitOperator:
     def lib(self):
         if self._lib is None:
             lib = ctypes.CDLL(compile_source(self.code))
-            for name in ("odil_jit_residual", "odil_jit_loss_grad"):
+            for name in ("odil_jit_residual", "odil_jit_loss_grad",
+                         "odil_jit_jacobian"):
                 fn = getattr(lib, name)
                 fn.restype = ctypes.c_int
                 fn.argtypes = [ctypes.c_void_p, ctypes.c_longlong,
@@ -899,7 +919,7 @@ class JitOperator:
     def _args(self, fields, device):
         g = self.graph
         if self._ext is None or self._ext[0] != device:
-            ext = [torch.as_tensor(a, dtype=self.dtype, device=device)
+            ext = [torch.tensor(a, dtype=self.dtype, device=device)
                    for a, _ in g.ext]
             self._ext = (device, ext)
         a = self._Args()
@@ -940,6 +960,32 @@ class JitOperator:
         if st != ODIL_OK:
             raise RuntimeError("odil_jit_residual failed (%d)" % st)
         return outs
+
+    def jacobian(self, fields):
+        """Coefficient fields of the Jacobian: a tensor [reads, *grid] and,
+        per (term, field), the read indices and shifts (row q holds
+        df_k(c)/du_j(c + s_q))."""
+        from ._capi import stream_handle
+        u0 = fields[self.fields[0]]
+        a, n = self._args(fields, u0.device)
+        dummy = torch.empty(1, dtype=self.dtype, device=u0.device)
+        for k in range(len(self.terms)):
+            a.out[k] = dummy.data_ptr()
+        coef = torch.empty((max(1, self.ncontrib), ) + self.graph.shape,
+                           dtype=self.dtype, device=u0.device)
+        for q in range(self.ncontrib):
+            a.contrib[q] = coef[q].data_ptr()
+        st = self.lib().odil_jit_jacobian(ctypes.byref(a), n, stream_handle())
+        if st != ODIL_OK:
+            raise RuntimeError("odil_jit_jacobian failed (%d)" % st)
+        blocks = {}
+        q = 0
+        for k, rd in enumerate(self.term_reads):
+            for name, sh in rd:
+                blocks.setdefault((k, self.fields.index(name)), []).append(
+                    (q, sh))
+                q += 1
+        return coef, blocks
 
     def loss_grad(self, fields):
         """(loss, {field: grad}, [mean(f_k^2)]) with the FP64 loss summed in

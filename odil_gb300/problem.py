@@ -145,6 +145,90 @@ class Jacobian:
                          self.kernels.shape).to_csr()
 
 
+class StencilJacobian:
+    """Jacobian of a compiled generic operator: one stencil per (term,
+    field) with the coefficient fields df_k(c)/du_j(c + s) (util_op.py:
+    585-614).  Rows are the terms stacked (term k: rows k N .. k N + N - 1),
+    columns the fields (field j: j N ..), as util_op.py:859-937 lays out
+    the CSR matrix; shifts wrap periodically."""
+
+    DENSE_MAX = 16384  # unknowns up to which `solve` is a dense direct solve
+
+    def __init__(self, coef, blocks, nterms, nfields, shape):
+        from .stencil import StencilOp
+        self.grid = tuple(shape)
+        self.n = int(np.prod(shape))
+        per = (True, ) * len(self.grid)
+        self.ops = {kj: StencilOp([sh for _, sh in lst],
+                                  coef[[q for q, _ in lst]], self.grid, 1, per)
+                    for kj, lst in blocks.items()}
+        self.nterms, self.nfields = nterms, nfields
+        self.shape = (nterms * self.n, nfields * self.n)
+        self.dtype, self.device = coef.dtype, coef.device
+
+    def matvec(self, v):
+        n = self.n
+        out = torch.zeros(self.shape[0], dtype=v.dtype, device=v.device)
+        for (k, j), op in self.ops.items():
+            op.mul_field(v[j * n:(j + 1) * n].reshape(self.grid).contiguous(),
+                         out=out[k * n:(k + 1) * n].view(self.grid), beta=1.0)
+        return out
+
+    def rmatvec(self, w):
+        n = self.n
+        out = torch.zeros(self.shape[1], dtype=w.dtype, device=w.device)
+        for (k, j), op in self.ops.items():
+            op.mul_transpose_field(
+                w[k * n:(k + 1) * n].reshape(self.grid).contiguous(),
+                out=out[j * n:(j + 1) * n].view(self.grid), beta=1.0)
+        return out
+
+    def to_csr(self):
+        """The matrix as a device CSR tensor (reference layout)."""
+        n = self.n
+        rows, cols, vals = [], [], []
+        for (k, j), op in self.ops.items():
+            b = op.to_csr().to_sparse_coo().coalesce()
+            i = b.indices()
+            rows.append(i[0] + k * n)
+            cols.append(i[1] + j * n)
+            vals.append(b.values())
+        coo = torch.sparse_coo_tensor(
+            torch.stack([torch.cat(rows), torch.cat(cols)]), torch.cat(vals),
+            self.shape).coalesce()
+        return coo.to_sparse_csr()
+
+    def solve(self, rhs, tol=1e-12, maxiter=None):
+        """d minimising |J d - rhs| (the normal equations of
+        linsolver.py:28-45): a dense direct solve up to DENSE_MAX unknowns,
+        else conjugate gradients on the normal equations, matrix-free."""
+        rhs = rhs.to(self.dtype)
+        if self.shape[1] <= self.DENSE_MAX:
+            J = self.to_csr().to_dense()
+            if self.shape[0] == self.shape[1]:
+                return torch.linalg.solve(J, rhs)
+            return torch.linalg.solve(J.T @ J, J.T @ rhs)
+        x = torch.zeros(self.shape[1], dtype=self.dtype, device=self.device)
+        r = rhs.clone()
+        z = self.rmatvec(r)
+        p = z.clone()
+        zz = torch.dot(z, z)
+        z0 = zz.sqrt().item()
+        maxiter = maxiter or 10 * self.shape[1]
+        for _ in range(maxiter):
+            if zz.sqrt().item() <= tol * max(z0, 1e-300):
+                break
+            w = self.matvec(p)
+            alpha = zz / torch.dot(w, w)
+            x += alpha * p
+            r -= alpha * w
+            z = self.rmatvec(r)
+            zn = torch.dot(z, z)
+            p = z + (zn / zz) * p
+            zz = zn
+        return x
+
+
 class Problem:
     """util_op.py:566-973."""
 
@@ -317,10 +401,16 @@ class Problem:
         """util_op.py:859-937: (const, J) with J matrix-free on the GPU."""
         self.init_missing(state)
         self._check_device(state)
+        if self.kernels is None and self.jit is not None:
+            const = self.jit.residual(state.fields)
+            coef, blocks = self.jit.jacobian(state.fields)
+            return const, StencilJacobian(coef, blocks, len(const),
+                                          len(self.domain.fieldnames),
+                                          self.domain.shape)
         if self.kernels is None:
             raise NotImplementedError(
-                "linearize needs a registered operator family; generic "
-                "operators use eval_loss_grad")
+                "linearize needs a registered operator family or an operator "
+                "the stencil compiler traces; others use eval_loss_grad")
         const = self.eval_operator(state, epoch)
         n = self.domain.cells()
         return const, Jacobian(self.kernels, (len(const) * n, n))
