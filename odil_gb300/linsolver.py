@@ -12,7 +12,8 @@ linsolver="mixed"     the same direct solve in FP32 on an FP64 right-hand
 linsolver="multigrid" matrix-free Krylov solve preconditioned by the
                       geometric multigrid V-cycle (families that provide it).
 Other reference choices (direct_cu, sparseqr, lsqr, lsqr_cu, bicgstab) map
-to "direct".
+to "direct".  With --beta or --betadiag set, every choice solves the relaxed
+normal equations of linsolver.py:35-41 (solve_regularized).
 """
 import torch
 
@@ -20,7 +21,67 @@ ALIASES = {"direct_cu": "direct", "sparseqr": "direct", "lsqr": "direct",
            "lsqr_cu": "direct", "bicgstab": "direct"}
 
 
+DENSE_MAX = 16384  # unknowns up to which the regularised solve is dense
+
+
+def solve_regularized(matr, rhs, beta=0.0, betadiag=0.0, tol=1e-12,
+                      maxiter=None):
+    """d of (J^T J + beta^2 I + betadiag^2 diag(J^T J + beta^2 I)) d = J^T rhs,
+    the relaxed normal equations of linsolver.py:35-41: dense (cuSOLVER
+    through torch) up to DENSE_MAX unknowns, else conjugate gradients with
+    J and J^T matrix-free."""
+    n = matr.shape[1]
+    rhs = rhs.to(torch.float64)
+    if n <= DENSE_MAX and hasattr(matr, "to_csr"):
+        J = matr.to_csr().to_dense().to(torch.float64)
+        A = J.T @ J
+        if beta:
+            A += beta**2 * torch.eye(n, dtype=A.dtype, device=A.device)
+        if betadiag:
+            A += betadiag**2 * torch.diag(torch.diagonal(A))
+        return torch.linalg.solve(A, J.T @ rhs)
+    diag = None
+    if betadiag:
+        if not hasattr(matr, "to_csr"):
+            raise ValueError("betadiag needs a Jacobian with to_csr()")
+        J = matr.to_csr().to_sparse_coo().coalesce()
+        diag = torch.zeros(n, dtype=torch.float64, device=rhs.device)
+        diag.index_add_(0, J.indices()[1], J.values().to(torch.float64)**2)
+        diag = betadiag**2 * (diag + beta**2)
+
+    def A(x):
+        y = matr.rmatvec(matr.matvec(x))
+        if beta:
+            y = y + beta**2 * x
+        if diag is not None:
+            y = y + diag * x
+        return y
+
+    b = matr.rmatvec(rhs)
+    x = torch.zeros_like(b)
+    r = b.clone()
+    p = r.clone()
+    rr = torch.dot(r, r)
+    r0 = rr.sqrt().item()
+    for _ in range(maxiter or 10 * n):
+        if rr.sqrt().item() <= tol * max(r0, 1e-300):
+            break
+        Ap = A(p)
+        alpha = rr / torch.dot(p, Ap)
+        x += alpha * p
+        r -= alpha * Ap
+        rn = torch.dot(r, r)
+        p = r + (rn / rr) * p
+        rr = rn
+    return x
+
+
 def solve(matr, rhs, args=None, dhistory=None, linsolver="direct"):
+    beta = float(getattr(args, "beta", 0) or 0)
+    betadiag = float(getattr(args, "betadiag", 0) or 0)
+    if beta or betadiag:
+        out = solve_regularized(matr, rhs, beta, betadiag)
+        return out.to(rhs.dtype)
     name = ALIASES.get(linsolver, linsolver)
     if name == "direct":
         return matr.solve(rhs)

@@ -516,3 +516,33 @@ def test_solve_host_out(cuda):
     with pytest.raises(ValueError):
         newton.solve(prob, st, "mixed", 1, from_zero=True,
                      host_out=torch.zeros((256, 256), dtype=torch.float64))
+
+
+@pytest.mark.parametrize("beta,betadiag", [(0.3, 0.0), (0.0, 0.5), (0.2, 0.4),
+                                           (30.0, 0.5)])
+def test_relaxed_normal_equations(cuda, beta, betadiag, monkeypatch):
+    """--beta / --betadiag: the relaxed normal equations of
+    linsolver.py:35-41, against the oracle's CSR Jacobian solved densely in
+    numpy; the matrix-free conjugate-gradient path agrees where the relaxed
+    system is well conditioned (large beta)."""
+    import argparse
+    from odil_gb300 import linsolver
+    from odil_gb300.problem import Jacobian
+    s = _setup(24, 20, seed=5, c=0.9)
+    k = _kernels(s, cuda)
+    J = Jacobian(k, (k.n, k.n))
+    rng = np.random.default_rng(6)
+    rhs = rng.standard_normal(k.n)
+    _, Jo = W.linearize(s, np.zeros(s.shape))
+    Jd = Jo.toarray()
+    A = Jd.T @ Jd + beta**2 * np.eye(k.n)
+    A += betadiag**2 * np.diag(np.diag(A))
+    ref = np.linalg.solve(A, Jd.T @ rhs)
+    args = argparse.Namespace(beta=beta, betadiag=betadiag)
+    rt = torch.as_tensor(rhs, device=cuda)
+    d = linsolver.solve(J, rt, args, None, "direct").cpu().numpy()
+    assert _rel(d, ref) < 1e-9
+    if beta >= 1:
+        monkeypatch.setattr(linsolver, "DENSE_MAX", 0)
+        d2 = linsolver.solve(J, rt, args, None, "direct").cpu().numpy()
+        assert _rel(d2, ref) < 1e-8
