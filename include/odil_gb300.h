@@ -112,6 +112,20 @@ int odil_wave_jtv_f32(const odil_wave_params* p, const float* w, float* out,
                       void* stream);
 int odil_wave_jtv_f64(const odil_wave_params* p, const double* w, double* out,
                       void* stream);
+/* The normal-equation matrix J^T J of linsolver.py:35-41, never formed:
+ * out = J^T J v in one pass (the fused adjoint with zero boundary data; the
+ * workspace, sized by odil_wave_jtj_workspace_bytes and zero-filled once,
+ * holds its reduction scratch), and out = diag(J^T J). */
+int64_t odil_wave_jtj_workspace_bytes(const odil_wave_params* p);
+int odil_wave_jtj_v_f32(const odil_wave_params* p, const float* v, float* out,
+                        void* workspace, int64_t workspace_bytes,
+                        void* stream);
+int odil_wave_jtj_v_f64(const odil_wave_params* p, const double* v,
+                        double* out, void* workspace, int64_t workspace_bytes,
+                        void* stream);
+int odil_wave_jtj_diag_f32(const odil_wave_params* p, float* out, void* stream);
+int odil_wave_jtj_diag_f64(const odil_wave_params* p, double* out,
+                           void* stream);
 
 /* Direct solve of J x = b by forward substitution along t (J is lower
  * triangular in C order).  Same solution as the normal equations that

@@ -156,6 +156,11 @@ SIGNATURES = {
     "odil_wave_jv_f64": (_INT, [_P, _P, _P, _P]),
     "odil_wave_jtv_f32": (_INT, [_P, _P, _P, _P]),
     "odil_wave_jtv_f64": (_INT, [_P, _P, _P, _P]),
+    "odil_wave_jtj_workspace_bytes": (_I64, [_P]),
+    "odil_wave_jtj_v_f32": (_INT, [_P, _P, _P, _P, _I64, _P]),
+    "odil_wave_jtj_v_f64": (_INT, [_P, _P, _P, _P, _I64, _P]),
+    "odil_wave_jtj_diag_f32": (_INT, [_P, _P, _P]),
+    "odil_wave_jtj_diag_f64": (_INT, [_P, _P, _P]),
     "odil_wave_march_f32": (_INT, [_P, _P, _P, _P]),
     "odil_wave_march_f64": (_INT, [_P, _P, _P, _P]),
     "odil_wave_initial_rhs_mixed": (_INT, [_P, _P, _P]),

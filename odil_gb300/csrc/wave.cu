@@ -575,11 +575,8 @@ void lv_launch(const LgPlan& pl, const WaveDev<T>& g, const T* u, T* grad, Reduc
 }
 
 template <typename T>
-void lg_launch(const LgPlan& pl, const WaveDev<T>& g, const T* u, T* grad, ReduceWs ws,
-               double* loss, cudaStream_t s) {
-    const double n = (double)g.nt * (double)g.nx;
-    const T gs = (T)(2.0 / n);
-    const double ls = 1.0 / n;
+void lg_launch_scaled(const LgPlan& pl, const WaveDev<T>& g, const T* u, T* grad, ReduceWs ws,
+                      double* loss, T gs, double ls, cudaStream_t s) {
     if (pl.vec) {
         if (pl.ty == 16) {
             lv_launch<T, 16>(pl, g, u, grad, ws, loss, gs, ls, s);
@@ -593,6 +590,83 @@ void lg_launch(const LgPlan& pl, const WaveDev<T>& g, const T* u, T* grad, Reduc
     } else {
         wave_loss_grad_kernel<T, 32><<<pl.grid, LG_WARPS * 32, 0, s>>>(g, u, grad, ws, loss, gs, ls);
     }
+}
+
+template <typename T>
+void lg_launch(const LgPlan& pl, const WaveDev<T>& g, const T* u, T* grad, ReduceWs ws,
+               double* loss, cudaStream_t s) {
+    const double n = (double)g.nt * (double)g.nx;
+    lg_launch_scaled<T>(pl, g, u, grad, ws, loss, (T)(2.0 / n), 1.0 / n, s);
+}
+
+// ---------------------------------------------------------------------------
+// Normal-equation pieces (the matrix J^T J of linsolver.py:35-41, never
+// formed).  J^T J v: the fused adjoint above with the boundary data taken as
+// zero (then F(v) = J v, F being affine in u) and the gradient scale 1, so
+// one pass reads v and writes J^T J v.  diag(J^T J): per column, the sum of
+// the squared coefficients of the rows that read it (the rows of
+// wave_gather).
+template <typename T>
+__global__ void __launch_bounds__(256) wave_jtj_diag_kernel(WaveDev<T> g, T* __restrict__ out) {
+    const int nt = g.nt, nx = g.nx;
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= (int64_t)nt * nx) return;
+    const int a = (int)(k / nx), b = (int)(k - (int64_t)a * nx);
+    const T cu = a == 0 ? T(1) : g.A;
+    T s = cu * cu;
+    if (a + 1 < nt) {
+        // Row (a+1, b) and its x-neighbours read u[a, b]; where they are the
+        // same row (nx <= 2) the coefficients add before squaring.
+        const T ctm = (a + 1 == 1 ? -g.A : T(-2) * g.A) + g.B * k_tm<T>(b, nx);
+        const int bp = (b + 1 == nx) ? 0 : b + 1;
+        const int bm = (b == 0) ? nx - 1 : b - 1;
+        const T cm = -g.B * k_xm<T>(bp, nx), cp = -g.B * k_xp<T>(bm, nx);
+        if (nx == 1) {
+            const T c = ctm + cm + cp;
+            s += c * c;
+        } else if (bp == bm) {
+            s += ctm * ctm + (cm + cp) * (cm + cp);
+        } else {
+            s += ctm * ctm + cm * cm + cp * cp;
+        }
+    }
+    if (a + 2 < nt) s += g.A * g.A;
+    out[k] = s;
+}
+
+template <typename T>
+int jtj_diag_impl(const odil_wave_params* p, T* out, void* stream) {
+    WaveDev<T> g;
+    int st = make_dev<T>(p, &g, false);
+    if (st) return st;
+    if (!out) return ODIL_ERR_ARG;
+    const int64_t n = (int64_t)g.nt * g.nx;
+    wave_jtj_diag_kernel<T><<<(unsigned)((n + 255) / 256), 256, 0, as_stream(stream)>>>(g, out);
+    return launch_status();
+}
+
+template <typename T>
+int64_t jtj_ws_bytes(const odil_wave_params* p) {
+    WaveDev<T> g;
+    if (make_dev<T>(p, &g, false)) return 0;
+    // Either loss-kernel plan, + the discarded loss scalar.
+    return reduce_ws_bytes(lg_max_blocks<T>(g.nt, g.nx)) + 256;
+}
+
+template <typename T>
+int jtj_v_impl(const odil_wave_params* p, const T* v, T* out, void* ws, int64_t ws_bytes,
+               void* stream) {
+    WaveDev<T> g;
+    int st = make_dev<T>(p, &g, false);  // no boundary data: F(v) = J v
+    if (st) return st;
+    if (!v || !out) return ODIL_ERR_ARG;
+    const LgPlan pl = lg_plan<T>(g.nt, g.nx, v, out);
+    if (pl.grid.y > 65535) return ODIL_ERR_SHAPE;
+    const int64_t need = reduce_ws_bytes(pl.blocks) + 256;
+    if (!ws || ws_bytes < need) return ODIL_ERR_WORKSPACE;
+    double* loss = reinterpret_cast<double*>(static_cast<char*>(ws) + need - 256);
+    lg_launch_scaled<T>(pl, g, v, out, reduce_ws(ws), loss, T(1), 0.0, as_stream(stream));
+    return launch_status();
 }
 
 // Columns per thread for a row of nx cells (at most 1024 threads).
@@ -808,6 +882,25 @@ ODIL_API int odil_wave_jtv_f32(const odil_wave_params* p, const float* w, float*
 ODIL_API int odil_wave_jtv_f64(const odil_wave_params* p, const double* w, double* out,
                                void* stream) {
     return jtv_impl<double>(p, w, out, stream);
+}
+
+ODIL_API int64_t odil_wave_jtj_workspace_bytes(const odil_wave_params* p) {
+    const int64_t a = jtj_ws_bytes<float>(p), b = jtj_ws_bytes<double>(p);
+    return a > b ? a : b;
+}
+ODIL_API int odil_wave_jtj_v_f32(const odil_wave_params* p, const float* v, float* out,
+                                 void* workspace, int64_t workspace_bytes, void* stream) {
+    return jtj_v_impl<float>(p, v, out, workspace, workspace_bytes, stream);
+}
+ODIL_API int odil_wave_jtj_v_f64(const odil_wave_params* p, const double* v, double* out,
+                                 void* workspace, int64_t workspace_bytes, void* stream) {
+    return jtj_v_impl<double>(p, v, out, workspace, workspace_bytes, stream);
+}
+ODIL_API int odil_wave_jtj_diag_f32(const odil_wave_params* p, float* out, void* stream) {
+    return jtj_diag_impl<float>(p, out, stream);
+}
+ODIL_API int odil_wave_jtj_diag_f64(const odil_wave_params* p, double* out, void* stream) {
+    return jtj_diag_impl<double>(p, out, stream);
 }
 ODIL_API int odil_wave_loss_grad_f32(const odil_wave_params* p, const float* u, float* grad,
                                      double* loss, void* workspace, int64_t workspace_bytes,

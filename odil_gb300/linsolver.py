@@ -42,15 +42,20 @@ def solve_regularized(matr, rhs, beta=0.0, betadiag=0.0, tol=1e-12,
         return torch.linalg.solve(A, J.T @ rhs)
     diag = None
     if betadiag:
-        if not hasattr(matr, "to_csr"):
-            raise ValueError("betadiag needs a Jacobian with to_csr()")
-        J = matr.to_csr().to_sparse_coo().coalesce()
-        diag = torch.zeros(n, dtype=torch.float64, device=rhs.device)
-        diag.index_add_(0, J.indices()[1], J.values().to(torch.float64)**2)
+        if hasattr(matr, "jtj_diag"):
+            diag = matr.jtj_diag().to(torch.float64)
+        elif hasattr(matr, "to_csr"):
+            J = matr.to_csr().to_sparse_coo().coalesce()
+            diag = torch.zeros(n, dtype=torch.float64, device=rhs.device)
+            diag.index_add_(0, J.indices()[1],
+                            J.values().to(torch.float64)**2)
+        else:
+            raise ValueError("betadiag needs diag(J^T J) or to_csr()")
         diag = betadiag**2 * (diag + beta**2)
+    jtj = getattr(matr, "jtj_v", None)
 
     def A(x):
-        y = matr.rmatvec(matr.matvec(x))
+        y = jtj(x) if jtj is not None else matr.rmatvec(matr.matvec(x))
         if beta:
             y = y + beta**2 * x
         if diag is not None:

@@ -130,6 +130,17 @@ class Jacobian:
     def rmatvec(self, w):
         return self.kernels.jtv(w.reshape(self.kernels.shape)).reshape(-1)
 
+    def jtj_v(self, v):
+        """J^T J v (one fused pass where the family provides it)."""
+        if hasattr(self.kernels, "jtj_v"):
+            return self.kernels.jtj_v(
+                v.reshape(self.kernels.shape).contiguous()).reshape(-1)
+        return self.rmatvec(self.matvec(v))
+
+    def jtj_diag(self):
+        """diag(J^T J), packed (families that provide it)."""
+        return self.kernels.jtj_diag().reshape(-1)
+
     def solve(self, rhs):
         return self.kernels.march(rhs.reshape(self.kernels.shape)).reshape(-1)
 

@@ -156,6 +156,28 @@ class WaveKernels:
         call("odil_wave_jtv_" + sfx, p, ptr(w), ptr(out), stream_handle())
         return out
 
+    def jtj_v(self, v, out=None):
+        """J^T J v in one pass (the normal-equation matrix of
+        linsolver.py:35-41, never formed)."""
+        self._check(v)
+        p, sfx = self._pp(v)
+        out = torch.empty_like(v) if out is None else out
+        ws = getattr(self, "_jtj_ws", None)
+        if ws is None:
+            nb = _capi.load().odil_wave_jtj_workspace_bytes(p)
+            ws = self._jtj_ws = torch.zeros(nb, dtype=torch.uint8,
+                                            device=self.device)
+        call("odil_wave_jtj_v_" + sfx, p, ptr(v), ptr(out), ptr(ws),
+             ws.numel(), stream_handle())
+        return out
+
+    def jtj_diag(self, dtype=torch.float64):
+        """diag(J^T J) as a field."""
+        out = torch.empty(self.shape, dtype=dtype, device=self.device)
+        p, sfx = self._pp(out)
+        call("odil_wave_jtj_diag_" + sfx, p, ptr(out), stream_handle())
+        return out
+
     def loss_grad(self, u, grad=None, loss=None):
         """Fused loss+adjoint: returns (loss [1] float64 tensor, grad)."""
         self._check(u)

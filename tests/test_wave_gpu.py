@@ -546,3 +546,24 @@ def test_relaxed_normal_equations(cuda, beta, betadiag, monkeypatch):
         monkeypatch.setattr(linsolver, "DENSE_MAX", 0)
         d2 = linsolver.solve(J, rt, args, None, "direct").cpu().numpy()
         assert _rel(d2, ref) < 1e-8
+
+
+@pytest.mark.parametrize("shape", [(1, 5), (2, 3), (3, 1), (17, 13), (40, 64),
+                                   (129, 256)])
+def test_jtj_v_and_diag(cuda, shape):
+    """J^T J v (one fused pass, boundary data ignored) and diag(J^T J)
+    against the oracle's CSR Jacobian (util_op.py:859-937 restated)."""
+    s = _setup(*shape, seed=7, c=0.9)
+    k = _kernels(s, cuda)
+    _, Jo = W.linearize(s, np.zeros(shape))
+    Jd = Jo.toarray()
+    v = np.random.default_rng(8).standard_normal(shape)
+    ref = (Jd.T @ (Jd @ v.ravel())).reshape(shape)
+    out = k.jtj_v(torch.as_tensor(v, device=cuda)).cpu().numpy()
+    assert _rel(out, ref) < 1e-12
+    out32 = k.jtj_v(torch.as_tensor(v, dtype=torch.float32,
+                                    device=cuda)).cpu().numpy()
+    assert _rel(out32, ref) < 1e-5
+    dref = (Jd**2).sum(0).reshape(shape)
+    assert _rel(k.jtj_diag().cpu().numpy(), dref) < 1e-14
+    assert _rel(k.jtj_diag(torch.float32).cpu().numpy(), dref) < 1e-6
