@@ -199,4 +199,35 @@ __device__ __forceinline__ void reduce_finish(double v, int64_t bid, int64_t nbl
     }
 }
 
+// Programmatic dependent launch.  pdl_trigger: this grid's dependents may
+// launch now (they still wait for its completion before reading its
+// output).  pdl_wait: wait until the grids this one depends on have
+// completed and their writes are visible (returns at once when the launch
+// had no programmatic dependency).
+__device__ __forceinline__ void pdl_trigger() {
+    asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory");
+}
+__device__ __forceinline__ void pdl_wait() {
+    asm volatile("griddepcontrol.wait;\n" ::: "memory");
+}
+
+// Launches `kern` on `st` with programmatic stream serialisation allowed, so
+// that it may start while the previous kernel in the stream finishes (it
+// must call pdl_wait before touching that kernel's output).
+template <typename... Args>
+cudaError_t launch_pdl(void (*kern)(Args...), dim3 grid, dim3 block, size_t smem,
+                       cudaStream_t st, Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kern, args...);
+}
+
 }  // namespace odil

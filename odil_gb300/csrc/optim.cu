@@ -502,6 +502,8 @@ __global__ void __launch_bounds__(VT) pair_to_f64_kernel(const float* __restrict
                                                          const float* __restrict__ lo,
                                                          double* __restrict__ out, int64_t n,
                                                          bool vec) {
+    pdl_trigger();
+    pdl_wait();  // hi / lo come from the kernel before (PDL launch)
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     const int64_t t0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (vec) {  // 4 elements per thread: 16-byte loads, two 16-byte stores
@@ -608,7 +610,8 @@ ODIL_API int odil_pair_to_f64(const float* hi, const float* lo, double* out, int
     if (n == 0) return ODIL_OK;
     if (!hi || !out) return ODIL_ERR_ARG;
     const bool vec = aligned16(hi) && aligned16(out) && (!lo || aligned16(lo));
-    pair_to_f64_kernel<<<stream_blocks(n, vec ? 4 : 1), VT, 0, as_stream(stream)>>>(hi, lo, out,
-                                                                                   n, vec);
+    if (launch_pdl(pair_to_f64_kernel, dim3(stream_blocks(n, vec ? 4 : 1)), dim3(VT), 0,
+                   as_stream(stream), hi, lo, out, n, vec) != cudaSuccess)
+        return launch_status();
     return launch_status();
 }

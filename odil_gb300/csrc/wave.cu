@@ -842,6 +842,32 @@ __global__ void __launch_bounds__(256) wave_bnd_rhs_kernel(WaveDev<double> g, Pa
     rhs[(int64_t)i * g.nx + j] = bnd_cell_rhs<KIND>(g, k, hi, lo, i, j);
 }
 
+// rhs = float(-F(0)) in one launch: the first `nbb` blocks compute the
+// boundary cells (FP64, packed into full warps), the others write zeros to
+// the interior (rows >= 2, columns 1 .. nx-2), where F(0) vanishes.
+__global__ void __launch_bounds__(256) wave_initial_rhs_kernel(WaveDev<double> g,
+                                                               float* __restrict__ rhs,
+                                                               int64_t count, int nbb) {
+    pdl_trigger();
+    if ((int)blockIdx.x < nbb) {
+        const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+        if (t >= count) return;
+        int i, j;
+        bnd_cell(t, g.nt, g.nx, &i, &j);
+        const PairCoef k{};
+        rhs[(int64_t)i * g.nx + j] = bnd_cell_rhs<0>(g, k, nullptr, nullptr, i, j);
+        return;
+    }
+    const int w = g.nx - 2;
+    if (g.nt <= 2 || w <= 0) return;
+    const int64_t n = (int64_t)(g.nt - 2) * w;
+    const int64_t stride = (int64_t)(gridDim.x - nbb) * blockDim.x;
+    for (int64_t t = (int64_t)(blockIdx.x - nbb) * blockDim.x + threadIdx.x; t < n; t += stride) {
+        const int64_t r = t / w;
+        rhs[(r + 2) * g.nx + 1 + (t - r * w)] = 0.f;
+    }
+}
+
 template <int CPT, int PF>
 int launch_march_shape(const WaveDev<float>& g, const float* b, float* x, cudaStream_t st) {
     return launch_march_cfg<float, CPT, PF>(g, b, x, st);
@@ -972,12 +998,12 @@ ODIL_API int odil_wave_initial_rhs_mixed(const odil_wave_params* p, float* rhs, 
     if (st) return st;
     if (!rhs) return ODIL_ERR_ARG;
     cudaStream_t s = as_stream(stream);
-    if (cudaMemsetAsync(rhs, 0, (size_t)g.nt * g.nx * sizeof(float), s) != cudaSuccess)
-        return ODIL_ERR_LAUNCH;
     const int64_t nb = bnd_count(g.nt, g.nx);
-    const PairCoef k{};
-    wave_bnd_rhs_kernel<0><<<(unsigned)((nb + 255) / 256), 256, 0, s>>>(g, k, nullptr, nullptr,
-                                                                       rhs, nb);
+    const int nbb = (int)((nb + 255) / 256);
+    const int64_t interior = (int64_t)(g.nt > 2 ? g.nt - 2 : 0) * (g.nx > 2 ? g.nx - 2 : 0);
+    int64_t nzb = (interior + 255) / 256;
+    if (nzb > 4 * 152) nzb = 4 * 152;  // grid-stride beyond this
+    wave_initial_rhs_kernel<<<(unsigned)(nbb + nzb), 256, 0, s>>>(g, rhs, nb, nbb);
     return launch_status();
 }
 

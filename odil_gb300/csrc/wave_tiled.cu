@@ -215,6 +215,10 @@ __global__ void __launch_bounds__(32 * kTiledMaxWarps) wave_march_tiled_kernel(
     for (int q = 0; q < PF; ++q)
 #pragma unroll
         for (int c = 0; c < CPT; ++c) pre[q][c] = T(0);
+    // Launched with programmatic serialisation: the right-hand side is the
+    // previous kernel's output.
+    pdl_trigger();
+    pdl_wait();
     const T* src = b + j0;  // row `next` of the right-hand side
     int next = 0;
     auto issue = [&](auto checked, int slot) {
@@ -411,11 +415,13 @@ int tiled_launch(const void* kern, int clusters, int warps, const WaveDev<T>& g,
     cfg.blockDim = dim3((unsigned)(32 * warps));
     cfg.dynamicSmemBytes = 0;
     cfg.stream = st;
-    cudaLaunchAttribute attr[1];
+    cudaLaunchAttribute attr[2];
     attr[0].id = cudaLaunchAttributeClusterDimension;
     attr[0].val.clusterDim.x = (unsigned)clusters;
     attr[0].val.clusterDim.y = 1;
     attr[0].val.clusterDim.z = 1;
+    attr[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[1].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     // The cluster must fit on the device at once (its CTAs run together);
@@ -439,6 +445,7 @@ int tiled_launch(const void* kern, int clusters, int warps, const WaveDev<T>& g,
     }
     if (!ok) return ODIL_ERR_SHAPE;
     void* args[] = {const_cast<WaveDev<T>*>(&g), &b, &x, &extra_wait};
+    cfg.numAttrs = 2;  // the occupancy query above saw the cluster only
     if (cudaLaunchKernelExC(&cfg, kern, args) != cudaSuccess) {
         cudaGetLastError();
         return ODIL_ERR_LAUNCH;
