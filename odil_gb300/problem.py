@@ -362,14 +362,28 @@ class Problem:
         """util_op.py:675-731: stochastic estimate of the diagonal of
         sum_k J_k^T J_k / N_k as the mean over `nsmp` samples of g^2, with
         g = sum_k J_k^T z_k / sqrt(N_k) and z_k ~ N(0, 1) per residual cell.
-        Registered families form J^T z with their adjoint kernel; generic
-        operators by autograd.  Returns the packed diagonal."""
+        Registered families form J^T z with their adjoint kernel, compiled
+        generic operators with their Jacobian stencils, others by autograd.
+        Returns the packed diagonal."""
         self.init_missing(state)
         self._check_device(state)
         names = self.domain.fieldnames
         acc = None
+        jac = None
+        if self.kernels is None and self.jit is not None:
+            const = self.jit.residual(state.fields)
+            coef, blocks = self.jit.jacobian(state.fields)
+            jac = StencilJacobian(coef, blocks, len(const), len(names),
+                                  self.domain.shape)
         for _ in range(nsmp):
-            if self.kernels is not None:
+            if jac is not None:
+                # one z_k per residual term, J^T z through the compiled
+                # Jacobian's stencils
+                z = torch.randn(jac.shape[0], dtype=jac.dtype,
+                                device=jac.device, generator=generator)
+                z /= float(jac.n)**0.5
+                g = jac.rmatvec(z)
+            elif self.kernels is not None:
                 k = self.kernels
                 u = state.fields[names[0]]
                 z = torch.randn(k.shape, dtype=u.dtype, device=u.device,

@@ -337,3 +337,90 @@ def test_compiled_newton_matches_fused(cuda):
     uf = torch.zeros_like(u)
     newton.solve(fused, State(fields={"u": uf}), "fp64", 2)
     assert _rel(u, uf) < 1e-11
+
+
+def _op1d(mod, ctx):
+    """1D: Burgers-like residual with a where on the boundary cell."""
+    u = ctx.field("u")
+    dx = ctx.step(0)
+    ix = ctx.cell_index(0)
+    um, up = ctx.field("u", -1), ctx.field("u", 1)
+    f = u * (up - um) / (2 * dx) - 0.05 * (up - 2 * u + um) / dx**2 + \
+        mod.cos(ctx.cell_center(0))
+    return [mod.where(ix == 0, u - 1.0, f)]
+
+
+def _op3d(mod, ctx):
+    """3D: upwind advection in t with a nonlinear source (periodic x, y)."""
+    p = ctx.field("p")
+    pt = ctx.field("p", -1, 0, 0)
+    px = ctx.field("p", 0, -1, 0)
+    py = ctx.field("p", 0, 0, -1)
+    dt, dx, dy = ctx.step(0), ctx.step(1), ctx.step(2)
+    it = ctx.cell_index(0)
+    f = (p - pt) / dt + 0.7 * (p - px) / dx - 0.4 * (p - py) / dy + \
+        0.1 * p * p
+    return [mod.where(it == 0, p - mod.sin(2 * np.pi * ctx.cell_center(1)), f)]
+
+
+def _dom(shape, names, device, fields):
+    from odil_gb300.domain import Domain
+    return Domain(ndim=len(shape), shape=shape, lower=(0, ) * len(shape),
+                  upper=(1, ) * len(shape), varnames=names, fieldnames=fields,
+                  device=device)
+
+
+def test_rank1_and_rank3_operators_compile():
+    from odil_gb300 import jit
+    for op, dom in ((_op1d, _dom((33, ), ("x", ), "cpu", ["u"])),
+                    (_op3d, _dom((6, 8, 10), ("t", "x", "y"), "cpu", ["p"]))):
+        J = jit.JitOperator(op, dom)
+        jit.compile_source(J.code)
+        assert J.ncontrib == len(jit.reads(J.terms[0]))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("rank", [1, 3])
+def test_rank1_and_rank3_match_torch_path(cuda, rank):
+    from odil_gb300.domain import State
+    from odil_gb300.problem import Problem
+    if rank == 1:
+        op, dom = _op1d, _dom((33, ), ("x", ), cuda, ["u"])
+    else:
+        op, dom = _op3d, _dom((6, 8, 10), ("t", "x", "y"), cuda, ["p"])
+    pj, pt = Problem(op, dom), Problem(op, dom, jit=False)
+    assert pj.jit is not None
+    rng = np.random.default_rng(9)
+    name = dom.fieldnames[0]
+    st = State(fields={name: torch.as_tensor(rng.uniform(-1, 1, dom.shape),
+                                             device=cuda)})
+    assert _rel(pj.eval_operator(st)[0], pt.eval_operator(st)[0]) < 1e-12
+    lj, gj, _, _ = pj.eval_loss_grad(st)
+    lt, gt, _, _ = pt.eval_loss_grad(st)
+    assert abs(lj.item() - lt.item()) <= 1e-12 * lt.item()
+    assert _rel(gj[name], gt[name]) < 1e-11
+    _, J = pj.linearize(st)
+    packed = pj.pack_fields(st.fields)
+
+    def res(x):
+        return torch.cat([t.reshape(-1) for t in pt._generic(
+            pt.unpack_fields(x), 0)])
+
+    ref = torch.autograd.functional.jacobian(res, packed)
+    D = J.to_csr().to_dense()
+    assert (D - ref).abs().max().item() <= 1e-12 * ref.abs().max().item()
+
+
+@pytest.mark.gpu
+def test_eval_diag_compiled_matches_torch_path(cuda):
+    """The stochastic diag(J^T J) estimate (util_op.py:675-731) through the
+    compiled Jacobian equals the autograd estimate for the same samples."""
+    from odil_gb300.domain import State
+    from odil_gb300.problem import Problem
+    dom = _dom((6, 8, 10), ("t", "x", "y"), cuda, ["p"])
+    pj, pt = Problem(_op3d, dom), Problem(_op3d, dom, jit=False)
+    st = State(fields={"p": torch.as_tensor(np.random.default_rng(3).uniform(
+        -1, 1, dom.shape), device=cuda)})
+    dj = pj.eval_diag(st, nsmp=4, generator=torch.Generator(cuda).manual_seed(5))
+    dt = pt.eval_diag(st, nsmp=4, generator=torch.Generator(cuda).manual_seed(5))
+    assert _rel(dj, dt) < 1e-12
