@@ -247,3 +247,44 @@ def test_stencil_coefficient_algebra(periodic):
     assert torch.equal(StencilOp.apply_stride(ut, 2), ut[::2, ::2])
     sh = StencilOp.apply_shift(ut, (1, -1)).numpy()
     assert sh[0, 1] == u[1, 0] and sh[0, 0] == 0 and sh[-1, 2] == 0
+
+
+def test_solve_regularized_host_logic(monkeypatch):
+    """linsolver.solve_regularized (linsolver.py:35-41 relaxed normal
+    equations) on CPU tensors through a small matrix-free Jacobian: the
+    dense path and the conjugate-gradient path against numpy."""
+    import argparse
+    import torch
+    from odil_gb300 import linsolver
+    rng = np.random.default_rng(11)
+    A = rng.standard_normal((30, 20)) + 3 * np.eye(30, 20)
+    At = torch.as_tensor(A)
+
+    class J:
+        shape = A.shape
+
+        def matvec(self, v):
+            return At @ v
+
+        def rmatvec(self, w):
+            return At.T @ w
+
+        def to_csr(self):
+            return At.to_sparse_csr()
+
+    b = rng.standard_normal(30)
+    for beta, bd in ((0.0, 0.0), (0.5, 0.0), (0.0, 0.7), (0.4, 0.3)):
+        M = A.T @ A + beta**2 * np.eye(20)
+        M += bd**2 * np.diag(np.diag(M))
+        ref = np.linalg.solve(M, A.T @ b)
+        got = linsolver.solve_regularized(J(), torch.as_tensor(b), beta, bd)
+        assert np.allclose(got.numpy(), ref, rtol=1e-10, atol=1e-12)
+        monkeypatch.setattr(linsolver, "DENSE_MAX", 0)
+        got = linsolver.solve_regularized(J(), torch.as_tensor(b), beta, bd,
+                                          tol=1e-14)
+        assert np.allclose(got.numpy(), ref, rtol=1e-8, atol=1e-10)
+        monkeypatch.setattr(linsolver, "DENSE_MAX", 16384)
+    args = argparse.Namespace(beta=0.5, betadiag=0.0)
+    out = linsolver.solve(J(), torch.as_tensor(b), args, None, "direct")
+    M = A.T @ A + 0.25 * np.eye(20)
+    assert np.allclose(out.numpy(), np.linalg.solve(M, A.T @ b))
