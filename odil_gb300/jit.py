@@ -189,6 +189,10 @@ class Graph:
     def index(self, axis):
         return self._mk("idx", (int(axis), ), _INT)
 
+    def param(self, name):
+        """A scalar set per launch (the epoch)."""
+        return self._mk("param", (name, ), _INT)
+
     def array(self, a):
         a = np.asarray(a)
         if a.size == 1:
@@ -499,11 +503,16 @@ class SymMod:
 class SymContext:
     """The ``ctx`` of util_op.py:432-563 during tracing."""
 
-    def __init__(self, domain, g, epoch=0, extra=None):
+    def __init__(self, domain, g, extra=None):
         self.domain = domain
         self.g = g
-        self.epoch = epoch
         self.extra = extra
+
+    @property
+    def epoch(self):
+        """A kernel argument: the compiled operator follows the epoch it is
+        evaluated at (Python branches on it are not traced)."""
+        return self.g.param("epoch")
 
     def cast(self, value, dtype=None):
         return value
@@ -540,11 +549,13 @@ class SymContext:
         return self.g.field(name, shift, frozen=freeze)
 
 
-def trace(operator, domain, extra=None, epoch=0):
-    """Traces ``operator`` on ``domain``; returns (graph, term nodes)."""
+def trace(operator, domain, extra=None):
+    """Traces ``operator`` on ``domain``; returns (graph, term nodes).
+    ``extra`` and the numpy arrays the operator reads are captured as they
+    are now; the epoch stays a kernel argument."""
     from .problem import Problem
     g = Graph(domain.shape)
-    terms = operator(SymMod(g), SymContext(domain, g, epoch, extra))
+    terms = operator(SymMod(g), SymContext(domain, g, extra))
     if not isinstance(terms, (list, tuple)):
         terms = [terms]
     out = []
@@ -624,6 +635,8 @@ class _Emitter:
             rhs = "a.f[%d][lin(a, %s)]" % (fi, idx)
         elif op == "idx":
             rhs = "i%d" % a[0]
+        elif op == "param":
+            rhs = "a.%s" % a[0]
         elif op == "ext":
             idx = " + ".join("(long long)i%d * a.es[%d][%d]" % (d, a[0], d)
                              for d in range(self.ndim))
@@ -678,6 +691,7 @@ struct Args {
     T* contrib[NC > 0 ? NC : 1];
     double* partial;
     int n[3];
+    int epoch;
     long long es[NE > 0 ? NE : 1][3];
     double scale[NK];
 };
@@ -899,6 +913,7 @@ class JitOperator:
                         ("contrib", ctypes.c_void_p * max(1, nc)),
                         ("partial", ctypes.c_void_p),
                         ("n", ctypes.c_int * 3),
+                        ("epoch", ctypes.c_int),
                         ("es", (ctypes.c_longlong * 3) * max(1, ne)),
                         ("scale", ctypes.c_double * nk)]
 
@@ -916,7 +931,7 @@ class JitOperator:
             self._lib = lib
         return self._lib
 
-    def _args(self, fields, device):
+    def _args(self, fields, device, epoch=0):
         g = self.graph
         if self._ext is None or self._ext[0] != device:
             ext = [torch.tensor(a, dtype=self.dtype, device=device)
@@ -945,13 +960,14 @@ class JitOperator:
         n = int(np.prod(g.shape))
         for k in range(len(self.terms)):
             a.scale[k] = 2.0 / n
+        a.epoch = int(epoch)
         return a, n
 
-    def residual(self, fields):
+    def residual(self, fields, epoch=0):
         """The residual fields f_k (list of tensors)."""
         from ._capi import stream_handle
         u0 = fields[self.fields[0]]
-        a, n = self._args(fields, u0.device)
+        a, n = self._args(fields, u0.device, epoch)
         outs = [torch.empty(self.graph.shape, dtype=self.dtype,
                             device=u0.device) for _ in self.terms]
         for k, o in enumerate(outs):
@@ -961,13 +977,13 @@ class JitOperator:
             raise RuntimeError("odil_jit_residual failed (%d)" % st)
         return outs
 
-    def jacobian(self, fields):
+    def jacobian(self, fields, epoch=0):
         """Coefficient fields of the Jacobian: a tensor [reads, *grid] and,
         per (term, field), the read indices and shifts (row q holds
         df_k(c)/du_j(c + s_q))."""
         from ._capi import stream_handle
         u0 = fields[self.fields[0]]
-        a, n = self._args(fields, u0.device)
+        a, n = self._args(fields, u0.device, epoch)
         dummy = torch.empty(1, dtype=self.dtype, device=u0.device)
         for k in range(len(self.terms)):
             a.out[k] = dummy.data_ptr()
@@ -987,13 +1003,13 @@ class JitOperator:
                 q += 1
         return coef, blocks
 
-    def loss_grad(self, fields):
+    def loss_grad(self, fields, epoch=0):
         """(loss, {field: grad}, [mean(f_k^2)]) with the FP64 loss summed in
         a fixed order."""
         from ._capi import stream_handle
         u0 = fields[self.fields[0]]
         dev = u0.device
-        a, n = self._args(fields, dev)
+        a, n = self._args(fields, dev, epoch)
         nk = len(self.terms)
         nb = (n + 255) // 256
         partial = torch.empty((nb, nk), dtype=torch.float64, device=dev)

@@ -326,7 +326,7 @@ class Problem:
             u = state.fields[self.domain.fieldnames[0]]
             return [self.kernels.residual(u)]
         if self.jit is not None:
-            return self.jit.residual(state.fields)
+            return self.jit.residual(state.fields, epoch)
         with torch.no_grad():
             ff = self._generic(state.fields, epoch)
         return [f.value if isinstance(f, Problem.Raw) else f for f in ff]
@@ -342,7 +342,7 @@ class Problem:
             loss = loss.reshape(()).clone()
             return loss, {names[0]: grad}, {}, [loss]
         if self.jit is not None:
-            loss, grads, split = self.jit.loss_grad(state.fields)
+            loss, grads, split = self.jit.loss_grad(state.fields, epoch)
             return loss, grads, {}, split
         fields = {k: v.detach().requires_grad_(True)
                   for k, v in state.fields.items()}
@@ -371,8 +371,8 @@ class Problem:
         acc = None
         jac = None
         if self.kernels is None and self.jit is not None:
-            const = self.jit.residual(state.fields)
-            coef, blocks = self.jit.jacobian(state.fields)
+            const = self.jit.residual(state.fields, epoch)
+            coef, blocks = self.jit.jacobian(state.fields, epoch)
             jac = StencilJacobian(coef, blocks, len(const), len(names),
                                   self.domain.shape)
         for _ in range(nsmp):
@@ -427,8 +427,8 @@ class Problem:
         self.init_missing(state)
         self._check_device(state)
         if self.kernels is None and self.jit is not None:
-            const = self.jit.residual(state.fields)
-            coef, blocks = self.jit.jacobian(state.fields)
+            const = self.jit.residual(state.fields, epoch)
+            coef, blocks = self.jit.jacobian(state.fields, epoch)
             return const, StencilJacobian(coef, blocks, len(const),
                                           len(self.domain.fieldnames),
                                           self.domain.shape)

@@ -424,3 +424,43 @@ def test_eval_diag_compiled_matches_torch_path(cuda):
     dj = pj.eval_diag(st, nsmp=4, generator=torch.Generator(cuda).manual_seed(5))
     dt = pt.eval_diag(st, nsmp=4, generator=torch.Generator(cuda).manual_seed(5))
     assert _rel(dj, dt) < 1e-12
+
+
+def _op_epoch(mod, ctx):
+    u = ctx.field("u")
+    return [u - ctx.field("u", -1) * 0.5 - 0.1 * ctx.epoch]
+
+
+def _op_branch(mod, ctx):
+    u = ctx.field("u")
+    return [u * 2 if ctx.epoch > 3 else u]
+
+
+def test_epoch_is_a_kernel_argument():
+    """ctx.epoch becomes a per-launch scalar; a Python branch on it is not
+    traced (the operator then runs op by op)."""
+    from odil_gb300 import jit
+    from odil_gb300.problem import Problem
+    dom = _dom((16, ), ("x", ), "cpu", ["u"])
+    g, terms = jit.trace(_op_epoch, dom)
+    assert any(n.op == "param" for n in g.nodes)
+    assert "a.epoch" in jit.JitOperator(_op_epoch, dom).code
+    with pytest.raises(jit.JitUnsupported):
+        jit.trace(_op_branch, dom)
+    assert Problem(_op_branch, dom).jit is None
+
+
+@pytest.mark.gpu
+def test_epoch_follows_the_evaluation(cuda):
+    from odil_gb300.domain import State
+    from odil_gb300.problem import Problem
+    dom = _dom((16, ), ("x", ), cuda, ["u"])
+    pj, pt = Problem(_op_epoch, dom), Problem(_op_epoch, dom, jit=False)
+    st = State(fields={"u": torch.linspace(0, 1, 16, dtype=torch.float64,
+                                           device=cuda)})
+    for ep in (0, 3, 7):
+        assert _rel(pj.eval_operator(st, ep)[0],
+                    pt.eval_operator(st, ep)[0]) < 1e-14
+        lj = pj.eval_loss_grad(st, ep)[0]
+        lt = pt.eval_loss_grad(st, ep)[0]
+        assert abs(lj.item() - lt.item()) <= 1e-13 * lt.item()
