@@ -149,6 +149,54 @@ class Domain:
     def size(self, i):
         return self.shape[self._axis(i)]
 
+    def cell_node_by_name(self, name):
+        """util_op.py:173-180: cell nodes along axis `name`, or None."""
+        if name in self.varnames:
+            return self.cell_node_by_dim(self.varnames.index(name))
+        return None
+
+    def custom_by_name(self, name):
+        """util_op.py:229-234: the named constant fields."""
+        import torch
+        dt = torch.float32 if np.dtype(self.dtype) == np.float32 \
+            else torch.float64
+        if name == "zeros":
+            return torch.zeros(self.shape, dtype=dt, device=self.device)
+        if name == "ones":
+            return torch.ones(self.shape, dtype=dt, device=self.device)
+        return None
+
+    def random_inner(self, size, rng=None):
+        """util_op.py:236-241: `size` Latin-hypercube points inside the
+        domain, as a list of coordinate arrays (one per axis)."""
+        from .problem import latin_hypercube
+        res = latin_hypercube(self.ndim, size, rng).T
+        for i in range(self.ndim):
+            res[i] = self.lower[i] + (self.upper[i] - self.lower[i]) * res[i]
+        return [p for p in res]
+
+    def random_boundary(self, normal, side, size, rng=None):
+        """util_op.py:243-263: `size` Latin-hypercube points on the face
+        normal to axis `normal` at side 0 (lower) or 1 (upper)."""
+        from .problem import latin_hypercube
+        assert normal < self.ndim
+        assert side in (0, 1)
+        res = latin_hypercube(self.ndim - 1, size, rng).T
+        res = np.vstack((res[:normal], np.full(size, float(side)),
+                         res[normal:]))
+        for i in range(self.ndim):
+            res[i] = self.lower[i] + (self.upper[i] - self.lower[i]) * res[i]
+        return [p for p in res]
+
+    def state_to_field(self, key, state, mod=None):
+        """util_op.py:309-315 (fields only: multigrid weights are not
+        supported)."""
+        return state.fields[key]
+
+    def add_field_to_state(self, u, key, state, mod=None):
+        """util_op.py:317-330 (fields only): state.fields[key] += u."""
+        state.fields[key] += u
+
     def assign_active_state(self, dst, src):
         """util_op.py:263-268."""
         for name in self.fieldnames:

@@ -21,6 +21,64 @@ from .domain import State
 from .mod import TorchMod
 
 
+def extrap_quadh(u0, u1, u1p):
+    """util_op.py:1017-1023: quadratic extrapolation from points 0, 1 and
+    1.5 to point 2 (the face value u1p sits half a cell out)."""
+    return (u0 - 6 * u1 + 8 * u1p) / 3
+
+
+def extrap_quad(u0, u1, u2):
+    """util_op.py:1026-1029: quadratic extrapolation from 0, 1, 2 to 3."""
+    return u0 - 3 * u1 + 3 * u2
+
+
+def extrap_linear(u0, u1):
+    """util_op.py:1032-1035: linear extrapolation from 0, 1 to 2."""
+    return 2 * u1 - u0
+
+
+def latin_hypercube(ndim, size, rng=None):
+    """util_op.py:1082-1098: `size` points of the unit cube [size, ndim],
+    one in each of the `size` equal strata of every axis, the strata matched
+    across axes by independent random permutations.  Draws from numpy's
+    global generator (as the reference does) unless `rng` (a numpy
+    Generator) is given."""
+    rand = np.random.rand if rng is None else (lambda *s: rng.random(s))
+    perm = np.random.permutation if rng is None else rng.permutation
+    pts = (np.arange(size)[:, None] + rand(size, ndim)) / size
+    for j in range(ndim):
+        pts[:, j] = pts[perm(size), j]
+    return pts
+
+
+def operator_laplace(mod, ctx):
+    """util_op.py:1038-1079: the reference's sample operator, Laplacians of
+    fields u and v on an (x, y) grid with linear extrapolation to the halo
+    cells, and a zero third term."""
+    dx, dy = ctx.step("x"), ctx.step("y")
+    ix, iy = ctx.cell_index("x"), ctx.cell_index("y")
+    nx, ny = ctx.size("x"), ctx.size("y")
+
+    def stencil_var(key):
+        return [ctx.field(key), ctx.field(key, -1, 0), ctx.field(key, 1, 0),
+                ctx.field(key, 0, -1), ctx.field(key, 0, 1)]
+
+    def apply_bc_extrap(st):
+        st[1] = mod.where(ix == 0, extrap_linear(st[2], st[0]), st[1])
+        st[2] = mod.where(ix == nx - 1, extrap_linear(st[1], st[0]), st[2])
+        st[3] = mod.where(iy == 0, extrap_linear(st[4], st[0]), st[3])
+        st[4] = mod.where(iy == ny - 1, extrap_linear(st[3], st[0]), st[4])
+        return st
+
+    def laplace(st):
+        q, qxm, qxp, qym, qyp = st
+        return (qxp - 2 * q + qxm) / dx**2 + (qyp - 2 * q + qym) / dy**2
+
+    u_st = apply_bc_extrap(stencil_var("u"))
+    v_st = apply_bc_extrap(stencil_var("v"))
+    return [laplace(u_st), laplace(v_st), ctx.field("zeros")]
+
+
 def _torch_dtype(np_dtype):
     return torch.float32 if np.dtype(np_dtype) == np.float32 else torch.float64
 

@@ -7,13 +7,76 @@ dispatches to ``optimize_newton`` (Newton with ``linsolver.solve``) or to
 protocol is the reference's: ``callback(packed, epoch, dhistory=None,
 opt=None)``.  States and packed vectors stay on the GPU.
 """
+import inspect
+import os
+import re
+import sys
 import time
 from collections import defaultdict
 
+import numpy as np
 import torch
 
 from . import linsolver
 from . import optimizer as optimizer_mod
+
+
+_log_file = sys.stderr
+_log_echo = False
+_time_prev = None
+
+
+def set_log_file(f, echo=False):
+    """util.py:46-49: where printlog writes (and whether it echoes to
+    stderr)."""
+    global _log_file, _log_echo
+    _log_file, _log_echo = f, echo
+
+
+def printlog(*msg):
+    """util.py:52-58: one line to the log file."""
+    m = " ".join(map(str, msg)) + "\n"
+    if _log_echo and _log_file is not sys.stderr:
+        sys.stderr.write(m)
+        sys.stderr.flush()
+    _log_file.write(m)
+    _log_file.flush()
+
+
+def TIMECLEAR():
+    """util.py:61-63: restarts the TIME stopwatch."""
+    global _time_prev
+    _time_prev = time.time()
+
+
+def TIME(pattern="{file}:{line}"):
+    """util.py:66-75: logs the caller's file:line and the seconds since the
+    previous TIME/TIMECLEAR."""
+    global _time_prev
+    now = time.time()
+    if _time_prev is None:
+        _time_prev = now
+    caller = inspect.stack()[1]
+    d = {"file": os.path.basename(caller[1]), "line": caller[2]}
+    printlog((pattern + " {:.3f}s".format(now - _time_prev)).format(**d))
+    _time_prev = time.time()
+
+
+def get_error(u, v):
+    """util.py:102-106: mean absolute, root-mean-square and maximum
+    difference (numpy arrays or tensors)."""
+    if isinstance(u, torch.Tensor) or isinstance(v, torch.Tensor):
+        d = (torch.as_tensor(u) - torch.as_tensor(v)).abs()
+        return (d.mean().item(), (d**2).mean().sqrt().item(),
+                d.max().item())
+    d = np.abs(np.asarray(u) - np.asarray(v))
+    return np.mean(d), np.mean(d**2)**0.5, np.max(d)
+
+
+def get_memory_usage_kb():
+    """util.py:373-379: resident set size of this process in KiB."""
+    with open("/proc/self/status") as f:
+        return int(re.findall(r"VmRSS:[^0-9]*([0-9]*)", f.read())[0])
 
 
 class Timer:

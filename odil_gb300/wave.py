@@ -15,9 +15,7 @@ from . import _capi
 from ._capi import call, ptr, stream_handle
 
 
-def extrap_quadh(u0, u1, u1p):
-    """util_op.py:1017-1023: quadratic extrapolation to the face value."""
-    return (u0 - 6 * u1 + 8 * u1p) / 3
+from .problem import extrap_quadh  # noqa: E402  (util_op.py:1017-1023)
 
 
 class WaveOperator:

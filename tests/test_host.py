@@ -288,3 +288,67 @@ def test_solve_regularized_host_logic(monkeypatch):
     out = linsolver.solve(J(), torch.as_tensor(b), args, None, "direct")
     M = A.T @ A + 0.25 * np.eye(20)
     assert np.allclose(out.numpy(), np.linalg.solve(M, A.T @ b))
+
+
+def test_util_op_helpers():
+    """util_op.py:1017-1098 and util.py:46-106, 373-379 host helpers."""
+    import io
+    import torch
+    from odil_gb300 import util
+    from odil_gb300.domain import Domain, State
+    from odil_gb300.problem import (extrap_linear, extrap_quad, extrap_quadh,
+                                    latin_hypercube)
+    # Extrapolations are exact on polynomials of their degree.
+    assert extrap_linear(1.0, 3.0) == 5.0
+    assert extrap_quad(1.0, 4.0, 9.0) == 16.0            # x^2 at 1, 2, 3 -> 4
+    f = lambda x: 2 * x * x - x + 1  # noqa: E731
+    assert abs(extrap_quadh(f(0), f(1), f(1.5)) - f(2)) < 1e-12
+    # Latin hypercube: one point per stratum on every axis.
+    rng = np.random.default_rng(0)
+    pts = latin_hypercube(3, 50, rng)
+    assert pts.shape == (50, 3) and pts.min() >= 0 and pts.max() < 1
+    for j in range(3):
+        assert sorted(np.floor(pts[:, j] * 50).astype(int)) == list(range(50))
+    np.random.seed(1)
+    a = latin_hypercube(2, 10)
+    np.random.seed(1)
+    assert np.array_equal(a, latin_hypercube(2, 10))
+    dom = Domain(ndim=2, shape=(8, 6), lower=(0, -1), upper=(2, 1),
+                 varnames=("x", "y"), fieldnames=["u"], device="cpu")
+    xs, ys = dom.random_inner(20, rng)
+    assert xs.min() >= 0 and xs.max() <= 2 and ys.min() >= -1 and ys.max() <= 1
+    bx, by = dom.random_boundary(1, 1, 7, rng)
+    assert np.all(by == 1) and bx.min() >= 0 and bx.max() <= 2
+    assert np.allclose(dom.cell_node_by_name("y"), np.linspace(-1, 1, 7))
+    assert dom.cell_node_by_name("z") is None
+    assert float(dom.custom_by_name("ones").sum()) == 48
+    assert dom.custom_by_name("other") is None
+    st = State(fields={"u": torch.zeros(8, 6, dtype=torch.float64)})
+    dom.add_field_to_state(torch.ones(8, 6, dtype=torch.float64), "u", st)
+    assert float(dom.state_to_field("u", st).sum()) == 48
+    # util: error norms, logging, memory.
+    e1, e2, ei = util.get_error(np.array([1.0, 2.0]), np.array([1.0, 4.0]))
+    assert (e1, ei) == (1.0, 2.0) and abs(e2 - 2**0.5) < 1e-15
+    buf = io.StringIO()
+    util.set_log_file(buf)
+    util.printlog("a", 1)
+    util.TIMECLEAR()
+    util.TIME()
+    util.set_log_file(__import__("sys").stderr)
+    lines = buf.getvalue().splitlines()
+    assert lines[0] == "a 1" and lines[1].startswith("test_host.py:")
+    assert util.get_memory_usage_kb() > 0
+
+
+def test_operator_laplace_is_traced():
+    """The reference's sample operator (util_op.py:1038-1079) traces into
+    the stencil compiler: three terms, the zero term constant."""
+    from odil_gb300 import jit
+    from odil_gb300.domain import Domain
+    from odil_gb300.problem import operator_laplace
+    dom = Domain(ndim=2, shape=(10, 12), lower=(0, 0), upper=(1, 1),
+                 varnames=("x", "y"), fieldnames=["u", "v"], device="cpu")
+    g, terms = jit.trace(operator_laplace, dom)
+    assert len(terms) == 3 and terms[2].op == "const"
+    assert {n for n, _ in jit.reads(terms[0])} == {"u"}
+    assert len(jit.reads(terms[1])) == 5
