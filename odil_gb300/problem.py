@@ -199,6 +199,16 @@ class Jacobian:
         """diag(J^T J), packed (families that provide it)."""
         return self.kernels.jtj_diag().reshape(-1)
 
+    def stencil_blocks(self):
+        """{(0, 0): StencilOp} from the family's per-slot coefficient fields
+        (families that expose them)."""
+        if not hasattr(self.kernels, "coefficients"):
+            raise NotImplementedError("this family has no coefficient fields")
+        from .stencil import StencilOp
+        return {(0, 0): StencilOp(self.kernels.SLOT_SHIFTS,
+                                  self.kernels.coefficients(),
+                                  self.kernels.shape)}
+
     def solve(self, rhs):
         return self.kernels.march(rhs.reshape(self.kernels.shape)).reshape(-1)
 
@@ -234,6 +244,10 @@ class StencilJacobian:
         self.nterms, self.nfields = nterms, nfields
         self.shape = (nterms * self.n, nfields * self.n)
         self.dtype, self.device = coef.dtype, coef.device
+
+    def stencil_blocks(self):
+        """{(term, field): StencilOp} of the Jacobian."""
+        return dict(self.ops)
 
     def matvec(self, v):
         n = self.n

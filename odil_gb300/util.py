@@ -211,6 +211,87 @@ def optimize_jacobi(args, problem, state, callback=None):
     return packed
 
 
+def optimize_multigrid(args, problem, state, callback=None):
+    """util.py:382-493: Newton epochs whose normal equations
+    J^T J d = -J^T r are solved by `linsolver_maxiter` (default 50) V-cycles
+    of the multigrid on the GPU (stencil.MultigridOp: Galerkin coarsening of
+    the J^T J stencils, damped Jacobi with `omega`, `smooth_pre` /
+    `smooth_post` sweeps, direct solve below `ndirect` cells per axis).
+    The Jacobian must provide its stencils (compiled generic operators and
+    families with coefficient fields do)."""
+    from .stencil import MultigridOp
+    opt = optimizer_mod.Optimizer(name='multigrid', displayname='Multigrid')
+    problem.init_missing(state)
+    packed = problem.pack_state(state)
+    dhistory = defaultdict(list)
+    dom = problem.domain
+    names = list(dom.fieldnames)
+    nvar = len(names)
+    shape = tuple(dom.shape)
+    n = int(np.prod(shape))
+    mg = None
+    omega = getattr(args, "omega", 0.6)
+    iters = getattr(args, "linsolver_maxiter", None) or 50
+
+    def smoother(level, u, f):
+        return mg.smoother_jacobi(level, u, f, omega=omega)
+
+    for epoch in range(getattr(args, "epoch_start", 0), args.epochs + 1):
+        s = problem.unpack_state(packed)
+        dom.assign_active_state(state, s)
+        const, J = problem.linearize(state, epoch=epoch)
+        opt.last_loss = sum(torch.mean(c**2) for c in const)
+        opt.last_residual = [torch.mean(c**2)**0.5 for c in const]
+        if callback:
+            callback(packed, epoch, dhistory=dhistory, opt=opt)
+        if epoch == args.epochs:
+            break
+        opt.evals += 1
+        blocks = J.stencil_blocks()
+        if mg is None:
+            # The transfer operators wrap where the stencils do; a periodic
+            # axis halves exactly, so the depth stops where a size turns odd.
+            per = next(iter(blocks.values())).periodic
+            nl = getattr(args, "nlvl", None)
+            while per and any(p for p in per) and (nl is None or nl > 1):
+                lv = nl if nl is not None else 64
+                if all(not p or sz % (1 << (lv - 1)) == 0
+                       for sz, p in zip(shape, per)):
+                    break
+                nl = lv - 1
+            mg = MultigridOp(shape, nvar=nvar, nlevels=nl,
+                             restriction=getattr(args, "restriction", "full"),
+                             periodic=per, dtype=packed.dtype,
+                             device=packed.device)
+        A = [[None] * nvar for _ in range(nvar)]
+        for (k, i), Bi in blocks.items():
+            for (k2, j), Bj in blocks.items():
+                if k2 != k:
+                    continue
+                C = Bi.mul_transpose_op(Bj)
+                A[i][j] = C if A[i][j] is None else A[i][j].add(C)
+        mg.update_A(A)
+        rhs = -J.rmatvec(torch.cat([c.reshape(-1) for c in const]))
+        f = [rhs[q * n:(q + 1) * n].reshape(shape).contiguous()
+             for q in range(nvar)]
+        sol = [torch.zeros_like(x) for x in f]
+        timer = Timer()
+        timer.push('linsolver')
+        for _ in range(iters):
+            sol = mg.step(sol, f, smoother,
+                          ndirect=getattr(args, "ndirect", 3),
+                          pre=getattr(args, "smooth_pre", 2),
+                          post=getattr(args, "smooth_post", 2))
+        timer.pop()
+        packed += torch.cat([x.reshape(-1) for x in sol])
+    s = problem.unpack_state(packed)
+    dom.assign_active_state(state, s)
+    return packed
+
+
+optimize_multigridop = optimize_multigrid
+
+
 def optimize(args, optname, problem, state, callback=None, **kwargs):
     """util.py:365-370."""
     if optname == 'newton':

@@ -464,3 +464,36 @@ def test_epoch_follows_the_evaluation(cuda):
         lj = pj.eval_loss_grad(st, ep)[0]
         lt = pt.eval_loss_grad(st, ep)[0]
         assert abs(lj.item() - lt.item()) <= 1e-13 * lt.item()
+
+
+@pytest.mark.gpu
+def test_optimize_multigrid_on_compiled_operator(cuda):
+    """util.optimize_multigrid (util.py:382-493): Newton with V-cycles on the
+    Galerkin J^T J stencils reaches the direct Newton solution of a
+    screened-Poisson operator."""
+    import argparse
+    from odil_gb300 import util
+    from odil_gb300.domain import Domain, State
+    from odil_gb300.problem import Problem
+    dom = Domain(ndim=2, shape=(16, 16), lower=(0, 0), upper=(1, 1),
+                 varnames=("x", "y"), fieldnames=["u"], device=cuda)
+
+    def op(mod, ctx):
+        u = ctx.field("u")
+        lap = (ctx.field("u", 1, 0) + ctx.field("u", -1, 0) +
+               ctx.field("u", 0, 1) + ctx.field("u", 0, -1) - 4 * u)
+        return [3 * u - 0.5 * lap - mod.sin(ctx.cell_center(0)) + 0.1 * u * u]
+
+    pj = Problem(op, dom)
+    ref = torch.zeros(dom.shape, dtype=torch.float64, device=cuda)
+    st = State(fields={"u": ref})
+    for _ in range(6):
+        const, J = pj.linearize(st)
+        ref += J.solve(-const[0].reshape(-1)).reshape(dom.shape)
+    args = argparse.Namespace(epochs=6, epoch_start=0, nlvl=3,
+                              restriction="full", omega=0.6,
+                              linsolver_maxiter=30, ndirect=3, smooth_pre=2,
+                              smooth_post=2)
+    u = torch.zeros(dom.shape, dtype=torch.float64, device=cuda)
+    util.optimize_multigrid(args, pj, State(fields={"u": u}))
+    assert _rel(u, ref) < 1e-8
