@@ -497,3 +497,43 @@ def test_optimize_multigrid_on_compiled_operator(cuda):
     u = torch.zeros(dom.shape, dtype=torch.float64, device=cuda)
     util.optimize_multigrid(args, pj, State(fields={"u": u}))
     assert _rel(u, ref) < 1e-8
+
+
+@pytest.mark.parametrize("case", ["wave", "advection", "nonlinear", "laplace",
+                                  "rank1"])
+def test_trace_matches_op_by_op_on_cpu(case):
+    """The traced graph, evaluated with numpy, equals the op-by-op torch
+    residual of the same operator on CPU tensors (the tracer's semantics:
+    shifts, masks, broadcast arrays, coordinates, constants)."""
+    from odil_gb300 import jit
+    from odil_gb300.domain import Domain
+    from odil_gb300.problem import Problem, operator_laplace
+    if case == "wave":
+        dom, op = _wave("cpu")
+    elif case == "advection":
+        from odil_gb300.advection import AdvectionOperator
+        dom = Domain(ndim=3, shape=(5, 6, 7), lower=(0, 0, 0),
+                     upper=(1, 1, 1), varnames=("t", "x", "y"),
+                     fieldnames=["p"], device="cpu")
+        A = AdvectionOperator(0.7, -0.3, np.random.default_rng(2)
+                              .standard_normal((6, 7)))
+        op = A.__call__
+    elif case == "nonlinear":
+        dom, op = _nonlinear_domain("cpu"), _nonlinear
+    elif case == "laplace":
+        dom = Domain(ndim=2, shape=(9, 11), lower=(0, 0), upper=(1, 2),
+                     varnames=("x", "y"), fieldnames=["u", "v"],
+                     device="cpu")
+        op = operator_laplace
+    else:
+        dom, op = _dom((33, ), ("x", ), "cpu", ["u"]), _op1d
+    g, terms = jit.trace(op, dom)
+    rng = np.random.default_rng(7)
+    fields = {n: rng.uniform(-1, 1, dom.shape) for n in dom.fieldnames}
+    pt = Problem(op, dom, jit=False)
+    ref = pt._generic({n: torch.as_tensor(v) for n, v in fields.items()}, 0)
+    assert len(ref) == len(terms)
+    for t, r in zip(terms, ref):
+        got = np.broadcast_to(_eval_np(g, t, fields, {}), dom.shape)
+        r = np.broadcast_to(torch.as_tensor(r).numpy(), dom.shape)
+        assert np.allclose(got, r, rtol=1e-13, atol=1e-13)
