@@ -193,6 +193,43 @@ class Graph:
         """A scalar set per launch (the epoch)."""
         return self._mk("param", (name, ), _INT)
 
+    def shifted(self, node, off, memo=None):
+        """`node` evaluated at cell c - off (numpy.roll by `off`, periodic):
+        field reads move their offset, index and array leaves read the
+        wrapped cell."""
+        off = tuple(int(o) for o in off)
+        if not any(off):
+            return node
+        memo = {} if memo is None else memo
+        if node.id in memo:
+            return memo[node.id]
+        op, a = node.op, node.args
+        if op in ("const", "param"):
+            r = node
+        elif op in ("field", "ffield"):
+            r = self._mk(op, (a[0], tuple(s - o for s, o in zip(a[1], off))),
+                         node.kind)
+        elif op == "idx":
+            o = off[a[0]]
+            r = node if o == 0 else self._mk("idxs", (a[0], o), _INT)
+        elif op == "idxs":
+            o = a[1] + off[a[0]]
+            r = self._mk("idx", (a[0], ), _INT) if o == 0 else \
+                self._mk("idxs", (a[0], o), _INT)
+        elif op in ("ext", "exts"):
+            arr = self.ext[a[0]][0]
+            base = a[1] if op == "exts" else (0, ) * len(off)
+            o = tuple(b + (d if arr.shape[ax] != 1 else 0)
+                      for ax, (b, d) in enumerate(zip(base, off)))
+            r = self._mk("ext", (a[0], ), node.kind) if not any(o) else \
+                self._mk("exts", (a[0], o), node.kind)
+        else:
+            args = tuple(self.shifted(x, off, memo) if isinstance(x, Node)
+                         else x for x in a)
+            r = self._mk(op, args, node.kind)
+        memo[node.id] = r
+        return r
+
     def array(self, a):
         a = np.asarray(a)
         if a.size == 1:
@@ -329,7 +366,8 @@ class Graph:
         zero = self.const(0.0)
         if op == "field":
             r = self.const(1.0) if (args[0], args[1]) == wrt else zero
-        elif op in ("const", "ffield", "idx", "ext") or node.kind != _FLOAT:
+        elif op in ("const", "ffield", "idx", "idxs", "ext", "exts") or \
+                node.kind != _FLOAT:
             r = zero
         elif op in ("add", "sub"):
             da = self.diff(args[0], wrt, memo)
@@ -435,10 +473,14 @@ class SymMod:
         return self.g.where(c, a, b)
 
     def roll(self, x, shift, axis):
-        if isinstance(x, Node):
-            raise JitUnsupported("roll of traced values (use ctx.field "
-                                 "shifts)")
-        return np.roll(np.asarray(x), shift, axis)
+        if not isinstance(x, Node):
+            return np.roll(np.asarray(x), shift, axis)
+        shifts = np.atleast_1d(shift)
+        axes = np.atleast_1d(list(axis) if isinstance(axis, range) else axis)
+        off = [0] * len(self.g.shape)
+        for s_, ax in zip(np.broadcast_to(shifts, axes.shape), axes):
+            off[int(ax)] += int(s_)
+        return self.g.shifted(x, off)
 
     def zeros(self, shape, dtype=None):
         return np.zeros(shape)
@@ -637,6 +679,15 @@ class _Emitter:
             rhs = "i%d" % a[0]
         elif op == "param":
             rhs = "a.%s" % a[0]
+        elif op == "idxs":
+            rhs = "wrap(i%d - (%d), a.n[%d])" % (a[0], a[1], a[0])
+        elif op == "exts":
+            idx = " + ".join(
+                "(long long)wrap(i%d - (%d), a.n[%d]) * a.es[%d][%d]"
+                % (d, a[1][d], d, a[0], d) for d in range(self.ndim))
+            rhs = "a.e[%d][%s]" % (a[0], idx)
+            if n.kind == _BOOL:
+                rhs = "(%s != T(0))" % rhs
         elif op == "ext":
             idx = " + ".join("(long long)i%d * a.es[%d][%d]" % (d, a[0], d)
                              for d in range(self.ndim))

@@ -40,6 +40,8 @@ class TorchMod:
         if isinstance(x, torch.Tensor):
             return x
         a = np.asarray(x)
+        if not a.flags.writeable:  # e.g. a broadcast view of the grid
+            a = a.copy()
         if a.dtype == bool:
             return torch.as_tensor(a, device=self.device)
         if np.issubdtype(a.dtype, np.integer):
