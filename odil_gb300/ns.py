@@ -40,6 +40,134 @@ class NsCavityOperator:
         self.pin = pin
         self.pin_weight = float(pin_weight)
 
+    def __call__(self, mod, ctx):
+        """Op-by-op form of ns_steady.py:142-433 (no-slip walls with the lid
+        u = 1 at y = 1 by quadratic extrapolation to the face, Rhie-Chow
+        continuity, deferred-correction upwinding): the generic path, which
+        the stencil compiler traces.  Terms: fu, fv, fp, then the imposed
+        points, the Laplacian penalty and the pressure pin when set."""
+        from .problem import extrap_linear, extrap_quadh
+        dx, dy = ctx.step(0), ctx.step(1)
+        ix, iy = ctx.cell_index(0), ctx.cell_index(1)
+        nx, ny = ctx.size(0), ctx.size(1)
+        mu = 1.0 / self.Re
+        zeros = ctx.field("zeros")
+        last_x, last_y = ix == nx - 1, iy == ny - 1
+        first_x, first_y = ix == 0, iy == 0
+
+        def var(key, freeze=False):
+            """q, qxm, qxp, qym, qyp"""
+            return [ctx.field(key, *sh, freeze=freeze) for sh in SHIFTS]
+
+        def walls(st, lid):
+            # halo values from the wall values (0, or `lid` at y = 1)
+            st[1] = mod.where(first_x, extrap_quadh(st[2], st[0], 0), st[1])
+            st[2] = mod.where(last_x, extrap_quadh(st[1], st[0], 0), st[2])
+            st[3] = mod.where(first_y, extrap_quadh(st[4], st[0], 0), st[3])
+            st[4] = mod.where(last_y, extrap_quadh(st[3], st[0], lid), st[4])
+            return st
+
+        def linear(st):
+            st[1] = mod.where(first_x, extrap_linear(st[2], st[0]), st[1])
+            st[2] = mod.where(last_x, extrap_linear(st[1], st[0]), st[2])
+            st[3] = mod.where(first_y, extrap_linear(st[4], st[0]), st[3])
+            st[4] = mod.where(last_y, extrap_linear(st[3], st[0]), st[4])
+            return st
+
+        def outer(st):
+            """qxmm, qxpp, qymm, qypp: second neighbours, the first ones
+            repeated at the walls."""
+            far = [mod.roll(st[1], shift=1, axis=0),
+                   mod.roll(st[2], shift=-1, axis=0),
+                   mod.roll(st[3], shift=1, axis=1),
+                   mod.roll(st[4], shift=-1, axis=1)]
+            edge = (first_x, last_x, first_y, last_y)
+            return [mod.where(e, st[q + 1], f)
+                    for q, (e, f) in enumerate(zip(edge, far))]
+
+        def upwind2(st, st5, a, b):
+            q, qxm, qxp, qym, qyp = st
+            qxmm, qxpp, qymm, qypp = st5
+            dxm = mod.where(first_x, (q - qxm) / dx,
+                            (qxmm - 4 * qxm + 3 * q) / (2 * dx))
+            dxp = mod.where(last_x, (qxp - q) / dx,
+                            (-3 * q + 4 * qxp - qxpp) / (2 * dx))
+            dym = mod.where(first_y, (q - qym) / dy,
+                            (qymm - 4 * qym + 3 * q) / (2 * dy))
+            dyp = mod.where(last_y, (qyp - q) / dy,
+                            (-3 * q + 4 * qyp - qypp) / (2 * dy))
+            return mod.where(a > 0, dxm, dxp), mod.where(b > 0, dym, dyp)
+
+        def upwind1(st, a, b):
+            q, qxm, qxp, qym, qyp = st
+            return (mod.where(a > 0, (q - qxm) / dx, (qxp - q) / dx),
+                    mod.where(b > 0, (q - qym) / dy, (qyp - q) / dy))
+
+        def second(st):
+            q, qxm, qxp, qym, qyp = st
+            return (qxp - 2 * q + qxm) / dx**2, (qyp - 2 * q + qym) / dy**2
+
+        u_st, uf_st = walls(var("u"), 1), walls(var("u", True), 1)
+        v_st, vf_st = walls(var("v"), 0), walls(var("v", True), 0)
+        p_st, pf_st = linear(var("p")), linear(var("p", True))
+        uf, vf = uf_st[0], vf_st[0]
+
+        def deferred(live, frozen):
+            # high order on the frozen field + (low order: live - frozen)
+            hx, hy = upwind2(frozen, outer(frozen), uf, vf)
+            lx, ly = upwind1(live, uf, vf)
+            fx, fy = upwind1(frozen, uf, vf)
+            return hx + lx - fx, hy + ly - fy
+
+        u_x, u_y = deferred(u_st, uf_st)
+        v_x, v_y = deferred(v_st, vf_st)
+        u_xx, u_yy = second(u_st)
+        v_xx, v_yy = second(v_st)
+        p, pxm, pxp, pym, pyp = p_st
+        fu = uf * u_x + vf * u_y - mu * (u_xx + u_yy) + (pxp - pxm) / (2 * dx)
+        fv = uf * v_x + vf * v_y - mu * (v_xx + v_yy) + (pyp - pym) / (2 * dy)
+
+        # Rhie-Chow face velocities (ns_steady.py:339-386) with the diagonal
+        # g of the frozen momentum operator.
+        g = mod.abs(uf) / dx + mod.abs(vf) / dy + mu * (2 / dx**2 + 2 / dy**2)
+        gxm, gxp = mod.roll(g, shift=1, axis=0), mod.roll(g, shift=-1, axis=0)
+        gym, gyp = mod.roll(g, shift=1, axis=1), mod.roll(g, shift=-1, axis=1)
+        pf, pfxm, pfxp, pfym, pfyp = pf_st
+        pfxmm, pfxpp, pfymm, pfypp = outer(pf_st)
+        u, uxm, uxp = u_st[0], u_st[1], u_st[2]
+        v, vym, vyp = v_st[0], v_st[3], v_st[4]
+        qxm = (u + uxm) * 0.5 + (1 / gxm * (pf - pfxmm) / (2 * dx)) * 0.5 + \
+            (1 / g * (pfxp - pfxm) / (2 * dx)) * 0.5 - \
+            (1 / gxm + 1 / g) * 0.5 * (p - pxm) / dx
+        qxp = (u + uxp) * 0.5 + (1 / gxp * (pfxpp - pf) / (2 * dx)) * 0.5 + \
+            (1 / g * (pfxp - pfxm) / (2 * dx)) * 0.5 - \
+            (1 / gxp + 1 / g) * 0.5 * (pxp - p) / dx
+        qym = (v + vym) * 0.5 + (1 / gym * (pf - pfymm) / (2 * dy)) * 0.5 + \
+            (1 / g * (pfyp - pfym) / (2 * dy)) * 0.5 - \
+            (1 / gym + 1 / g) * 0.5 * (p - pym) / dy
+        qyp = (v + vyp) * 0.5 + (1 / gyp * (pfypp - pf) / (2 * dy)) * 0.5 + \
+            (1 / g * (pfyp - pfym) / (2 * dy)) * 0.5 - \
+            (1 / gyp + 1 / g) * 0.5 * (pyp - p) / dy
+        qxm = mod.where(first_x, zeros, qxm)
+        qxp = mod.where(last_x, zeros, qxp)
+        qym = mod.where(first_y, zeros, qym)
+        qyp = mod.where(last_y, zeros, qyp)
+        fp = (qxp - qxm) / dx + (qyp - qym) / dy
+        res = [fu, fv, fp]
+        if self.mask is not None:
+            coeff = self.alpha * nx * ny / float(np.sum(self.mask))
+            m = mod.constant(self.mask)
+            res += [m * (u - mod.constant(self.u_imp)) * coeff,
+                    m * (v - mod.constant(self.v_imp)) * coeff]
+        if self.kreg:
+            k = self.kreg
+            res += [u_xx * k, u_yy * k, v_xx * k, v_yy * k]
+        if self.pin is not None:
+            pin = np.zeros((nx, ny))
+            pin[tuple(self.pin)] = 1.0
+            res += [mod.constant(pin) * p * self.pin_weight]
+        return res
+
     def bind(self, domain):
         assert domain.ndim == 2 and tuple(domain.fieldnames[:3]) == FIELDS
         n = domain.shape[0]

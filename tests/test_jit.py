@@ -614,3 +614,70 @@ def test_roll_compiled_matches_torch_path(cuda):
     lt, gt, _, _ = pt.eval_loss_grad(st)
     assert abs(lj.item() - lt.item()) <= 1e-12 * lt.item()
     assert _rel(gj["u"], gt["u"]) < 1e-11
+
+
+@pytest.mark.parametrize("extras", [False, True])
+def test_ns_generic_form_matches_oracle(extras):
+    """NsCavityOperator's op-by-op form (ns_steady.py:142-433) equals the
+    oracle's restatement term by term on CPU tensors, and its traced graph
+    (which rolls traced stencils) evaluates to the same values."""
+    from odil_gb300 import jit
+    from odil_gb300.domain import Domain
+    from odil_gb300.ns import NsCavityOperator
+    from odil_gb300.problem import Problem
+    from oracle import ns as NS
+    n = 12
+    rng = np.random.default_rng(5)
+    kw = {}
+    if extras:
+        mask = (rng.random((n, n)) < 0.2).astype(np.float64)
+        kw = dict(mask=mask, u_imp=rng.standard_normal((n, n)),
+                  v_imp=rng.standard_normal((n, n)), alpha=0.7, kreg=1e-3,
+                  pin=(2, 3), pin_weight=2.0)
+    op = NsCavityOperator(400.0, **kw)
+    dom = Domain(ndim=2, shape=(n, n), lower=(0, 0), upper=(1, 1),
+                 varnames=("x", "y"), fieldnames=["u", "v", "p"],
+                 device="cpu")
+    state = {k: rng.uniform(-1, 1, (n, n)) for k in ("u", "v", "p")}
+    setup = NS.NsSetup(n, 400.0, **kw)
+    ref = NS.residual(setup, state)
+    pt = Problem(lambda mod, ctx: op(mod, ctx), dom, jit=False)
+    assert pt.kernels is None
+    got = pt._generic({k: torch.as_tensor(v) for k, v in state.items()}, 0)
+    assert len(got) == len(ref)
+    for a, b in zip(got, ref):
+        assert np.allclose(torch.as_tensor(a).numpy(), b, rtol=1e-12,
+                           atol=1e-12 * np.abs(b).max())
+    g, terms = jit.trace(op, dom)
+    for t, b in zip(terms, ref):
+        ev = np.broadcast_to(_eval_np(g, t, state, {}), (n, n))
+        assert np.allclose(ev, b, rtol=1e-12, atol=1e-12 * np.abs(b).max())
+    if not extras:
+        jit.compile_source(jit.JitOperator(op, dom).code)
+
+
+@pytest.mark.gpu
+def test_ns_compiled_matches_torch_path(cuda):
+    """The NS cavity operator's generic form, compiled, against its
+    op-by-op torch path: residual, loss and gradient of all three fields."""
+    from odil_gb300.domain import Domain, State
+    from odil_gb300.ns import NsCavityOperator
+    from odil_gb300.problem import Problem
+    n = 16
+    op = NsCavityOperator(400.0, kreg=1e-3)
+    dom = Domain(ndim=2, shape=(n, n), lower=(0, 0), upper=(1, 1),
+                 varnames=("x", "y"), fieldnames=["u", "v", "p"],
+                 device=cuda)
+    generic = lambda mod, ctx: op(mod, ctx)  # noqa: E731
+    pj, pt = Problem(generic, dom), Problem(generic, dom, jit=False)
+    assert pj.jit is not None
+    rng = np.random.default_rng(6)
+    st = State(fields={k: torch.as_tensor(rng.uniform(-1, 1, (n, n)),
+                                          device=cuda) for k in "uvp"})
+    for a, b in zip(pj.eval_operator(st), pt.eval_operator(st)):
+        assert _rel(a, b) < 1e-11
+    lj, gj, _, _ = pj.eval_loss_grad(st)
+    lt, gt, _, _ = pt.eval_loss_grad(st)
+    assert abs(lj.item() - lt.item()) <= 1e-11 * lt.item()
+    for k in "uvp":
+        assert _rel(gj[k], gt[k]) < 1e-10, k
