@@ -342,6 +342,11 @@ class Problem:
                 self.jit = JitOperator(operator, domain, extra)
             except JitUnsupported:
                 self.jit = None
+            except Exception as e:  # an operator the tracer did not foresee
+                import warnings
+                warnings.warn("stencil compiler: %s: %s; the operator runs "
+                              "op by op" % (type(e).__name__, e))
+                self.jit = None
 
     # -- state handling (util_op.py:733-857) --------------------------------
     @property

@@ -681,3 +681,23 @@ def test_ns_compiled_matches_torch_path(cuda):
     assert abs(lj.item() - lt.item()) <= 1e-11 * lt.item()
     for k in "uvp":
         assert _rel(gj[k], gt[k]) < 1e-10, k
+
+
+def test_unforeseen_tracing_error_falls_back():
+    """An operator that fails under tracing in a way the tracer does not
+    model (here: asking a traced field for its numpy array) still gets a
+    Problem, on the op-by-op path, with a warning."""
+    import warnings
+    from odil_gb300.problem import Problem
+    dom = _dom((8, ), ("x", ), "cpu", ["u"])
+
+    def odd(mod, ctx):
+        u = ctx.field("u")
+        _ = u.numpy()
+        return [u]
+
+    with warnings.catch_warnings(record=True) as w:
+        warnings.simplefilter("always")
+        p = Problem(odd, dom)
+    assert p.jit is None
+    assert any("op by op" in str(x.message) for x in w)
