@@ -348,6 +348,21 @@ class Problem:
                               "op by op" % (type(e).__name__, e))
                 self.jit = None
 
+    def _jit_ready(self):
+        """True when the compiled operator can run; a failed build (no nvcc,
+        or a compiler error) drops to the op-by-op path with a warning."""
+        if self.jit is None:
+            return False
+        try:
+            self.jit.lib()
+            return True
+        except (RuntimeError, OSError) as e:
+            import warnings
+            warnings.warn("stencil compiler: build failed (%s); the operator "
+                          "runs op by op" % str(e).splitlines()[0])
+            self.jit = None
+            return False
+
     # -- state handling (util_op.py:733-857) --------------------------------
     @property
     def tdtype(self):
@@ -402,7 +417,7 @@ class Problem:
         if self.kernels is not None:
             u = state.fields[self.domain.fieldnames[0]]
             return [self.kernels.residual(u)]
-        if self.jit is not None:
+        if self._jit_ready():
             return self.jit.residual(state.fields, epoch)
         with torch.no_grad():
             ff = self._generic(state.fields, epoch)
@@ -418,7 +433,7 @@ class Problem:
             loss, grad = self.kernels.loss_grad(u)
             loss = loss.reshape(()).clone()
             return loss, {names[0]: grad}, {}, [loss]
-        if self.jit is not None:
+        if self._jit_ready():
             loss, grads, split = self.jit.loss_grad(state.fields, epoch)
             return loss, grads, {}, split
         fields = {k: v.detach().requires_grad_(True)
@@ -447,7 +462,7 @@ class Problem:
         names = self.domain.fieldnames
         acc = None
         jac = None
-        if self.kernels is None and self.jit is not None:
+        if self.kernels is None and self._jit_ready():
             const = self.jit.residual(state.fields, epoch)
             coef, blocks = self.jit.jacobian(state.fields, epoch)
             jac = StencilJacobian(coef, blocks, len(const), len(names),
@@ -492,7 +507,7 @@ class Problem:
         over the fused adjoint for registered families)."""
         if self.kernels is not None:
             return FusedLoss.apply(u.reshape(self.kernels.shape), self.kernels)
-        if self.jit is not None:
+        if self._jit_ready():
             return JitLoss.apply(u, self)
         fields = self.unpack_fields(u)
         ff = self._generic(fields, 0)
@@ -503,7 +518,7 @@ class Problem:
         """util_op.py:859-937: (const, J) with J matrix-free on the GPU."""
         self.init_missing(state)
         self._check_device(state)
-        if self.kernels is None and self.jit is not None:
+        if self.kernels is None and self._jit_ready():
             const = self.jit.residual(state.fields, epoch)
             coef, blocks = self.jit.jacobian(state.fields, epoch)
             return const, StencilJacobian(coef, blocks, len(const),

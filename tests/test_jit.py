@@ -701,3 +701,24 @@ def test_unforeseen_tracing_error_falls_back():
         p = Problem(odd, dom)
     assert p.jit is None
     assert any("op by op" in str(x.message) for x in w)
+
+
+def test_failed_build_falls_back(monkeypatch):
+    """A build failure at first use drops the operator to the op-by-op path
+    with a warning instead of failing the evaluation."""
+    import warnings
+    from odil_gb300 import jit
+    from odil_gb300.problem import Problem
+    dom = _dom((8, ), ("x", ), "cpu", ["u"])
+    p = Problem(_op1d, dom)
+    assert p.jit is not None
+
+    def broken(code):
+        raise RuntimeError("nvcc failed on the generated operator:\\nboom")
+
+    monkeypatch.setattr(jit, "compile_source", broken)
+    with warnings.catch_warnings(record=True) as w:
+        warnings.simplefilter("always")
+        assert p._jit_ready() is False
+    assert p.jit is None
+    assert any("build failed" in str(x.message) for x in w)
