@@ -149,6 +149,12 @@ class Domain:
     def size(self, i):
         return self.shape[self._axis(i)]
 
+    def get_minimal(self):
+        """util_op.py:112-113: a picklable copy of the geometry
+        (util_min.py:5-28): ndim, lower, upper, varnames, fieldnames,
+        dtype, shape, and the step and cell-centre helpers."""
+        return MinimalDomain(self)
+
     def cell_node_by_name(self, name):
         """util_op.py:173-180: cell nodes along axis `name`, or None."""
         if name in self.varnames:
@@ -201,6 +207,31 @@ class Domain:
         """util_op.py:263-268."""
         for name in self.fieldnames:
             dst.fields[name].copy_(src.fields[name])
+
+
+class MinimalDomain:
+    """util_min.py:5-28: the geometry of a Domain without device state."""
+
+    def __init__(self, domain):
+        self.ndim = int(domain.ndim)
+        self.lower = np.array(domain.lower, np.float64)
+        self.upper = np.array(domain.upper, np.float64)
+        self.varnames = np.array(domain.varnames)
+        self.fieldnames = np.array(domain.fieldnames)
+        self.dtype = domain.dtype
+        self.shape = tuple(domain.shape)
+
+    def step_by_dim(self, i):
+        return (self.upper[i] - self.lower[i]) / self.shape[i]
+
+    def cell_center_1d(self, i):
+        s = self.shape[i]
+        return np.asarray(self.lower[i] + (np.arange(s) + 0.5) / s *
+                          (self.upper[i] - self.lower[i]), dtype=self.dtype)
+
+    def cell_center_all(self):
+        return np.meshgrid(*[self.cell_center_1d(i) for i in range(self.ndim)],
+                           indexing='ij')
 
 
 class State:

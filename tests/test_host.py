@@ -352,3 +352,16 @@ def test_operator_laplace_is_traced():
     assert len(terms) == 3 and terms[2].op == "const"
     assert {n for n, _ in jit.reads(terms[0])} == {"u"}
     assert len(jit.reads(terms[1])) == 5
+
+
+def test_minimal_domain_pickles():
+    """Domain.get_minimal (util_op.py:112-113, util_min.py:5-28)."""
+    import pickle
+    from odil_gb300.domain import Domain
+    dom = Domain(ndim=2, shape=(8, 6), lower=(0, -1), upper=(2, 1),
+                 varnames=("x", "y"), fieldnames=["u"], device="cpu")
+    m = pickle.loads(pickle.dumps(dom.get_minimal()))
+    assert m.shape == (8, 6) and m.step_by_dim(1) == dom.step(1)
+    x, y = m.cell_center_all()
+    assert np.allclose(x[:, 0], dom.cell_center_1d(0))
+    assert np.allclose(y[0], dom.cell_center_1d(1))
