@@ -35,9 +35,11 @@ extern "C" {
 #define ODIL_ERR_WORKSPACE (-7) /* workspace missing or too small */
 #define ODIL_ERR_ARG (-8)       /* null pointer or invalid scalar argument */
 
-/* Library version as MAJOR*10000 + MINOR*100 + PATCH. */
+/* Library version as MAJOR*10000 + MINOR*100 + PATCH.
+ * No counterpart in the reference (library metadata). */
 int odil_version(void);
-/* Static, human-readable text for a status code. */
+/* Static, human-readable text for a status code.
+ * No counterpart in the reference (the C ABI reports errors by status). */
 const char* odil_status_string(int status);
 
 /* ------------------------------------------------------------------------
@@ -63,7 +65,9 @@ typedef struct odil_wave_params {
     const void* right_u; /* [nt] u at x = upper */
 } odil_wave_params;
 
-/* Workspace bytes needed by odil_wave_loss_grad_*. */
+/* Workspace bytes needed by odil_wave_loss_grad_*.
+ * Scratch of the loss reduction of util_op.py:627-654; no counterpart (the
+ * reference allocates through TF). */
 int64_t odil_wave_workspace_bytes(const odil_wave_params* p);
 
 /* f = F(u).  Replaces Problem.eval_operator (util_op.py:968-973) for
@@ -107,7 +111,8 @@ int odil_wave_jv_f32(const odil_wave_params* p, const float* v, float* out,
                      void* stream);
 int odil_wave_jv_f64(const odil_wave_params* p, const double* v, double* out,
                      void* stream);
-/* out = J^T w. */
+/* out = J^T w.
+ * The transposed CSR product J^T w that linsolver.py:37-41 forms. */
 int odil_wave_jtv_f32(const odil_wave_params* p, const float* w, float* out,
                       void* stream);
 int odil_wave_jtv_f64(const odil_wave_params* p, const double* w, double* out,
@@ -151,7 +156,8 @@ int odil_wave_update_residual_mixed(const odil_wave_params* p, const double* u,
 
 /* rhs = (float)(-F(0)): the first right-hand side of a mixed Newton solve
  * from u = 0.  FP64 work only where boundary data enter (rows 0 and 1,
- * columns 0 and nx-1); all other cells are 0. */
+ * columns 0 and nx-1); all other cells are 0.
+ * Part of the Newton step of util.py:242-268 (-F at the start state). */
 int odil_wave_initial_rhs_mixed(const odil_wave_params* p, float* rhs,
                                 void* stream);
 /* rhs = (float)(-F(hi + lo)) for a field held as the unevaluated sum of two
@@ -166,7 +172,8 @@ int odil_wave_pair_residual_mixed(const odil_wave_params* p, const float* hi,
 /* odil_wave_march_f32 with an explicit launch shape: cpt columns per thread
  * (1, 2, 4, 8) and pf right-hand-side rows prefetched into registers (8,
  * 16); the block (nx / cpt threads rounded up to 32) may hold at most 1024,
- * 512 or 256 threads for cpt pf <= 16, <= 32 or more (ODIL_ERR_SHAPE). */
+ * 512 or 256 threads for cpt pf <= 16, <= 32 or more (ODIL_ERR_SHAPE).
+ * The direct solve of linsolver.py:35-45, as odil_wave_march_f32. */
 int odil_wave_march_shape_f32(const odil_wave_params* p, const float* b,
                               float* x, int32_t cpt, int32_t pf, void* stream);
 
@@ -183,7 +190,8 @@ int odil_wave_march_shape_f32(const odil_wave_params* p, const float* b,
  * (2, 16, 16), (4, 8, 8), (4, 16, 16), (4, 24, 8), (4, 32, 16), (8, 32, 16),
  * (8, 64, 16).  FP64: cpt pf <= 64.  warps = tiles per block, 1..4; the
  * cluster (ceil(nx / (32 cpt - 2 halo)) / warps blocks) must hold at most 16
- * blocks and fit on the device; nx >= 2.  ODIL_ERR_SHAPE otherwise. */
+ * blocks and fit on the device; nx >= 2.  ODIL_ERR_SHAPE otherwise.
+ * The direct solve of linsolver.py:35-45, as odil_wave_march_f32. */
 int odil_wave_march_tiled_f32(const odil_wave_params* p, const float* b,
                               float* x, int32_t cpt, int32_t halo, int32_t pf,
                               int32_t warps, int32_t exchange, void* stream);
@@ -200,7 +208,8 @@ int odil_wave_march_tiled_planted_wait_f32(const odil_wave_params* p,
                                            int32_t missing_bytes,
                                            void* stream);
 /* Number of halo waits that gave up since the last reset (synchronises the
- * device). */
+ * device).
+ * No counterpart in the reference (diagnostics of the bounded wait). */
 int odil_wave_march_tiled_wait_failures(int64_t* count, int32_t reset);
 
 /* ------------------------------------------------------------------------
@@ -242,18 +251,22 @@ typedef struct odil_wave_batch {
     int64_t total_bnd;
 } odil_wave_batch;
 
-/* Fills the derived constants of a device descriptor array. */
+/* Fills the derived constants of a device descriptor array.
+ * Set-up of the batched solver that replaces the per-instance runs of
+ * vary_wave.py:37-43; no direct counterpart. */
 int odil_wave_batch_setup(odil_wave_instance* inst, int32_t ninst,
                           void* stream);
 int64_t odil_wave_batch_workspace_bytes(const odil_wave_batch* b);
 /* FP64 step of a mixed Newton epoch for every instance: as
- * odil_wave_update_residual_mixed on the packed arrays. */
+ * odil_wave_update_residual_mixed on the packed arrays.
+ * util.py:242-268 per instance (the batched form of vary_wave.py:37-43). */
 int odil_wave_batch_update_residual_mixed(const odil_wave_batch* b,
                                           const double* u, const float* d,
                                           double* u_out, float* rhs,
                                           void* stream);
 /* Batched odil_wave_initial_rhs_mixed / odil_wave_pair_residual_mixed on
- * the packed arrays (one block per row task, FP64 only on boundary cells). */
+ * the packed arrays (one block per row task, FP64 only on boundary cells).
+ * util.py:242-268 per instance (the batched form of vary_wave.py:37-43). */
 int odil_wave_batch_initial_rhs_mixed(const odil_wave_batch* b, float* rhs,
                                       void* stream);
 int odil_wave_batch_pair_residual_mixed(const odil_wave_batch* b,
@@ -262,7 +275,8 @@ int odil_wave_batch_pair_residual_mixed(const odil_wave_batch* b,
 /* FP32 forward substitution of every instance in one persistent launch:
  * blocks_per_sm x #SM blocks of `threads` threads take instances from an
  * atomic work queue in `order`; threads * cpt >= max_nx; (cpt, pf) in
- * {1, 2, 4} x {8, 16} (pf = prefetched right-hand-side rows). */
+ * {1, 2, 4} x {8, 16} (pf = prefetched right-hand-side rows).
+ * linsolver.py:35-45 per instance (the batched form of vary_wave.py:37-43). */
 int odil_wave_batch_march_f32(const odil_wave_batch* b, const float* rhs,
                               float* x, int32_t threads, int32_t cpt,
                               int32_t pf, int32_t blocks_per_sm,
@@ -307,7 +321,8 @@ int odil_advect_loss_grad_f64(const odil_advect_params* p, const double* u,
                               double* grad, double* loss, void* workspace,
                               int64_t workspace_bytes, void* stream);
 /* FP64 step of the mixed-precision Newton loop, as
- * odil_wave_update_residual_mixed. */
+ * odil_wave_update_residual_mixed.
+ * The Newton loop of advection_2d.py:527-604 (FP64 residual and update). */
 int odil_advect_update_residual_mixed(const odil_advect_params* p,
                                       const double* u, const float* d,
                                       double* u_out, float* rhs,
@@ -322,14 +337,19 @@ int odil_advect_mg_jacobi(const odil_advect_params* p, const float* x,
                           const float* b, float* x_out, float omega,
                           float* r_out, void* stream);
 /* Full-weighting restriction (nt, nx, ny) -> halves: weights
- * (1, 3, 3, 1)/8 per axis, x and y periodic, t clamped. */
+ * (1, 3, 3, 1)/8 per axis, x and y periodic, t clamped.
+ * Restriction of multigrid.py:496-534, rediscretised V-cycle (the reference
+ * uses pyamg, linsolver.py:81-89). */
 int odil_advect_mg_restrict(int64_t nt, int64_t nx, int64_t ny,
                             const float* r, float* rc, void* stream);
-/* x += trilinear prolongation of the half-size correction e. */
+/* x += trilinear prolongation of the half-size correction e.
+ * Prolongation of multigrid.py:471-494 (the reference uses pyamg,
+ * linsolver.py:81-89). */
 int odil_advect_mg_prolong_add(int64_t nt, int64_t nx, int64_t ny,
                                const float* e, float* x, void* stream);
 /* Dense FP64 matrix of the operator (nt*nx*ny <= 1024), for the coarsest
- * level's direct solve. */
+ * level's direct solve.
+ * Coarsest-level direct solve (multigrid.py:322-323). */
 int odil_advect_dense(const odil_advect_params* p, double* A, void* stream);
 /* x = Ainv b with a dense FP64 n x n matrix (n <= 1024): the coarsest-level
  * direct solve (multigrid.py:307-310) by the precomputed inverse. */
@@ -358,9 +378,11 @@ typedef struct odil_ns_params {
     double pin_weight;
 } odil_ns_params;
 
-/* Number of residual terms for these parameters (or a negative status). */
+/* Number of residual terms for these parameters (or a negative status).
+ * The term count of ns_steady.py:388-411. */
 int odil_ns_num_equations(const odil_ns_params* q);
-/* f[e*n*n + cell] = residual term e at (u, v, p) (frozen = live = state). */
+/* f[e*n*n + cell] = residual term e at (u, v, p) (frozen = live = state).
+ * The residual terms of ns_steady.py:142-433 (util_op.py:968-973). */
 int odil_ns_residual_f32(const odil_ns_params* q, const float* u,
                          const float* v, const float* p, float* f,
                          void* stream);
@@ -400,14 +422,16 @@ int odil_ns_direct_solve(int64_t n, const double* coef, int64_t pin,
  * with partial pivoting.  Ainv comes out in the layout A goes in (row- or
  * column-major): the inverse of the transpose is the transpose of the
  * inverse.  ODIL_ERR_NONFINITE for an exactly singular matrix; synchronises
- * the stream. */
+ * the stream.
+ * Coarsest-level direct solve of multigrid.py:322-323 (spsolve there). */
 int64_t odil_dense_inverse_workspace_bytes(int64_t n);
 int odil_dense_inverse_f64(int64_t n, const double* A, double* Ainv,
                            void* workspace, int64_t workspace_bytes,
                            void* stream);
 
 /* The transposed solve J'^T x = b with the same factors (the preconditioner
- * (J'^T J')^-1 of the inverse problem's normal equations needs both). */
+ * (J'^T J')^-1 of the inverse problem's normal equations needs both).
+ * Part of the normal-equation solve of linsolver.py:35-45 for the cavity. */
 int odil_ns_direct_solve_t(int64_t n, const double* coef, int64_t pin,
                            void* workspace, int64_t workspace_bytes,
                            const float* b, float* x, void* stream);
@@ -445,7 +469,9 @@ int odil_stencil_apply_t_f32(const odil_stencil* A, const float* uh,
 int odil_stencil_apply_t_f64(const odil_stencil* A, const double* uh,
                              double* out, double alpha, double beta,
                              void* stream);
-/* Small device scratch for the two set-up products below. */
+/* Small device scratch for the two set-up products below.
+ * Scratch of the SparseOperator products of multigrid.py:1035-1071, 125-131;
+ * no counterpart. */
 int64_t odil_stencil_pair_workspace_bytes(void);
 /* C = A^T B as a stencil (multigrid.py:1035-1071); C->shifts must list every
  * difference b - a of the shifts of A and B; C->coef is written.  Set-up
@@ -508,12 +534,14 @@ int odil_axpby_f64(double* z, const double* x, const double* y, int64_t n,
                    double a, double b, void* stream);
 
 /* out = u + (double)d (n elements): the FP64 update after the last FP32
- * correction of a mixed-precision Newton solve. */
+ * correction of a mixed-precision Newton solve.
+ * The update packed += d of util.py:242-268. */
 int odil_add_f32_to_f64(const double* u, const float* d, double* out,
                         int64_t n, void* stream);
 
 /* out = (double)hi + (double)lo (n elements; lo may be NULL): the FP64
- * iterate of a mixed Newton solve kept as FP32 corrections. */
+ * iterate of a mixed Newton solve kept as FP32 corrections.
+ * The update packed += d of util.py:242-268, for the float-pair iterate. */
 int odil_pair_to_f64(const float* hi, const float* lo, double* out, int64_t n,
                      void* stream);
 
@@ -523,7 +551,9 @@ int odil_pair_to_f64(const float* hi, const float* lo, double* out, int64_t n,
  * rho = rho'; phase 1: alpha = rho / dots[0] (= <r^, v>); phase 2: omega =
  * dots[1] / dots[0] (= <t, s> / <t, t>).  Updates (n % 4 == 0, 16-byte
  * aligned FP32 vectors): p = r + beta (p - omega v); s = r - alpha v;
- * x += alpha ph (+ omega sh), r = s - omega t when with_s. */
+ * x += alpha ph (+ omega sh), r = s - omega t when with_s.
+ * The inner Krylov solve of linsolver.py:75-107 (bicgstab /
+ * multigrid-preconditioned). */
 int odil_bicgstab_scalars(const double* dots, double* sc, int32_t phase,
                           void* stream);
 int odil_bicgstab_update_p(float* p, const float* r, const float* v,
@@ -553,7 +583,9 @@ int odil_multidot_f64(const double* M, int64_t ld, int k,
                       void* workspace, int64_t workspace_bytes, void* stream);
 
 /* out = coef[k] * x + sum_{i<k} coef[i] * M[i*ld ...]; coef is a device array
- * of k+1 doubles; k <= 256. */
+ * of k+1 doubles; k <= 256.
+ * The direction update of the L-BFGS two-loop in optimizer.py:61-99 (scipy
+ * there). */
 int odil_lincomb_f32(float* out, const float* x, const float* M, int64_t ld,
                      int k, const double* coef, int64_t n, void* stream);
 int odil_lincomb_f64(double* out, const double* x, const double* M,
