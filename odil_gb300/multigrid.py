@@ -1,0 +1,234 @@
+"""Geometric multigrid on assembled matrices (multigrid.py:70-339), with the
+reference's module layout.
+
+``Multigrid`` keeps the interface of the reference's CSR class: node-based
+coarsening nnw[l+1] = (nnw[l] - 1) // 2 + 1 while 2^(L+1) < min(nw),
+full-weighting (or half / injection) restriction with injection at the
+coarse boundary nodes, multilinear interpolation, Galerkin coarse matrices
+A_{l+1} = R A_l T (block-diagonal R and T for `nvar` fields), damped Jacobi
+on the diagonal blocks (or on the per-cell nvar x nvar blocks with
+``full=True``), a direct solve on the coarsest level, and the recursive
+V-cycle ``step``.  Matrices are torch sparse CSR tensors on whatever device
+the operator lives on (cuSPARSE products on the GPU); the transfer
+operators are built once on the host.  The stencil-form classes are
+re-exported under the reference's names: ``MultigridOp`` and
+``SparseOperator`` (``odil_gb300.stencil.StencilOp``).
+
+Two deliberate differences: the reference sizes its transfer operators with
+n // 2 + 1 while its levels use (n - 1) // 2 + 1, which fails for even
+sizes; here both use (n - 1) // 2 + 1.  Its recursive call does not pass
+`pre` and `post` down (multigrid.py:327-329), which is kept.  The
+smoothers return a new vector rather than updating `u` in place.
+"""
+import itertools
+import warnings
+
+import numpy as np
+import torch
+
+warnings.filterwarnings("ignore", message="Sparse CSR tensor support is in beta")
+
+from .stencil import MultigridOp, StencilOp
+
+SparseOperator = StencilOp
+
+__all__ = ["Multigrid", "MultigridOp", "SparseOperator"]
+
+
+def _flat(idx, nw):
+    """Flat C-order index of multi-indices idx [m, dim] on a grid nw."""
+    return np.ravel_multi_index(tuple(idx.T), tuple(nw))
+
+
+def _csr(rows, cols, vals, shape, dtype, device):
+    m = torch.sparse_coo_tensor(
+        torch.as_tensor(np.stack([rows, cols])),
+        torch.as_tensor(np.asarray(vals, np.float64), dtype=dtype), shape,
+        check_invariants=False)
+    return m.coalesce().to_sparse_csr().to(device)
+
+
+def _block_diag(m, nvar):
+    if nvar == 1:
+        return m
+    coo = m.to_sparse_coo().coalesce()
+    r, c = coo.indices()
+    n0, n1 = m.shape
+    rows = torch.cat([r + k * n0 for k in range(nvar)])
+    cols = torch.cat([c + k * n1 for k in range(nvar)])
+    vals = torch.cat([coo.values()] * nvar)
+    return torch.sparse_coo_tensor(torch.stack([rows, cols]), vals,
+                                   (n0 * nvar, n1 * nvar),
+                                   check_invariants=False).coalesce() \
+        .to_sparse_csr()
+
+
+class Multigrid:
+    """multigrid.py:70-339 on torch sparse CSR matrices."""
+
+    def __init__(self, nw, nvar=1, nlevels=None, restriction="full",
+                 dtype=torch.float64, device="cuda"):
+        nw = np.array(nw)
+        max_nlevels = 0
+        while 2**(max_nlevels + 1) < min(nw):
+            max_nlevels += 1
+        nlevels = max_nlevels if nlevels is None else min(nlevels, max_nlevels)
+        nnw = [nw]
+        for _ in range(1, nlevels):
+            nnw.append((nnw[-1] - 1) // 2 + 1)
+        self.dim = len(nw)
+        self.nvar = nvar
+        self.nlevels = nlevels
+        self.nnw = [tuple(int(v) for v in n) for n in nnw]
+        self.restriction = restriction
+        self.dtype = dtype
+        self.device = device
+        self.RRsingle = [self.get_R(n, restriction, dtype, device)
+                         for n in self.nnw]
+        self.RR = [_block_diag(R, nvar) for R in self.RRsingle]
+        self.TT = [_block_diag(self.get_T(n, dtype, device), nvar)
+                   for n in self.nnw]
+
+    @staticmethod
+    def get_T(nw, dtype=torch.float64, device="cuda"):
+        """multigrid.py:194-227: interpolation [prod(nw), prod(nwh)]; fine
+        node iw takes coarse nodes iw // 2 + dw, dw in {0, 1}^dim with
+        dw <= iw % 2, weight 0.5^sum(iw % 2)."""
+        nw = np.array(nw)
+        dim = len(nw)
+        nwh = (nw - 1) // 2 + 1
+        iw = np.array(list(itertools.product(*[range(n) for n in nw])))
+        rw = iw % 2
+        rows, cols, vals = [], [], []
+        for dw in itertools.product([0, 1], repeat=dim):
+            dw = np.array(dw)
+            ok = np.all(dw <= rw, axis=1)
+            rows.append(_flat(iw[ok], nw))
+            cols.append(_flat(iw[ok] // 2 + dw, nwh))
+            vals.append(0.5**rw[ok].sum(1))
+        return _csr(np.concatenate(rows), np.concatenate(cols),
+                    np.concatenate(vals), (int(nw.prod()), int(nwh.prod())),
+                    dtype, device)
+
+    @staticmethod
+    def get_R(nw, restriction="full", dtype=torch.float64, device="cuda"):
+        """multigrid.py:229-281: restriction [prod(nwh), prod(nw)]; inner
+        coarse nodes average the 3^dim fine nodes around 2 iwh with the
+        normalised weights of `restriction`, boundary coarse nodes inject."""
+        nw = np.array(nw)
+        dim = len(nw)
+        nwh = (nw - 1) // 2 + 1
+        if restriction == "full":
+            coeff = lambda dw: 0.5**np.abs(dw).sum()  # noqa: E731
+        elif restriction == "half":
+            coeff = lambda dw: (2 * dim if np.abs(dw).sum() == 0 else  # noqa
+                                1 if np.abs(dw).sum() == 1 else 0)
+        elif restriction == "injection":
+            coeff = lambda dw: 1 if np.abs(dw).sum() == 0 else 0  # noqa
+        else:
+            raise ValueError("Unknown restriction=" + restriction)
+        ddw = [np.array(d) for d in itertools.product([-1, 0, 1], repeat=dim)]
+        csum = sum(coeff(d) for d in ddw)
+        iwh = np.array(list(itertools.product(*[range(n) for n in nwh])))
+        inner = np.all(iwh > 0, axis=1) & np.all(iwh + 1 < nwh, axis=1)
+        rows, cols, vals = [], [], []
+        for d in ddw:
+            c = coeff(d) / csum
+            if c == 0:
+                continue
+            rows.append(_flat(iwh[inner], nwh))
+            cols.append(_flat(iwh[inner] * 2 + d, nw))
+            vals.append(np.full(int(inner.sum()), c))
+        b = ~inner
+        rows.append(_flat(iwh[b], nwh))
+        cols.append(_flat(iwh[b] * 2, nw))
+        vals.append(np.ones(int(b.sum())))
+        return _csr(np.concatenate(rows), np.concatenate(cols),
+                    np.concatenate(vals), (int(nwh.prod()), int(nw.prod())),
+                    dtype, device)
+
+    def update_A(self, A0, DD=None, compute_lower=False):
+        """multigrid.py:116-156: the matrices of every level (A0 a sparse
+        matrix of the finest level, or a list of one per level) and the
+        diagonals of their nvar x nvar blocks."""
+        if isinstance(A0, list):
+            assert len(A0) == self.nlevels
+            AA = [a.to_sparse_csr() for a in A0]
+        else:
+            AA = [A0.to_sparse_csr()]
+            for level in range(1, self.nlevels):
+                AA.append(self.RR[level - 1] @ AA[-1] @ self.TT[level - 1])
+        nvar = self.nvar
+        DD = []
+        for A in AA:
+            coo = A.to_sparse_coo().coalesce()
+            r, c = coo.indices()
+            ns = A.shape[0] // nvar
+            d = torch.zeros((nvar, nvar, ns), dtype=A.dtype, device=A.device)
+            same = (r % ns) == (c % ns)
+            d.index_put_(((r[same] // ns), (c[same] // ns), (r[same] % ns)),
+                         coo.values()[same], accumulate=True)
+            DD.append(d)
+        self.AA = AA
+        self.DD = DD
+        # Lower triangles with the diagonal for Gauss-Seidel (the reference's
+        # compute_lower path raises NameError at multigrid.py:149).
+        self.LL = [self._tril(A) for A in AA] if compute_lower \
+            else [None] * self.nlevels
+        self._inv = {}
+
+    @staticmethod
+    def _tril(A):
+        coo = A.to_sparse_coo().coalesce()
+        r, c = coo.indices()
+        keep = c <= r
+        return torch.sparse_coo_tensor(coo.indices()[:, keep],
+                                       coo.values()[keep], A.shape,
+                                       check_invariants=False) \
+            .coalesce().to_sparse_csr()
+
+    def smoother_jacobi(self, level, u, f, omega=1.0, full=False):
+        """multigrid.py:283-299: u += omega D^-1 (f - A u), with D the
+        diagonal blocks (full=False) or the per-cell nvar x nvar blocks."""
+        A, D = self.AA[level], self.DD[level]
+        r = f - A @ u
+        if full:
+            ns = A.shape[0] // self.nvar
+            d = D.permute(2, 0, 1)  # [ns, nvar, nvar]
+            du = torch.linalg.solve(d, r.reshape(self.nvar, ns).T.unsqueeze(-1))
+            du = du.squeeze(-1).T.reshape(-1)
+        else:
+            du = r / torch.cat([D[i, i] for i in range(self.nvar)])
+        return u + du * omega
+
+    def smoother_gauss_seidel(self, level, u, f, omega=1.0):
+        """multigrid.py:301-305: u += omega (L^-1 (f - (A - L) u) - u), L
+        the lower triangle of A with its diagonal (update_A with
+        compute_lower=True)."""
+        A, L = self.AA[level], self.LL[level]
+        b = (f - (A @ u - L @ u)).reshape(-1, 1)
+        x = torch.triangular_solve(b, L, upper=False).solution.reshape(-1)
+        return u + (x - u) * omega
+
+    def smoother_direct(self, level, u, f):
+        """multigrid.py:307-310: the direct solve of the level (a dense LU
+        of the assembled matrix, formed once per update_A)."""
+        lu = self._inv.get(level)
+        if lu is None:
+            lu = self._inv[level] = torch.linalg.lu_factor(
+                self.AA[level].to_dense())
+        return torch.linalg.lu_solve(*lu, f.reshape(-1, 1)).reshape(-1)
+
+    def step(self, u, f, smoother, level=0, ndirect=5, pre=2, post=2):
+        """multigrid.py:312-339: one V-cycle from `u`."""
+        if level + 1 >= self.nlevels or min(self.nnw[level]) <= ndirect:
+            return self.smoother_direct(level, u, f)
+        for _ in range(pre):
+            u = smoother(level, u, f)
+        A, R, T = self.AA[level], self.RR[level], self.TT[level]
+        r = R @ (f - A @ u)
+        u = u + T @ self.step(torch.zeros_like(r), r, smoother,
+                              level=level + 1, ndirect=ndirect)
+        for _ in range(post):
+            u = smoother(level, u, f)
+        return u

@@ -212,7 +212,61 @@ def optimize_jacobi(args, problem, state, callback=None):
 
 
 def optimize_multigrid(args, problem, state, callback=None):
-    """util.py:382-493: Newton epochs whose normal equations
+    """util.py:382-495 (without the per-level `datalevels` problems): Newton
+    epochs whose normal equations J^T J d = -J^T r, assembled as sparse CSR
+    matrices on the fields' device, are solved by `linsolver_maxiter`
+    (default 50) V-cycles of the CSR multigrid (multigrid.Multigrid: R A T
+    coarsening, damped Jacobi on the diagonal blocks with `omega`,
+    `smooth_pre` / `smooth_post` sweeps on the finest level, direct solve
+    below `ndirect` nodes per axis).  The Jacobian must provide `to_csr`
+    (compiled generic operators and families with coefficient fields do)."""
+    from .multigrid import Multigrid
+    opt = optimizer_mod.Optimizer(name='multigrid', displayname='Multigrid')
+    problem.init_missing(state)
+    packed = problem.pack_state(state)
+    dhistory = defaultdict(list)
+    dom = problem.domain
+    mg = Multigrid(tuple(dom.shape), nvar=len(dom.fieldnames),
+                   nlevels=getattr(args, "nlvl", None),
+                   restriction=getattr(args, "restriction", "full"),
+                   dtype=packed.dtype, device=packed.device)
+    omega = getattr(args, "omega", 0.6)
+    iters = getattr(args, "linsolver_maxiter", None) or 50
+
+    def smoother(level, u, f):
+        return mg.smoother_jacobi(level, u, f, omega=omega, full=False)
+
+    for epoch in range(getattr(args, "epoch_start", 0), args.epochs + 1):
+        s = problem.unpack_state(packed)
+        dom.assign_active_state(state, s)
+        const, J = problem.linearize(state, epoch=epoch)
+        opt.last_loss = sum(torch.mean(c**2) for c in const)
+        opt.last_residual = [torch.mean(c**2)**0.5 for c in const]
+        if callback:
+            callback(packed, epoch, dhistory=dhistory, opt=opt)
+        if epoch == args.epochs:
+            break
+        opt.evals += 1
+        timer = Timer()
+        timer.push('linsolver')
+        m = J.to_csr()
+        rhs = -(m.t() @ torch.cat([c.reshape(-1) for c in const]))
+        mg.update_A(m.t().to_sparse_csr() @ m)
+        sol = torch.zeros_like(rhs)
+        for _ in range(iters):
+            sol = mg.step(sol, rhs, smoother,
+                          ndirect=getattr(args, "ndirect", 5),
+                          pre=getattr(args, "smooth_pre", 2),
+                          post=getattr(args, "smooth_post", 2))
+        timer.pop()
+        packed += sol
+    s = problem.unpack_state(packed)
+    dom.assign_active_state(state, s)
+    return packed
+
+
+def optimize_multigridop(args, problem, state, callback=None):
+    """util.py:509-617: Newton epochs whose normal equations
     J^T J d = -J^T r are solved by `linsolver_maxiter` (default 50) V-cycles
     of the multigrid on the GPU (stencil.MultigridOp: Galerkin coarsening of
     the J^T J stencils, damped Jacobi with `omega`, `smooth_pre` /
@@ -220,7 +274,8 @@ def optimize_multigrid(args, problem, state, callback=None):
     The Jacobian must provide its stencils (compiled generic operators and
     families with coefficient fields do)."""
     from .stencil import MultigridOp
-    opt = optimizer_mod.Optimizer(name='multigrid', displayname='Multigrid')
+    opt = optimizer_mod.Optimizer(name='multigridop',
+                                  displayname='MultigridOp')
     problem.init_missing(state)
     packed = problem.pack_state(state)
     dhistory = defaultdict(list)
@@ -289,7 +344,10 @@ def optimize_multigrid(args, problem, state, callback=None):
     return packed
 
 
-optimize_multigridop = optimize_multigrid
+# The reference's CuPy variants (util.py:498-506, 619-629); both forms
+# above already run on the fields' device.
+optimize_multigridcp = optimize_multigrid
+optimize_multigridopcp = optimize_multigridop
 
 
 def optimize(args, optname, problem, state, callback=None, **kwargs):

@@ -16,6 +16,9 @@ Fixtures
                         backend) on small odd grids: restriction and
                         interpolation operators, stencil products, Galerkin
                         coarsening, transposed products (see make_multigrid).
+  multigrid_csr_ref.npz outputs of the reference's CSR Multigrid class on SPD
+                        matrices: coarse matrices, block diagonals, V-cycle
+                        iterates, one Gauss-Seidel sweep (make_multigrid_csr).
   cavity_N128.npz       u, v, p fields of the reference's FP64 Newton cavity
                         solutions cases/cavity_stream/cavity_N128_Re{100,400}.
 """
@@ -116,6 +119,79 @@ def make_multigrid(ref):
     return out
 
 
+def make_multigrid_csr(ref):
+    """Evaluates the reference's CSR Multigrid (multigrid.py:70-339) with its
+    default transfer operators (g_reuse_multigridop = True) on SPD matrices
+    M^T M of random stencils: the coarse matrices of every level, the
+    block diagonals, and the iterates of a few V-cycles."""
+    sys.path.insert(0, os.path.join(ref, "code"))
+    import types
+    from functools import partial
+    sys.modules.setdefault("multigrid_plot", types.ModuleType("multigrid_plot"))
+    import scipy.sparse as sp
+    import multigrid as mg
+
+    mod = mg.ModNumpy(np, sp)
+    out = {}
+    rng = np.random.default_rng(7)
+
+    def stencil_csr(nw):
+        dim = len(nw)
+        shifts = [tuple(s) for s in np.array(np.meshgrid(
+            *[[-1, 0, 1]] * dim, indexing="ij")).reshape(dim, -1).T]
+        stf = {s: rng.uniform(-0.3, 0.3, nw) for s in shifts}
+        stf[(0, ) * dim] = stf[(0, ) * dim] + 2.0
+        return mg.SparseOperator(stf, np.array(nw), mod=mod,
+                                 dtype=np.float64).tocsr()
+
+    cases = [
+        # name, nw, nvar, restriction, ndirect, pre, post, cycles
+        ("p17", (17, 17), 1, "full", 5, 2, 2, 3),
+        ("h17", (17, 17), 1, "half", 5, 2, 2, 3),
+        ("i33", (33, ), 1, "injection", 5, 2, 2, 3),
+        ("v9", (9, 9), 2, "full", 3, 2, 2, 2),
+        ("d3", (5, 5, 9), 1, "full", 2, 1, 3, 2),
+    ]
+    for name, nw, nvar, restr, ndirect, pre, post, cycles in cases:
+        n = int(np.prod(nw))
+        B = sp.bmat([[stencil_csr(nw) for _ in range(nvar)]
+                     for _ in range(nvar)]).tocsr()
+        A = (B.T @ B).tocsr()
+        f = rng.standard_normal(n * nvar)
+        m = mg.Multigrid(np.array(nw), nvar=nvar, restriction=restr, mod=mod,
+                         dtype=np.float64)
+        m.update_A(A)
+        out["%s_nnw" % name] = np.array([list(v) for v in m.nnw])
+        out["%s_A0" % name] = A.toarray()
+        out["%s_f" % name] = f
+        for level in range(1, m.nlevels):
+            out["%s_A%d" % (name, level)] = m.AA[level].toarray()
+        for level in range(m.nlevels):
+            out["%s_D%d" % (name, level)] = np.array(
+                [[np.asarray(d) for d in row] for row in m.DD[level]])
+        u = np.zeros_like(f)
+        for it in range(cycles):
+            u = m.step(u.copy(), f, ndirect=ndirect, pre=pre, post=post,
+                       smoother=partial(m.smoother_jacobi, omega=0.7))
+            out["%s_u%d" % (name, it)] = u.copy()
+        if nvar == 1:
+            # update_A(compute_lower=True) raises NameError in the reference
+            # (multigrid.py:149 names an undefined `mod`); its intended
+            # lower-triangular parts are set directly.
+            m.LL = [sp.tril(a).tocsr() for a in m.AA]
+            v = m.smoother_gauss_seidel(0, f * 0.1, f, omega=0.9)
+            out["%s_gs" % name] = v.copy()
+    # The variant the reference's unit tests use (test_multigrid.py:4):
+    # transfer operators from node multi-indices, first axis fastest.
+    mg.g_reuse_multigridop = False
+    out["fortran_R_9x5"] = mg.Multigrid.get_R(np.array((9, 5)), mod=mod,
+                                              dtype=np.float64).toarray()
+    out["fortran_T_9x5"] = mg.Multigrid.get_T(np.array((9, 5)), mod=mod,
+                                              dtype=np.float64).toarray()
+    mg.g_reuse_multigridop = True
+    return out
+
+
 def make_cavity(ref):
     res = {}
     for re_ in (100, 400):
@@ -133,7 +209,8 @@ def main():
     ap.add_argument("--ref", default="/root/reference")
     ap.add_argument("--only", default=None)
     a = ap.parse_args()
-    todo = a.only.split(",") if a.only else ["wave", "multigrid", "cavity"]
+    todo = a.only.split(",") if a.only else ["wave", "multigrid", "multigrid_csr",
+                                                  "cavity"]
     if "wave" in todo:
         for name in ("fd_newton", "fd_lbfgsb"):
             with open(os.path.join(HERE, "wave_%s.json" % name), "w") as f:
@@ -141,6 +218,9 @@ def main():
     if "multigrid" in todo:
         np.savez_compressed(os.path.join(HERE, "multigrid_ref.npz"),
                             **make_multigrid(a.ref))
+    if "multigrid_csr" in todo:
+        np.savez_compressed(os.path.join(HERE, "multigrid_csr_ref.npz"),
+                            **make_multigrid_csr(a.ref))
     if "cavity" in todo:
         np.savez_compressed(os.path.join(HERE, "cavity_N128.npz"),
                             **make_cavity(a.ref))

@@ -472,7 +472,7 @@ def test_epoch_follows_the_evaluation(cuda):
 
 @pytest.mark.gpu
 def test_optimize_multigrid_on_compiled_operator(cuda):
-    """util.optimize_multigrid (util.py:382-493): Newton with V-cycles on the
+    """util.optimize_multigridop (util.py:509-617): Newton with V-cycles on the
     Galerkin J^T J stencils reaches the direct Newton solution of a
     screened-Poisson operator."""
     import argparse
@@ -499,7 +499,7 @@ def test_optimize_multigrid_on_compiled_operator(cuda):
                               linsolver_maxiter=30, ndirect=3, smooth_pre=2,
                               smooth_post=2)
     u = torch.zeros(dom.shape, dtype=torch.float64, device=cuda)
-    util.optimize_multigrid(args, pj, State(fields={"u": u}))
+    util.optimize_multigridop(args, pj, State(fields={"u": u}))
     assert _rel(u, ref) < 1e-8
 
 
