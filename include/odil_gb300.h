@@ -592,6 +592,38 @@ int odil_lincomb_f64(double* out, const double* x, const double* M,
                      int64_t ld, int k, const double* coef, int64_t n,
                      void* stream);
 
+/* ------------------------------------------------------------------------
+ * Multigrid decomposition of a field: the field is the sum over levels l of
+ * the level-l weights refined l times.
+ *
+ * Replaces MultigridDecomp.interp_node_field / interp_cell_field
+ * (multigrid.py:1220-1362, one level per call) as composed by
+ * weights_to_field (multigrid.py:1409-1426); the adjoint replaces the
+ * reverse-mode differentiation TensorFlow applies through them.
+ * `n` is a host array of `dim` (1..3) coarse sizes.  cell = 0 refines nodes,
+ * n -> 2n - 1 per axis (multilinear); cell = 1 refines cells, n -> 2n
+ * (weights 3/4, 1/4 over a halo of linearly extrapolated cells; n >= 2).
+ * ---------------------------------------------------------------------- */
+/* out = alpha * refine(in) + beta * add, on the fine grid; add may be NULL;
+ * out must not overlap in or add. */
+int odil_mgdecomp_refine_f32(int32_t dim, const int64_t* n, int32_t cell,
+                             const float* in, float* out, double alpha,
+                             const float* add, double beta, void* stream);
+int odil_mgdecomp_refine_f64(int32_t dim, const int64_t* n, int32_t cell,
+                             const double* in, double* out, double alpha,
+                             const double* add, double beta, void* stream);
+/* Adjoint: with a = refine^T g (coarse grid), gc = a and wc = alpha_c * a,
+ * and wf = beta_f * g on the fine grid; each of gc, wc, wf may be NULL (not
+ * all three); none may overlap g. */
+int odil_mgdecomp_refine_t_f32(int32_t dim, const int64_t* n, int32_t cell,
+                               const float* g, float* gc, float* wc,
+                               double alpha_c, float* wf, double beta_f,
+                               void* stream);
+int odil_mgdecomp_refine_t_f64(int32_t dim, const int64_t* n, int32_t cell,
+                               const double* g, double* gc, double* wc,
+                               double alpha_c, double* wf, double beta_f,
+                               void* stream);
+
 #ifdef __cplusplus
 }
 #endif

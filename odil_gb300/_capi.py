@@ -13,6 +13,7 @@ from . import _build
 
 ODIL_OK = 0
 ODIL_ERR_SHAPE = -1
+ODIL_ERR_ARG = -8
 _STATUS = {
     -1: "ODIL_ERR_SHAPE",
     -2: "ODIL_ERR_DTYPE",
@@ -244,6 +245,14 @@ SIGNATURES = {
                                  _P]),
     "odil_lincomb_f32": (_INT, [_P, _P, _P, _I64, _INT, _P, _I64, _P]),
     "odil_lincomb_f64": (_INT, [_P, _P, _P, _I64, _INT, _P, _I64, _P]),
+    "odil_mgdecomp_refine_f32": (_INT, [ctypes.c_int32, _P, ctypes.c_int32, _P,
+                                        _P, _D, _P, _D, _P]),
+    "odil_mgdecomp_refine_f64": (_INT, [ctypes.c_int32, _P, ctypes.c_int32, _P,
+                                        _P, _D, _P, _D, _P]),
+    "odil_mgdecomp_refine_t_f32": (_INT, [ctypes.c_int32, _P, ctypes.c_int32,
+                                          _P, _P, _P, _D, _P, _D, _P]),
+    "odil_mgdecomp_refine_t_f64": (_INT, [ctypes.c_int32, _P, ctypes.c_int32,
+                                          _P, _P, _P, _D, _P, _D, _P]),
 }
 
 _lib = None

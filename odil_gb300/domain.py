@@ -10,9 +10,9 @@ import numpy as np
 class Domain:
     """Cell-centred grid; same constructor arguments as util_op.py:17-35.
 
-    ``device`` (default "cuda") is where fields are created.  Multigrid
-    decomposition (``multigrid=True``) and neural-network weights are not part
-    of the GPU hot path and raise NotImplementedError.
+    ``device`` (default "cuda") is where fields are created.  Unknowns held
+    as a multigrid decomposition (``multigrid=True``) and neural-network
+    weights raise NotImplementedError.
     """
 
     def __init__(self,
@@ -37,8 +37,10 @@ class Domain:
             shape = tuple(int(s) for s in shape)
         if multigrid:
             raise NotImplementedError(
-                "multigrid decomposition of unknowns (util_op.py:61-95) is "
-                "not on the GPU hot path")
+                "multigrid decomposition of unknowns (util_op.py:61-95) needs "
+                "MultigridDecomp.check_nnw and field_to_weights, which the "
+                "reference does not define; the decomposition itself is "
+                "odil_gb300.multigrid.MultigridDecomp")
         if neuralnets:
             raise NotImplementedError(
                 "neural-network unknowns (util_op.py:354-429) are not on the "

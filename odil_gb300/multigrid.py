@@ -20,6 +20,7 @@ sizes; here both use (n - 1) // 2 + 1.  Its recursive call does not pass
 `pre` and `post` down (multigrid.py:327-329), which is kept.  The
 smoothers return a new vector rather than updating `u` in place.
 """
+import ctypes
 import itertools
 import warnings
 
@@ -28,11 +29,12 @@ import torch
 
 warnings.filterwarnings("ignore", message="Sparse CSR tensor support is in beta")
 
-from .stencil import MultigridOp, StencilOp
+from ._capi import call, ptr, stream_handle
+from .stencil import MultigridOp, StencilOp, _sfx
 
 SparseOperator = StencilOp
 
-__all__ = ["Multigrid", "MultigridOp", "SparseOperator"]
+__all__ = ["Multigrid", "MultigridDecomp", "MultigridOp", "SparseOperator"]
 
 
 def _flat(idx, nw):
@@ -232,3 +234,209 @@ class Multigrid:
         for _ in range(post):
             u = smoother(level, u, f)
         return u
+
+
+# -- multigrid decomposition of a field (multigrid.py:1217-1426) -------------
+
+
+def _sizes(shape):
+    arr = (ctypes.c_int64 * len(shape))(*[int(v) for v in shape])
+    return arr
+
+
+def _fine(shape, cell):
+    return tuple(2 * n if cell else 2 * n - 1 for n in shape)
+
+
+def _check(u, cell):
+    if not u.is_cuda:
+        raise ValueError("MultigridDecomp runs on CUDA tensors (libodil_gb300); "
+                         "got device %s" % u.device)
+    if u.dtype not in (torch.float32, torch.float64):
+        raise ValueError("MultigridDecomp supports float32 and float64")
+    if not 1 <= u.dim() <= 3:
+        raise NotImplementedError("MultigridDecomp supports 1 to 3 axes, got %d"
+                                  % u.dim())
+    if cell and min(u.shape) < 2:
+        raise ValueError("cell refinement needs at least 2 cells per axis")
+
+
+def _refine(u, cell, alpha=1.0, add=None, beta=0.0):
+    """alpha * (one level of refinement of u) + beta * add, on the device."""
+    u = u.contiguous()
+    out = torch.empty(_fine(u.shape, cell), dtype=u.dtype, device=u.device)
+    n = _sizes(u.shape)
+    call("odil_mgdecomp_refine_" + _sfx(u), u.dim(), n, int(cell), ptr(u),
+         ptr(out), float(alpha), ptr(None if add is None else add.contiguous()),
+         float(beta), stream_handle(u.device))
+    return out
+
+
+def _refine_t(g, coarse, cell, want_gc=True, wc_alpha=None, wf_beta=None):
+    """Adjoint of one refinement level: (refine^T g, wc_alpha * refine^T g,
+    wf_beta * g), each None when not asked for."""
+    g = g.contiguous()
+    mk = lambda shape: torch.empty(shape, dtype=g.dtype, device=g.device)  # noqa
+    gc = mk(coarse) if want_gc else None
+    wc = mk(coarse) if wc_alpha is not None else None
+    wf = mk(g.shape) if wf_beta is not None else None
+    call("odil_mgdecomp_refine_t_" + _sfx(g), len(coarse), _sizes(coarse),
+         int(cell), ptr(g), ptr(gc), ptr(wc),
+         float(wc_alpha if wc_alpha is not None else 0.0), ptr(wf),
+         float(wf_beta if wf_beta is not None else 0.0),
+         stream_handle(g.device))
+    return gc, wc, wf
+
+
+class _Refine(torch.autograd.Function):
+
+    @staticmethod
+    def forward(ctx, u, cell):
+        ctx.cell = cell
+        ctx.coarse = tuple(u.shape)
+        return _refine(u, cell)
+
+    @staticmethod
+    def backward(ctx, g):
+        gc, _, _ = _refine_t(g, ctx.coarse, ctx.cell)
+        return gc, None
+
+
+class _WeightsToField(torch.autograd.Function):
+    """weights_to_field as one autograd node: L refinement launches forward
+    (each fused with the scale and add of its level), L adjoint launches
+    backward (each fused with the scaled copies into the weights' gradient)."""
+
+    @staticmethod
+    def forward(ctx, uw, nnw, factors, cell):
+        ctx.nnw, ctx.factors, ctx.cell = nnw, factors, cell
+        levels = _split(uw, nnw)
+        L = len(nnw)
+        if L == 1:
+            return levels[0] * factors[0]
+        res = levels[L - 1]
+        alpha = factors[L - 1]
+        for lv in range(L - 2, -1, -1):
+            res = _refine(res, cell, alpha, levels[lv], factors[lv])
+            alpha = 1.0
+        return res
+
+    @staticmethod
+    def backward(ctx, g):
+        nnw, factors, cell = ctx.nnw, ctx.factors, ctx.cell
+        L = len(nnw)
+        if L == 1:
+            return (g * factors[0]).reshape(-1), None, None, None
+        parts = [None] * L
+        for lv in range(L - 1):
+            last = lv + 1 == L - 1
+            gc, wc, wf = _refine_t(g, nnw[lv + 1], cell, want_gc=not last,
+                                   wc_alpha=factors[L - 1] if last else None,
+                                   wf_beta=factors[lv])
+            parts[lv] = wf
+            if last:
+                parts[L - 1] = wc
+            g = gc
+        return torch.cat([p.reshape(-1) for p in parts]), None, None, None
+
+
+def _split(uw, nnw):
+    out, s = [], 0
+    for nw in nnw:
+        n = int(np.prod(nw))
+        out.append(uw[s:s + n].reshape(nw))
+        s += n
+    if s != uw.numel():
+        raise ValueError("weights have %d entries, levels %s need %d"
+                         % (uw.numel(), nnw, s))
+    return out
+
+
+def _method(method, dim, cell):
+    if method is None:
+        return
+    if method == "conv":
+        assert dim <= 3, "method={} requires dim=1,2,3".format(method)
+    elif method == "manual":
+        if dim > (2 if cell else 3):
+            raise NotImplementedError(
+                "Expected dim=1,2{}, got {:}".format("" if cell else ",3", dim))
+    elif method != "roll":
+        raise NotImplementedError("Unknown method=" + method)
+
+
+class MultigridDecomp:
+    """multigrid.py:1217-1426: a field as the sum of weights on levels
+    (finest first) refined to the finest grid.  Node levels refine
+    n -> 2n - 1 (multilinear), cell levels n -> 2n (weights 3/4, 1/4 with
+    linearly extrapolated halo cells).  Every refinement runs in
+    libodil_gb300 (mgdecomp.cu) on CUDA tensors and is differentiable
+    (the adjoint runs there too).  The reference's interpolation methods
+    ('conv', 'roll', 'manual') give one result; `method` is validated as
+    the reference does and otherwise ignored.  `mod` is accepted for
+    signature compatibility.  Up to 3 axes."""
+
+    @staticmethod
+    def interp_node_field(u, depth=1, mod=None, method=None):
+        return MultigridDecomp.interp_field(u, depth, mod, method, cell=False)
+
+    @staticmethod
+    def interp_cell_field(u, depth=1, mod=None, method=None):
+        return MultigridDecomp.interp_field(u, depth, mod, method, cell=True)
+
+    @staticmethod
+    def interp_field(u, depth=1, mod=None, method=None, cell=False):
+        if depth == 0:
+            return u
+        _method(method, u.dim(), cell)
+        _check(u, cell)
+        for _ in range(depth):
+            u = _Refine.apply(u, bool(cell))
+        return u
+
+    @staticmethod
+    def weights_to_fields(uw, nnw, mod=None, method=None, factors=None,
+                          cell=False):
+        nnw = _check_levels(nnw, cell)
+        factors = [1.0] * len(nnw) if factors is None else factors
+        return [MultigridDecomp.interp_field(u * float(f), i, mod, method,
+                                             cell)
+                for i, (u, f) in enumerate(zip(_split(uw, nnw), factors))]
+
+    @staticmethod
+    def get_weights_coarse_ones(nnw, dtype, mod=None, device="cuda"):
+        return torch.cat([torch.full((int(np.prod(nw)), ),
+                                     float(i == len(nnw) - 1), dtype=dtype,
+                                     device=device)
+                          for i, nw in enumerate(nnw)])
+
+    @staticmethod
+    def weights_to_field(uw, nnw, mod=None, method=None, factors=None,
+                         cell=False):
+        nnw = _check_levels(nnw, cell)
+        factors = [float(f) for f in
+                   ([1.0] * len(nnw) if factors is None else factors)]
+        if len(factors) != len(nnw):
+            raise ValueError("%d factors for %d levels" % (len(factors),
+                                                           len(nnw)))
+        _method(method, len(nnw[0]), cell)
+        _check(uw, False)
+        if uw.dim() != 1:
+            raise ValueError("weights must be a flat vector")
+        return _WeightsToField.apply(uw, nnw, factors, bool(cell))
+
+
+def _check_levels(nnw, cell):
+    """Level sizes, finest first; each level must refine onto the next
+    finer one exactly (the sum of weights_to_field is taken point by point)."""
+    nnw = [tuple(int(v) for v in nw) for nw in nnw]
+    if not nnw or any(len(nw) != len(nnw[0]) for nw in nnw):
+        raise ValueError("levels must be non-empty and of one rank: %s" % nnw)
+    if not 1 <= len(nnw[0]) <= 3:
+        raise NotImplementedError("MultigridDecomp supports 1 to 3 axes")
+    for lv in range(len(nnw) - 1):
+        if min(nnw[lv + 1]) < (2 if cell else 1) or \
+                _fine(nnw[lv + 1], cell) != nnw[lv]:
+            raise ValueError("level %d %s does not refine onto level %d %s"
+                             % (lv + 1, nnw[lv + 1], lv, nnw[lv]))
+    return nnw

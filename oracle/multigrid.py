@@ -279,3 +279,104 @@ class MultigridOp:
         for _ in range(post):
             u = smoother(level, u, f)
         return u
+
+
+# -- multigrid decomposition of a field (multigrid.py:1217-1426) -------------
+#
+# A field on the finest grid is the sum over levels l of the level-l weights
+# interpolated l times.  Node grids refine n -> 2n - 1 by multilinear
+# interpolation; cell grids refine n -> 2n with weights 3/4 and 1/4 per axis
+# after a halo of linearly extrapolated cells, ghost = 2 u[edge] - u[next],
+# taken on all axes at once (multigrid.py:1298-1302: 2 * symmetric pad -
+# reflect pad; a corner ghost is 2 u[0, 0] - u[1, 1]).
+
+
+def interp_node(u):
+    """One level of interp_node_field (multigrid.py:1220-1289): fine node 2i
+    takes u[i], fine node 2i + 1 the mean of u[i] and u[i + 1], per axis."""
+    u = np.asarray(u, np.float64)
+    for ax in range(u.ndim):
+        n = u.shape[ax]
+        shape = list(u.shape)
+        shape[ax] = 2 * n - 1
+        out = np.zeros(shape)
+        ev = [slice(None)] * u.ndim
+        od = [slice(None)] * u.ndim
+        ev[ax] = slice(0, None, 2)
+        od[ax] = slice(1, None, 2)
+        lo = [slice(None)] * u.ndim
+        hi = [slice(None)] * u.ndim
+        lo[ax] = slice(0, n - 1)
+        hi[ax] = slice(1, n)
+        out[tuple(ev)] = u
+        out[tuple(od)] = 0.5 * (u[tuple(lo)] + u[tuple(hi)])
+        u = out
+    return u
+
+
+def pad_extrap(u):
+    """The halo of interp_cell_field (multigrid.py:1298-1302): one ghost
+    cell per side on every axis, 2 * (symmetric pad) - (reflect pad)."""
+    u = np.asarray(u, np.float64)
+    return 2 * np.pad(u, 1, mode="symmetric") - np.pad(u, 1, mode="reflect")
+
+
+def interp_cell(u):
+    """One level of interp_cell_field (multigrid.py:1291-1362): fine cell 2k
+    takes 3/4 u[k] + 1/4 u[k - 1], fine cell 2k + 1 takes 3/4 u[k] + 1/4
+    u[k + 1], per axis, over the extrapolated halo."""
+    up = pad_extrap(u)
+    dim = up.ndim
+    n = [s - 2 for s in up.shape]
+    out = np.zeros([2 * v for v in n])
+    for par in itertools.product((0, 1), repeat=dim):
+        acc = 0.0
+        for nb in itertools.product((0, 1), repeat=dim):
+            w = 1.0
+            sel = []
+            for d in range(dim):
+                # neighbour offset -1 (par 0) or +1 (par 1) when nb[d] = 1
+                off = 0 if nb[d] == 0 else (-1 if par[d] == 0 else 1)
+                w *= 0.25 if nb[d] else 0.75
+                sel.append(slice(1 + off, 1 + off + n[d]))
+            acc = acc + w * up[tuple(sel)]
+        out[tuple(slice(p, None, 2) for p in par)] = acc
+    return out
+
+
+def interp_field(u, depth=1, cell=False):
+    """multigrid.py:1364-1375: `depth` levels of refinement."""
+    for _ in range(depth):
+        u = interp_cell(u) if cell else interp_node(u)
+    return np.asarray(u, np.float64)
+
+
+def _levels(uw, nnw, factors):
+    factors = [1.0] * len(nnw) if factors is None else factors
+    out, s = [], 0
+    for nw, f in zip(nnw, factors):
+        n = int(np.prod(nw))
+        out.append(np.asarray(uw[s:s + n], np.float64).reshape(nw) * f)
+        s += n
+    return out
+
+
+def weights_to_fields(uw, nnw, factors=None, cell=False):
+    """multigrid.py:1377-1394: level l interpolated l times, per level."""
+    return [interp_field(u, i, cell) for i, u in enumerate(
+        _levels(uw, nnw, factors))]
+
+
+def weights_to_field(uw, nnw, factors=None, cell=False):
+    """multigrid.py:1409-1426: from the coarsest level, refine and add."""
+    res = None
+    for u in reversed(_levels(uw, nnw, factors)):
+        res = u if res is None else interp_field(res, 1, cell) + u
+    return res
+
+
+def weights_coarse_ones(nnw):
+    """multigrid.py:1396-1407: zero weights except ones on the coarsest
+    level."""
+    return np.concatenate([np.full(int(np.prod(nw)), float(i == len(nnw) - 1))
+                           for i, nw in enumerate(nnw)])

@@ -19,6 +19,10 @@ Fixtures
   multigrid_csr_ref.npz outputs of the reference's CSR Multigrid class on SPD
                         matrices: coarse matrices, block diagonals, V-cycle
                         iterates, one Gauss-Seidel sweep (make_multigrid_csr).
+  mgdecomp_ref.npz      outputs of the reference's MultigridDecomp (node and
+                        cell interpolation, weights to fields) with every
+                        interpolation method, run on NumPy statements of
+                        the TensorFlow primitives it calls (make_mgdecomp).
   cavity_N128.npz       u, v, p fields of the reference's FP64 Newton cavity
                         solutions cases/cavity_stream/cavity_N128_Re{100,400}.
 """
@@ -192,6 +196,106 @@ def make_multigrid_csr(ref):
     return out
 
 
+class _TfPrimitives:
+    """NumPy statements of the TensorFlow primitives MultigridDecomp calls
+    (the reference's NumPy `mod` lacks them), from their documented
+    semantics: batch_to_space (the batch index is the C-order index of the
+    block offset, then crops), nn.conv_transpose with VALID padding and
+    stride s (out[s i + t] += w[t] x[i], no kernel flip), pad with REFLECT /
+    SYMMETRIC modes, concat."""
+
+    def __init__(self, base):
+        self._base = base
+        self.nn = self
+
+    def __getattr__(self, k):
+        return getattr(self._base, k)
+
+    @staticmethod
+    def batch_to_space(uu, block_shape, crops):
+        uu = np.asarray(uu)
+        dim = len(block_shape)
+        shape = uu.shape[1:1 + dim]
+        out = np.zeros(tuple(n * b for n, b in zip(shape, block_shape)))
+        for k, off in enumerate(np.ndindex(*block_shape)):
+            sel = tuple(slice(o, None, b) for o, b in zip(off, block_shape))
+            out[sel] = uu[k]
+        sel = tuple(slice(c0, out.shape[d] - c1)
+                    for d, (c0, c1) in enumerate(crops))
+        return out[sel][None]
+
+    @staticmethod
+    def conv_transpose(u, filters, output_shape, strides, padding):
+        assert padding == "VALID"
+        x = np.asarray(u)[0, ..., 0]
+        w = np.asarray(filters)[..., 0, 0]
+        out = np.zeros(tuple(output_shape[1:-1]))
+        for t in np.ndindex(*w.shape):
+            sel = tuple(slice(td, td + strides * (n - 1) + 1, strides)
+                        for td, n in zip(t, x.shape))
+            out[sel] += w[t] * x
+        return out[None, ..., None]
+
+    @staticmethod
+    def pad(u, paddings, mode="CONSTANT", constant_values=0):
+        if mode == "CONSTANT":
+            return np.pad(u, paddings, constant_values=constant_values)
+        return np.pad(u, paddings, mode={"REFLECT": "reflect",
+                                         "SYMMETRIC": "symmetric"}[mode])
+
+    @staticmethod
+    def concat(xs, axis):
+        return np.concatenate(xs, axis)
+
+
+def make_mgdecomp(ref):
+    """Evaluates the reference's MultigridDecomp (multigrid.py:1217-1426)
+    with every interpolation method it defines, on the NumPy statements of
+    the TensorFlow primitives above; the methods must agree."""
+    sys.path.insert(0, os.path.join(ref, "code"))
+    import types
+    sys.modules.setdefault("multigrid_plot", types.ModuleType("multigrid_plot"))
+    import scipy.sparse as sp
+    import multigrid as mg
+    D = mg.MultigridDecomp
+    mod = _TfPrimitives(mg.ModNumpy(np, sp))
+    rng = np.random.default_rng(17)
+    out = {}
+    for cell, shapes in ((False, [(5, ), (9, ), (5, 9), (3, 5, 5)]),
+                         (True, [(4, ), (6, ), (3, 5), (2, 3, 4)])):
+        kind = "cell" if cell else "node"
+        for shape in shapes:
+            u = rng.standard_normal(shape)
+            key = "%s_%s" % (kind, "x".join(map(str, shape)))
+            out[key + "_u"] = u
+            for depth in (1, 2):
+                methods = ["conv", "roll"]
+                if len(shape) <= (2 if cell else 3):
+                    methods.append("manual")
+                res = [D.interp_field(u, depth=depth, mod=mod, method=m,
+                                      cell=cell) for m in methods]
+                for m, r in zip(methods[1:], res[1:]):
+                    assert np.allclose(r, res[0], rtol=0, atol=1e-13), (key, m)
+                out["%s_d%d" % (key, depth)] = res[0]
+    # Weights on levels (finest first) to one field and to per-level fields.
+    for cell, nnw in ((False, [(9, 17), (5, 9), (3, 5)]),
+                      (True, [(8, 12), (4, 6), (2, 3)])):
+        kind = "cell" if cell else "node"
+        n = sum(int(np.prod(nw)) for nw in nnw)
+        uw = rng.standard_normal(n)
+        factors = [1.0, 0.5, 2.0]
+        out["w2f_%s_uw" % kind] = uw
+        out["w2f_%s_nnw" % kind] = np.array(nnw)
+        out["w2f_%s_field" % kind] = D.weights_to_field(
+            uw, nnw, mod, factors=factors, cell=cell)
+        for i, f in enumerate(D.weights_to_fields(uw, nnw, mod, factors=factors,
+                                                  cell=cell)):
+            out["w2f_%s_fields%d" % (kind, i)] = f
+        out["w2f_%s_ones" % kind] = D.get_weights_coarse_ones(
+            nnw, np.float64, mod)
+    return out
+
+
 def make_cavity(ref):
     res = {}
     for re_ in (100, 400):
@@ -210,7 +314,7 @@ def main():
     ap.add_argument("--only", default=None)
     a = ap.parse_args()
     todo = a.only.split(",") if a.only else ["wave", "multigrid", "multigrid_csr",
-                                                  "cavity"]
+                                                  "mgdecomp", "cavity"]
     if "wave" in todo:
         for name in ("fd_newton", "fd_lbfgsb"):
             with open(os.path.join(HERE, "wave_%s.json" % name), "w") as f:
@@ -221,6 +325,9 @@ def main():
     if "multigrid_csr" in todo:
         np.savez_compressed(os.path.join(HERE, "multigrid_csr_ref.npz"),
                             **make_multigrid_csr(a.ref))
+    if "mgdecomp" in todo:
+        np.savez_compressed(os.path.join(HERE, "mgdecomp_ref.npz"),
+                            **make_mgdecomp(a.ref))
     if "cavity" in todo:
         np.savez_compressed(os.path.join(HERE, "cavity_N128.npz"),
                             **make_cavity(a.ref))

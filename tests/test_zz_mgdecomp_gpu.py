@@ -1,0 +1,83 @@
+"""The multigrid decomposition kernels (mgdecomp.cu) through
+odil_gb300.multigrid.MultigridDecomp on the GPU: refinement of node and
+cell grids, weights to field(s), against the reference's MultigridDecomp
+outputs (tests/golden/mgdecomp_ref.npz), and the adjoint kernels against
+finite differences (torch.autograd.gradcheck).
+
+Collected near the end on purpose: the same per-point arithmetic is checked
+on the CPU by a host build of mgdecomp.cuh (test_mgdecomp_cpu_emulation.py),
+so a stop at the first failure here has already run the parity tests of the
+solver path."""
+import os
+
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+G = np.load(os.path.join(os.path.dirname(__file__), "golden",
+                         "mgdecomp_ref.npz"))
+KEYS = ["node_5", "node_9", "node_5x9", "node_3x5x5", "cell_4", "cell_6",
+        "cell_3x5", "cell_2x3x4"]
+
+
+@pytest.mark.parametrize("key", KEYS)
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+def test_interp_matches_reference(cuda, key, dtype):
+    from odil_gb300.multigrid import MultigridDecomp as D
+    cell = key.startswith("cell")
+    u = torch.as_tensor(G[key + "_u"], dtype=dtype, device=cuda)
+    tol = 1e-13 if dtype == torch.float64 else 3e-6
+    for depth in (1, 2):
+        r = D.interp_field(u, depth, cell=cell)
+        np.testing.assert_allclose(r.double().cpu().numpy(),
+                                   G["%s_d%d" % (key, depth)], rtol=tol,
+                                   atol=tol)
+    fn = D.interp_cell_field if cell else D.interp_node_field
+    np.testing.assert_allclose(fn(u, 1, method="roll").double().cpu().numpy(),
+                               G[key + "_d1"], rtol=tol, atol=tol)
+
+
+@pytest.mark.parametrize("kind", ["node", "cell"])
+def test_weights_to_field_matches_reference(cuda, kind):
+    from odil_gb300.multigrid import MultigridDecomp as D
+    cell = kind == "cell"
+    uw = torch.as_tensor(G["w2f_%s_uw" % kind], device=cuda)
+    nnw = [tuple(v) for v in G["w2f_%s_nnw" % kind]]
+    factors = [1.0, 0.5, 2.0]
+    f = D.weights_to_field(uw, nnw, factors=factors, cell=cell)
+    np.testing.assert_allclose(f.cpu().numpy(), G["w2f_%s_field" % kind],
+                               rtol=1e-13, atol=1e-13)
+    for i, fi in enumerate(D.weights_to_fields(uw, nnw, factors=factors,
+                                               cell=cell)):
+        np.testing.assert_allclose(fi.cpu().numpy(),
+                                   G["w2f_%s_fields%d" % (kind, i)],
+                                   rtol=1e-13, atol=1e-13)
+    ones = D.get_weights_coarse_ones(nnw, torch.float64, device=cuda)
+    np.testing.assert_array_equal(ones.cpu().numpy(), G["w2f_%s_ones" % kind])
+
+
+@pytest.mark.parametrize("shape,cell", [((5, ), False), ((3, 4), True),
+                                        ((2, 3, 2), True), ((3, 2, 3), False)])
+def test_interp_gradient(cuda, shape, cell):
+    from odil_gb300.multigrid import MultigridDecomp as D
+    u = torch.randn(shape, dtype=torch.float64, device=cuda,
+                    generator=torch.Generator(cuda).manual_seed(1),
+                    requires_grad=True)
+    assert torch.autograd.gradcheck(
+        lambda x: D.interp_field(x, 2, cell=cell), (u, ))
+
+
+@pytest.mark.parametrize("cell", [False, True])
+def test_weights_to_field_gradient(cuda, cell):
+    from odil_gb300.multigrid import MultigridDecomp as D
+    nnw = [(8, 4), (4, 2)] if cell else [(9, 5), (5, 3), (3, 2)]
+    n = sum(int(np.prod(v)) for v in nnw)
+    uw = torch.randn(n, dtype=torch.float64, device=cuda,
+                     generator=torch.Generator(cuda).manual_seed(2),
+                     requires_grad=True)
+    factors = [1.5, -0.5, 2.0][:len(nnw)]
+    assert torch.autograd.gradcheck(
+        lambda x: D.weights_to_field(x, nnw, factors=factors, cell=cell),
+        (uw, ))
