@@ -22,12 +22,9 @@ smoothers return a new vector rather than updating `u` in place.
 """
 import ctypes
 import itertools
-import warnings
 
 import numpy as np
 import torch
-
-warnings.filterwarnings("ignore", message="Sparse CSR tensor support is in beta")
 
 from ._capi import call, ptr, stream_handle
 from .stencil import MultigridOp, StencilOp, _sfx
@@ -212,11 +209,20 @@ class Multigrid:
         x = torch.triangular_solve(b, L, upper=False).solution.reshape(-1)
         return u + (x - u) * omega
 
+    DIRECT_MAX = 16384  # unknowns of a level the direct solve accepts
+
     def smoother_direct(self, level, u, f):
         """multigrid.py:307-310: the direct solve of the level (a dense LU
-        of the assembled matrix, formed once per update_A)."""
+        of the assembled matrix, formed once per update_A).  The reference's
+        spsolve has no size limit; a dense factor here is kept below
+        DIRECT_MAX unknowns (2 GiB in FP64)."""
         lu = self._inv.get(level)
         if lu is None:
+            n = self.AA[level].shape[0]
+            if n > self.DIRECT_MAX:
+                raise ValueError(
+                    "direct solve of %d unknowns on level %d; use more levels "
+                    "or a smaller ndirect" % (n, level))
             lu = self._inv[level] = torch.linalg.lu_factor(
                 self.AA[level].to_dense())
         return torch.linalg.lu_solve(*lu, f.reshape(-1, 1)).reshape(-1)
