@@ -24,7 +24,15 @@ def checkpoint_load(state, path, fields_to_load=None, weights_to_load=None,
     """util_op.py:992-1014; fields go to `device` as torch tensors when given
     (numpy arrays otherwise, converted by Problem.init_missing)."""
     with open(path, "rb") as f:
-        s = pickle.load(f)
+        try:
+            s = pickle.load(f)
+        except (pickle.UnpicklingError, EOFError, AttributeError,
+                ImportError, IndexError, TypeError, ValueError) as e:
+            raise ValueError("corrupt checkpoint %s: %s: %s"
+                             % (path, type(e).__name__, e)) from e
+    if not isinstance(s, dict):
+        raise ValueError("checkpoint %s holds %s, not the {'fields', "
+                         "'weights'} dict" % (path, type(s).__name__))
     fields = s.get("fields", None)
     if fields is not None:
         for k in (fields.keys() if fields_to_load is None else fields_to_load):

@@ -67,6 +67,28 @@ def test_checkpoint_layout_roundtrip(tmp_path):
                         skip_missing=False)
 
 
+def test_corrupt_checkpoint_is_reported(tmp_path):
+    """Failure injection on the host: a truncated checkpoint, a file that is
+    not a pickle, and a pickle of the wrong layout raise ValueError naming
+    the file; the state is left untouched."""
+    from odil_gb300.checkpoint import checkpoint_save, checkpoint_load
+    path = str(tmp_path / "state.pickle")
+    checkpoint_save(State(fields={"u": torch.ones(64, 64)}), path)
+    data = open(path, "rb").read()
+    bad = []
+    for i, blob in enumerate([data[:len(data) // 2], b"not a pickle",
+                              pickle.dumps([1, 2, 3])]):
+        q = str(tmp_path / ("bad%d.pickle" % i))
+        with open(q, "wb") as f:
+            f.write(blob)
+        bad.append(q)
+    for q in bad:
+        st = State(fields={"u": torch.zeros(2)})
+        with pytest.raises(ValueError, match="checkpoint"):
+            checkpoint_load(st, q)
+        assert list(st.fields) == ["u"] and float(st.fields["u"].sum()) == 0
+
+
 def test_reference_cavity_pickle_loads(tmp_path):
     """The reference's checkpoint layout (fields u, v, p, psi) loads as a
     state; here from the committed fixture rewritten in that layout."""

@@ -81,3 +81,40 @@ def test_weights_to_field_gradient(cuda, cell):
     assert torch.autograd.gradcheck(
         lambda x: D.weights_to_field(x, nnw, factors=factors, cell=cell),
         (uw, ))
+
+
+@pytest.mark.parametrize("shape,cell", [((7, ), False), ((3, 5), True),
+                                        ((2, 3, 4), True), ((3, 3, 2), False)])
+def test_guard_bands_untouched(cuda, shape, cell):
+    """Canary bands of 4096 sentinels before and after every output of both
+    entry points (called through the C ABI on views into larger buffers)
+    stay intact, and every output element is written."""
+    import ctypes
+    from odil_gb300 import _capi
+    lib = _capi.load()
+    G, sentinel = 4096, -12345.5
+    fine = tuple(2 * v if cell else 2 * v - 1 for v in shape)
+    nc, nf = int(np.prod(shape)), int(np.prod(fine))
+    n = (ctypes.c_int64 * len(shape))(*shape)
+    st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    u = torch.randn(nc, dtype=torch.float64, device=cuda)
+    g = torch.randn(nf, dtype=torch.float64, device=cuda)
+    bufs = [torch.full((nf + 2 * G, ), sentinel, dtype=torch.float64,
+                       device=cuda) for _ in range(2)] + \
+        [torch.full((nc + 2 * G, ), sentinel, dtype=torch.float64,
+                    device=cuda) for _ in range(2)]
+    out, wf, gc, wc = [b[G:-G] for b in bufs]
+    assert lib.odil_mgdecomp_refine_f64(len(shape), n, int(cell),
+                                        u.data_ptr(), out.data_ptr(), 1.0,
+                                        None, 0.0, st) == 0
+    assert lib.odil_mgdecomp_refine_t_f64(len(shape), n, int(cell),
+                                          g.data_ptr(), gc.data_ptr(),
+                                          wc.data_ptr(), 2.0, wf.data_ptr(),
+                                          3.0, st) == 0
+    torch.cuda.synchronize()
+    for b in bufs:
+        assert bool(torch.all(b[:G] == sentinel))
+        assert bool(torch.all(b[-G:] == sentinel))
+        assert not bool(torch.any(b[G:-G] == sentinel))
+    torch.testing.assert_close(wf, 3.0 * g, rtol=0, atol=0)
+    torch.testing.assert_close(wc, 2.0 * gc, rtol=1e-15, atol=0)
