@@ -1,7 +1,8 @@
 """The allocation-free fused loss entry point, called through the C ABI.
 
-Collected last on purpose: it shares one device array across calls, so a
-stop at the first failure has already run every other test.  Callers that
+Collected near the end on purpose: it shares one device array across
+calls, so a stop at the first failure has already run the other parity
+tests (only the GPU runs of code also checked on the CPU come after it).  Callers that
 cannot allocate device memory use this variant; it must agree with the
 workspace-taking entry point on consecutive calls (the array keeps the
 previous call's contents, which must not leak into the next result)."""

@@ -1,13 +1,13 @@
-"""The multigrid decomposition kernels (mgdecomp.cu) through
-odil_gb300.multigrid.MultigridDecomp on the GPU: refinement of node and
-cell grids, weights to field(s), against the reference's MultigridDecomp
-outputs (tests/golden/mgdecomp_ref.npz), and the adjoint kernels against
-finite differences (torch.autograd.gradcheck).
+"""GPU tests of the multigrid decomposition kernels (mgdecomp.cu) through
+odil_gb300.multigrid.MultigridDecomp: refinement of node and cell grids,
+weights to field(s), against the reference's MultigridDecomp outputs
+(tests/golden/mgdecomp_ref.npz), the adjoint kernels against finite
+differences (torch.autograd.gradcheck), guard bands; and of the CSR
+multigrid and the iterative linear solvers on CUDA tensors.
 
-Collected near the end on purpose: the same per-point arithmetic is checked
-on the CPU by a host build of mgdecomp.cuh (test_mgdecomp_cpu_emulation.py),
-so a stop at the first failure here has already run the parity tests of the
-solver path."""
+Collected last on purpose: all of this is checked on the CPU as well (a
+host build of mgdecomp.cuh, the same torch code on CPU tensors), so a stop
+at the first failure here has already run every other GPU test."""
 import os
 
 import numpy as np
@@ -118,3 +118,51 @@ def test_guard_bands_untouched(cuda, shape, cell):
         assert not bool(torch.any(b[G:-G] == sentinel))
     torch.testing.assert_close(wf, 3.0 * g, rtol=0, atol=0)
     torch.testing.assert_close(wc, 2.0 * gc, rtol=1e-15, atol=0)
+
+
+@pytest.mark.parametrize("name", ["p17", "v9", "d3"])
+def test_multigrid_csr_on_cuda(cuda, name):
+    """The CSR multigrid on cuSPARSE matches the reference's outputs
+    (tests/golden/multigrid_csr_ref.npz) as on the CPU."""
+    import sys
+    sys.path.insert(0, os.path.dirname(__file__))
+    import test_multigrid_csr as T
+    T._run(name, cuda, gauss_seidel=False)
+
+
+def test_iterative_solvers_on_cuda(cuda):
+    """bicgstab and lsqr on CUDA tensors equal their CPU runs (which match
+    scipy), and the multigrid-preconditioned CG reaches the direct
+    solution."""
+    import argparse
+    import sys
+    sys.path.insert(0, os.path.dirname(__file__))
+    import test_linsolver_host as L
+    from odil_gb300 import linsolver
+    rng = np.random.default_rng(0)
+    J = L._screened(6, rng) + 0.3 * rng.standard_normal((36, 36))
+    rhs = rng.standard_normal(36)
+
+    class CudaJ(L.DenseJacobian):
+        def __init__(self, M, grid=None):
+            super().__init__(M, grid)
+            self.M = self.M.to(cuda)
+
+    xs = []
+    for dev, Jw in (("cpu", L.DenseJacobian(J)), (cuda, CudaJ(J))):
+        r = torch.as_tensor(rhs, device=dev)
+        xs.append((linsolver.bicgstab(Jw, r, 1e-8, 15, 0.1, 0.2).cpu(),
+                   linsolver.lsqr(Jw, r, 0.3, 1e-10, 1e-10, iter_lim=8).cpu()))
+    torch.testing.assert_close(xs[0][0], xs[1][0], rtol=1e-9, atol=1e-11)
+    torch.testing.assert_close(xs[0][1], xs[1][1], rtol=1e-9, atol=1e-11)
+    n = 17
+    Jp = L._screened(n, np.random.default_rng(2))
+    b = np.random.default_rng(3).standard_normal(n * n)
+    args = argparse.Namespace(linsolver_tol=1e-10, linsolver_maxiter=60,
+                              nlvl=None, restriction="full", omega=0.6,
+                              ndirect=3, smooth_pre=2, smooth_post=2,
+                              beta=0.0, betadiag=0.0)
+    x = linsolver.solve(CudaJ(Jp, (n, n)), torch.as_tensor(b, device=cuda),
+                        args, {}, "multigrid")
+    np.testing.assert_allclose(x.cpu().numpy(), np.linalg.solve(Jp, b),
+                               rtol=1e-8, atol=1e-9)
