@@ -9,8 +9,16 @@ from .domain import Domain, State
 from .problem import Context, Problem
 from .wave import WaveOperator, WaveKernels, extrap_quadh
 from ._capi import OdilError
+# The names of the reference's facade module (odil.py): the solver modules,
+# History and MultigridDecomp.
+from . import history, linsolver, optimizer, util
+from .history import History
+from .multigrid import MultigridDecomp
+
+util_history = history
 
 __all__ = [
     "Domain", "State", "Context", "Problem", "WaveOperator", "WaveKernels",
-    "extrap_quadh", "OdilError"
+    "extrap_quadh", "OdilError", "History", "MultigridDecomp", "util",
+    "linsolver", "optimizer", "history", "util_history"
 ]
