@@ -597,25 +597,6 @@ def test_roll_of_traced_expressions():
     jit.compile_source(J.code)
 
 
-@pytest.mark.gpu
-def test_roll_compiled_matches_torch_path(cuda):
-    """The compiled form of an operator that rolls traced expressions (the
-    wrapped index and array reads of the generated code) against the
-    op-by-op torch path."""
-    from odil_gb300.domain import State
-    from odil_gb300.problem import Problem
-    dom = _dom((9, 7), ("x", "y"), cuda, ["u"])
-    pj, pt = Problem(_op_roll, dom), Problem(_op_roll, dom, jit=False)
-    assert pj.jit is not None
-    st = State(fields={"u": torch.as_tensor(np.random.default_rng(4).uniform(
-        -1, 1, dom.shape), device=cuda)})
-    assert _rel(pj.eval_operator(st)[0], pt.eval_operator(st)[0]) < 1e-12
-    lj, gj, _, _ = pj.eval_loss_grad(st)
-    lt, gt, _, _ = pt.eval_loss_grad(st)
-    assert abs(lj.item() - lt.item()) <= 1e-12 * lt.item()
-    assert _rel(gj["u"], gt["u"]) < 1e-11
-
-
 @pytest.mark.parametrize("extras", [False, True])
 def test_ns_generic_form_matches_oracle(extras):
     """NsCavityOperator's op-by-op form (ns_steady.py:142-433) equals the
@@ -654,33 +635,6 @@ def test_ns_generic_form_matches_oracle(extras):
         assert np.allclose(ev, b, rtol=1e-12, atol=1e-12 * np.abs(b).max())
     if not extras:
         jit.compile_source(jit.JitOperator(op, dom).code)
-
-
-@pytest.mark.gpu
-def test_ns_compiled_matches_torch_path(cuda):
-    """The NS cavity operator's generic form, compiled, against its
-    op-by-op torch path: residual, loss and gradient of all three fields."""
-    from odil_gb300.domain import Domain, State
-    from odil_gb300.ns import NsCavityOperator
-    from odil_gb300.problem import Problem
-    n = 16
-    op = NsCavityOperator(400.0, kreg=1e-3)
-    dom = Domain(ndim=2, shape=(n, n), lower=(0, 0), upper=(1, 1),
-                 varnames=("x", "y"), fieldnames=["u", "v", "p"],
-                 device=cuda)
-    generic = lambda mod, ctx: op(mod, ctx)  # noqa: E731
-    pj, pt = Problem(generic, dom), Problem(generic, dom, jit=False)
-    assert pj.jit is not None
-    rng = np.random.default_rng(6)
-    st = State(fields={k: torch.as_tensor(rng.uniform(-1, 1, (n, n)),
-                                          device=cuda) for k in "uvp"})
-    for a, b in zip(pj.eval_operator(st), pt.eval_operator(st)):
-        assert _rel(a, b) < 1e-11
-    lj, gj, _, _ = pj.eval_loss_grad(st)
-    lt, gt, _, _ = pt.eval_loss_grad(st)
-    assert abs(lj.item() - lt.item()) <= 1e-11 * lt.item()
-    for k in "uvp":
-        assert _rel(gj[k], gt[k]) < 1e-10, k
 
 
 def test_unforeseen_tracing_error_falls_back():

@@ -1,20 +1,30 @@
-"""GPU tests of the multigrid decomposition kernels (mgdecomp.cu) through
-odil_gb300.multigrid.MultigridDecomp: refinement of node and cell grids,
-weights to field(s), against the reference's MultigridDecomp outputs
-(tests/golden/mgdecomp_ref.npz), the adjoint kernels against finite
-differences (torch.autograd.gradcheck), guard bands; and of the CSR
-multigrid and the iterative linear solvers on CUDA tensors.
+"""GPU runs of code whose arithmetic is also checked on the CPU.
 
-Collected last on purpose: all of this is checked on the CPU as well (a
-host build of mgdecomp.cuh, the same torch code on CPU tensors), so a stop
-at the first failure here has already run every other GPU test."""
+* the multigrid decomposition kernels (mgdecomp.cu) through
+  odil_gb300.multigrid.MultigridDecomp: refinement of node and cell grids,
+  weights to field(s), against the reference's MultigridDecomp outputs
+  (tests/golden/mgdecomp_ref.npz), the adjoint kernels against finite
+  differences (torch.autograd.gradcheck), guard bands (CPU check: a host
+  build of mgdecomp.cuh);
+* the CSR multigrid and the iterative linear solvers on CUDA tensors (CPU
+  check: the same torch code on CPU tensors);
+* compiled generic operators that roll traced expressions, and the NS
+  cavity's generic form compiled (CPU check: the generated kernels built
+  with g++, test_jit_cpu_emulation.py).
+
+Collected last on purpose: a stop at the first failure here has already run
+every other GPU test."""
 import os
+import sys
 
 import numpy as np
 import pytest
 import torch
 
 pytestmark = pytest.mark.gpu
+
+sys.path.insert(0, os.path.dirname(__file__))
+from test_jit import _dom, _op_roll, _rel  # noqa: E402
 
 G = np.load(os.path.join(os.path.dirname(__file__), "golden",
                          "mgdecomp_ref.npz"))
@@ -166,3 +176,49 @@ def test_iterative_solvers_on_cuda(cuda):
                         args, {}, "multigrid")
     np.testing.assert_allclose(x.cpu().numpy(), np.linalg.solve(Jp, b),
                                rtol=1e-8, atol=1e-9)
+
+
+@pytest.mark.gpu
+def test_roll_compiled_matches_torch_path(cuda):
+    """The compiled form of an operator that rolls traced expressions (the
+    wrapped index and array reads of the generated code) against the
+    op-by-op torch path."""
+    from odil_gb300.domain import State
+    from odil_gb300.problem import Problem
+    dom = _dom((9, 7), ("x", "y"), cuda, ["u"])
+    pj, pt = Problem(_op_roll, dom), Problem(_op_roll, dom, jit=False)
+    assert pj.jit is not None
+    st = State(fields={"u": torch.as_tensor(np.random.default_rng(4).uniform(
+        -1, 1, dom.shape), device=cuda)})
+    assert _rel(pj.eval_operator(st)[0], pt.eval_operator(st)[0]) < 1e-12
+    lj, gj, _, _ = pj.eval_loss_grad(st)
+    lt, gt, _, _ = pt.eval_loss_grad(st)
+    assert abs(lj.item() - lt.item()) <= 1e-12 * lt.item()
+    assert _rel(gj["u"], gt["u"]) < 1e-11
+
+
+@pytest.mark.gpu
+def test_ns_compiled_matches_torch_path(cuda):
+    """The NS cavity operator's generic form, compiled, against its
+    op-by-op torch path: residual, loss and gradient of all three fields."""
+    from odil_gb300.domain import Domain, State
+    from odil_gb300.ns import NsCavityOperator
+    from odil_gb300.problem import Problem
+    n = 16
+    op = NsCavityOperator(400.0, kreg=1e-3)
+    dom = Domain(ndim=2, shape=(n, n), lower=(0, 0), upper=(1, 1),
+                 varnames=("x", "y"), fieldnames=["u", "v", "p"],
+                 device=cuda)
+    generic = lambda mod, ctx: op(mod, ctx)  # noqa: E731
+    pj, pt = Problem(generic, dom), Problem(generic, dom, jit=False)
+    assert pj.jit is not None
+    rng = np.random.default_rng(6)
+    st = State(fields={k: torch.as_tensor(rng.uniform(-1, 1, (n, n)),
+                                          device=cuda) for k in "uvp"})
+    for a, b in zip(pj.eval_operator(st), pt.eval_operator(st)):
+        assert _rel(a, b) < 1e-11
+    lj, gj, _, _ = pj.eval_loss_grad(st)
+    lt, gt, _, _ = pt.eval_loss_grad(st)
+    assert abs(lj.item() - lt.item()) <= 1e-11 * lt.item()
+    for k in "uvp":
+        assert _rel(gj[k], gt[k]) < 1e-10, k
