@@ -360,7 +360,7 @@ def optimize(args, optname, problem, state, callback=None, **kwargs):
 
 
 def add_arguments(parser):
-    """The solver flags of util.py:109-239 that the GPU engine uses."""
+    """The flags of util.py:109-239 (solver flags, then driver flags)."""
     parser.add_argument('--epochs', type=int, default=None,
                         help="Maximum epochs")
     parser.add_argument('--epoch_start', type=int, default=0,
@@ -385,3 +385,45 @@ def add_arguments(parser):
                         help="Jacobi: weight of the new samples")
     parser.add_argument('--jac_epsilon', type=float, default=1e-8,
                         help="Jacobi: added to the diagonal")
+    # Driver flags of util.py:109-239, same names, types and defaults, so
+    # that a driver's command line parses unchanged.  Their consumers
+    # (plots, frames, reports, checkpoint files) are the driver's own;
+    # --multigrid and --nn_initializer select unknowns this engine does not
+    # hold (Domain raises for them).
+    parser.add_argument('--every_factor', type=int, default=1,
+                        help="Multiplier for all *_every options")
+    parser.add_argument('--plot_every', type=int, default=5,
+                        help="Epochs between plots")
+    parser.add_argument('--report_every', type=int, default=10,
+                        help="Epochs between reports to stdout")
+    parser.add_argument('--history_every', type=int, default=1,
+                        help="Epochs between entries of training history")
+    parser.add_argument('--checkpoint_every', type=int, default=5,
+                        help="Epochs between checkpoints")
+    parser.add_argument('--frames', type=int, default=10,
+                        help="Frames to plot. Zero disables first frame.")
+    parser.add_argument('--plot_title', type=int, default=0,
+                        help="Enable title in plots")
+    parser.add_argument('--plotext', type=str, default='pdf',
+                        help="Extension of plots")
+    parser.add_argument('--history_full', type=int, default=0,
+                        help="Number of epochs to write history at every "
+                        "point")
+    parser.add_argument('--montage', type=int, default=1,
+                        help="Run montage after plotting")
+    parser.add_argument('--frame_start', type=int, default=0,
+                        help="Initial value of frame")
+    parser.add_argument('--checkpoint', type=str,
+                        help="Continue from checkpoint in state_*.pickle")
+    parser.add_argument('--checkpoint_train', type=str,
+                        help="Continue from history in state_*_train.pickle")
+    parser.add_argument('--multigrid', type=int, default=0,
+                        help="Use multigrid decomposition")
+    parser.add_argument('--mg_interp', type=str, default='conv',
+                        choices=['roll', 'conv', 'manual'],
+                        help="Multigrid interpolation method")
+    parser.add_argument('--dump_data', type=int, default=1,
+                        help="Dump data_*.pickle with every plot")
+    parser.add_argument('--nn_initializer', type=str, default='legacy',
+                        choices=['legacy', 'glorot', 'lecun', 'he'],
+                        help="Initializer for weights of neural networks")

@@ -115,6 +115,14 @@ def test_argparse_flags_match_reference_names():
                        "--precision", "mixed", "--epochs", "3"])
     assert a.optimizer == "lbfgsb" and a.nlvl == 4 and a.bfgs_m == 20
     assert a.smooth_pre == 2 and a.ndirect == 3 and a.restriction == "full"
+    # the driver flags of util.py:109-239 parse with the reference defaults
+    b = ap.parse_args(["--frames", "3", "--checkpoint", "s.pickle",
+                       "--mg_interp", "roll", "--history_full", "2"])
+    assert (b.frames, b.checkpoint, b.mg_interp, b.history_full) == \
+        (3, "s.pickle", "roll", 2)
+    assert (b.report_every, b.plot_every, b.checkpoint_every,
+            b.history_every, b.every_factor, b.plotext, b.multigrid,
+            b.nn_initializer) == (10, 5, 5, 1, 1, "pdf", 0, "legacy")
 
 
 def test_unknown_names_raise_value_error():
