@@ -211,15 +211,22 @@ def optimize_jacobi(args, problem, state, callback=None):
     return packed
 
 
-def optimize_multigrid(args, problem, state, callback=None):
-    """util.py:382-495 (without the per-level `datalevels` problems): Newton
-    epochs whose normal equations J^T J d = -J^T r, assembled as sparse CSR
-    matrices on the fields' device, are solved by `linsolver_maxiter`
-    (default 50) V-cycles of the CSR multigrid (multigrid.Multigrid: R A T
-    coarsening, damped Jacobi on the diagonal blocks with `omega`,
-    `smooth_pre` / `smooth_post` sweeps on the finest level, direct solve
-    below `ndirect` nodes per axis).  The Jacobian must provide `to_csr`
-    (compiled generic operators and families with coefficient fields do)."""
+def optimize_multigrid(args, problem, state, callback=None, datalevels=None):
+    """util.py:382-495: Newton epochs whose normal equations
+    J^T J d = -J^T r, assembled as sparse CSR matrices on the fields' device,
+    are solved by `linsolver_maxiter` (default 50) V-cycles of the CSR
+    multigrid (multigrid.Multigrid: R A T coarsening, damped Jacobi on the
+    diagonal blocks with `omega`, `smooth_pre` / `smooth_post` sweeps on the
+    finest level, direct solve below `ndirect` nodes per axis).  The
+    Jacobian must provide `to_csr` (compiled generic operators and families
+    with coefficient fields do).
+
+    With `datalevels` (one object per multigrid level with `.problem` and
+    `.state`, level 0 the given problem), the matrix of every level is the
+    J^T J of that level's own problem, linearised at the previous level's
+    fields restricted by the level's single-field restriction
+    (util.py:414-441), instead of R A T.  `opt.last_residual` is the finest
+    level's (the reference keeps the coarsest level's)."""
     from .multigrid import Multigrid
     opt = optimizer_mod.Optimizer(name='multigrid', displayname='Multigrid')
     problem.init_missing(state)
@@ -251,7 +258,23 @@ def optimize_multigrid(args, problem, state, callback=None):
         timer.push('linsolver')
         m = J.to_csr()
         rhs = -(m.t() @ torch.cat([c.reshape(-1) for c in const]))
-        mg.update_A(m.t().to_sparse_csr() @ m)
+        if datalevels is None:
+            mg.update_A(m.t().to_sparse_csr() @ m)
+        else:
+            AA = [m.t().to_sparse_csr() @ m]
+            for level in range(1, mg.nlevels):
+                lproblem = datalevels[level].problem
+                lstate = datalevels[level].state
+                fine = datalevels[level - 1].state
+                R = mg.RRsingle[level - 1]
+                for k in dom.fieldnames:
+                    f = fine.fields[k]
+                    lstate.fields[k] = (R @ f.reshape(-1).to(R.dtype)).reshape(
+                        tuple(lproblem.domain.shape))
+                lconst, lJ = lproblem.linearize(lstate, epoch=epoch)
+                lm = lJ.to_csr()
+                AA.append(lm.t().to_sparse_csr() @ lm)
+            mg.update_A(AA)
         sol = torch.zeros_like(rhs)
         for _ in range(iters):
             sol = mg.step(sol, rhs, smoother,

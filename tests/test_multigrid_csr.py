@@ -188,3 +188,52 @@ def test_optimize_multigrid_reaches_newton_solution():
                             seen.append(epoch))
     assert seen == list(range(7))
     assert float((u - ref).abs().max() / ref.abs().max()) < 1e-8
+
+
+def test_optimize_multigrid_with_per_level_problems():
+    """util.optimize_multigrid with `datalevels` (util.py:414-441): the
+    coarse matrices come from the same operator on the coarse grids,
+    linearised at the restricted fields; the fine-level smoothing and
+    residuals keep the iteration on the fine problem, which reaches its
+    Newton solution."""
+    import argparse
+    from types import SimpleNamespace
+    from odil_gb300 import util
+    from odil_gb300.domain import Domain, State
+
+    def op(mod, ctx):
+        u = ctx.field("u")
+        lap = (ctx.field("u", 1, 0) + ctx.field("u", -1, 0) +
+               ctx.field("u", 0, 1) + ctx.field("u", 0, -1) - 4 * u)
+        return [3 * u - 0.5 * lap - mod.sin(ctx.cell_center(0)) + 0.1 * u * u]
+
+    def make(n):
+        return Domain(ndim=2, shape=(n, n), lower=(0, 0), upper=(1, 1),
+                      varnames=("x", "y"), fieldnames=["u"], device="cpu")
+
+    dom = make(17)
+    pj = _CpuProblem(op, dom)
+    ref = torch.zeros(dom.shape, dtype=torch.float64)
+    st = State(fields={"u": ref})
+    for _ in range(6):
+        const, J = pj.linearize(st)
+        ref += torch.linalg.solve(J.to_csr().to_dense(),
+                                  -const[0].reshape(-1)).reshape(dom.shape)
+    u = torch.zeros(dom.shape, dtype=torch.float64)
+    state = State(fields={"u": u})
+    levels = [SimpleNamespace(problem=pj, state=state)]
+    for n in (9, 5, 3):
+        d = make(n)
+        levels.append(SimpleNamespace(
+            problem=_CpuProblem(op, d),
+            state=State(fields={"u": torch.zeros(d.shape,
+                                                 dtype=torch.float64)})))
+    args = argparse.Namespace(epochs=6, epoch_start=0, nlvl=None,
+                              restriction="full", omega=0.6,
+                              linsolver_maxiter=40, ndirect=3, smooth_pre=2,
+                              smooth_post=2)
+    util.optimize_multigrid(args, pj, state, datalevels=levels)
+    assert float((u - ref).abs().max() / ref.abs().max()) < 1e-7
+    # the coarse states hold the restricted fine fields of the last epoch
+    assert levels[1].state.fields["u"].shape == (9, 9)
+    assert float(levels[1].state.fields["u"].abs().max()) > 0
