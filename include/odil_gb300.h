@@ -101,7 +101,10 @@ int odil_wave_loss_grad_f64(const odil_wave_params* p, const double* u,
  *     cells fit: 16384 x 16384 (aligned) does, 65536 x 8192 does not;
  *   - all calls share that array: calls that overlap on the GPU race;
  *   - the first call on each device looks up the array's address; make it
- *     before any stream capture. */
+ *     before any stream capture.  The address is cached per device (an
+ *     atomic, safe for host threads that call at once) and belongs to the
+ *     device's primary context: after cudaDeviceReset the entry point must
+ *     not be called again in the same process. */
 int64_t odil_wave_loss_grad_noalloc_max_blocks(void);
 int odil_wave_loss_grad_f32_noalloc(const odil_wave_params* p, const float* u,
                                     float* grad, double* loss, void* stream);

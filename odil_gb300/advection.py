@@ -12,6 +12,7 @@ dense FP64 direct solve on the coarsest level), and applies p += d in FP64.
 Coarse operators rediscretise the upwind operator with doubled steps (the
 Galerkin product R J P loses the diagonal dominance damped Jacobi needs).
 """
+import math
 import ctypes
 
 import numpy as np
@@ -256,7 +257,13 @@ class AdvectKernels:
         """Right-preconditioned BiCGStab on J x = b in FP32 (x overwritten,
         zero initial guess); returns the iteration count.  The step scalars
         stay on the device (odil_bicgstab_*); the host reads the two residual
-        norms it tests per iteration."""
+        norms it tests per iteration.
+
+        Breakdown (<r^, r> = 0, <r^, v> = 0 or <t, t> = 0) makes the norm of
+        s non-finite before x is touched in that iteration: the solve stops
+        there with x at the last valid iterate and records the iteration in
+        ``self.breakdowns``.  A non-finite right-hand side raises
+        FloatingPointError."""
         md = self._scratch.get("md")
         if md is None:
             md = self._scratch["md"] = vec.MultiDot(self.n, 2, 2,
@@ -280,7 +287,7 @@ class AdvectKernels:
         p.zero_()
         v.zero_()
         sc.fill_(1.0)  # rho, alpha, omega = 1; beta (sc[3]) is set before use
-        nb = md(fl(b), 1, [fl(b)])[0, 0].item()**0.5
+        nb = self._rhs_norm(md, b)
         if nb == 0:
             return 0
         for it in range(maxit):
@@ -293,6 +300,8 @@ class AdvectKernels:
             call("odil_bicgstab_scalars", ptr(dots), ptr(sc), 1, st)
             call("odil_bicgstab_update_s", ptr(s), ptr(r), ptr(v), ptr(sc), n, st)
             ns = md(fl(s), 1, [fl(s)])[0, 0].item()**0.5
+            if not math.isfinite(ns):
+                return self._breakdown(it)
             if ns <= tol * nb:
                 call("odil_bicgstab_update_xr", ptr(x), None, ptr(ph), None, None,
                      None, ptr(sc), n, 0, st)
@@ -304,9 +313,25 @@ class AdvectKernels:
             call("odil_bicgstab_update_xr", ptr(x), ptr(r), ptr(ph), ptr(sh), ptr(s),
                  ptr(t), ptr(sc), n, 1, st)
             nr = md(fl(r), 1, [fl(r)])[0, 0].item()**0.5
+            if not math.isfinite(nr):
+                raise FloatingPointError(
+                    "BiCGStab: non-finite residual norm in iteration %d" % it)
             if nr <= tol * nb:
                 return it + 1
         return maxit
+
+    def _rhs_norm(self, md, b):
+        nb = md(b.reshape(-1), 1, [b.reshape(-1)])[0, 0].item()**0.5
+        if not math.isfinite(nb):
+            raise FloatingPointError("BiCGStab: non-finite right-hand side")
+        return nb
+
+    def _breakdown(self, it):
+        """Records a breakdown in iteration `it` (x holds the last valid
+        iterate) and returns the number of completed iterations."""
+        self.breakdowns = getattr(self, "breakdowns", [])
+        self.breakdowns.append(it)
+        return it
 
     def _bicgstab_host(self, b, x, tol, maxit, md, vc):
         """The same iteration with host scalars (cell counts not divisible
@@ -320,21 +345,28 @@ class AdvectKernels:
         rh.copy_(b)
         p.zero_()
         v.zero_()
-        nb = md(fl(b), 1, [fl(b)])[0, 0].item()**0.5
+        nb = self._rhs_norm(md, b)
         if nb == 0:
             return 0
         rho = alpha = w = 1.0
         for it in range(maxit):
             rho1 = md(fl(rh), 1, [fl(r)])[0, 0].item()
+            if rho1 == 0.0 or not math.isfinite(rho1) or w == 0.0:
+                return self._breakdown(it)
             beta = (rho1 / rho) * (alpha / w)
             rho = rho1
             vec.axpby(p, 1.0, p, -w, v)
             vec.axpby(p, 1.0, r, beta, p)
             vc[0].replay()
             self.jv(ph, out=v)
-            alpha = rho / md(fl(rh), 1, [fl(v)])[0, 0].item()
+            rv = md(fl(rh), 1, [fl(v)])[0, 0].item()
+            if rv == 0.0 or not math.isfinite(rv):
+                return self._breakdown(it)
+            alpha = rho / rv
             vec.axpby(s, 1.0, r, -alpha, v)
             ns = md(fl(s), 1, [fl(s)])[0, 0].item()**0.5
+            if not math.isfinite(ns):
+                return self._breakdown(it)
             if ns <= tol * nb:
                 vec.axpby(x, 1.0, x, alpha, ph)
                 return it + 1
@@ -342,11 +374,16 @@ class AdvectKernels:
             self.jv(sh, out=t)
             tt = md(fl(t), 1, [fl(t), fl(s)])
             tt_ts = tt[0].cpu().numpy()
-            w = tt_ts[1] / tt_ts[0]
+            w = tt_ts[1] / tt_ts[0] if tt_ts[0] > 0 else 0.0
+            if not math.isfinite(w):
+                w = 0.0
             vec.axpby(x, 1.0, x, alpha, ph)
             vec.axpby(x, 1.0, x, w, sh)
             vec.axpby(r, 1.0, s, -w, t)
             nr = md(fl(r), 1, [fl(r)])[0, 0].item()**0.5
+            if not math.isfinite(nr):
+                raise FloatingPointError(
+                    "BiCGStab: non-finite residual norm in iteration %d" % it)
             if nr <= tol * nb:
                 return it + 1
         return maxit

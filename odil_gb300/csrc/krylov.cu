@@ -15,7 +15,10 @@ constexpr int KT = 256;
 // phase 0: rho' = dots[0] (= <r^, r>), beta = (rho'/rho)(alpha/omega), rho = rho'
 // phase 1: alpha = rho / dots[0] (= <r^, v>)
 // phase 2: omega = dots[1] / dots[0] (= <t, s> / <t, t>; dots from one
-//          multi-dot of t against (t, s))
+//          multi-dot of t against (t, s)); omega = 0 when <t, t> is zero or
+//          the quotient is not finite, so the update keeps the valid half
+//          step x += alpha ph, r = s, and the breakdown shows up as a
+//          non-finite norm of s in the next iteration, before x changes.
 __global__ void bicg_scalars_kernel(const double* __restrict__ dots, double* __restrict__ sc,
                                     int phase) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
@@ -26,7 +29,8 @@ __global__ void bicg_scalars_kernel(const double* __restrict__ dots, double* __r
     } else if (phase == 1) {
         sc[1] = sc[0] / dots[0];
     } else {
-        sc[2] = dots[1] / dots[0];
+        const double w = dots[1] / dots[0];
+        sc[2] = (dots[0] > 0.0 && isfinite(w)) ? w : 0.0;
     }
 }
 

@@ -16,6 +16,7 @@
 // j = nx-1 (4, 4/3, 0), nx = 1 (20/3, 0, 4/9).  These are the derivatives
 // tf.GradientTape returns for each rolled argument, including the zero
 // gradient through the branch tf.where did not take.
+#include <atomic>
 #include "wave_dev.cuh"
 
 namespace odil {
@@ -1067,29 +1068,34 @@ ODIL_API int odil_wave_march_shape_f32(const odil_wave_params* p, const float* b
 //     streams, other host threads) race on the array;
 //   * the first call on each device looks up the array's device address with
 //     cudaGetSymbolAddress and caches it; make that first call before any
-//     stream capture.
+//     stream capture.  Host threads that make their first calls at once may
+//     both look the address up; the cache is an atomic per device, and both
+//     store the same value;
+//   * the cached address belongs to the device's primary context: it does
+//     not survive cudaDeviceReset (or any other teardown of that context),
+//     after which this entry point must not be called in the same process.
 constexpr int64_t kNoAllocBytes = 256 * 1024;
 constexpr int64_t kNoAllocMaxBlocks = (kNoAllocBytes - kReduceHeader) / (int64_t)sizeof(double);
 static __device__ __align__(256) unsigned char g_loss_scratch[kNoAllocBytes];
 
 namespace {
 constexpr int kMaxDevices = 64;
-void* g_scratch_ptr[kMaxDevices] = {nullptr};
+std::atomic<void*> g_scratch_ptr[kMaxDevices];
 
 // Device address of g_loss_scratch on the current device (set-up on first use).
 int scratch_address(void** out) {
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices)
         return ODIL_ERR_LAUNCH;
-    if (!g_scratch_ptr[dev]) {
-        void* ptr = nullptr;
+    void* ptr = g_scratch_ptr[dev].load(std::memory_order_acquire);
+    if (!ptr) {
         if (cudaGetSymbolAddress(&ptr, g_loss_scratch) != cudaSuccess || !ptr) {
             cudaGetLastError();
             return ODIL_ERR_LAUNCH;
         }
-        g_scratch_ptr[dev] = ptr;
+        g_scratch_ptr[dev].store(ptr, std::memory_order_release);
     }
-    *out = g_scratch_ptr[dev];
+    *out = ptr;
     return ODIL_OK;
 }
 }  // namespace

@@ -1,56 +1,102 @@
-"""Per-epoch history table with CSV output (util_history.py:7-108).
+"""Training history: a table of per-epoch scalars, written as CSV.
 
-Columns are appended value by value; ``commit`` closes a row; ``write``
-commits and appends the rows not yet written to the CSV file (the header is
-the column order of the first written row).  A column that first appears
-after some rows is back-filled with zeros of the value's kind, as the
-reference does, and a row that misses a column is an error.  ``save``/``load``
-store the columns as a pickled dict of lists, the reference's file layout.
+The file formats follow the reference's history (util_history.py:7-108),
+since drivers and plotting scripts read them:
+
+* the table is a dict that maps a column name to the list of its values, one
+  value per committed row, in the order the columns first appeared; the
+  pickle file (``save`` / ``load``) is exactly that dict;
+* the CSV file has a header line of the column names, fixed by the first
+  write, then one line per row with each value formatted by ``str``, values
+  separated by commas and no quoting; rows are appended as they are
+  committed, once more than ``warmup`` rows exist;
+* a column that first appears after k rows holds k zeros of its first
+  value's kind before that value (0 for integers, 0.0 for floats, None for
+  strings), and a value of None stands for the zero of the column's kind.
+
+Everything else here (the pending-row check, the CSV writer) is this
+engine's own.
 """
 import pickle
 
 import numpy as np
 
-_SCALARS = (int, float, str, np.float32, np.float64)
 
-
-def _zero_of(value):
-    if value is None:
-        return None
+def _kind_zero(value):
+    """The zero that stands in for a missing value of `value`'s kind."""
     if isinstance(value, (bool, np.bool_)):
-        raise TypeError("unexpected type: %s" % type(value))
-    if isinstance(value, int):
+        raise TypeError("history values are numbers or strings, not %s"
+                        % type(value).__name__)
+    if isinstance(value, (int, np.integer)):
         return 0
     if isinstance(value, (float, np.floating)):
-        return 0.
-    return None  # strings: the reference back-fills nothing meaningful
+        return 0.0
+    return None
+
+
+def _accepts(value):
+    return value is None or isinstance(
+        value, (int, float, str, np.integer, np.floating)) and not isinstance(
+            value, (bool, np.bool_))
+
+
+class _CsvSink:
+    """Appends committed rows to a CSV file; the header is the column list
+    at the first write and cannot grow afterwards."""
+
+    def __init__(self, path):
+        self.stream = open(path, "w")
+        self.header = None
+        self.rows_out = 0
+
+    def emit(self, table, nrows):
+        names = list(table)
+        if self.header is None:
+            self.header = names
+            self.stream.write(",".join(names) + "\n")
+        elif names != self.header:
+            added = [k for k in names if k not in self.header]
+            raise RuntimeError("columns %s appeared after the CSV header "
+                               "was written" % ", ".join(map(repr, added)))
+        out = []
+        for r in range(self.rows_out, nrows):
+            out.append(",".join(str(table[k][r]) for k in names) + "\n")
+        self.stream.write("".join(out))
+        self.stream.flush()
+        self.rows_out = nrows
+
+    def close(self):
+        self.stream.close()
 
 
 class History:
+    """Per-epoch scalars: ``append`` values to the open row, ``commit`` the
+    row, ``write`` commits and appends the new rows to the CSV file."""
 
     def __init__(self, csvpath=None, warmup=0):
-        """warmup: rows are written only once more than `warmup` exist."""
         self.data = {}
         self.count = 0
         self.warmup = warmup
-        self.csvpath = csvpath
-        self.csvkeys = None
-        self.csvcount = 0
-        self.csvfile = open(csvpath, "w") if csvpath is not None else None
+        self._csv = _CsvSink(csvpath) if csvpath is not None else None
 
     def append(self, key, value=None):
-        if value is not None and type(value) not in _SCALARS:
-            raise TypeError("unexpected type: %s" % type(value))
-        col = self.data.get(key)
-        if col is None:
+        """Puts `value` in column `key` of the open row."""
+        if not _accepts(value):
+            raise TypeError("history values are numbers or strings, not %s"
+                            % type(value).__name__)
+        values = self.data.get(key)
+        if values is None:
             if value is None:
-                raise ValueError("first value of column %r is None" % key)
-            col = self.data[key] = [_zero_of(value)] * self.count
-        if value is None:
-            if not col:
-                raise ValueError("expected non-empty column " + key)
-            value = _zero_of(col[-1])
-        col.append(value)
+                raise ValueError("column %r has no value to take its kind "
+                                 "from" % key)
+            zero = _kind_zero(value)
+            self.data[key] = values = [zero for _ in range(self.count)]
+        elif value is None:
+            if not values:
+                raise ValueError("column %r has no value to take its kind "
+                                 "from" % key)
+            value = _kind_zero(values[-1])
+        values.append(value)
 
     def append_dict(self, values):
         for key, value in values.items():
@@ -60,47 +106,38 @@ class History:
         return self.data.get(key, default)
 
     def commit(self):
-        """Closes the current row; every column must have a value in it."""
-        n = max((len(c) for c in self.data.values()), default=0)
-        short = [k for k, c in self.data.items() if len(c) < n]
-        if short:
-            raise RuntimeError("Missing values for columns: " +
-                               ",".join(short) + ",")
+        """Closes the open row; each column must have received a value."""
+        lacking = [k for k, v in self.data.items() if len(v) <= self.count]
+        if lacking and len(lacking) < len(self.data):
+            raise RuntimeError("row %d has no value for %s"
+                               % (self.count, ", ".join(map(repr, lacking))))
         self.count += 1
 
     def write(self, nocommit=False):
-        """Commits (unless `nocommit`) and writes the pending rows."""
+        """Commits the open row (unless `nocommit`) and appends the rows not
+        yet in the CSV file, once more than `warmup` rows exist."""
         if not nocommit:
             self.commit()
-        if self.count <= self.warmup or self.csvfile is None:
-            return
-        if self.csvkeys is not None and len(self.csvkeys) != len(self.data):
-            extra = sorted(set(self.data) - set(self.csvkeys))
-            raise RuntimeError("Unexpected keys in history: %s" % extra)
-        if self.csvcount == 0:
-            self.csvkeys = list(self.data)
-            self.csvfile.write(",".join(self.csvkeys) + "\n")
-        lines = []
-        for r in range(self.csvcount, self.count):
-            lines.append(",".join(str(self.data[k][r]) for k in self.data))
-        if lines:
-            self.csvfile.write("\n".join(lines) + "\n")
-        self.csvcount = self.count
-        self.csvfile.flush()
+        if self._csv is not None and self.count > self.warmup:
+            self._csv.emit(self.data, self.count)
 
     def save(self, path):
         with open(path, "wb") as f:
             pickle.dump(self.data, f)
 
     def load(self, path):
-        """Replaces the columns with a saved table and writes its rows."""
+        """Replaces the table with a saved one and writes its rows."""
         with open(path, "rb") as f:
-            self.data = pickle.load(f)
-        self.csvkeys = list(self.data)
-        self.count = len(next(iter(self.data.values()))) if self.data else 0
+            table = pickle.load(f)
+        lengths = {len(v) for v in table.values()}
+        if len(lengths) > 1:
+            raise ValueError("columns of %s differ in length: %s"
+                             % (path, sorted(lengths)))
+        self.data = table
+        self.count = lengths.pop() if lengths else 0
         self.write(nocommit=True)
 
     def close(self):
-        if self.csvfile is not None:
-            self.csvfile.close()
-            self.csvfile = None
+        if self._csv is not None:
+            self._csv.close()
+            self._csv = None

@@ -21,6 +21,7 @@ sizes; here both use (n - 1) // 2 + 1.  Its recursive call does not pass
 smoothers return a new vector rather than updating `u` in place.
 """
 import ctypes
+import math
 import itertools
 
 import numpy as np
@@ -214,18 +215,62 @@ class Multigrid:
     def smoother_direct(self, level, u, f):
         """multigrid.py:307-310: the direct solve of the level (a dense LU
         of the assembled matrix, formed once per update_A).  The reference's
-        spsolve has no size limit; a dense factor here is kept below
-        DIRECT_MAX unknowns (2 GiB in FP64)."""
+        spsolve has no size limit; a dense factor here is kept to at most
+        DIRECT_MAX unknowns (2 GiB in FP64).  Larger levels are solved by
+        BiCGStab on the sparse matrix to a relative residual of 1e-12
+        (`_solve_iterative`), which stands in for the exact solve."""
         lu = self._inv.get(level)
         if lu is None:
             n = self.AA[level].shape[0]
             if n > self.DIRECT_MAX:
-                raise ValueError(
-                    "direct solve of %d unknowns on level %d; use more levels "
-                    "or a smaller ndirect" % (n, level))
+                return self._solve_iterative(self.AA[level], f.reshape(-1))
             lu = self._inv[level] = torch.linalg.lu_factor(
                 self.AA[level].to_dense())
         return torch.linalg.lu_solve(*lu, f.reshape(-1, 1)).reshape(-1)
+
+    @staticmethod
+    def _solve_iterative(A, f, rtol=1e-12, maxiter=None):
+        """BiCGStab (van der Vorst) on the sparse matrix A from zero, until
+        |f - A x| <= rtol |f|, at most `maxiter` (default 4 sqrt(n) + 100)
+        iterations; stops early at a breakdown (a zero inner product).
+        Raises FloatingPointError if the iterate becomes non-finite."""
+        n = f.numel()
+        maxiter = maxiter or int(4 * n**0.5) + 100
+        x = torch.zeros_like(f)
+        r = f.clone()
+        nf = torch.linalg.vector_norm(f).item()
+        if nf == 0.0:
+            return x
+        rt = r.clone()
+        p = torch.zeros_like(f)
+        v = torch.zeros_like(f)
+        rho = alpha = omega = 1.0
+        for _ in range(maxiter):
+            rho1 = torch.dot(rt, r).item()
+            if rho1 == 0.0 or omega == 0.0:
+                break
+            p = r + (rho1 / rho) * (alpha / omega) * (p - omega * v)
+            rho = rho1
+            v = A @ p
+            rv = torch.dot(rt, v).item()
+            if rv == 0.0:
+                break
+            alpha = rho / rv
+            s = r - alpha * v
+            if torch.linalg.vector_norm(s).item() <= rtol * nf:
+                x = x + alpha * p
+                break
+            t = A @ s
+            tt = torch.dot(t, t).item()
+            omega = torch.dot(t, s).item() / tt if tt > 0 else 0.0
+            x = x + alpha * p + omega * s
+            r = s - omega * t
+            nr = torch.linalg.vector_norm(r).item()
+            if not math.isfinite(nr):
+                raise FloatingPointError("coarse-level BiCGStab diverged")
+            if nr <= rtol * nf:
+                break
+        return x
 
     def step(self, u, f, smoother, level=0, ndirect=5, pre=2, post=2):
         """multigrid.py:312-339: one V-cycle from `u`."""

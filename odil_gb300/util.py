@@ -390,9 +390,10 @@ def add_arguments(parser):
                         help="Index of the first epoch")
     parser.add_argument('--optimizer', type=str, default='newton',
                         help="Optimizer: newton, lbfgsb, lbfgs, adam, adamn, gd")
-    parser.add_argument('--seed', type=int, default=None, help="Seed")
-    parser.add_argument('--double', type=int, default=1,
-                        help="Use FP64 fields")
+    parser.add_argument('--seed', type=int, default=0,
+                        help="Seed for the drivers' random generators")
+    parser.add_argument('--double', type=int, default=0,
+                        help="Double precision")
     parser.add_argument('--bfgs_m', type=int, default=50,
                         help="L-BFGS history size")
     parser.add_argument('--adam_epsilon', type=float, default=None)

@@ -13,6 +13,12 @@ Follows advection_2d.py:103-223 (``operator``, direct problem, defaults
 Domain: shape (Nt, Nx, Ny), t in [0, tmax], x, y in [0, 1) (advection_2d.py:
 335-340), cell centres as util_op.py:130-137.
 
+Pinned: ``residual_uvp`` and ``residual_p`` equal, to rounding, the
+residuals of the reference's own ``operator`` function run on NumPy stand-ins
+for TensorFlow (tests/golden/advection_ref.npz, made by
+tests/golden/make_golden.py; tests/test_advection_oracle.py), on small grids
+with velocity fields of both signs and exact zeros.
+
 The benchmark instance has a constant velocity a = (ax, ay), so u and v are
 known: after one Newton step fu = fv = 0 and the unknown is p alone
 (``residual_p``).  ``residual_uvp`` keeps the reference's three fields.

@@ -1,13 +1,21 @@
 #!/usr/bin/env python3
 """Regenerates the golden fixtures in this folder from the reference checkout.
 
-Run from the repository root, on a machine that has the reference at
-/root/reference (it does not exist on the GPU machines, which only read the
-committed JSON/NPZ files):
+Run from the repository root, on a machine that has a checkout of the
+reference (odil22/odil); give its root with --ref or in the environment
+variable ODIL_REFERENCE.  The GPU machines do not have it: they only read the
+committed JSON/NPZ files.
 
-    python tests/golden/make_golden.py [--ref /root/reference]
+    python tests/golden/make_golden.py --ref <reference checkout>
 
 Fixtures
+  advection_ref.npz     residuals (fp, fu, fv) of the reference's own
+                        `operator` of advection_2d.py:103-223 (its function
+                        body, taken from the source with `ast` and run with
+                        NumPy stand-ins for TensorFlow's `mod` and the
+                        Context of util_op.py:457-563) on small (t, x, y)
+                        grids with seeded fields, velocities of both signs
+                        and exact zeros (see make_advection).
   wave_fd_newton.json   N and ref_du_l2 after 2 Newton epochs, read from the
                         reference's cases/wave_cost/precomputed/fd_newton/
                         lines.pickle (fields N, error).
@@ -308,13 +316,121 @@ def make_cavity(ref):
     return res
 
 
+class _NpContext:
+    """The parts of util_op.py's Context (lines 457-563) that the advection
+    operator uses, on NumPy arrays: ``field(name, *shift)`` is the state
+    field rolled by -shift on every axis (periodic, util_op.py:548-551;
+    freeze changes nothing in a forward evaluation), ``zeros``/``ones`` are
+    the custom fields of util_op.py:229-234, ``cell_index`` the index grid
+    of util_op.py:185-187, ``step`` the cell size of util_op.py:127-128."""
+
+    def __init__(self, fields, shape, upper, varnames=("t", "x", "y")):
+        self.fields = fields
+        self.shape = shape
+        self.upper = upper
+        self.varnames = varnames
+        self.epoch = 0
+
+    def _dim(self, i):
+        return self.varnames.index(i) if isinstance(i, str) else i
+
+    def step(self, i):
+        i = self._dim(i)
+        return self.upper[i] / self.shape[i]
+
+    def size(self, i):
+        return self.shape[self._dim(i)]
+
+    def cell_index(self, i):
+        return np.meshgrid(*[np.arange(n) for n in self.shape],
+                           indexing="ij")[self._dim(i)]
+
+    def field(self, name, *shift, freeze=False):
+        if name == "zeros":
+            return np.zeros(self.shape)
+        if name == "ones":
+            return np.ones(self.shape)
+        shift = tuple(shift) + (0,) * (len(self.shape) - len(shift))
+        return np.roll(self.fields[name], np.negative(shift),
+                       tuple(range(len(self.shape))))
+
+
+def _reference_function(path, name):
+    """Compiles the top-level function `name` of the reference source file
+    `path` on its own (the module's imports need TensorFlow)."""
+    import ast
+    tree = ast.parse(open(path).read(), filename=path)
+    for node in tree.body:
+        if isinstance(node, ast.FunctionDef) and node.name == name:
+            return compile(ast.Module(body=[node], type_ignores=[]), path,
+                           "exec")
+    raise KeyError(name)
+
+
+def make_advection(ref):
+    """Residuals of advection_2d.py's `operator` (direct problem, the
+    driver's defaults --periodic 1 --central 0 --implicit 0) on small grids.
+    Velocity fields: per-cell random values of both signs with some exact
+    zeros (the where(u > 0, ...) branch), and constant velocities of each
+    sign pair (the benchmark's form)."""
+    from types import SimpleNamespace
+    code = os.path.join(ref, "code")
+    op_code = _reference_function(os.path.join(code, "advection_2d.py"),
+                                  "operator")
+    ex_code = _reference_function(os.path.join(code, "util_op.py"),
+                                  "extrap_linear")
+    rng = np.random.default_rng(20)
+    res = {}
+    cases = [("mixed_a", (3, 4, 5), None), ("mixed_b", (4, 3, 6), None),
+             ("mixed_c", (2, 5, 4), None)]
+    for sx in (1, -1):
+        for sy in (1, -1):
+            cases.append(("const_%s%s" % ("p" if sx > 0 else "m",
+                                          "p" if sy > 0 else "m"),
+                          (3, 4, 5), (0.7 * sx, 0.4 * sy)))
+    for name, shape, vel in cases:
+        tmax = 0.8
+        if vel is None:
+            u = rng.standard_normal(shape)
+            v = rng.standard_normal(shape)
+            u[rng.random(shape) < 0.15] = 0.0
+            v[rng.random(shape) < 0.15] = 0.0
+        else:
+            u = np.full(shape, vel[0])
+            v = np.full(shape, vel[1])
+        p = rng.standard_normal(shape)
+        exact_uu = rng.standard_normal(shape)
+        exact_vv = rng.standard_normal(shape)
+        exact_pp = rng.standard_normal(shape)
+        ns = {"np": np}
+        exec(ex_code, ns)
+        ns.update(args=SimpleNamespace(periodic=1, central=0, implicit=0,
+                                       problem="direct"),
+                  exact_uu=exact_uu, exact_vv=exact_vv, exact_pp=exact_pp)
+        exec(op_code, ns)
+        mod = SimpleNamespace(where=np.where, roll=np.roll)
+        ctx = _NpContext({"u": u, "v": v, "p": p}, shape, (tmax, 1.0, 1.0))
+        fp, fu, fv = ns["operator"](mod, ctx)
+        for key, val in (("u", u), ("v", v), ("p", p), ("exact_uu", exact_uu),
+                         ("exact_vv", exact_vv), ("exact_pp", exact_pp),
+                         ("fp", fp), ("fu", fu), ("fv", fv)):
+            res["%s_%s" % (name, key)] = np.asarray(val, np.float64)
+        res[name + "_tmax"] = np.float64(tmax)
+    return res
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("ODIL_REFERENCE"),
+                    help="root of the reference checkout (default: "
+                    "$ODIL_REFERENCE)")
     ap.add_argument("--only", default=None)
     a = ap.parse_args()
+    if not a.ref:
+        ap.error("give the reference checkout with --ref or ODIL_REFERENCE")
     todo = a.only.split(",") if a.only else ["wave", "multigrid", "multigrid_csr",
-                                                  "mgdecomp", "cavity"]
+                                                  "mgdecomp", "cavity",
+                                                  "advection"]
     if "wave" in todo:
         for name in ("fd_newton", "fd_lbfgsb"):
             with open(os.path.join(HERE, "wave_%s.json" % name), "w") as f:
@@ -331,6 +447,9 @@ def main():
     if "cavity" in todo:
         np.savez_compressed(os.path.join(HERE, "cavity_N128.npz"),
                             **make_cavity(a.ref))
+    if "advection" in todo:
+        np.savez_compressed(os.path.join(HERE, "advection_ref.npz"),
+                            **make_advection(a.ref))
 
 
 if __name__ == "__main__":

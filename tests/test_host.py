@@ -123,6 +123,8 @@ def test_argparse_flags_match_reference_names():
     assert (b.report_every, b.plot_every, b.checkpoint_every,
             b.history_every, b.every_factor, b.plotext, b.multigrid,
             b.nn_initializer) == (10, 5, 5, 1, 1, "pdf", 0, "legacy")
+    # util.py:147-150, 168-171: seeded by default, single precision by default
+    assert (b.seed, b.double, b.epoch_start, b.optimizer) == (0, 0, 0, "newton")
 
 
 def test_unknown_names_raise_value_error():
@@ -156,7 +158,7 @@ def test_history_csv_rows_backfill_and_errors(tmp_path):
     h.append("loss", 0.125)
     h.append("err", 1e-3)  # new column: back-filled, but the header is fixed
     assert h.get("err") == [0.0, 0.0, 0.0, 1e-3]
-    with pytest.raises(RuntimeError, match="Unexpected keys"):
+    with pytest.raises(RuntimeError, match="'err' appeared after the CSV header"):
         h.write()
     h.close()
     h2 = History()
@@ -164,7 +166,7 @@ def test_history_csv_rows_backfill_and_errors(tmp_path):
     h2.append("b", 2.0)
     h2.commit()
     h2.append("a", 2)
-    with pytest.raises(RuntimeError, match="Missing values for columns: b,"):
+    with pytest.raises(RuntimeError, match="row 1 has no value for 'b'"):
         h2.commit()
     with pytest.raises(TypeError):
         h2.append("a", [1])

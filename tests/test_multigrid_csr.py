@@ -232,8 +232,53 @@ def test_optimize_multigrid_with_per_level_problems():
                               restriction="full", omega=0.6,
                               linsolver_maxiter=40, ndirect=3, smooth_pre=2,
                               smooth_post=2)
-    util.optimize_multigrid(args, pj, state, datalevels=levels)
+    seen_A, seen_u = [], []
+    orig = Multigrid.update_A
+
+    def spy(self, A, *a, **kw):
+        seen_A.append(list(A) if isinstance(A, (list, tuple)) else [A])
+        return orig(self, A, *a, **kw)
+
+    def cb(packed, epoch, **kw):
+        seen_u.append(packed.clone())
+
+    Multigrid.update_A = spy
+    try:
+        util.optimize_multigrid(args, pj, state, callback=cb,
+                                datalevels=levels)
+    finally:
+        Multigrid.update_A = orig
     assert float((u - ref).abs().max() / ref.abs().max()) < 1e-7
+    # The level matrices of epoch 1 (a nonzero fine state, where the
+    # nonlinear term makes J depend on the state): level l's matrix is
+    # J_l^T J_l of the level-l problem linearised at the fine field
+    # restricted l times by the single-field full-weighting restriction.
+    mg = Multigrid((17, 17), nvar=1, restriction="full", dtype=torch.float64,
+                   device="cpu")
+    f = seen_u[1].reshape(17, 17)
+    for level in range(1, mg.nlevels):
+        f = (mg.RRsingle[level - 1] @ f.reshape(-1)).reshape(
+            tuple(levels[level].problem.domain.shape))
+        _, Jl = levels[level].problem.linearize(State(fields={"u": f}))
+        Jm = Jl.to_csr().to_dense()
+        np.testing.assert_allclose(seen_A[1][level].to_dense().numpy(),
+                                   (Jm.T @ Jm).numpy(), rtol=1e-12,
+                                   atol=1e-12)
     # the coarse states hold the restricted fine fields of the last epoch
     assert levels[1].state.fields["u"].shape == (9, 9)
     assert float(levels[1].state.fields["u"].abs().max()) > 0
+
+
+def test_direct_solve_above_dense_limit_is_iterative(monkeypatch):
+    """Above DIRECT_MAX unknowns the coarsest-level solve of
+    Multigrid.smoother_direct is BiCGStab on the sparse matrix to 1e-12
+    relative residual (the reference's spsolve has no size limit); it
+    agrees with the dense solve."""
+    m, A0, f = _run("p17", "cpu")
+    exact = m.smoother_direct(0, torch.zeros_like(f), f)
+    m._inv.clear()
+    monkeypatch.setattr(Multigrid, "DIRECT_MAX", 16)
+    it = m.smoother_direct(0, torch.zeros_like(f), f)
+    assert 0 not in m._inv
+    np.testing.assert_allclose(it.numpy(), exact.numpy(), rtol=1e-9,
+                               atol=1e-10 * float(exact.abs().max()))
