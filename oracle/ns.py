@@ -295,3 +295,22 @@ def newton_pinned(s, state, epochs=1, pin=(0, 0)):
         for i, k in enumerate(FIELDS):
             st[k] = st[k] + d[i * N:(i + 1) * N].reshape(s.shape)
     return st
+
+
+def loss_grad_live(s, state):
+    """loss = sum_e mean(f_e^2) and its gradient through the live (rolled)
+    arguments only, the reference's tape gradient (util_op.py:627-654), by
+    one reverse pass: returns (list of residual rms, loss, {field: grad})."""
+    frozen = {k: torch.as_tensor(np.asarray(state[k], np.float64))
+              for k in FIELDS}
+    live = _live_from(state, requires_grad=True)
+    ff = operator(s, live, frozen)
+    loss = sum((f**2).mean() for f in ff)
+    keys = list(live)
+    gs = torch.autograd.grad(loss, [live[k] for k in keys], allow_unused=True)
+    g = {k: torch.zeros(s.shape, dtype=torch.float64) for k in FIELDS}
+    for (k, sh), ga in zip(keys, gs):
+        if ga is not None:
+            g[k] += torch.roll(ga, (sh[0], sh[1]), (0, 1))  # undo _roll
+    rms = [float(f.detach().pow(2).mean().sqrt()) for f in ff]
+    return rms, float(loss.detach()), {k: v.numpy() for k, v in g.items()}

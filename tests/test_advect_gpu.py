@@ -86,7 +86,7 @@ def test_multigrid_pieces_match_oracle(cuda):
     assert _rel(v, A.vcycle(levels, b)) < 1e-4
 
 
-@pytest.mark.parametrize("n,seed", [(32, 0), (32, 4), (64, 1)])
+@pytest.mark.parametrize("n,seed", [(32, 0), (32, 4), (64, 1), (128, 1)])
 def test_mixed_newton_mg_reaches_oracle(cuda, n, seed):
     """FP64 Newton with the FP32 BiCGStab + V-cycle inner solve reaches
     rel err <= 1e-5 against the FP64 direct solution."""

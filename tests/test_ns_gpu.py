@@ -182,3 +182,52 @@ def test_gauss_newton_inverse_step_matches_oracle(cuda):
     dp = (t[2].cpu().numpy() - st["p"]) - (ref["p"] - st["p"])
     scale = np.abs(ref["p"] - st["p"] - (ref["p"] - st["p"]).mean()).max()
     assert np.abs(dp - dp.mean()).max() <= 1e-6 * scale
+
+
+def test_forward_solution_is_root_of_oracle_operator(cuda):
+    """The forward check of the cavity configuration at a reduced size
+    (64^2, Re 400): at the GPU Newton solution the restated reference
+    operator leaves a residual rms <= 1e-9 in every term, and its loss
+    gradient is ~0."""
+    from odil_gb300.ns import NsDirectNewton
+    n = 64
+    k = _kernels(n, 400.0, {}, cuda)
+    t = [torch.zeros((n, n), dtype=torch.float64, device=cuda)
+         for _ in range(3)]
+    NsDirectNewton(k).solve(*t, epochs=60, tol=1e-11)
+    rms, loss, g = NS.loss_grad_live(NS.NsSetup(n, 400.0),
+                                     {c: x.cpu().numpy() for c, x in
+                                      zip("uvp", t)})
+    assert max(rms) <= 1e-9, rms
+    assert loss <= 1e-18
+
+
+def test_inverse_solution_is_stationary_for_oracle_loss(cuda):
+    """The inverse check at a reduced size (48^2, Re 400, 64 noisy imposed
+    points, penalty 1e-4): after Gauss-Newton the gradient of the restated
+    reference loss at the GPU's FP64 fields is below 1e-6 of its value at
+    the start, and the loss is at the noise level."""
+    from odil_gb300.ns import NsDirectNewton, NsGaussNewton
+    n = 48
+    fk = _kernels(n, 400.0, {}, cuda)
+    fw = [torch.zeros((n, n), dtype=torch.float64, device=cuda)
+          for _ in range(3)]
+    NsDirectNewton(fk).solve(*fw, epochs=60, tol=1e-11)
+    rng = np.random.default_rng(1)
+    mask = np.zeros((n, n))
+    mask.ravel()[rng.choice(n * n, 64, replace=False)] = 1.0
+    kw = dict(mask=mask, kreg=1e-4,
+              u_imp=fw[0].cpu().numpy() + 0.01 * rng.standard_normal((n, n)),
+              v_imp=fw[1].cpu().numpy() + 0.01 * rng.standard_normal((n, n)))
+    k = _kernels(n, 400.0, kw, cuda)
+    t = [torch.zeros((n, n), dtype=torch.float64, device=cuda)
+         for _ in range(3)]
+    NsGaussNewton(k).solve(*t, epochs=10, rtol=1e-6)
+    s = NS.NsSetup(n, 400.0, mask=mask, u_imp=kw["u_imp"],
+                   v_imp=kw["v_imp"], kreg=1e-4)
+    _, l0, g0 = NS.loss_grad_live(s, {c: np.zeros((n, n)) for c in "uvp"})
+    _, l1, g1 = NS.loss_grad_live(s, {c: x.cpu().numpy() for c, x in
+                                      zip("uvp", t)})
+    norm = lambda g: np.sqrt(sum(np.sum(x**2) for x in g.values()))
+    assert norm(g1) <= 1e-6 * norm(g0), (norm(g1), norm(g0))
+    assert l1 < 1e-3 * l0

@@ -127,11 +127,13 @@ def test_loss_grad_deterministic_and_workspace_reset(cuda):
     assert int(k.workspace[:4].view(torch.int32).item()) == 0
 
 
-def test_gradient_against_autodiff_and_fd(cuda):
+@pytest.mark.parametrize("n", [96, 1024])
+def test_gradient_against_autodiff_and_fd(cuda, n):
     """Fused FP32 adjoint gradient vs (a) the FP64 autodiff gradient of the
     op-by-op operator and (b) central finite differences (step 1e-3, FP64) on
-    64 seeded coordinates."""
-    nt = nx = 96
+    64 seeded coordinates; n = 1024 is the 1024^2 wave configuration itself
+    (16-mode profile, seed 1)."""
+    nt = nx = n
     s = W.make_setup(nt, nx, "sine", seed=1, nmodes=16)
     k = _kernels(s, cuda)
     rng = np.random.default_rng(11)
