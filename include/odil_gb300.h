@@ -440,6 +440,74 @@ int odil_ns_direct_solve_t(int64_t n, const double* coef, int64_t pin,
                            const float* b, float* x, void* stream);
 
 /* ------------------------------------------------------------------------
+ * Cavity multigrid on the normal equations.  The reference solves a Newton
+ * (or Gauss-Newton) step J^T J d = -J^T f with V-cycles of its multigrid on
+ * J^T J (util.py:509-604 with multigrid.py:429-469, 543-602; the normal
+ * equations of linsolver.py:35-45).  Here the levels are cell-centred (n,
+ * n/2, ... while even; the reference's node-based transfer needs odd
+ * sizes): bilinear prolongation P (3/4, 1/4 per axis, the outer weight moved
+ * to the wall cell at a wall), R = P^T / 4, Galerkin R A P.
+ *   vectors: [3][n][n] (u, v, p); coef: the [neq][15][n][n] coefficients of
+ *   odil_ns_jacobian_*; 25-point operators: [9][25][n][n], block 3 f + g,
+ *   point (dx + 2) * 5 + (dy + 2); dinv: [9][n][n] inverses of the 3 x 3
+ *   per-cell diagonal blocks.
+ * ---------------------------------------------------------------------- */
+/* w = J x (the util_op.py:877-896 product, from the stencil coefficients) */
+int odil_nsmg_jx_f32(int64_t n, int32_t neq, const float* coef, const float* x,
+                     float* w, void* stream);
+int odil_nsmg_jx_f64(int64_t n, int32_t neq, const double* coef,
+                     const double* x, double* w, void* stream);
+/* y = J^T w (linsolver.py:37-41); mode 0: out = y, 1: out = b - y,
+ * 2: out = x + omega dinv (b - y) (damped block Jacobi, multigrid.py:
+ * 283-299 with the per-cell blocks of multigrid.py:288-295). */
+int odil_nsmg_jtw_f32(int64_t n, int32_t neq, const float* coef,
+                      const float* w, const float* b, const float* x,
+                      const float* dinv, float* out, float omega, int32_t mode,
+                      void* stream);
+int odil_nsmg_jtw_f64(int64_t n, int32_t neq, const double* coef,
+                      const double* w, double* out, void* stream);
+/* A = J^T J as 25-point stencils and its block-diagonal inverses (the
+ * matrix linsolver.py:35-41 assembles, in stencil form). */
+int odil_nsmg_fine_ata(int64_t n, int32_t neq, const float* coef, float* A,
+                       float* dinv, void* stream);
+/* Ac = R A P on the n/2 grid and its block-diagonal inverses
+ * (multigrid.py:125-131, 390-427). */
+int odil_nsmg_galerkin(int64_t n, const float* A, float* Ac, float* dinv_c,
+                       void* stream);
+/* 25-point level operator; mode 0: out = A x, 1: out = b - A x,
+ * 2: out = x + omega dinv (b - A x) (multigrid.py:283-299). */
+int odil_nsmg_smooth(int64_t n, const float* A, const float* dinv,
+                     const float* x, const float* b, float* out, float omega,
+                     int32_t mode, void* stream);
+/* out = omega dinv b: the first Jacobi sweep from zero. */
+int odil_nsmg_jacobi0(int64_t n, const float* dinv, const float* b,
+                      float* out, float omega, void* stream);
+/* rc = R r on the n/2 grid; x += P e from the n/2 grid (multigrid.py:
+ * 590-598, the transfers of a V-cycle). */
+int odil_nsmg_restrict(int64_t n, const float* r, float* rc, void* stream);
+int odil_nsmg_prolong_add(int64_t n, const float* e, float* x, void* stream);
+/* Coarsest level (3 n^2 <= 1024 unknowns): the dense FP64 inverse of the
+ * 25-point operator (Gauss-Jordan, one block; a pivot at or below 1e-13 of
+ * the largest diagonal entry drops that direction), and x = minv b.
+ * Replaces multigrid.py:307-310 (spsolve on the coarsest matrix). */
+int odil_nsmg_coarse_inverse(int64_t n, const float* A, double* minv,
+                             void* stream);
+int odil_nsmg_coarse_apply(int64_t n, const double* minv, const float* b,
+                           float* x, void* stream);
+/* Preconditioned conjugate gradients with the step scalars on the device
+ * (sc = [<r, z>, alpha, beta], FP64).  phase 0: alpha = sc[0] / dots[0]
+ * (dots[0] = <p, A p>); phase 1: beta = dots[0] / sc[0], sc[0] = dots[0]
+ * (dots[0] = <r, z>); phase 2: sc[0] = dots[0], beta = 0 (first step).
+ * update_xr: x += alpha p, r -= alpha q; update_p: p = z + beta p.
+ * No counterpart in the reference (its CG is scipy's, on the host). */
+int odil_pcg_scalars(const double* dots, double* sc, int32_t phase,
+                     void* stream);
+int odil_pcg_update_xr(int64_t n, float* x, float* r, const float* p,
+                       const float* q, const double* sc, void* stream);
+int odil_pcg_update_p(int64_t n, float* p, const float* z, const double* sc,
+                      void* stream);
+
+/* ------------------------------------------------------------------------
  * Operators in stencil form (the reference's SparseOperator,
  * multigrid.py:877-1214): shifts s with one coefficient field C_s each on the
  * output grid,  (A u)[c] = sum_s C_s[c] u[stride*c + s], zero outside the

@@ -200,6 +200,23 @@ SIGNATURES = {
     "odil_wave_batch_march_f32": (_INT, [_P, _P, _P, ctypes.c_int32,
                                          ctypes.c_int32, ctypes.c_int32,
                                          ctypes.c_int32, _P, _I64, _P]),
+    "odil_nsmg_jx_f32": (_INT, [_I64, ctypes.c_int32, _P, _P, _P, _P]),
+    "odil_nsmg_jx_f64": (_INT, [_I64, ctypes.c_int32, _P, _P, _P, _P]),
+    "odil_nsmg_jtw_f32": (_INT, [_I64, ctypes.c_int32, _P, _P, _P, _P, _P, _P,
+                                 ctypes.c_float, ctypes.c_int32, _P]),
+    "odil_nsmg_jtw_f64": (_INT, [_I64, ctypes.c_int32, _P, _P, _P, _P]),
+    "odil_nsmg_fine_ata": (_INT, [_I64, ctypes.c_int32, _P, _P, _P, _P]),
+    "odil_nsmg_galerkin": (_INT, [_I64, _P, _P, _P, _P]),
+    "odil_nsmg_smooth": (_INT, [_I64, _P, _P, _P, _P, _P, ctypes.c_float,
+                                ctypes.c_int32, _P]),
+    "odil_nsmg_jacobi0": (_INT, [_I64, _P, _P, _P, ctypes.c_float, _P]),
+    "odil_nsmg_restrict": (_INT, [_I64, _P, _P, _P]),
+    "odil_nsmg_prolong_add": (_INT, [_I64, _P, _P, _P]),
+    "odil_nsmg_coarse_inverse": (_INT, [_I64, _P, _P, _P]),
+    "odil_nsmg_coarse_apply": (_INT, [_I64, _P, _P, _P, _P]),
+    "odil_pcg_scalars": (_INT, [_P, _P, ctypes.c_int32, _P]),
+    "odil_pcg_update_xr": (_INT, [_I64, _P, _P, _P, _P, _P, _P]),
+    "odil_pcg_update_p": (_INT, [_I64, _P, _P, _P, _P]),
     "odil_ns_num_equations": (_INT, [_P]),
     "odil_ns_residual_f32": (_INT, [_P, _P, _P, _P, _P, _P]),
     "odil_ns_residual_f64": (_INT, [_P, _P, _P, _P, _P, _P]),

@@ -8,6 +8,7 @@ split-shift linearize, util_op.py:585-614) and applied as stencil operators:
 J v and J^T w run through libodil_gb300's stencil kernels.
 """
 import ctypes
+import math
 
 import numpy as np
 import torch
@@ -515,4 +516,253 @@ class NsGaussNewton:
             if callback is not None:
                 callback(ep, loss)
         f = self.k.residual(u, v, p)
+        return float((f**2).mean(dim=(1, 2)).sum())
+
+
+class _MgLevel:
+    pass
+
+
+class NsMultigridNewton:
+    """Newton (forward problem) and Gauss-Newton (imposed points, penalty)
+    for the cavity with the normal equations J^T J d = -J^T f solved by
+    preconditioned conjugate gradients in FP32, preconditioned by one V-cycle
+    of a cell-centred geometric multigrid on J^T J -- the method of the
+    reference's util.optimize_multigridop_base (util.py:509-604, V-cycles of
+    multigrid.py:543-602 on the normal equations of linsolver.py:35-45),
+    here as hand-written kernels (csrc/ns_mg.cu):
+
+      * fine level: J^T J applied matrix-free from the FP32 Jacobian
+        coefficients (w = J x, y = J^T w), damped 3 x 3 block Jacobi;
+      * coarse levels (n/2, n/4, ... while even and >= `nmin`): Galerkin
+        R A P of the explicit 25-point J^T J with bilinear cell-centred
+        transfers (the reference's node-based transfer needs odd sizes, the
+        configuration's grid is even), same smoother;
+      * coarsest level: FP64 dense inverse (Gauss-Jordan on the device);
+      * each Newton step: FP64 residual f and right-hand side -J^T f, FP32
+        PCG to `rtol` (device-side step scalars; one host read of |r| per
+        `check` iterations), FP64 update of the fields.
+
+    The operator must carry the pressure pin term (NsCavityOperator(...,
+    pin=(i, j))): it removes the constant-pressure null space, so J^T J is
+    definite on every level.  Forward solutions equal those with the pinned
+    continuity row (p[pin] = 0); compare pressures up to a constant with the
+    reference, which leaves the constant free."""
+
+    def __init__(self, kernels, omega=0.5, pre=3, post=3, nmin=4, check=2):
+        if kernels.op.pin is None:
+            raise ValueError("NsMultigridNewton needs the pressure pin term: "
+                             "NsCavityOperator(..., pin=(i, j))")
+        self.k = kernels
+        self.n = n = kernels.n
+        self.neq = kernels.neq
+        self.omega, self.pre, self.post = float(omega), int(pre), int(post)
+        self.check = max(1, int(check))
+        dev = kernels.device
+        f32 = dict(dtype=torch.float32, device=dev)
+        self.coef64 = torch.empty((self.neq, 15, n, n), dtype=torch.float64,
+                                  device=dev)
+        self.coef32 = torch.empty((self.neq, 15, n, n), **f32)
+        self.w32 = torch.empty((self.neq, n, n), **f32)
+        self.w64 = torch.empty((self.neq, n, n), dtype=torch.float64,
+                               device=dev)
+        self.b64 = torch.empty((3, n, n), dtype=torch.float64, device=dev)
+        sizes = [n]
+        while sizes[-1] % 2 == 0 and sizes[-1] // 2 >= nmin:
+            sizes.append(sizes[-1] // 2)
+        if 3 * sizes[-1]**2 > 1024:
+            raise ValueError("cavity side %d: the coarsest multigrid level "
+                             "(%d) is too large for the dense solve; use a "
+                             "side of the form m 2^k with m <= 18" %
+                             (n, sizes[-1]))
+        self.levels = []
+        for m in sizes:
+            L = _MgLevel()
+            L.n = m
+            L.A = torch.empty((9, 25, m, m), **f32)
+            L.dinv = torch.empty((9, m, m), **f32)
+            for name in ("x", "x2", "b", "r", "e"):
+                setattr(L, name, torch.empty((3, m, m), **f32))
+            self.levels.append(L)
+        last = self.levels[-1]
+        K = 3 * last.n**2
+        last.minv = torch.empty((K, K), dtype=torch.float64, device=dev)
+        # PCG vectors and device scalars.
+        from . import vec
+        self.md = vec.MultiDot(3 * n * n, 1, 2, device=dev)
+        self.x, self.r, self.z, self.p, self.q = [
+            torch.empty((3, n, n), **f32) for _ in range(5)]
+        self.sc = torch.zeros(4, dtype=torch.float64, device=dev)
+        self._graph = None
+        self.stats = []
+
+    # -- operators ---------------------------------------------------------
+    def _fine_apply(self, x, out, b=None, mode=0, xin=None):
+        st = stream_handle()
+        call("odil_nsmg_jx_f32", self.n, self.neq, ptr(self.coef32), ptr(x),
+             ptr(self.w32), st)
+        call("odil_nsmg_jtw_f32", self.n, self.neq, ptr(self.coef32),
+             ptr(self.w32), ptr(b), ptr(xin), ptr(self.levels[0].dinv),
+             ptr(out), self.omega, mode, st)
+        return out
+
+    def setup(self):
+        """Coefficients at the current state (call `linearize` first): FP32
+        copy, explicit fine J^T J, Galerkin hierarchy, coarsest inverse."""
+        st = stream_handle()
+        self.coef32.copy_(self.coef64)
+        L0 = self.levels[0]
+        call("odil_nsmg_fine_ata", self.n, self.neq, ptr(self.coef32),
+             ptr(L0.A), ptr(L0.dinv), st)
+        for L, C in zip(self.levels[:-1], self.levels[1:]):
+            call("odil_nsmg_galerkin", L.n, ptr(L.A), ptr(C.A), ptr(C.dinv), st)
+        last = self.levels[-1]
+        call("odil_nsmg_coarse_inverse", last.n, ptr(last.A), ptr(last.minv),
+             st)
+
+    def _smooth(self, lvl, x, b, out, mode):
+        L = self.levels[lvl]
+        if lvl == 0:
+            return self._fine_apply(x, out, b=b, mode=mode, xin=x)
+        call("odil_nsmg_smooth", L.n, ptr(L.A), ptr(L.dinv), ptr(x), ptr(b),
+             ptr(out), self.omega, mode, stream_handle())
+        return out
+
+    def vcycle(self, b, out, lvl=0):
+        """out = V(b): one V-cycle from zero on level `lvl` (FP32)."""
+        L = self.levels[lvl]
+        st = stream_handle()
+        if lvl == len(self.levels) - 1:
+            call("odil_nsmg_coarse_apply", L.n, ptr(L.minv), ptr(b), ptr(out),
+                 st)
+            return out
+        cur, nxt = L.x, L.x2
+        call("odil_nsmg_jacobi0", L.n, ptr(L.dinv), ptr(b), ptr(cur),
+             self.omega, st)
+        for _ in range(self.pre - 1):
+            self._smooth(lvl, cur, b, nxt, 2)
+            cur, nxt = nxt, cur
+        self._smooth(lvl, cur, b, L.r, 1)
+        C = self.levels[lvl + 1]
+        call("odil_nsmg_restrict", L.n, ptr(L.r), ptr(C.b), st)
+        self.vcycle(C.b, C.e, lvl + 1)
+        call("odil_nsmg_prolong_add", L.n, ptr(C.e), ptr(cur), st)
+        for k in range(self.post):
+            dst = out if k == self.post - 1 else nxt
+            self._smooth(lvl, cur, b, dst, 2)
+            cur, nxt = dst, cur
+        if self.post == 0:
+            out.copy_(cur)
+        return out
+
+    def apply_normal(self, x, out):
+        """out = J^T J x in FP32 (matrix-free)."""
+        return self._fine_apply(x, out, mode=0)
+
+    # -- PCG ---------------------------------------------------------------
+    def _iteration(self):
+        """One PCG iteration on the device (q = A p, alpha, x, r, z = V(r),
+        beta, p); returns nothing, dots of r kept in self.md.out."""
+        st = stream_handle()
+        N = 3 * self.n * self.n
+        fl = lambda a: a.reshape(-1)
+        self.apply_normal(self.p, self.q)
+        d = self.md(fl(self.p), 1, [fl(self.q)])
+        call("odil_pcg_scalars", ptr(d), ptr(self.sc), 0, st)
+        call("odil_pcg_update_xr", N, ptr(self.x), ptr(self.r), ptr(self.p),
+             ptr(self.q), ptr(self.sc), st)
+        self.vcycle(self.r, self.z)
+        d = self.md(fl(self.r), 1, [fl(self.z), fl(self.r)])
+        self.rr.copy_(d[0, 1:2])
+        call("odil_pcg_scalars", ptr(d), ptr(self.sc), 1, st)
+        call("odil_pcg_update_p", N, ptr(self.p), ptr(self.z), ptr(self.sc),
+             st)
+
+    def _graphs(self):
+        if self._graph is not None:
+            return self._graph
+        dev = self.k.device
+        self.rr = torch.zeros(1, dtype=torch.float64, device=dev)
+        self._iteration()  # warm-up outside capture
+        torch.cuda.synchronize(dev)
+        side = torch.cuda.Stream(dev)
+        side.wait_stream(torch.cuda.current_stream(dev))
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, stream=side):
+            for _ in range(self.check):
+                self._iteration()
+        torch.cuda.current_stream(dev).wait_stream(side)
+        self._graph = g
+        return g
+
+    def pcg(self, b32, rtol=1e-2, maxit=500):
+        """x ~= (J^T J)^-1 b32 by PCG from zero to |r| <= rtol |b|; returns
+        the iteration count.  Uses the hierarchy of the last setup()."""
+        st = stream_handle()
+        fl = lambda a: a.reshape(-1)
+        self.x.zero_()
+        self.r.copy_(b32)
+        nb = float(self.md(fl(b32), 1, [fl(b32)])[0, 0])**0.5
+        if not math.isfinite(nb):
+            raise FloatingPointError("PCG: non-finite right-hand side")
+        if nb == 0.0:
+            return 0
+        self.vcycle(self.r, self.z)
+        d = self.md(fl(self.r), 1, [fl(self.z)])
+        call("odil_pcg_scalars", ptr(d), ptr(self.sc), 2, st)
+        self.p.copy_(self.z)
+        first = self._graph is None
+        g = self._graphs()  # its first build runs one iteration eagerly
+        it = 1 if first else 0
+        while it < maxit:
+            g.replay()
+            it += self.check
+            rn = float(self.rr.item())**0.5
+            if not math.isfinite(rn):
+                raise FloatingPointError("PCG: non-finite residual")
+            if rn <= rtol * nb:
+                break
+        return it
+
+    # -- Newton ------------------------------------------------------------
+    def linearize(self, u, v, p):
+        q = ctypes.byref(self.k.params[torch.float64])
+        call("odil_ns_jacobian_f64", q, ptr(u), ptr(v), ptr(p),
+             ptr(self.coef64), stream_handle())
+
+    def step(self, u, v, p, rtol=1e-2, maxit=500, f=None):
+        """One (Gauss-)Newton step in place; returns the loss
+        sum_e mean(f_e^2) of the state before the step (FP64).  `f`: the
+        FP64 residual at the state, if already computed."""
+        f = self.k.residual(u, v, p) if f is None else f
+        loss = float((f**2).mean(dim=(1, 2)).sum())
+        rms = float(torch.sqrt((f[:3]**2).mean()))
+        self.linearize(u, v, p)
+        # -J^T f in FP64 from the FP64 coefficients.
+        call("odil_nsmg_jtw_f64", self.n, self.neq, ptr(self.coef64), ptr(f),
+             ptr(self.b64), stream_handle())
+        self.setup()
+        b32 = self.levels[0].b
+        b32.copy_(self.b64)
+        b32.neg_()
+        its = self.pcg(b32, rtol=rtol, maxit=maxit)
+        self.stats.append({"loss": loss, "rms": rms, "pcg": its})
+        u += self.x[0]
+        v += self.x[1]
+        p += self.x[2]
+        return loss
+
+    def solve(self, u, v, p, epochs=100, tol=1e-10, rtol=1e-2, callback=None):
+        """(Gauss-)Newton epochs until the rms of the three flow terms is at
+        most `tol` (checked before each step) or `epochs` steps are done;
+        returns the final loss."""
+        for ep in range(epochs):
+            f = self.k.residual(u, v, p)
+            if float(torch.sqrt((f[:3]**2).mean())) <= tol:
+                break
+            self.step(u, v, p, rtol=rtol, f=f)
+            if callback is not None:
+                callback(ep, self.stats[-1])
+        f = self.k.residual(u, v, p)
+        self.final_rms = float(torch.sqrt((f[:3]**2).mean()))
         return float((f**2).mean(dim=(1, 2)).sum())

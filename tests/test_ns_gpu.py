@@ -222,7 +222,17 @@ def test_inverse_solution_is_stationary_for_oracle_loss(cuda):
     k = _kernels(n, 400.0, kw, cuda)
     t = [torch.zeros((n, n), dtype=torch.float64, device=cuda)
          for _ in range(3)]
-    NsGaussNewton(k).solve(*t, epochs=10, rtol=1e-6)
+    # Gauss-Newton with the tape Jacobian converges linearly (the frozen
+    # deferred-correction part is not differentiated, as in the reference):
+    # run it until the GPU's loss gradient has fallen by 1e-7.
+    gn = NsGaussNewton(k)
+    gnorm = lambda: float(torch.sqrt(sum((x**2).sum() for x in
+                                         k.loss_grad(*t)[1])))
+    g_start = gnorm()
+    for _ in range(80):
+        gn.step(*t, rtol=1e-6)
+        if gnorm() <= 1e-7 * g_start:
+            break
     s = NS.NsSetup(n, 400.0, mask=mask, u_imp=kw["u_imp"],
                    v_imp=kw["v_imp"], kreg=1e-4)
     _, l0, g0 = NS.loss_grad_live(s, {c: np.zeros((n, n)) for c in "uvp"})
