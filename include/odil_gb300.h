@@ -663,6 +663,43 @@ int odil_lincomb_f64(double* out, const double* x, const double* M,
                      int64_t ld, int k, const double* coef, int64_t n,
                      void* stream);
 
+/* L-BFGS with the compact-form algebra on the device (replaces the host
+ * side of optimizer.py:61-99, scipy's fmin_l_bfgs_b two-loop and line-search
+ * driver; the state layout is documented in csrc/lbfgs.cu):
+ *   coef: coef[0 .. gidx] of d = -H_k g = sum_{row < gidx} coef[row] H[row]
+ *         + coef[gidx] g from the held pairs (compact representation);
+ *   trial: xt = x + a d, a = 1 (or min(1, 1/|g|) with no pair held),
+ *          phi'(0) = dots[0] recorded;
+ *   accept: the Wolfe / approximate-Wolfe test of the trial -> sc[6];
+ *   pair: s = a d, y = g_trial - g into sy[0:n], sy[n:2n] (accepted only);
+ *   update: ring, S^T Y, Y^T Y, gamma and the dots with the new gradient
+ *           from P ([rows][3] dots of H's rows with (g_trial, s, y)) and
+ *           Q ([[s.y, s.g_trial], [y.y, y.g_trial]]);
+ *   commit: H rows of the updated slot <- (s, y). */
+int odil_lbfgs_coef(int32_t m, int32_t gidx, const int* ring, const double* SY,
+                    const double* YY, const double* dg, const double* sc,
+                    double* coef, void* stream);
+int odil_lbfgs_trial_f32(int64_t n, float* xt, const float* x, const float* d,
+                         const double* dots, const int* ring, double* sc,
+                         void* stream);
+int odil_lbfgs_trial_f64(int64_t n, double* xt, const double* x,
+                         const double* d, const double* dots, const int* ring,
+                         double* sc, void* stream);
+int odil_lbfgs_accept(const double* ft, const double* dpa, double* sc,
+                      void* stream);
+int odil_lbfgs_pair_f32(int64_t n, float* sy, const float* d, const float* gt,
+                        const float* g, const double* sc, void* stream);
+int odil_lbfgs_pair_f64(int64_t n, double* sy, const double* d,
+                        const double* gt, const double* g, const double* sc,
+                        void* stream);
+int odil_lbfgs_update(int* ring, double* SY, double* YY, double* dg,
+                      double* sc, const double* P, int32_t rows,
+                      const double* Q, void* stream);
+int odil_lbfgs_commit_f32(int64_t n, float* H, int64_t ld, const float* sy,
+                          const int* ring, const double* sc, void* stream);
+int odil_lbfgs_commit_f64(int64_t n, double* H, int64_t ld, const double* sy,
+                          const int* ring, const double* sc, void* stream);
+
 /* ------------------------------------------------------------------------
  * Multigrid decomposition of a field: the field is the sum over levels l of
  * the level-l weights refined l times.

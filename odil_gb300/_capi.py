@@ -217,6 +217,17 @@ SIGNATURES = {
     "odil_pcg_scalars": (_INT, [_P, _P, ctypes.c_int32, _P]),
     "odil_pcg_update_xr": (_INT, [_I64, _P, _P, _P, _P, _P, _P]),
     "odil_pcg_update_p": (_INT, [_I64, _P, _P, _P, _P]),
+    "odil_lbfgs_coef": (_INT, [ctypes.c_int32, ctypes.c_int32, _P, _P, _P, _P,
+                               _P, _P, _P]),
+    "odil_lbfgs_trial_f32": (_INT, [_I64, _P, _P, _P, _P, _P, _P, _P]),
+    "odil_lbfgs_trial_f64": (_INT, [_I64, _P, _P, _P, _P, _P, _P, _P]),
+    "odil_lbfgs_accept": (_INT, [_P, _P, _P, _P]),
+    "odil_lbfgs_pair_f32": (_INT, [_I64, _P, _P, _P, _P, _P, _P]),
+    "odil_lbfgs_pair_f64": (_INT, [_I64, _P, _P, _P, _P, _P, _P]),
+    "odil_lbfgs_update": (_INT, [_P, _P, _P, _P, _P, _P, ctypes.c_int32, _P,
+                                 _P]),
+    "odil_lbfgs_commit_f32": (_INT, [_I64, _P, _I64, _P, _P, _P, _P]),
+    "odil_lbfgs_commit_f64": (_INT, [_I64, _P, _I64, _P, _P, _P, _P]),
     "odil_ns_num_equations": (_INT, [_P]),
     "odil_ns_residual_f32": (_INT, [_P, _P, _P, _P, _P, _P]),
     "odil_ns_residual_f64": (_INT, [_P, _P, _P, _P, _P, _P]),

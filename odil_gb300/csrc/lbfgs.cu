@@ -1,0 +1,317 @@
+// L-BFGS in the compact representation (Byrd, Nocedal and Schnabel 1994;
+// Nocedal & Wright eq. 7.24) with its small algebra on the device, so that
+// an iteration whose first trial step satisfies the Wolfe conditions needs
+// no host round trip but the one read of its status.  Replaces the host side
+// of the reference's L-BFGS driver (optimizer.py:61-99: scipy's
+// fmin_l_bfgs_b, m = 50, maxls = 50, pgtol = 1e-16, factr = 0, no bounds).
+//
+// Device state (caller-owned):
+//   ring  int32[4]: [0] k pairs held, [1] head (slot of the oldest pair),
+//         [2] m, [3] slot written by the last update (-1: none)
+//   SY, YY  FP64[m][m] by slot: SY[a][b] = s_a . y_b, YY[a][b] = y_a . y_b
+//   dg    FP64[2m]: dg[2 j] = s_j . g, dg[2 j + 1] = y_j . g at the iterate
+//   sc    FP64[16]: [0] f, [1] gamma, [2] phi'(0) = g . d, [3] trial step,
+//         [4] f at the trial, [5] phi'(step) = g_trial . d, [6] status
+//         (0 accepted, 1 rejected: the host line search takes over,
+//         2 d is not a descent direction), [7] c1, [8] c2, [9] eps (the
+//         approximate-Wolfe tolerance of phi(0) relative), [10] first-step
+//         flag (1: the trial is the steepest-descent step min(1, 1/|g|))
+// Pairs: rows 2 j (s_j) and 2 j + 1 (y_j) of H [2m][n]; the pair of order
+// c (0 = oldest) lives in slot (head + c) mod m.
+#include "common.cuh"
+
+namespace odil {
+namespace {
+
+constexpr int LT = 256;
+constexpr int kMaxM = 128;
+
+// coef[gidx + 1] of d = sum_{row < gidx} coef[row] H[row] + coef[gidx] g =
+// -H_k g; gidx (even, 2 <= gidx <= 2m) covers every held slot.
+__global__ void __launch_bounds__(32) lbfgs_coef_kernel(int gidx, const int* __restrict__ ring,
+                                                        const double* __restrict__ SY,
+                                                        const double* __restrict__ YY,
+                                                        const double* __restrict__ dg,
+                                                        const double* __restrict__ sc,
+                                                        double* __restrict__ coef) {
+    __shared__ double a[kMaxM], b[kMaxM], t[kMaxM], w[kMaxM], p[kMaxM];
+    __shared__ int slot[kMaxM];
+    const int lane = threadIdx.x;
+    const int k = ring[0], head = ring[1], m = ring[2];
+    for (int r = lane; r <= gidx; r += 32) coef[r] = 0.0;
+    __syncwarp();
+    if (k == 0) {
+        if (lane == 0) coef[gidx] = -1.0;
+        return;
+    }
+    const double gamma = sc[1];
+    for (int c = lane; c < k; c += 32) {
+        const int j = (head + c) % m;
+        slot[c] = j;
+        a[c] = dg[2 * j];
+        b[c] = dg[2 * j + 1];
+    }
+    __syncwarp();
+    // t = R^-1 a, R = triu(S^T Y) in pair order (backward substitution).
+    for (int r = k - 1; r >= 0; --r) {
+        double s = 0.0;
+        for (int c = r + 1 + lane; c < k; c += 32) s += SY[slot[r] * m + slot[c]] * t[c];
+        s = warp_sum(s);
+        if (lane == 0) t[r] = (a[r] - s) / SY[slot[r] * m + slot[r]];
+        __syncwarp();
+    }
+    // w = (D + gamma Y^T Y) t - gamma b
+    for (int c = lane; c < k; c += 32) {
+        double s = SY[slot[c] * m + slot[c]] * t[c];
+        for (int e = 0; e < k; ++e) s += gamma * YY[slot[c] * m + slot[e]] * t[e];
+        w[c] = s - gamma * b[c];
+    }
+    __syncwarp();
+    // p = R^-T w (forward substitution)
+    for (int r = 0; r < k; ++r) {
+        double s = 0.0;
+        for (int c = lane; c < r; c += 32) s += SY[slot[c] * m + slot[r]] * p[c];
+        s = warp_sum(s);
+        if (lane == 0) p[r] = (w[r] - s) / SY[slot[r] * m + slot[r]];
+        __syncwarp();
+    }
+    for (int c = lane; c < k; c += 32) {
+        coef[2 * slot[c]] = -p[c];
+        coef[2 * slot[c] + 1] = gamma * t[c];
+    }
+    if (lane == 0) coef[gidx] = -gamma;
+}
+
+// xt = x + a d with the trial step a chosen on the device from phi'(0) =
+// dots[0]: the steepest-descent step min(1, 1/|g|) while no pair is held,
+// else 1.  Block 0 records phi'(0) and a.
+template <typename T>
+__global__ void __launch_bounds__(LT) lbfgs_trial_kernel(int64_t n, T* __restrict__ xt,
+                                                         const T* __restrict__ x,
+                                                         const T* __restrict__ d,
+                                                         const double* __restrict__ dots,
+                                                         const int* __restrict__ ring,
+                                                         double* __restrict__ sc) {
+    const double dphi0 = dots[0];
+    double a = 1.0;
+    if (ring[0] == 0) {
+        const double gn = sqrt(fmax(-dphi0, 0.0));
+        a = fmin(1.0, 1.0 / fmax(gn, 1e-300));
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        sc[2] = dphi0;
+        sc[3] = a;
+        sc[10] = ring[0] == 0 ? 1.0 : 0.0;
+    }
+    const T at = (T)a;
+    const int64_t stride = (int64_t)gridDim.x * LT;
+    for (int64_t i = (int64_t)blockIdx.x * LT + threadIdx.x; i < n; i += stride)
+        xt[i] = x[i] + at * d[i];
+}
+
+// The Wolfe test of the trial (phi(a) <= phi(0) + c1 a phi'(0) and phi'(a) >=
+// c2 phi'(0)), or the approximate Wolfe conditions of Hager and Zhang
+// (phi(a) <= phi(0) + eps |phi(0)|, c2 phi'(0) <= phi'(a) <= (2 c1 - 1)
+// phi'(0)), as the host line search accepts a step.
+__global__ void lbfgs_accept_kernel(const double* __restrict__ ft,
+                                    const double* __restrict__ dpa_dots,
+                                    double* __restrict__ sc) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const double f0 = sc[0], dphi0 = sc[2], a = sc[3], c1 = sc[7], c2 = sc[8];
+    const double fa = ft[0], dpa = dpa_dots[0];
+    const double eps = sc[9] * fabs(f0);
+    sc[4] = fa;
+    sc[5] = dpa;
+    double status;
+    if (!(dphi0 < 0.0)) {
+        status = 2.0;
+    } else if (!isfinite(fa) || !isfinite(dpa) || dpa < c2 * dphi0) {
+        status = 1.0;
+    } else if (fa <= f0 + c1 * a * dphi0) {
+        status = 0.0;
+    } else if (fa <= f0 + eps && dpa <= (2.0 * c1 - 1.0) * dphi0) {
+        status = 0.0;
+    } else {
+        status = 1.0;
+    }
+    sc[6] = status;
+}
+
+// The new pair s = a d, y = g_trial - g into rows 0 and 1 of sy (accepted
+// trials only).
+template <typename T>
+__global__ void __launch_bounds__(LT) lbfgs_pair_kernel(int64_t n, T* __restrict__ sy,
+                                                        const T* __restrict__ d,
+                                                        const T* __restrict__ gt,
+                                                        const T* __restrict__ g,
+                                                        const double* __restrict__ sc) {
+    if (sc[6] != 0.0) return;
+    const T a = (T)sc[3];
+    const int64_t stride = (int64_t)gridDim.x * LT;
+    for (int64_t i = (int64_t)blockIdx.x * LT + threadIdx.x; i < n; i += stride) {
+        sy[i] = a * d[i];
+        sy[n + i] = gt[i] - g[i];
+    }
+}
+
+// Ring and matrix update after an accepted step.  P: [rows][3] dots of the
+// stored rows with (g_trial, s, y); Q: [2][2] = [[s.y, s.g_trial],
+// [y.y, y.g_trial]].  The pair is kept when s.y > 1e-12 y.y (the curvature
+// condition, as the host version); the dots with g_trial become dg.
+__global__ void __launch_bounds__(32) lbfgs_update_kernel(int* __restrict__ ring,
+                                                          double* __restrict__ SY,
+                                                          double* __restrict__ YY,
+                                                          double* __restrict__ dg,
+                                                          double* __restrict__ sc,
+                                                          const double* __restrict__ P, int rows,
+                                                          const double* __restrict__ Q) {
+    __shared__ int s_slot;
+    const int lane = threadIdx.x;
+    if (sc[6] != 0.0) return;
+    const int k = ring[0], head = ring[1], m = ring[2];
+    const double sy = Q[0], sgt = Q[1], yy = Q[2], ygt = Q[3];
+    // dots of the held pairs with the new gradient
+    for (int r = lane; r < 2 * m; r += 32) dg[r] = r < rows ? P[r * 3] : 0.0;
+    __syncwarp();
+    if (lane == 0) {
+        s_slot = -1;
+        if (isfinite(sy) && isfinite(yy) && sy > 1e-12 * yy) {
+            int slot;
+            if (k < m) {
+                slot = (head + k) % m;
+                ring[0] = k + 1;
+            } else {
+                slot = head;
+                ring[1] = (head + 1) % m;
+            }
+            s_slot = slot;
+            sc[1] = sy / yy;
+        }
+        ring[3] = s_slot;
+        sc[0] = sc[4];
+    }
+    __syncwarp();
+    const int slot = s_slot;
+    if (slot < 0) return;
+    const int k2 = ring[0], head2 = ring[1];
+    for (int c = lane; c < k2; c += 32) {
+        const int j = (head2 + c) % m;
+        if (j == slot) continue;
+        SY[slot * m + j] = P[(2 * j + 1) * 3 + 1];  // s_new . y_j
+        SY[j * m + slot] = P[(2 * j) * 3 + 2];      // s_j . y_new
+        const double v = P[(2 * j + 1) * 3 + 2];    // y_j . y_new
+        YY[slot * m + j] = v;
+        YY[j * m + slot] = v;
+    }
+    if (lane == 0) {
+        SY[slot * m + slot] = sy;
+        YY[slot * m + slot] = yy;
+        dg[2 * slot] = sgt;
+        dg[2 * slot + 1] = ygt;
+    }
+}
+
+// H rows of the slot written by the last update <- (s, y) (accepted only).
+template <typename T>
+__global__ void __launch_bounds__(LT) lbfgs_commit_kernel(int64_t n, T* __restrict__ H, int64_t ld,
+                                                          const T* __restrict__ sy,
+                                                          const int* __restrict__ ring,
+                                                          const double* __restrict__ sc) {
+    const int slot = ring[3];
+    if (sc[6] != 0.0 || slot < 0) return;
+    T* hs = H + (int64_t)(2 * slot) * ld;
+    T* hy = hs + ld;
+    const int64_t stride = (int64_t)gridDim.x * LT;
+    for (int64_t i = (int64_t)blockIdx.x * LT + threadIdx.x; i < n; i += stride) {
+        hs[i] = sy[i];
+        hy[i] = sy[n + i];
+    }
+}
+
+inline unsigned lgrid(int64_t n) {
+    int64_t b = (n + LT - 1) / LT;
+    const int64_t cap = 152 * 8;
+    return (unsigned)(b < 1 ? 1 : (b > cap ? cap : b));
+}
+
+template <typename T>
+int trial_impl(int64_t n, T* xt, const T* x, const T* d, const double* dots, const int* ring,
+               double* sc, void* stream) {
+    if (n < 1) return ODIL_ERR_SHAPE;
+    if (!xt || !x || !d || !dots || !ring || !sc) return ODIL_ERR_ARG;
+    lbfgs_trial_kernel<T><<<lgrid(n), LT, 0, as_stream(stream)>>>(n, xt, x, d, dots, ring, sc);
+    return launch_status();
+}
+
+template <typename T>
+int pair_impl(int64_t n, T* sy, const T* d, const T* gt, const T* g, const double* sc,
+              void* stream) {
+    if (n < 1) return ODIL_ERR_SHAPE;
+    if (!sy || !d || !gt || !g || !sc) return ODIL_ERR_ARG;
+    lbfgs_pair_kernel<T><<<lgrid(n), LT, 0, as_stream(stream)>>>(n, sy, d, gt, g, sc);
+    return launch_status();
+}
+
+template <typename T>
+int commit_impl(int64_t n, T* H, int64_t ld, const T* sy, const int* ring, const double* sc,
+                void* stream) {
+    if (n < 1 || ld < n) return ODIL_ERR_SHAPE;
+    if (!H || !sy || !ring || !sc) return ODIL_ERR_ARG;
+    lbfgs_commit_kernel<T><<<lgrid(n), LT, 0, as_stream(stream)>>>(n, H, ld, sy, ring, sc);
+    return launch_status();
+}
+
+}  // namespace
+}  // namespace odil
+
+using namespace odil;
+
+ODIL_API int odil_lbfgs_coef(int32_t m, int32_t gidx, const int* ring, const double* SY,
+                             const double* YY, const double* dg, const double* sc, double* coef,
+                             void* stream) {
+    if (m < 1 || m > kMaxM || gidx < 2 || gidx > 2 * m || gidx % 2) return ODIL_ERR_SHAPE;
+    if (!ring || !SY || !YY || !dg || !sc || !coef) return ODIL_ERR_ARG;
+    lbfgs_coef_kernel<<<1, 32, 0, as_stream(stream)>>>(gidx, ring, SY, YY, dg, sc, coef);
+    return launch_status();
+}
+
+ODIL_API int odil_lbfgs_trial_f32(int64_t n, float* xt, const float* x, const float* d,
+                                  const double* dots, const int* ring, double* sc, void* stream) {
+    return trial_impl<float>(n, xt, x, d, dots, ring, sc, stream);
+}
+ODIL_API int odil_lbfgs_trial_f64(int64_t n, double* xt, const double* x, const double* d,
+                                  const double* dots, const int* ring, double* sc, void* stream) {
+    return trial_impl<double>(n, xt, x, d, dots, ring, sc, stream);
+}
+
+ODIL_API int odil_lbfgs_accept(const double* ft, const double* dpa, double* sc, void* stream) {
+    if (!ft || !dpa || !sc) return ODIL_ERR_ARG;
+    lbfgs_accept_kernel<<<1, 32, 0, as_stream(stream)>>>(ft, dpa, sc);
+    return launch_status();
+}
+
+ODIL_API int odil_lbfgs_pair_f32(int64_t n, float* sy, const float* d, const float* gt,
+                                 const float* g, const double* sc, void* stream) {
+    return pair_impl<float>(n, sy, d, gt, g, sc, stream);
+}
+ODIL_API int odil_lbfgs_pair_f64(int64_t n, double* sy, const double* d, const double* gt,
+                                 const double* g, const double* sc, void* stream) {
+    return pair_impl<double>(n, sy, d, gt, g, sc, stream);
+}
+
+ODIL_API int odil_lbfgs_update(int* ring, double* SY, double* YY, double* dg, double* sc,
+                               const double* P, int32_t rows, const double* Q, void* stream) {
+    if (rows < 0) return ODIL_ERR_SHAPE;
+    if (!ring || !SY || !YY || !dg || !sc || !Q || (rows > 0 && !P)) return ODIL_ERR_ARG;
+    lbfgs_update_kernel<<<1, 32, 0, as_stream(stream)>>>(ring, SY, YY, dg, sc, P, rows, Q);
+    return launch_status();
+}
+
+ODIL_API int odil_lbfgs_commit_f32(int64_t n, float* H, int64_t ld, const float* sy,
+                                   const int* ring, const double* sc, void* stream) {
+    return commit_impl<float>(n, H, ld, sy, ring, sc, stream);
+}
+ODIL_API int odil_lbfgs_commit_f64(int64_t n, double* H, int64_t ld, const double* sy,
+                                   const int* ring, const double* sc, void* stream) {
+    return commit_impl<double>(n, H, ld, sy, ring, sc, stream);
+}

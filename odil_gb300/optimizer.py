@@ -91,6 +91,118 @@ class LbfgsOptimizer(Optimizer):
 
     def run(self, x0, loss_grad, epochs=None, callback=None, epoch_start=0,
             **kwargs):
+        """The device form (`run_device`) for CUDA vectors and m <= 128;
+        the host-algebra form (`run_host`) otherwise."""
+        if x0.is_cuda and self.m <= 128 and x0.dtype in (torch.float32,
+                                                         torch.float64):
+            return self.run_device(x0, loss_grad, epochs, callback,
+                                   epoch_start)
+        return self.run_host(x0, loss_grad, epochs, callback, epoch_start)
+
+    def run_device(self, x0, loss_grad, epochs=None, callback=None,
+                   epoch_start=0):
+        """The same iteration with the compact-form algebra, the first trial
+        step, its Wolfe test and the pair/ring update on the device
+        (csrc/lbfgs.cu): per iteration one direction (coefficient kernel +
+        one linear combination), one loss+gradient at the trial point, one
+        multi-dot of the stored rows with (g_new, s, y), and one host read of
+        the 16 scalars (the status).  A trial that fails the Wolfe test
+        (rare once pairs are held) falls back to the host line search from
+        the same state."""
+        from ._capi import call, ptr, stream_handle
+        x = x0.detach().clone()
+        n = x.numel()
+        dev = x.device
+        m = self.m
+        sfx = "f32" if x.dtype == torch.float32 else "f64"
+        H = torch.zeros((2 * m, n), dtype=x.dtype, device=dev)
+        SYp = torch.zeros((2, n), dtype=x.dtype, device=dev)
+        md = vec.MultiDot(n, 2 * m, 3, device=dev)
+        md1 = vec.MultiDot(n, 1, 1, device=dev)
+        md2 = vec.MultiDot(n, 2, 2, device=dev)
+        coef = torch.zeros(2 * m + 1, dtype=torch.float64, device=dev)
+        ring = torch.tensor([0, 0, m, -1], dtype=torch.int32, device=dev)
+        SY = torch.zeros((m, m), dtype=torch.float64, device=dev)
+        YY = torch.zeros((m, m), dtype=torch.float64, device=dev)
+        dg = torch.zeros(2 * m, dtype=torch.float64, device=dev)
+        sc = torch.zeros(16, dtype=torch.float64, device=dev)
+        sc_host = torch.zeros(16, dtype=torch.float64).pin_memory()
+        d = torch.empty_like(x)
+        xt = torch.empty_like(x)
+        self.epoch = epoch_start
+        loss, g, res = loss_grad(x, self.epoch)
+        g = g.detach().clone()
+        self.evals += 1
+        eps = 1e-6 if x.dtype == torch.float32 else 1e-12
+        sc[0] = loss.double() if isinstance(loss, torch.Tensor) else float(loss)
+        sc[1] = 1.0
+        sc[7], sc[8], sc[9] = self.c1, self.c2, eps
+        self.last_loss, self.last_residual = float(sc[0]), res
+        info = Namespace(epochs=0, evals=1, task="", fallbacks=0)
+        epochs = epochs if epochs is not None else 1 << 30
+        accepted = 0  # upper bound of the pairs held: rows the dots need
+        st = stream_handle()
+        it = 0
+        while it < epochs:
+            rows = 2 * min(accepted, m)
+            if rows:
+                call("odil_lbfgs_coef", m, rows, ptr(ring), ptr(SY), ptr(YY),
+                     ptr(dg), ptr(sc), ptr(coef), st)
+                vec.lincomb(d, g, H, rows, coef)
+            else:
+                vec.axpby(d, -1.0, g, 0.0, g)
+            dots = md1(g, 1, [d])
+            call("odil_lbfgs_trial_" + sfx, n, ptr(xt), ptr(x), ptr(d),
+                 ptr(dots), ptr(ring), ptr(sc), st)
+            ft, gt, res = loss_grad(xt, self.epoch)
+            self.evals += 1
+            ft_dev = ft.reshape(1).double() if isinstance(ft, torch.Tensor) \
+                else torch.tensor([float(ft)], dtype=torch.float64, device=dev)
+            dpa = md1(gt, 1, [d])
+            call("odil_lbfgs_accept", ptr(ft_dev), ptr(dpa), ptr(sc), st)
+            sc_host.copy_(sc, non_blocking=True)
+            torch.cuda.current_stream(dev).synchronize()
+            status = int(sc_host[6])
+            if status == 2:
+                # Not a descent direction: restart from steepest descent.
+                if int(ring[0].item()) == 0:
+                    info.task = "CONVERGENCE: zero gradient"
+                    break
+                ring.copy_(torch.tensor([0, 0, m, -1], dtype=torch.int32))
+                continue
+            if status == 1:
+                info.fallbacks += 1
+                f0 = float(sc_host[0])
+                dphi0 = float(sc_host[2])
+                ok, alpha, fa, gt = self._line_search(
+                    x, d, xt, f0, dphi0, float(sc_host[3]), loss_grad, md1)
+                if not ok:
+                    info.task = "ABNORMAL_TERMINATION_IN_LNSRCH"
+                    break
+                sc[3], sc[4], sc[6] = alpha, fa, 0.0
+            call("odil_lbfgs_pair_" + sfx, n, ptr(SYp), ptr(d), ptr(gt), ptr(g),
+                 ptr(sc), st)
+            P = md(H, max(rows, 1), [gt, SYp[0], SYp[1]]) if rows else None
+            Q = md2(SYp, 2, [SYp[1], gt])
+            call("odil_lbfgs_update", ptr(ring), ptr(SY), ptr(YY), ptr(dg),
+                 ptr(sc), ptr(P), rows, ptr(Q), st)
+            call("odil_lbfgs_commit_" + sfx, n, ptr(H), n, ptr(SYp), ptr(ring),
+                 ptr(sc), st)
+            g.copy_(gt)
+            accepted += 1
+            x, xt = xt, x
+            self.last_loss = float(sc_host[4]) if status == 0 else float(fa)
+            self.last_residual = res
+            self.epoch += 1
+            info.epochs += 1
+            it += 1
+            if callback:
+                callback(x, self.epoch, opt=self)
+        info.evals = self.evals
+        return x, info
+
+    def run_host(self, x0, loss_grad, epochs=None, callback=None,
+                 epoch_start=0, **kwargs):
         x = x0.detach().clone()
         n = x.numel()
         dev = x.device

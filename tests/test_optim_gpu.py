@@ -227,3 +227,47 @@ def test_eval_diag_and_jacobi_optimizer(cuda):
     util.optimize_jacobi(args, fused, st,
                          lambda p, e, **kw: losses.append(float(kw["opt"].last_loss)))
     assert np.isfinite(losses).all() and losses[-1] < 0.5 * losses[0]
+
+
+@pytest.mark.parametrize("m", [5, 50])
+def test_device_lbfgs_matches_host_algebra(cuda, m):
+    """The device form of L-BFGS (compact algebra, first trial, Wolfe test
+    and ring update on the GPU) follows the host-algebra form iterate by
+    iterate on the FP64 48^2 wave (ring wrap-around with m = 5)."""
+    from odil_gb300.optimizer import LbfgsOptimizer
+    n = 48
+    inst, prob = _wave_problem(n, cuda)
+
+    def lg(x, epoch):
+        loss, g = prob.kernels.loss_grad(x.reshape(n, n))
+        return loss, g.reshape(-1).clone(), [loss]
+
+    x0 = torch.zeros(n * n, dtype=torch.float64, device=cuda)
+    xd, infod = LbfgsOptimizer(m=m).run_device(x0, lg, epochs=40)
+    xh, infoh = LbfgsOptimizer(m=m).run_host(x0, lg, epochs=40)
+    assert infod.epochs == infoh.epochs == 40
+    ld = prob.kernels.loss_grad(xd.reshape(n, n))[0].item()
+    lh = prob.kernels.loss_grad(xh.reshape(n, n))[0].item()
+    assert abs(ld - lh) <= 1e-8 * lh, (ld, lh)
+    assert float((xd - xh).norm() / xh.norm()) < 1e-6
+
+
+def test_device_lbfgs_one_sync_per_iteration_fp32_1024(cuda):
+    """The 1024^2 FP32 wave through the fused adjoint: 20 device L-BFGS
+    iterations complete with the loss not increasing; the host line search
+    is the exception, not the rule."""
+    from odil_gb300.optimizer import LbfgsOptimizer
+    n = 1024
+    inst, prob = _wave_problem(n, cuda, dtype=np.float32)
+    k = prob.kernels
+
+    def lg(x, epoch):
+        loss, g = k.loss_grad(x.reshape(n, n))
+        return loss, g.reshape(-1), [loss]
+
+    x0 = torch.zeros(n * n, dtype=torch.float32, device=cuda)
+    l0 = k.loss_grad(x0.reshape(n, n))[0].item()
+    x, info = LbfgsOptimizer().run_device(x0, lg, epochs=20)
+    assert info.epochs == 20
+    assert k.loss_grad(x.reshape(n, n))[0].item() <= l0
+    assert info.fallbacks <= 5
