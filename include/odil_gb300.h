@@ -254,6 +254,23 @@ typedef struct odil_wave_batch {
     int64_t total_bnd;
 } odil_wave_batch;
 
+/* Loss and fused adjoint gradient of every instance in one launch (FP32):
+ * loss[i] = mean(f_i^2) over instance i's cells, grad_i = (2/N_i) J_i^T f_i
+ * (util_op.py:627-654 per instance), total = sum_i loss[i] (the loss of the
+ * batch as one optimisation problem).  tile_start [ninst + 1]: first tile of
+ * each instance, tiles of 120 columns x 16 rows numbered instance by
+ * instance (ceil(nx/120) * ceil(nt/16) per instance), ntiles the total;
+ * init_u .. right_u: the packed boundary arrays in FP32; partials: ntiles
+ * doubles of scratch; total may be null.  Requires odil_wave_batch_setup.
+ * The batched form of the per-run loss of vary_wave.py:37-43. */
+int odil_wave_batch_loss_grad_f32(const odil_wave_batch* b,
+                                  const int64_t* tile_start, int64_t ntiles,
+                                  const float* init_u, const float* init_ut,
+                                  const float* left_u, const float* right_u,
+                                  const float* u, float* grad,
+                                  double* partials, double* loss,
+                                  double* total, void* stream);
+
 /* Fills the derived constants of a device descriptor array.
  * Set-up of the batched solver that replaces the per-instance runs of
  * vary_wave.py:37-43; no direct counterpart. */

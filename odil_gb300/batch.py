@@ -89,6 +89,19 @@ class WaveBatch:
         self.ws = torch.zeros(256, dtype=torch.uint8, device=dev)
         self.march_cfg = None
         self.graph = None
+        # Fused loss + gradient of all instances: FP32 boundary data and the
+        # tile table (120-column x 16-row tiles, instance by instance).
+        self.bc32 = [t.float() for t in self.bc]
+        tiles = [((nx + 119) // 120) * ((nt + 15) // 16)
+                 for nt, nx in self.shapes]
+        self.ntiles = int(sum(tiles))
+        self.tile_start = torch.as_tensor(
+            np.concatenate([[0], np.cumsum(tiles)]).astype(np.int64),
+            device=dev)
+        self.lg_partials = torch.zeros(self.ntiles, dtype=torch.float64,
+                                       device=dev)
+        self.loss_inst = torch.zeros(self.n, dtype=torch.float64, device=dev)
+        self.loss_total = torch.zeros(1, dtype=torch.float64, device=dev)
 
     # -- launches -------------------------------------------------------------
     def update_residual(self, u, d, u_out, rhs):
@@ -109,6 +122,47 @@ class WaveBatch:
         call("odil_wave_batch_march_f32", ctypes.byref(self.b), ptr(rhs), ptr(x),
              cfg["threads"], cfg["cpt"], cfg["pf"], cfg["blocks_per_sm"],
              ptr(self.ws), self.ws.numel(), stream_handle())
+
+    def loss_grad(self, u32, grad32):
+        """Per-instance losses mean(f_i^2) (self.loss_inst), their sum
+        (returned, a device scalar) and the fused adjoint gradients
+        (2/N_i) J_i^T f_i into grad32, for the packed FP32 fields u32; one
+        launch over all instances plus one small reduction."""
+        call("odil_wave_batch_loss_grad_f32", ctypes.byref(self.b),
+             ptr(self.tile_start), self.ntiles, *[ptr(t) for t in self.bc32],
+             ptr(u32), ptr(grad32), ptr(self.lg_partials), ptr(self.loss_inst),
+             ptr(self.loss_total), stream_handle())
+        return self.loss_total, grad32
+
+    def lbfgs_warm_start(self, iters=20, m=10):
+        """The FP32 fused-adjoint L-BFGS stage of the batch: L-BFGS on the
+        packed vector for the sum of the instance losses (the instances are
+        independent, so its minimisers are each instance's), from u = 0;
+        returns the FP32 iterate and the optimizer info."""
+        from .optimizer import LbfgsOptimizer
+        grad = torch.empty(self.total, dtype=torch.float32, device=self.device)
+
+        def lg(x, epoch):
+            loss, g = self.loss_grad(x, grad)
+            return loss, g, [loss]
+
+        x0 = torch.zeros(self.total, dtype=torch.float32, device=self.device)
+        return LbfgsOptimizer(m=m).run_device(x0, lg, epochs=iters)
+
+    def refine(self, u0, epochs=2):
+        """Mixed-precision Newton epochs from the FP64 iterate u0 (FP64
+        residual and update, FP32 forward substitution): self.u holds the
+        result."""
+        self.u.copy_(u0)
+        u, ub = self.u, self.ub
+        self.update_residual(u, None, None, self.rhs)
+        for _ in range(epochs):
+            self.march(self.rhs, self.d)
+            self.update_residual(u, self.d, ub, self.rhs)
+            u, ub = ub, u
+        if u is not self.u:
+            self.u.copy_(u)
+        return self.u
 
     def tune(self, cache=True):
         """Chooses the persistent march's launch shape by timing candidates

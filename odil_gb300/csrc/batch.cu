@@ -257,10 +257,95 @@ int launch_batch_march(const odil_wave_batch* b, const float* rhs, float* x, uns
     return launch_status();
 }
 
+// Fused loss + adjoint gradient of every instance in one launch (FP32): one
+// block per tile of the single-instance strip march (lg_strip, 16-row
+// tiles), blocks numbered instance by instance (tile_start: first block of
+// each instance, tile_start[ninst] = total), the instance of a block by
+// binary search.  Each instance's gradient is (2 / N_i) J_i^T f_i, the
+// gradient of its own loss mean(f_i^2); the per-block sums go to partials.
+constexpr int BLG_TY = 16;
+
+__global__ void __launch_bounds__(LG_WARPS * 32) batch_loss_grad_kernel(
+    const odil_wave_instance* __restrict__ inst, int ninst,
+    const int64_t* __restrict__ tile_start, const float* __restrict__ iu,
+    const float* __restrict__ iut, const float* __restrict__ lu, const float* __restrict__ ru,
+    const float* __restrict__ u, float* __restrict__ grad, double* __restrict__ partials) {
+    const int64_t blk = blockIdx.x;
+    int lo = 0, hi = ninst - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldg(tile_start + mid) <= blk) lo = mid;
+        else hi = mid - 1;
+    }
+    const odil_wave_instance& d = inst[lo];
+    WaveDev<float> g;
+    g.nt = (int)d.nt;
+    g.nx = (int)d.nx;
+    g.inv_dt = (float)d.inv_dt;
+    g.inv_dx2 = (float)d.inv_dx2;
+    g.c2 = (float)d.c2;
+    g.half_dt = (float)d.half_dt;
+    g.A = (float)d.a;
+    g.B = (float)d.b;
+    g.dt2 = (float)d.dt2;
+    g.lam2 = (float)d.lam2;
+    g.init_u = iu + d.offset_x;
+    g.init_ut = iut + d.offset_x;
+    g.left_u = lu + d.offset_t;
+    g.right_u = ru + d.offset_t;
+    const int gx = (g.nx + LG_WARPS * LG_OUT - 1) / (LG_WARPS * LG_OUT);
+    const int64_t t = blk - __ldg(tile_start + lo);
+    const int bx = (int)(t % gx), by = (int)(t / gx);
+    const float gscale = (float)(2.0 / ((double)g.nt * (double)g.nx));
+    const float lsum = lg_strip<float, BLG_TY>(g, u + d.offset, grad + d.offset, bx, by, gscale);
+    const double sblk = block_sum((double)lsum);
+    if (threadIdx.x == 0) partials[blk] = sblk;
+}
+
+// loss[i] = (sum of instance i's block sums) / N_i, each by one warp in a
+// fixed order; total = sum_i loss[i], by the block in a fixed order.
+__global__ void __launch_bounds__(1024) batch_loss_finish_kernel(
+    const odil_wave_instance* __restrict__ inst, int ninst,
+    const int64_t* __restrict__ tile_start, const double* __restrict__ partials,
+    double* __restrict__ loss, double* __restrict__ total) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int q = warp; q < ninst; q += nw) {
+        const int64_t a = tile_start[q], b = tile_start[q + 1];
+        double s = 0.0;
+        for (int64_t k = a + lane; k < b; k += 32) s += partials[k];
+        s = warp_sum(s);
+        if (lane == 0) loss[q] = s / ((double)inst[q].nt * (double)inst[q].nx);
+    }
+    __syncthreads();
+    __threadfence_block();
+    const double t = sum_partials(loss, ninst);
+    if (threadIdx.x == 0 && total) total[0] = t;
+}
+
 }  // namespace
 }  // namespace odil
 
 using namespace odil;
+
+ODIL_API int odil_wave_batch_loss_grad_f32(const odil_wave_batch* b, const int64_t* tile_start,
+                                           int64_t ntiles, const float* init_u,
+                                           const float* init_ut, const float* left_u,
+                                           const float* right_u, const float* u, float* grad,
+                                           double* partials, double* loss, double* total,
+                                           void* stream) {
+    int st = check_batch(b);
+    if (st) return st;
+    if (ntiles < 1 || ntiles > (int64_t)1 << 31) return ODIL_ERR_SHAPE;
+    if (!tile_start || !init_u || !init_ut || !left_u || !right_u || !u || !grad || !partials ||
+        !loss)
+        return ODIL_ERR_ARG;
+    cudaStream_t s = as_stream(stream);
+    batch_loss_grad_kernel<<<(unsigned)ntiles, LG_WARPS * 32, 0, s>>>(
+        b->inst, b->ninst, tile_start, init_u, init_ut, left_u, right_u, u, grad, partials);
+    batch_loss_finish_kernel<<<1, 1024, 0, s>>>(b->inst, b->ninst, tile_start, partials, loss,
+                                                total);
+    return launch_status();
+}
 
 ODIL_API int odil_wave_batch_setup(odil_wave_instance* inst, int32_t ninst, void* stream) {
     if (!inst || ninst < 1) return ODIL_ERR_ARG;

@@ -123,6 +123,115 @@ __device__ __forceinline__ T wave_gather(const WaveDev<T>& g, int a, int b, T f_
 
 
 // ---------------------------------------------------------------------------
+// Fused loss + adjoint gradient, one warp per 32-column strip marching down a
+// tile of rows.  Lane l holds column c0 - 1 + l; lanes 1..30 produce outputs,
+// lanes 0 and 31 are the halo.  Per row the warp loads u once (coalesced; the
+// two halo lanes load one extra neighbour), gets the x-neighbours of the
+// previous row by shuffles, evaluates the residual of the row (kept in
+// registers, never stored), and gathers J^T f for the row two above:
+//   g(a, b) = sum over the rows (a, b), (a+1, b), (a+2, b), (a+1, b-1),
+//             (a+1, b+1) that read u(a, b), of coefficient * f.
+// Warps whose rows and columns avoid the boundary classes use the constant
+// interior coefficients; the others use the general class functions.
+// lg_strip runs the strips of tile (bx, by) (column group bx of LG_WARPS
+// strips, rows [TY by, TY by + TY)) and returns the thread's share of the
+// sum of f^2 over the tile's output rows; the single-instance kernel and the
+// batched one (batch.cu) call it.
+constexpr int LG_WARPS = 4;
+constexpr int LG_OUT = 30;  // output columns per warp
+
+template <typename T, int TY>
+__device__ __forceinline__ T lg_strip(const WaveDev<T>& g, const T* __restrict__ u,
+                                      T* __restrict__ grad, int bx, int by, T gscale) {
+    const int nt = g.nt, nx = g.nx;
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    const int c0 = (bx * LG_WARPS + warp) * LG_OUT;  // first output column
+    const int a0 = by * TY;
+    const int col = c0 - 1 + lane;
+    const bool out_lane = lane >= 1 && lane <= LG_OUT && col < nx;
+    const int colw = wrapn(col, nx);
+    const int colm = wrapn(col - 1, nx);  // lane 0's extra load
+    const int colp = wrapn(col + 1, nx);  // lane 31's extra load
+    const bool fast = (c0 >= 2) && (c0 + LG_OUT + 2 <= nx) && (a0 >= 1) && (a0 + TY + 2 < nt);
+    const T A = g.A, B = g.B;
+    const T ctm_int = T(-2) * A + T(2) * B;
+
+    T u1 = 0, u2 = 0, e1 = 0;   // u rows r-1, r-2 at this lane; e1: lane-0/31 extra of row r-1
+    T f1 = 0, f2 = 0;           // f rows r-1, r-2
+    T f1m = 0, f1p = 0;         // f row r-1 at col-1, col+1
+    // Per-thread loss partial in the working precision (at most TY terms);
+    // FP64 only across threads and blocks, off the per-cell path.
+    T lsum = T(0);
+    // Rows stream in chunks of LGQ; the loads of chunk c+1 are issued before
+    // chunk c is processed, so each warp keeps up to 2 LGQ row loads in
+    // flight while the shuffle chain of the march runs.
+    constexpr int LGQ = 4;
+    static_assert((TY + 4) % LGQ == 0, "row chunking");
+    T uq[LGQ], eq[LGQ], un[LGQ], en[LGQ];
+    auto load_chunk = [&](int q0, T* uu, T* ee) {
+#pragma unroll
+        for (int j = 0; j < LGQ; ++j) {
+            const int r = a0 - 2 + q0 + j;
+            uu[j] = T(0);
+            ee[j] = T(0);
+            if (q0 + j < TY + 4 && r >= 0 && r < nt) {
+                const T* row = u + (int64_t)r * nx;
+                uu[j] = __ldg(row + colw);
+                if (lane == 0) ee[j] = __ldg(row + colm);
+                if (lane == 31) ee[j] = __ldg(row + colp);
+            }
+        }
+    };
+    load_chunk(0, uq, eq);
+    for (int q0 = 0; q0 < TY + 4; q0 += LGQ) {
+        load_chunk(q0 + LGQ, un, en);
+#pragma unroll
+        for (int j = 0; j < LGQ; ++j) {
+            const int q = q0 + j;
+            const int r = a0 - 2 + q;
+            const T u0 = uq[j], e0 = eq[j];
+            // x-neighbours of row r-1 at this lane.
+            T um = __shfl_up_sync(0xffffffffu, u1, 1);
+            T up = __shfl_down_sync(0xffffffffu, u1, 1);
+            if (lane == 0) um = e1;
+            if (lane == 31) up = e1;
+            if (q >= 2) {
+                T f0 = T(0);
+                if (r < nt) f0 = wave_f(g, r, colw, u0, u1, u2, um, up);
+                // Gradient of row a = r - 2 (f rows a, a+1 with neighbours, a+2).
+                if (q >= 4 && out_lane) {
+                    const int a = r - 2;
+                    if (a < nt) {
+                        T gs;
+                        if (fast) {
+                            gs = A * (f2 + f0) + ctm_int * f1 - B * (f1p + f1m);
+                        } else {
+                            gs = wave_gather(g, a, col, f2, f1, f0, f1p, f1m);
+                        }
+                        grad[(int64_t)a * nx + col] = gs * gscale;
+                        lsum += f2 * f2;
+                    }
+                }
+                f2 = f1;
+                f1 = f0;
+                f1m = __shfl_up_sync(0xffffffffu, f0, 1);
+                f1p = __shfl_down_sync(0xffffffffu, f0, 1);
+            }
+            u2 = u1;
+            u1 = u0;
+            e1 = e0;
+        }
+#pragma unroll
+        for (int j = 0; j < LGQ; ++j) {
+            uq[j] = un[j];
+            eq[j] = en[j];
+        }
+    }
+    return lsum;
+}
+
+// ---------------------------------------------------------------------------
 // Accurate residual of a field held as an unevaluated sum of two FP32 arrays,
 // hi + lo, without FP64 arithmetic at interior cells.  In the interior (i >= 2,
 // 0 < j < nx-1) the residual of wave_f equals

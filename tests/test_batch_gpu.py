@@ -103,3 +103,55 @@ def test_batch_three_epochs(cuda):
     b.solve_mixed(epochs=3)
     for inst, u in zip(insts, b.unpack()):
         assert W.rel_err(u, _oracle(inst)) <= 1e-10, (inst["nt"], inst["c"])
+
+
+def test_batch_loss_grad_matches_single_instance_and_oracle(cuda):
+    """The one-launch fused loss + adjoint of the batch gives, per
+    instance, the single-instance fused kernel's loss and gradient (FP32)
+    and the oracle's FP64 values (util_op.py:627-654) to FP32 accuracy."""
+    from odil_gb300.batch import WaveBatch
+    from odil_gb300.wave import WaveKernels
+    insts = _small_batch()
+    b = WaveBatch(insts, device=cuda)
+    rng = np.random.default_rng(5)
+    u = torch.as_tensor(0.1 * rng.standard_normal(b.total),
+                        dtype=torch.float32, device=cuda)
+    g = torch.full_like(u, float("nan"))
+    total, _ = b.loss_grad(u, g)
+    losses = b.loss_inst.cpu().numpy()
+    assert abs(total.item() - losses.sum()) <= 1e-12 * losses.sum()
+    for q, (inst, off, (nt, nx)) in enumerate(zip(insts, b.offsets,
+                                                  b.shapes)):
+        sl = slice(off, off + nt * nx)
+        uq = u[sl].view(nt, nx).contiguous()
+        k = WaveKernels(nt, nx, inst["dt"], inst["dx"], inst["c"],
+                        inst["init_u"], inst["init_ut"], inst["left_u"],
+                        inst["right_u"], device=cuda)
+        l1, g1 = k.loss_grad(uq)
+        gq = g[sl].view(nt, nx)
+        assert abs(losses[q] - l1.item()) <= 1e-5 * l1.item()
+        assert float((gq - g1).abs().max()) <= 1e-4 * float(g1.abs().max())
+        s = W.WaveSetup(nt, nx, inst["init_u"], inst["init_ut"],
+                        inst["left_u"], inst["right_u"], c=inst["c"])
+        lo, go = W.loss_grad(s, uq.double().cpu().numpy())
+        assert abs(losses[q] - lo) <= 1e-4 * lo
+        assert np.abs(gq.double().cpu().numpy() - go).max() <= \
+            1e-3 * np.abs(go).max()
+
+
+def test_batch_lbfgs_stage_then_newton_refinement(cuda):
+    """The batch's FP32 fused-adjoint L-BFGS stage lowers the summed loss,
+    and FP64 Newton refinement from its iterate brings every instance to
+    rel err <= 1e-5 against the FP64 oracle."""
+    from odil_gb300.batch import WaveBatch
+    from odil_gb300.workloads import wave_batch_instances
+    insts = wave_batch_instances(count=512)[:24]
+    b = WaveBatch(insts, device=cuda)
+    g = torch.empty(b.total, dtype=torch.float32, device=cuda)
+    l0 = b.loss_grad(torch.zeros_like(g), g)[0].item()
+    x, info = b.lbfgs_warm_start(iters=10, m=5)
+    assert info.epochs == 10
+    assert b.loss_grad(x, g)[0].item() < l0
+    b.refine(x.double(), epochs=3)
+    errs = [W.rel_err(u, _oracle(inst)) for inst, u in zip(insts, b.unpack())]
+    assert max(errs) <= 1e-5, max(errs)
