@@ -67,7 +67,8 @@ def parse():
                     choices=("march", "march64", "update_residual", "loss_grad",
                              "loss_grad64", "loss_grad_big", "lbfgs_iter",
                              "adam_iter", "batch", "ns_newton", "advect",
-                             "ns_inverse", "ns_mg", "generic"),
+                             "ns_inverse", "ns_mg", "generic", "cavity",
+                             "batch_block"),
                     help="run one kernel of the workload --steps times (for "
                     "profiler captures) instead of the benchmark")
     return ap.parse_args()
@@ -319,6 +320,7 @@ def run_optimizers(problem, inst, dev, with_oracle):
         loss, _ = (kk if dt == torch.float32 else k64).loss_grad(
             x.reshape(NT, NX))
         ent = {"iterations": int(info.epochs), "evals": int(info.evals),
+               "host_line_searches": getattr(info, "fallbacks", None),
                "wall_s": wall, "ms_per_iter": 1000 * wall / max(1, info.epochs),
                "initial_loss": l0, "final_loss": float(loss.item()),
                "err_vs_exact_l2": float(np.mean((xs - inst.exact_u)**2)**0.5)}
@@ -346,7 +348,10 @@ def run_optimizers(problem, inst, dev, with_oracle):
     return res
 
 
-def run_batch(dev, with_oracle, steps=5):
+LBFGS_ITERS, LBFGS_M, REFINE_EPOCHS = 20, 10, 2
+
+
+def run_batch(dev, with_oracle, steps=5, hbm=6800.0):
     """512 wave instances, sides U{64..512}, c in [0.5, 2], 5-mode profiles:
     mixed Newton for the whole batch as one CUDA-graph replay (right-hand
     sides with FP64 only on boundary cells, persistent FP32 forward
@@ -404,7 +409,52 @@ def run_batch(dev, with_oracle, steps=5):
     torch.cuda.synchronize(dev)
     plain_ms = e0.elapsed_time(e1)
     cells = sum(i["nt"] * i["nx"] for i in insts)
+    # The fused loss + adjoint of all instances in one launch (FP32, 8 B per
+    # cell: read u, write the gradient; 424 MB > L2).
+    u32 = torch.randn(b.total, dtype=torch.float32, device=dev) * 0.1
+    g32 = torch.empty_like(u32)
+    for _ in range(3):
+        b.loss_grad(u32, g32)
+    torch.cuda.synchronize(dev)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    reps = 10
+    e0.record(st)
+    for _ in range(reps):
+        b.loss_grad(u32, g32)
+    e1.record(st)
+    torch.cuda.synchronize(dev)
+    lg_ms = e0.elapsed_time(e1) / reps
+    del u32, g32
+    # The configured pipeline: FP32 fused-adjoint L-BFGS stage on the whole
+    # batch (LBFGS_ITERS iterations, history LBFGS_M), then FP64 Newton
+    # refinement (REFINE_EPOCHS epochs, FP32 forward substitution).
+    b.lbfgs_warm_start(iters=2, m=LBFGS_M)  # warm-up
+    torch.cuda.synchronize(dev)
+    e0.record(st)
+    xw, winfo = b.lbfgs_warm_start(iters=LBFGS_ITERS, m=LBFGS_M)
+    e1.record(st)
+    b.refine(xw.double(), epochs=REFINE_EPOCHS)
+    e2 = torch.cuda.Event(enable_timing=True)
+    e2.record(st)
+    torch.cuda.synchronize(dev)
+    stage_ms, refine_ms = e0.elapsed_time(e1), e1.elapsed_time(e2)
+    u_pipe = b.unpack()
     out = {"instances": len(insts), "cells": cells,
+           "loss_grad_batched": {
+               "ms": lg_ms, "launches": 2,
+               "roofline": {"kernel": "batch_loss_grad_kernel", "bound": "hbm",
+                            "achieved": 8 * cells / (lg_ms * 1e6),
+                            "peak": hbm, "unit": "GB/s",
+                            "frac": 8 * cells / (lg_ms * 1e6) / hbm}},
+           "lbfgs_then_newton": {
+               "lbfgs_iters": LBFGS_ITERS, "lbfgs_m": LBFGS_M,
+               "lbfgs_fallbacks": winfo.fallbacks,
+               "refine_epochs": REFINE_EPOCHS,
+               "lbfgs_ms": stage_ms, "refine_ms": refine_ms,
+               "ms_per_batch": stage_ms + refine_ms,
+               "value": len(insts) / ((stage_ms + refine_ms) / 1000.0),
+               "unit": "solves/s"},
            "ms_per_batch": ms, "value": len(insts) / (ms / 1000.0),
            "unit": "solves/s", "march_cfg": cfg,
            # kernels: rhs (interior + boundary), march, then per further
@@ -424,6 +474,11 @@ def run_batch(dev, with_oracle, steps=5):
                             c=inst["c"])
             errs.append(W.rel_err(u, W.solve_march(s, rounds=2)))
         out["rel_err_vs_oracle_max"] = max(errs)
+        refs = [W.solve_march(W.WaveSetup(
+            i["nt"], i["nx"], i["init_u"], i["init_ut"], i["left_u"],
+            i["right_u"], c=i["c"]), rounds=2) for i in insts]
+        out["lbfgs_then_newton"]["rel_err_vs_oracle_max"] = max(
+            W.rel_err(u, r) for u, r in zip(u_pipe, refs))
         errs_p = [W.rel_err(u.cpu().numpy(), W.solve_march(W.WaveSetup(
             i["nt"], i["nx"], i["init_u"], i["init_ut"], i["left_u"],
             i["right_u"], c=i["c"]), rounds=2)) for i, u in
@@ -463,7 +518,7 @@ def graph_time_ms(fn, dev, reps=10, rounds=5):
 
 
 ADV_N = 256
-NS_INV_EPOCHS = 8
+NS_INV_EPOCHS = 40
 ADV_EPOCHS = 3
 # DRAM bytes of one full fine-level Jacobi sweep at 256^3 FP32 (read x, b;
 # write x) from an ncu --set full capture of `bench.py --case advect`.
@@ -560,76 +615,118 @@ def _cavity_oracle_check(op_kw, n, fields):
 
 
 def run_cavity_block(dev, with_oracle):
-    """Steady lid-driven cavity, Re 400 (the cavity configuration):
-    forward solve on 512^2 from rest to a residual rms of 1e-10, then the
-    inverse solve that reconstructs the flow from 256 seeded interior
-    velocity points of the forward solution with Gaussian noise (sigma
-    0.01) and a Laplacian penalty of 1e-4.  Wall time per solve, and the
-    checks against the oracle: the restated reference operator's residual
+    """Steady lid-driven cavity, Re 400, pressure pinned at cell (0, 0) (the
+    cavity configuration): forward solve on 512^2 from rest to a flow
+    residual rms of 1e-10, then the inverse solve that reconstructs the flow
+    from 256 seeded interior velocity points of the forward solution with
+    Gaussian noise (sigma 0.01) and a Laplacian penalty of 1e-4, until the
+    loss gradient has fallen by 1e-7 (at most NS_INV_EPOCHS Gauss-Newton
+    steps).  Both with Newton / Gauss-Newton on the normal equations,
+    multigrid-preconditioned FP32 PCG, FP64 residuals (NsMultigridNewton);
+    the forward problem also with the FP32 block-LU direct solver for
+    comparison.  Wall time per solve (CUDA synchronised), and the checks
+    against the oracle: the restated reference operator's residual
     (forward) and loss gradient (inverse) at the GPU's FP64 solution, plus
-    the same forward solver at 128^2 against the reference's own FP64
-    solution (cavity_N128_Re400)."""
+    the multigrid Newton at 128^2 against the reference's own FP64 solution
+    (cavity_N128_Re400)."""
     import torch
     from odil_gb300.ns import (NsCavityOperator, NsKernels, NsDirectNewton,
-                               NsGaussNewton)
+                               NsMultigridNewton)
     n = NS_N
-    out = {"grid": [n, n], "Re": NS_RE}
-    # Forward.
-    fk = NsKernels(n, NsCavityOperator(NS_RE), device=dev)
+    pin = (0, 0)
+    out = {"grid": [n, n], "Re": NS_RE, "pin": list(pin)}
+
+    def timed_solve(fn):
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        r = fn()
+        torch.cuda.synchronize(dev)
+        return time.perf_counter() - t0, r
+
+    # Forward, multigrid Newton (one untimed solve first: set-up, capture).
+    fk = NsKernels(n, NsCavityOperator(NS_RE, pin=pin), device=dev)
     fw = [torch.zeros((n, n), dtype=torch.float64, device=dev)
           for _ in range(3)]
-    solver = NsDirectNewton(fk)
-    torch.cuda.synchronize(dev)
-    t0 = time.perf_counter()
-    rms = solver.solve(*fw, epochs=80, tol=1e-10)
-    torch.cuda.synchronize(dev)
-    t_fwd = time.perf_counter() - t0
+    NsMultigridNewton(fk).solve(*[torch.zeros_like(x) for x in fw],
+                                epochs=3)
+    mg = NsMultigridNewton(fk)
+    t_fwd, _ = timed_solve(lambda: mg.solve(*fw, epochs=150, tol=1e-10))
+    # Forward, block-LU direct solver (pinned continuity row).
+    fk0 = NsKernels(n, NsCavityOperator(NS_RE), device=dev)
+    fd = [torch.zeros((n, n), dtype=torch.float64, device=dev)
+          for _ in range(3)]
+    direct = NsDirectNewton(fk0, pin=pin)
+    t_dir, rms_dir = timed_solve(lambda: direct.solve(*fd, epochs=80,
+                                                      tol=1e-10))
+    fwh = [x.cpu().numpy() for x in fw]
+    fdh = [x.cpu().numpy() for x in fd]
     out["forward"] = {
-        "method": "newton, FP32 block-tridiagonal LU + FP64 refinement",
-        "s_per_solve": t_fwd, "epochs": len(solver.stats),
-        "factorisations": sum(st["factored"] for st in solver.stats),
-        "final_rms": rms}
+        "method": "newton on the normal equations: FP32 PCG with a "
+                  "cell-centred multigrid V-cycle (Galerkin J^T J, 3+3 block "
+                  "Jacobi sweeps, FP64 dense coarsest solve), FP64 residual",
+        "s_per_solve": t_fwd, "epochs": len(mg.stats),
+        "pcg_iters_total": sum(st["pcg"] for st in mg.stats),
+        "final_rms": mg.final_rms,
+        "direct_block_lu": {"s_per_solve": t_dir,
+                            "epochs": len(direct.stats),
+                            "final_rms": rms_dir,
+                            "speedup_multigrid_over_direct": t_dir / t_fwd},
+        "uv_rel_diff_multigrid_vs_direct": max(
+            float(np.abs(a - b).max() / np.abs(b).max())
+            for a, b in zip(fwh[:2], fdh[:2]))}
+    del fd, direct
     # Inverse from the forward solution's noisy samples.
     rng = np.random.default_rng(SEED)
     mask = np.zeros((n, n))
     mask.ravel()[rng.choice(n * n, NS_NIMP, replace=False)] = 1.0
-    fwh = [x.cpu().numpy() for x in fw]
     uimp = fwh[0] + NS_NOISE * rng.standard_normal((n, n))
     vimp = fwh[1] + NS_NOISE * rng.standard_normal((n, n))
-    op_kw = dict(mask=mask, u_imp=uimp, v_imp=vimp, kreg=NS_KREG)
+    op_kw = dict(mask=mask, u_imp=uimp, v_imp=vimp, kreg=NS_KREG, pin=pin,
+                 pin_weight=1.0)
     k = NsKernels(n, NsCavityOperator(NS_RE, **op_kw), device=dev)
     t = [torch.zeros((n, n), dtype=torch.float64, device=dev)
          for _ in range(3)]
-    gn = NsGaussNewton(k)
-    torch.cuda.synchronize(dev)
-    t0 = time.perf_counter()
-    loss = gn.solve(*t, epochs=NS_INV_EPOCHS, rtol=1e-3)
-    torch.cuda.synchronize(dev)
-    t_inv = time.perf_counter() - t0
+    gn = NsMultigridNewton(k)
+
+    def gnorm():
+        return float(torch.sqrt(sum((x**2).sum() for x in
+                                    k.loss_grad(*t)[1])))
+
+    def inverse():
+        g0 = gnorm()
+        for _ in range(NS_INV_EPOCHS):
+            gn.step(*t, rtol=1e-2)
+            if gnorm() <= 1e-7 * g0:
+                break
+        f = k.residual(*t)
+        return float((f**2).mean(dim=(1, 2)).sum())
+
+    t_inv, loss = timed_solve(inverse)
     th = [x.cpu().numpy() for x in t]
     out["inverse"] = {
-        "method": "Gauss-Newton, PCG on the normal equations (block-LU "
-                  "preconditioner)", "imposed": NS_NIMP, "noise": NS_NOISE,
-        "kreg": NS_KREG, "s_per_solve": t_inv, "epochs": len(gn.stats),
-        "cg_iters": [st["cg"] for st in gn.stats],
+        "method": "Gauss-Newton on the normal equations, same multigrid PCG",
+        "imposed": NS_NIMP, "noise": NS_NOISE, "kreg": NS_KREG,
+        "s_per_solve": t_inv, "epochs": len(gn.stats),
+        "pcg_iters": [st["pcg"] for st in gn.stats],
         "loss_history": [st["loss"] for st in gn.stats], "final_loss": loss,
         "rel_err_uv_vs_forward": [
             float(np.linalg.norm(a - b) / np.linalg.norm(b))
             for a, b in zip(th[:2], fwh[:2])]}
     if with_oracle:
-        out["forward"].update(_cavity_oracle_check({}, n, fwh))
+        out["forward"].update(_cavity_oracle_check(
+            {"pin": pin, "pin_weight": 1.0}, n, fwh))
         chk = _cavity_oracle_check(op_kw, n, th)
         chk0 = _cavity_oracle_check(op_kw, n, [np.zeros((n, n))] * 3)
         chk["oracle_grad_norm_rel_to_start"] = (chk["oracle_grad_norm"] /
                                                chk0["oracle_grad_norm"])
         out["inverse"].update(chk)
-        # The forward solver at 128^2 against the reference's own solution.
+        # The multigrid Newton at 128^2 against the reference's solution.
         gold = np.load(os.path.join(HERE, "tests", "golden",
                                     "cavity_N128.npz"))
-        k128 = NsKernels(128, NsCavityOperator(NS_RE), device=dev)
+        k128 = NsKernels(128, NsCavityOperator(NS_RE, pin=pin), device=dev)
         w = [torch.zeros((128, 128), dtype=torch.float64, device=dev)
              for _ in range(3)]
-        NsDirectNewton(k128).solve(*w, epochs=60, tol=1e-11)
+        NsMultigridNewton(k128).solve(*w, epochs=150, tol=1e-11)
         wh = [x.cpu().numpy() for x in w]
         dp = wh[2] - gold["Re400_p"]
         out["forward"]["n128_vs_reference_solution"] = {
@@ -762,8 +859,6 @@ def run_ours(args):
     t_lg_big = timed(lambda: kb.loss_grad(ubig, grad=gbig), 10, 3)
     del ubig, gbig, kb
 
-    # The batched configuration: 512 uneven instances in one graph replay.
-    batch_info = run_batch(dev, with_oracle)
 
     # The workload's optimizer runs (FP32 fused adjoint gradient).
     opt_info = run_optimizers(problem, inst, dev, with_oracle)
@@ -773,6 +868,8 @@ def run_ours(args):
                 .get("hbm_gbs") if os.path.exists(
                     os.path.join(HERE, "MEASURED_PEAKS.json")) else None) \
         or 6800.0
+    # The batched configuration: 512 uneven instances in one graph replay.
+    batch_info = run_batch(dev, with_oracle, hbm=hbm_peak)
     advect_info = run_advect_block(dev, with_oracle, hbm=hbm_peak)
     cavity_info = run_cavity_block(dev, with_oracle)
 
@@ -1199,6 +1296,12 @@ def main():
         run_ns_inverse(args)
     elif args.case == "ns_mg":
         run_ns_mg(args)
+    elif args.case in ("cavity", "batch_block"):
+        import torch
+        dev = torch.device("cuda", 0)
+        fn = run_cavity_block if args.case == "cavity" else run_batch
+        print(json.dumps({"case": args.case,
+                          **fn(dev, not args.no_cpu_baseline)}))
     elif args.case == "generic":
         run_generic(args)
     elif args.case:
