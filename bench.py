@@ -68,7 +68,8 @@ def parse():
                              "loss_grad64", "loss_grad_big", "lbfgs_iter",
                              "adam_iter", "batch", "ns_newton", "advect",
                              "ns_inverse", "ns_mg", "generic", "cavity",
-                             "batch_block"),
+                             "batch_block", "pair_residual", "batch_lg",
+                             "ns_kernels", "stencil", "mgdecomp"),
                     help="run one kernel of the workload --steps times (for "
                     "profiler captures) instead of the benchmark")
     return ap.parse_args()
@@ -382,6 +383,7 @@ def run_batch(dev, with_oracle, steps=5, hbm=6800.0):
         ts.append((e0, e1))
     torch.cuda.synchronize(dev)
     ms = statistics.mean(a.elapsed_time(c) for a, c in ts)
+    u_newton = b.unpack()
     # Plain FP64 method, one instance after the other (BATCH_FP64_EPOCHS each).
     kk = [WaveKernels(i["nt"], i["nx"], i["dt"], i["dx"], i["c"], i["init_u"],
                       i["init_ut"], i["left_u"], i["right_u"], device=dev)
@@ -468,7 +470,7 @@ def run_batch(dev, with_oracle, steps=5, hbm=6800.0):
     if with_oracle:
         from oracle import wave as W
         errs = []
-        for inst, u in zip(insts, b.unpack()):
+        for inst, u in zip(insts, u_newton):
             s = W.WaveSetup(inst["nt"], inst["nx"], inst["init_u"],
                             inst["init_ut"], inst["left_u"], inst["right_u"],
                             c=inst["c"])
@@ -1205,14 +1207,58 @@ def run_case(args):
         kb = Problem(big.operator, big.domain).kernels
         ubig = torch.randn((BIG, BIG), dtype=torch.float32, device=dev)
         gbig = torch.empty_like(ubig)
-    if args.case == "batch":
+    if args.case in ("batch", "batch_lg"):
         from odil_gb300.batch import WaveBatch
         from odil_gb300.workloads import wave_batch_instances
         wb = WaveBatch(wave_batch_instances(count=512), device=dev)
         wb.initial_rhs(wb.rhs)
+        bu = torch.randn(wb.total, dtype=torch.float32, device=dev) * 0.1
+        bg = torch.empty_like(bu)
+    if args.case in ("ns_kernels", "stencil"):
+        # 512^2 cavity at a smooth state: FP64 residual and Jacobian
+        # coefficients, the multigrid's fine-level J x / J^T w sweep pair
+        # and 25-point coarse sweep, and a stencil-operator product.
+        from odil_gb300.ns import (NsCavityOperator, NsKernels,
+                                   NsMultigridNewton)
+        from odil_gb300.stencil import StencilOp
+        nn = 512
+        nk = NsKernels(nn, NsCavityOperator(400.0, pin=(0, 0)), device=dev)
+        x1 = (torch.arange(nn, dtype=torch.float64, device=dev) + 0.5) / nn
+        xx, yy = torch.meshgrid(x1, x1, indexing="ij")
+        fields = [0.5 * torch.sin(np.pi * xx) * torch.sin(2 * np.pi * yy),
+                  -0.5 * torch.sin(2 * np.pi * xx) * torch.sin(np.pi * yy),
+                  0.1 * torch.cos(np.pi * xx)]
+        fields = [f.contiguous() for f in fields]
+        mgn = NsMultigridNewton(nk)
+        mgn.linearize(*fields)
+        mgn.setup()
+        for lv in mgn.levels:
+            lv.x.normal_()
+            lv.b.normal_()
+        vb = torch.randn((3, nn, nn), dtype=torch.float32, device=dev)
+        vo = torch.empty_like(vb)
+        J = nk.jacobian(*fields)
+        sop = J[0][0]
+        sv = torch.randn((nn, nn), dtype=torch.float64, device=dev)
+        so = torch.empty_like(sv)
+    if args.case == "mgdecomp":
+        from odil_gb300.multigrid import MultigridDecomp
+        w2 = torch.randn((1025, 1025), dtype=torch.float32, device=dev)
+        c2 = torch.randn((1024, 1024), dtype=torch.float32, device=dev)
     fn = {
         "loss_grad_big": lambda: kb.loss_grad(ubig, grad=gbig),
         "batch": lambda: wb.solve_mixed(),
+        "batch_lg": lambda: wb.loss_grad(bu, bg),
+        "pair_residual": lambda: k.pair_residual(d32, None, rhs),
+        "ns_kernels": lambda: (nk.residual(*fields),
+                               mgn.linearize(*fields),
+                               mgn._smooth(0, vb, vb, vo, 2),
+                               mgn._smooth(1, mgn.levels[1].x,
+                                           mgn.levels[1].b,
+                                           mgn.levels[1].x2, 2)),
+        "stencil": lambda: sop.mul_field(sv, out=so),
+        "mgdecomp": lambda: (MultigridDecomp.interp_node_field(w2, 1),
+                             MultigridDecomp.interp_cell_field(c2, 1)),
         "march": lambda: k.march_tuned(rhs, d32),
         "march64": lambda: k.march_tuned(u, ub),
         "update_residual": lambda: k.update_residual_mixed(u, d32, ub, rhs),

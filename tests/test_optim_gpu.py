@@ -254,8 +254,8 @@ def test_device_lbfgs_matches_host_algebra(cuda, m):
 
 def test_device_lbfgs_one_sync_per_iteration_fp32_1024(cuda):
     """The 1024^2 FP32 wave through the fused adjoint: 20 device L-BFGS
-    iterations complete with the loss not increasing; the host line search
-    is the exception, not the rule."""
+    iterations complete with the loss not increasing beyond its FP32
+    resolution; the host line search is the exception, not the rule."""
     from odil_gb300.optimizer import LbfgsOptimizer
     n = 1024
     inst, prob = _wave_problem(n, cuda, dtype=np.float32)
@@ -269,5 +269,7 @@ def test_device_lbfgs_one_sync_per_iteration_fp32_1024(cuda):
     l0 = k.loss_grad(x0.reshape(n, n))[0].item()
     x, info = LbfgsOptimizer().run_device(x0, lg, epochs=20)
     assert info.epochs == 20
-    assert k.loss_grad(x.reshape(n, n))[0].item() <= l0
+    # FP32 steps are accepted by the approximate Wolfe conditions, which let
+    # the loss rise by up to 1e-6 of itself (below its FP32 resolution).
+    assert k.loss_grad(x.reshape(n, n))[0].item() <= l0 * (1 + 1e-6)
     assert info.fallbacks <= 5
