@@ -258,13 +258,15 @@ typedef struct odil_wave_batch {
  * loss[i] = mean(f_i^2) over instance i's cells, grad_i = (2/N_i) J_i^T f_i
  * (util_op.py:627-654 per instance), total = sum_i loss[i] (the loss of the
  * batch as one optimisation problem).  tile_start [ninst + 1]: first tile of
- * each instance, tiles of 120 columns x 16 rows numbered instance by
- * instance (ceil(nx/120) * ceil(nt/16) per instance), ntiles the total;
- * init_u .. right_u: the packed boundary arrays in FP32; partials: ntiles
- * doubles of scratch; total may be null.  Requires odil_wave_batch_setup.
+ * each instance, tiles of 120 columns x 32 rows numbered instance by
+ * instance (ceil(nx/120) * ceil(nt/32) per instance), ntiles the total;
+ * tile_inst [ntiles]: the instance of each tile; init_u .. right_u: the
+ * packed boundary arrays in FP32; partials: ntiles doubles of scratch; total
+ * may be null.  Requires odil_wave_batch_setup.
  * The batched form of the per-run loss of vary_wave.py:37-43. */
 int odil_wave_batch_loss_grad_f32(const odil_wave_batch* b,
-                                  const int64_t* tile_start, int64_t ntiles,
+                                  const int64_t* tile_start,
+                                  const int32_t* tile_inst, int64_t ntiles,
                                   const float* init_u, const float* init_ut,
                                   const float* left_u, const float* right_u,
                                   const float* u, float* grad,
@@ -661,7 +663,8 @@ int odil_bicgstab_update_xr(float* x, float* r, const float* ph,
  * This and odil_lincomb_* are the two streaming passes of the compact L-BFGS
  * direction that replaces scipy's fmin_l_bfgs_b (optimizer.py:61-99):
  * [S; Y] . g (plus the new correction pair's products), then
- * d = c0 g + sum_i coef[i] [S; Y]_i. */
+ * d = c0 g + sum_i coef[i] [S; Y]_i.  With more than 8 results a second
+ * launch adds the chunk partials, one warp per result. */
 int64_t odil_multidot_workspace_bytes(int64_t n, int k, int r);
 int odil_multidot_f32(const float* M, int64_t ld, int k, const void* const* q,
                       int r, int64_t n, double* out, void* workspace,

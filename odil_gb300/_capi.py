@@ -228,8 +228,8 @@ SIGNATURES = {
                                  _P]),
     "odil_lbfgs_commit_f32": (_INT, [_I64, _P, _I64, _P, _P, _P, _P]),
     "odil_lbfgs_commit_f64": (_INT, [_I64, _P, _I64, _P, _P, _P, _P]),
-    "odil_wave_batch_loss_grad_f32": (_INT, [_P, _P, _I64, _P, _P, _P, _P, _P,
-                                             _P, _P, _P, _P, _P]),
+    "odil_wave_batch_loss_grad_f32": (_INT, [_P, _P, _P, _I64, _P, _P, _P, _P,
+                                             _P, _P, _P, _P, _P, _P]),
     "odil_ns_num_equations": (_INT, [_P]),
     "odil_ns_residual_f32": (_INT, [_P, _P, _P, _P, _P, _P]),
     "odil_ns_residual_f64": (_INT, [_P, _P, _P, _P, _P, _P]),

@@ -90,14 +90,16 @@ class WaveBatch:
         self.march_cfg = None
         self.graph = None
         # Fused loss + gradient of all instances: FP32 boundary data and the
-        # tile table (120-column x 16-row tiles, instance by instance).
+        # tile tables (120-column x 32-row tiles, instance by instance).
         self.bc32 = [t.float() for t in self.bc]
-        tiles = [((nx + 119) // 120) * ((nt + 15) // 16)
+        tiles = [((nx + 119) // 120) * ((nt + 31) // 32)
                  for nt, nx in self.shapes]
         self.ntiles = int(sum(tiles))
         self.tile_start = torch.as_tensor(
             np.concatenate([[0], np.cumsum(tiles)]).astype(np.int64),
             device=dev)
+        self.tile_inst = torch.as_tensor(
+            np.repeat(np.arange(self.n, dtype=np.int32), tiles), device=dev)
         self.lg_partials = torch.zeros(self.ntiles, dtype=torch.float64,
                                        device=dev)
         self.loss_inst = torch.zeros(self.n, dtype=torch.float64, device=dev)
@@ -129,7 +131,8 @@ class WaveBatch:
         (2/N_i) J_i^T f_i into grad32, for the packed FP32 fields u32; one
         launch over all instances plus one small reduction."""
         call("odil_wave_batch_loss_grad_f32", ctypes.byref(self.b),
-             ptr(self.tile_start), self.ntiles, *[ptr(t) for t in self.bc32],
+             ptr(self.tile_start), ptr(self.tile_inst), self.ntiles,
+             *[ptr(t) for t in self.bc32],
              ptr(u32), ptr(grad32), ptr(self.lg_partials), ptr(self.loss_inst),
              ptr(self.loss_total), stream_handle())
         return self.loss_total, grad32

@@ -258,25 +258,20 @@ int launch_batch_march(const odil_wave_batch* b, const float* rhs, float* x, uns
 }
 
 // Fused loss + adjoint gradient of every instance in one launch (FP32): one
-// block per tile of the single-instance strip march (lg_strip, 16-row
+// block per tile of the single-instance strip march (lg_strip, 32-row
 // tiles), blocks numbered instance by instance (tile_start: first block of
-// each instance, tile_start[ninst] = total), the instance of a block by
-// binary search.  Each instance's gradient is (2 / N_i) J_i^T f_i, the
-// gradient of its own loss mean(f_i^2); the per-block sums go to partials.
-constexpr int BLG_TY = 16;
+// each instance, tile_start[ninst] = total; tile_inst: the instance of each
+// block).  Each instance's gradient is (2 / N_i) J_i^T f_i, the gradient of
+// its own loss mean(f_i^2); the per-block sums go to partials.
+constexpr int BLG_TY = 32;
 
 __global__ void __launch_bounds__(LG_WARPS * 32) batch_loss_grad_kernel(
-    const odil_wave_instance* __restrict__ inst, int ninst,
+    const odil_wave_instance* __restrict__ inst, const int32_t* __restrict__ tile_inst,
     const int64_t* __restrict__ tile_start, const float* __restrict__ iu,
     const float* __restrict__ iut, const float* __restrict__ lu, const float* __restrict__ ru,
     const float* __restrict__ u, float* __restrict__ grad, double* __restrict__ partials) {
     const int64_t blk = blockIdx.x;
-    int lo = 0, hi = ninst - 1;
-    while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (__ldg(tile_start + mid) <= blk) lo = mid;
-        else hi = mid - 1;
-    }
+    const int lo = __ldg(tile_inst + blk);
     const odil_wave_instance& d = inst[lo];
     WaveDev<float> g;
     g.nt = (int)d.nt;
@@ -302,24 +297,28 @@ __global__ void __launch_bounds__(LG_WARPS * 32) batch_loss_grad_kernel(
     if (threadIdx.x == 0) partials[blk] = sblk;
 }
 
-// loss[i] = (sum of instance i's block sums) / N_i, each by one warp in a
-// fixed order; total = sum_i loss[i], by the block in a fixed order.
-__global__ void __launch_bounds__(1024) batch_loss_finish_kernel(
+// loss[i] = (sum of instance i's block sums) / N_i, one warp per instance
+// (lane-strided, fixed tree: deterministic).
+__global__ void __launch_bounds__(256) batch_loss_finish_kernel(
     const odil_wave_instance* __restrict__ inst, int ninst,
     const int64_t* __restrict__ tile_start, const double* __restrict__ partials,
-    double* __restrict__ loss, double* __restrict__ total) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    for (int q = warp; q < ninst; q += nw) {
-        const int64_t a = tile_start[q], b = tile_start[q + 1];
-        double s = 0.0;
-        for (int64_t k = a + lane; k < b; k += 32) s += partials[k];
-        s = warp_sum(s);
-        if (lane == 0) loss[q] = s / ((double)inst[q].nt * (double)inst[q].nx);
-    }
-    __syncthreads();
-    __threadfence_block();
+    double* __restrict__ loss) {
+    const int q = (int)(((int64_t)blockIdx.x * 256 + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
+    if (q >= ninst) return;
+    const int64_t a = tile_start[q], b = tile_start[q + 1];
+    double s = 0.0;
+    for (int64_t k = a + lane; k < b; k += 32) s += __ldcg(partials + k);
+    s = warp_sum(s);
+    if (lane == 0) loss[q] = s / ((double)inst[q].nt * (double)inst[q].nx);
+}
+
+// total = sum_i loss[i] in a fixed order (one block).
+__global__ void __launch_bounds__(256) batch_loss_total_kernel(const double* __restrict__ loss,
+                                                               int ninst,
+                                                               double* __restrict__ total) {
     const double t = sum_partials(loss, ninst);
-    if (threadIdx.x == 0 && total) total[0] = t;
+    if (threadIdx.x == 0) total[0] = t;
 }
 
 }  // namespace
@@ -328,7 +327,8 @@ __global__ void __launch_bounds__(1024) batch_loss_finish_kernel(
 using namespace odil;
 
 ODIL_API int odil_wave_batch_loss_grad_f32(const odil_wave_batch* b, const int64_t* tile_start,
-                                           int64_t ntiles, const float* init_u,
+                                           const int32_t* tile_inst, int64_t ntiles,
+                                           const float* init_u,
                                            const float* init_ut, const float* left_u,
                                            const float* right_u, const float* u, float* grad,
                                            double* partials, double* loss, double* total,
@@ -336,14 +336,15 @@ ODIL_API int odil_wave_batch_loss_grad_f32(const odil_wave_batch* b, const int64
     int st = check_batch(b);
     if (st) return st;
     if (ntiles < 1 || ntiles > (int64_t)1 << 31) return ODIL_ERR_SHAPE;
-    if (!tile_start || !init_u || !init_ut || !left_u || !right_u || !u || !grad || !partials ||
-        !loss)
+    if (!tile_start || !tile_inst || !init_u || !init_ut || !left_u || !right_u || !u || !grad ||
+        !partials || !loss)
         return ODIL_ERR_ARG;
     cudaStream_t s = as_stream(stream);
     batch_loss_grad_kernel<<<(unsigned)ntiles, LG_WARPS * 32, 0, s>>>(
-        b->inst, b->ninst, tile_start, init_u, init_ut, left_u, right_u, u, grad, partials);
-    batch_loss_finish_kernel<<<1, 1024, 0, s>>>(b->inst, b->ninst, tile_start, partials, loss,
-                                                total);
+        b->inst, tile_inst, tile_start, init_u, init_ut, left_u, right_u, u, grad, partials);
+    batch_loss_finish_kernel<<<(unsigned)((b->ninst * 32 + 255) / 256), 256, 0, s>>>(
+        b->inst, b->ninst, tile_start, partials, loss);
+    if (total) batch_loss_total_kernel<<<1, 256, 0, s>>>(loss, b->ninst, total);
     return launch_status();
 }
 

@@ -215,6 +215,7 @@ __global__ void __launch_bounds__(VT) multidot_kernel(const T* __restrict__ M, i
             }
         }
     }
+    if (counter == nullptr) return;  // multidot_finish_kernel adds them
     __shared__ bool is_last;
     if (threadIdx.x == 0) {
         __threadfence();
@@ -317,6 +318,7 @@ __global__ void __launch_bounds__(VT, 3) multidot_vec_kernel(
                 partials[((int64_t)(g0 + g) * R + j) * nchunk + c] = sum;
         }
     }
+    if (counter == nullptr) return;  // multidot_finish_kernel adds them
     __shared__ bool is_last;
     if (threadIdx.x == 0) {
         __threadfence();
@@ -333,6 +335,26 @@ __global__ void __launch_bounds__(VT, 3) multidot_vec_kernel(
         if (threadIdx.x == 0) out[o] = sum;
     }
     if (threadIdx.x == 0) *counter = 0u;
+}
+
+// The chunk partials of each of `outputs` results added by one warp per
+// result: lane l takes partials l, l + 32, ... and the warp adds the lanes in
+// a fixed tree (deterministic).  Used when a multi-dot has more than
+// kMdFinishInKernel results, where the last block of the multi-dot would
+// otherwise add them one after the other.
+constexpr int kMdFinishInKernel = 8;
+
+__global__ void __launch_bounds__(256) multidot_finish_kernel(const double* __restrict__ partials,
+                                                              int64_t nchunk, int64_t outputs,
+                                                              double* __restrict__ out) {
+    const int64_t o = ((int64_t)blockIdx.x * 256 + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (o >= outputs) return;
+    const double* p = partials + o * nchunk;
+    double s = 0.0;
+    for (int64_t c = lane; c < nchunk; c += 32) s += __ldcg(p + c);
+    s = warp_sum(s);
+    if (lane == 0) out[o] = s;
 }
 
 // out = c0 * x + sum_i coef[i] * M_i  (coef, c0 read from device memory).
@@ -472,14 +494,25 @@ int multidot_impl(const T* M, int64_t ld, int k, const void* const* q, int r, in
     ReduceWs w = reduce_ws(ws);
     dim3 grid((k + MD_G - 1) / MD_G, (unsigned)nchunk);
     cudaStream_t st = as_stream(stream);
+    // Many results: the multi-dot only writes partials, a second launch adds
+    // them in parallel; few: its last block adds them.
+    const int64_t outputs = (int64_t)k * r;
+    const bool sep = outputs > kMdFinishInKernel;
+    if (sep) w.counter = nullptr;
+    int rc;
     if (vec) {
         // Row groups of G = min(k, 4) rows (k = 3 loads row 2 twice).
-        if (k == 1) return md_vec_launch<T, 1>(grid, st, M, ld, k, qs, r, n, chunk, w, out);
-        if (k == 2) return md_vec_launch<T, 2>(grid, st, M, ld, k, qs, r, n, chunk, w, out);
-        return md_vec_launch<T, MD_G>(grid, st, M, ld, k, qs, r, n, chunk, w, out);
+        if (k == 1) rc = md_vec_launch<T, 1>(grid, st, M, ld, k, qs, r, n, chunk, w, out);
+        else if (k == 2) rc = md_vec_launch<T, 2>(grid, st, M, ld, k, qs, r, n, chunk, w, out);
+        else rc = md_vec_launch<T, MD_G>(grid, st, M, ld, k, qs, r, n, chunk, w, out);
+    } else {
+        multidot_kernel<T><<<grid, VT, 0, st>>>(M, ld, k, qs, r, n, chunk, w.partials, w.counter,
+                                                out, vec);
+        rc = launch_status();
     }
-    multidot_kernel<T><<<grid, VT, 0, st>>>(M, ld, k, qs, r, n, chunk, w.partials, w.counter, out,
-                                            vec);
+    if (rc || !sep) return rc;
+    multidot_finish_kernel<<<(unsigned)((outputs * 32 + 255) / 256), 256, 0, st>>>(
+        w.partials, nchunk, outputs, out);
     return launch_status();
 }
 

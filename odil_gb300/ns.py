@@ -564,6 +564,8 @@ class NsMultigridNewton:
                                   device=dev)
         self.coef32 = torch.empty((self.neq, 15, n, n), **f32)
         self.w32 = torch.empty((self.neq, n, n), **f32)
+        self.s32 = torch.empty((3, n, n), **f32)
+        self.fw32 = torch.empty((self.neq, n, n), **f32)
         self.w64 = torch.empty((self.neq, n, n), dtype=torch.float64,
                                device=dev)
         self.b64 = torch.empty((3, n, n), dtype=torch.float64, device=dev)
@@ -607,10 +609,9 @@ class NsMultigridNewton:
         return out
 
     def setup(self):
-        """Coefficients at the current state (call `linearize` first): FP32
-        copy, explicit fine J^T J, Galerkin hierarchy, coarsest inverse."""
+        """Hierarchy from the FP32 coefficients of the last linearisation:
+        explicit fine J^T J, Galerkin levels, coarsest inverse."""
         st = stream_handle()
-        self.coef32.copy_(self.coef64)
         L0 = self.levels[0]
         call("odil_nsmg_fine_ata", self.n, self.neq, ptr(self.coef32),
              ptr(L0.A), ptr(L0.dinv), st)
@@ -726,9 +727,24 @@ class NsMultigridNewton:
 
     # -- Newton ------------------------------------------------------------
     def linearize(self, u, v, p):
+        """FP64 Jacobian coefficients at the state (coef64) and their FP32
+        copy (coef32)."""
         q = ctypes.byref(self.k.params[torch.float64])
         call("odil_ns_jacobian_f64", q, ptr(u), ptr(v), ptr(p),
              ptr(self.coef64), stream_handle())
+        self.coef32.copy_(self.coef64)
+
+    def _linearize32(self, u, v, p):
+        """FP32 Jacobian coefficients at the state rounded to FP32 (the
+        preconditioned FP32 solve needs no more; GB300's FP64 pipe makes the
+        FP64 coefficient kernel ~15x slower)."""
+        s = self.s32
+        s[0].copy_(u)
+        s[1].copy_(v)
+        s[2].copy_(p)
+        q = ctypes.byref(self.k.params[torch.float32])
+        call("odil_ns_jacobian_f32", q, ptr(s[0]), ptr(s[1]), ptr(s[2]),
+             ptr(self.coef32), stream_handle())
 
     def step(self, u, v, p, rtol=1e-2, maxit=500, f=None):
         """One (Gauss-)Newton step in place; returns the loss
@@ -737,14 +753,16 @@ class NsMultigridNewton:
         f = self.k.residual(u, v, p) if f is None else f
         loss = float((f**2).mean(dim=(1, 2)).sum())
         rms = float(torch.sqrt((f[:3]**2).mean()))
-        self.linearize(u, v, p)
-        # -J^T f in FP64 from the FP64 coefficients.
-        call("odil_nsmg_jtw_f64", self.n, self.neq, ptr(self.coef64), ptr(f),
-             ptr(self.b64), stream_handle())
-        self.setup()
+        self._linearize32(u, v, p)
+        # b = -J^T f in FP32 (the FP64 residual rounded; the FP32 PCG solves
+        # to rtol >= 1e-6 of it, and the FP64 residual drives convergence).
+        self.fw32.copy_(f)
         b32 = self.levels[0].b
-        b32.copy_(self.b64)
+        call("odil_nsmg_jtw_f32", self.n, self.neq, ptr(self.coef32),
+             ptr(self.fw32), None, None, None, ptr(b32), 1.0, 0,
+             stream_handle())
         b32.neg_()
+        self.setup()
         its = self.pcg(b32, rtol=rtol, maxit=maxit)
         self.stats.append({"loss": loss, "rms": rms, "pcg": its})
         u += self.x[0]
