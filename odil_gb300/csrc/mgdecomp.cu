@@ -14,39 +14,82 @@ using mgd::Grid;
 constexpr int kThreads = 256;
 
 // DIM and CELL are fixed per instantiation so that the per-axis loops of
-// mgdecomp.cuh unroll and their small arrays stay in registers.
-template <typename T, int DIM, int CELL>
+// mgdecomp.cuh unroll and their small arrays stay in registers.  ROWS: the
+// launch grid is the index grid itself (x: the last axis in blocks of
+// kThreads, y and z: the other axes, each at most 65535), so a thread finds
+// its point without the 64-bit divisions of unflatten; otherwise a
+// grid-stride loop over the flat index.
+template <int DIM, bool ROWS>
+__device__ __forceinline__ bool row_index(const int64_t* size, int64_t* o, int64_t* i) {
+    const int64_t last = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (last >= size[DIM - 1]) return false;
+    o[0] = o[1] = o[2] = 0;
+    o[DIM - 1] = last;
+    if (DIM >= 2) o[DIM - 2] = blockIdx.y;
+    if (DIM == 3) o[0] = blockIdx.z;
+    *i = (o[0] * size[1] + o[1]) * size[2] + o[2];
+    return true;
+}
+
+template <typename T, int DIM, int CELL, bool ROWS>
 __global__ void __launch_bounds__(kThreads)
     mgd_refine_kernel(Grid g, const T* __restrict__ in, T* __restrict__ out, T alpha,
                       const T* __restrict__ add, T beta, int64_t total) {
     g.dim = DIM;
     g.cell = CELL;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
-         i += (int64_t)gridDim.x * blockDim.x) {
-        int64_t o[3] = {0, 0, 0};
-        mgd::unflatten(g.m, g.dim, i, o);
+    if constexpr (ROWS) {
+        int64_t o[3], i;
+        if (!row_index<DIM, ROWS>(g.m, o, &i)) return;
         T v = alpha * mgd::refine_point(g, in, o);
         if (add) v += beta * add[i];
         out[i] = v;
+    } else {
+        for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
+             i += (int64_t)gridDim.x * blockDim.x) {
+            int64_t o[3] = {0, 0, 0};
+            mgd::unflatten(g.m, g.dim, i, o);
+            T v = alpha * mgd::refine_point(g, in, o);
+            if (add) v += beta * add[i];
+            out[i] = v;
+        }
     }
 }
 
-template <typename T, int DIM, int CELL>
+template <typename T, int DIM, int CELL, bool ROWS>
 __global__ void __launch_bounds__(kThreads)
     mgd_refine_t_kernel(Grid g, const T* __restrict__ gf, T* __restrict__ gc,
                         T* __restrict__ wc, T alpha_c, T* __restrict__ wf, T beta_f,
                         int64_t total) {
     g.dim = DIM;
     g.cell = CELL;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
-         i += (int64_t)gridDim.x * blockDim.x) {
-        int64_t q[3] = {0, 0, 0};
-        mgd::unflatten(g.n, g.dim, i, q);
+    if constexpr (ROWS) {
+        int64_t q[3], i;
+        if (!row_index<DIM, ROWS>(g.n, q, &i)) return;
         const T v = mgd::refine_adjoint_point(g, gf, q);
         if (gc) gc[i] = v;
         if (wc) wc[i] = alpha_c * v;
         if (wf) mgd::scale_owned(g, gf, wf, beta_f, q);
+    } else {
+        for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
+             i += (int64_t)gridDim.x * blockDim.x) {
+            int64_t q[3] = {0, 0, 0};
+            mgd::unflatten(g.n, g.dim, i, q);
+            const T v = mgd::refine_adjoint_point(g, gf, q);
+            if (gc) gc[i] = v;
+            if (wc) wc[i] = alpha_c * v;
+            if (wf) mgd::scale_owned(g, gf, wf, beta_f, q);
+        }
     }
+}
+
+// The row grid of an index grid `size` of `dim` axes, if it fits.
+bool row_grid(const int64_t* size, int dim, dim3* grid) {
+    const int64_t bx = (size[dim - 1] + kThreads - 1) / kThreads;
+    const int64_t by = dim >= 2 ? size[dim - 2] : 1;
+    const int64_t bz = dim == 3 ? size[0] : 1;
+    if (bx > 0x7fffffff || by > 65535 || bz > 65535) return false;
+    *grid = dim3((unsigned)bx, (unsigned)by, (unsigned)bz);
+    return true;
 }
 
 int make_grid(int32_t dim, const int64_t* n, int32_t cell, Grid* g) {
@@ -80,17 +123,26 @@ int refine_impl(int32_t dim, const int64_t* n, int32_t cell, const T* in, T* out
     if (st) return st;
     if (!in || !out) return ODIL_ERR_ARG;
     const int64_t total = g.m[0] * g.m[1] * g.m[2];
-    decltype(&mgd_refine_kernel<T, 1, 0>) kern;
-    switch (dim * 2 + cell) {
-        case 2: kern = mgd_refine_kernel<T, 1, 0>; break;
-        case 3: kern = mgd_refine_kernel<T, 1, 1>; break;
-        case 4: kern = mgd_refine_kernel<T, 2, 0>; break;
-        case 5: kern = mgd_refine_kernel<T, 2, 1>; break;
-        case 6: kern = mgd_refine_kernel<T, 3, 0>; break;
-        default: kern = mgd_refine_kernel<T, 3, 1>; break;
+    dim3 rg;
+    const bool rows = row_grid(g.m, dim, &rg);
+    decltype(&mgd_refine_kernel<T, 1, 0, true>) kern;
+#define ODIL_MGD_PICK(R)                                                  \
+    switch (dim * 2 + cell) {                                             \
+        case 2: kern = mgd_refine_kernel<T, 1, 0, R>; break;              \
+        case 3: kern = mgd_refine_kernel<T, 1, 1, R>; break;              \
+        case 4: kern = mgd_refine_kernel<T, 2, 0, R>; break;              \
+        case 5: kern = mgd_refine_kernel<T, 2, 1, R>; break;              \
+        case 6: kern = mgd_refine_kernel<T, 3, 0, R>; break;              \
+        default: kern = mgd_refine_kernel<T, 3, 1, R>; break;             \
     }
-    kern<<<grid_blocks(total), kThreads, 0, as_stream(stream)>>>(g, in, out, (T)alpha, add,
-                                                                 (T)beta, total);
+    if (rows) {
+        ODIL_MGD_PICK(true)
+    } else {
+        ODIL_MGD_PICK(false)
+    }
+#undef ODIL_MGD_PICK
+    const dim3 grid = rows ? rg : dim3((unsigned)grid_blocks(total));
+    kern<<<grid, kThreads, 0, as_stream(stream)>>>(g, in, out, (T)alpha, add, (T)beta, total);
     return launch_status();
 }
 
@@ -102,17 +154,27 @@ int refine_t_impl(int32_t dim, const int64_t* n, int32_t cell, const T* gf, T* g
     if (st) return st;
     if (!gf || (!gc && !wc && !wf)) return ODIL_ERR_ARG;
     const int64_t total = g.n[0] * g.n[1] * g.n[2];
-    decltype(&mgd_refine_t_kernel<T, 1, 0>) kern;
-    switch (dim * 2 + cell) {
-        case 2: kern = mgd_refine_t_kernel<T, 1, 0>; break;
-        case 3: kern = mgd_refine_t_kernel<T, 1, 1>; break;
-        case 4: kern = mgd_refine_t_kernel<T, 2, 0>; break;
-        case 5: kern = mgd_refine_t_kernel<T, 2, 1>; break;
-        case 6: kern = mgd_refine_t_kernel<T, 3, 0>; break;
-        default: kern = mgd_refine_t_kernel<T, 3, 1>; break;
+    dim3 rg;
+    const bool rows = row_grid(g.n, dim, &rg);
+    decltype(&mgd_refine_t_kernel<T, 1, 0, true>) kern;
+#define ODIL_MGD_PICK(R)                                                  \
+    switch (dim * 2 + cell) {                                             \
+        case 2: kern = mgd_refine_t_kernel<T, 1, 0, R>; break;            \
+        case 3: kern = mgd_refine_t_kernel<T, 1, 1, R>; break;            \
+        case 4: kern = mgd_refine_t_kernel<T, 2, 0, R>; break;            \
+        case 5: kern = mgd_refine_t_kernel<T, 2, 1, R>; break;            \
+        case 6: kern = mgd_refine_t_kernel<T, 3, 0, R>; break;            \
+        default: kern = mgd_refine_t_kernel<T, 3, 1, R>; break;           \
     }
-    kern<<<grid_blocks(total), kThreads, 0, as_stream(stream)>>>(g, gf, gc, wc, (T)alpha_c, wf,
-                                                                 (T)beta_f, total);
+    if (rows) {
+        ODIL_MGD_PICK(true)
+    } else {
+        ODIL_MGD_PICK(false)
+    }
+#undef ODIL_MGD_PICK
+    const dim3 grid = rows ? rg : dim3((unsigned)grid_blocks(total));
+    kern<<<grid, kThreads, 0, as_stream(stream)>>>(g, gf, gc, wc, (T)alpha_c, wf, (T)beta_f,
+                                                   total);
     return launch_status();
 }
 
