@@ -66,6 +66,7 @@ def parse():
     ap.add_argument("--case", default=None,
                     choices=("march", "march64", "update_residual", "loss_grad",
                              "loss_grad64", "loss_grad_big", "lbfgs_iter",
+                             "lbfgs_run",
                              "adam_iter", "batch", "ns_newton", "advect",
                              "ns_inverse", "ns_mg", "generic", "cavity",
                              "batch_block", "pair_residual", "batch_lg",
@@ -308,7 +309,10 @@ def run_optimizers(problem, inst, dev, with_oracle):
                          ("adam", lg, torch.float32),
                          ("lbfgsb_fp64", lg64, torch.float64),
                          ("adamn_fp64", lg64, torch.float64)):
-        opt = make_optimizer(name.replace("_fp64", ""))
+        # L-BFGS replays each steady-state iteration from a CUDA graph (the
+        # loss_grad here is capturable); same iterates as eager launches.
+        opt = make_optimizer(name.replace("_fp64", ""),
+                             **({"graph": True} if "lbfgs" in name else {}))
         x0 = torch.zeros(NT * NX, dtype=dt, device=dev)
         torch.cuda.synchronize(dev)
         t0 = time.perf_counter()
@@ -322,6 +326,7 @@ def run_optimizers(problem, inst, dev, with_oracle):
             x.reshape(NT, NX))
         ent = {"iterations": int(info.epochs), "evals": int(info.evals),
                "host_line_searches": getattr(info, "fallbacks", None),
+               "graph_replays": getattr(info, "replays", None),
                "wall_s": wall, "ms_per_iter": 1000 * wall / max(1, info.epochs),
                "initial_loss": l0, "final_loss": float(loss.item()),
                "err_vs_exact_l2": float(np.mean((xs - inst.exact_u)**2)**0.5)}
@@ -350,6 +355,7 @@ def run_optimizers(problem, inst, dev, with_oracle):
 
 
 LBFGS_ITERS, LBFGS_M, REFINE_EPOCHS = 20, 10, 2
+LBFGS_RUN_ITERS = 80
 
 
 def run_batch(dev, with_oracle, steps=5, hbm=6800.0):
@@ -517,6 +523,36 @@ def graph_time_ms(fn, dev, reps=10, rounds=5):
     e1.record(st)
     torch.cuda.synchronize(dev)
     return e0.elapsed_time(e1) / (reps * rounds)
+
+
+def graph_time_rotating_ms(fns, dev, rounds=5):
+    """Per-launch device time of the thunks `fns` (the same kernel on
+    different buffers, together larger than L2) captured back to back into
+    one CUDA graph and replayed `rounds` times between CUDA events: no host
+    gap between launches, and each launch reads data that the launches in
+    between have evicted from L2."""
+    import torch
+    for f in fns:
+        f()
+    torch.cuda.synchronize(dev)
+    side = torch.cuda.Stream(dev)
+    side.wait_stream(torch.cuda.current_stream(dev))
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=side):
+        for f in fns:
+            f()
+    torch.cuda.current_stream(dev).wait_stream(side)
+    g.replay()
+    torch.cuda.synchronize(dev)
+    st = torch.cuda.current_stream(dev)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    for _ in range(rounds):
+        g.replay()
+    e1.record(st)
+    torch.cuda.synchronize(dev)
+    return e0.elapsed_time(e1) / (len(fns) * rounds)
 
 
 ADV_N = 256
@@ -851,6 +887,13 @@ def run_ours(args):
     u32 = u.float()
     g32 = torch.empty_like(u32)
     t_lg = timed(lambda: k.loss_grad(u32, grad=g32), 20, 3)
+    # The same launch as it runs inside an optimizer iteration (graph
+    # replay, no host gap), rotating over 24 field/gradient pairs (192 MiB,
+    # more than L2) so that every launch reads its field from HBM.
+    rot = [(u32 + 0.0, torch.empty_like(u32)) for _ in range(24)]
+    lg_graph_ms = graph_time_rotating_ms(
+        [lambda a=a, b=b: k.loss_grad(a, grad=b) for a, b in rot], dev)
+    del rot
     # The same fused loss+adjoint kernel on an 8192^2 grid (256 MiB in,
     # 256 MiB out): HBM-bound, so its roofline fraction is meaningful.
     big = WaveInstance(BIG, BIG, profile="sine", seed=SEED, nmodes=NMODES,
@@ -990,6 +1033,10 @@ def run_ours(args):
             "march_f64_ms": statistics.mean(t_march64),
             "loss_grad_f32_ms": statistics.mean(t_lg),
             "loss_grad_f32_GBs": lg_bytes / (statistics.mean(t_lg) * 1e6),
+            "loss_grad_f32_graph_ms": lg_graph_ms,
+            "loss_grad_f32_graph_GBs": lg_bytes / (lg_graph_ms * 1e6),
+            "loss_grad_f32_graph_frac_of_measured_hbm":
+                lg_bytes / (lg_graph_ms * 1e6) / (hbm or 6800.0),
             "loss_grad_f32_8192sq_ms": statistics.mean(t_lg_big),
             "loss_grad_f32_8192sq_GBs": 8 * BIG * BIG /
                                         (statistics.mean(t_lg_big) * 1e6),
@@ -1241,6 +1288,19 @@ def run_case(args):
         sop = J[0][0]
         sv = torch.randn((nn, nn), dtype=torch.float64, device=dev)
         so = torch.empty_like(sv)
+    if args.case == "lbfgs_run":
+        # The device L-BFGS (m = 50, graph replays from iteration 51) on the
+        # 1024^2 FP32 wave loss: one call = LBFGS_RUN_ITERS iterations.
+        from odil_gb300.optimizer import LbfgsOptimizer
+        i32 = WaveInstance(NT, NX, profile="sine", seed=SEED, nmodes=NMODES,
+                           c=C, dtype=np.float32, device=dev)
+        k32 = Problem(i32.operator, i32.domain).kernels
+
+        def lg32(x, epoch):
+            loss, gg = k32.loss_grad(x.reshape(NT, NX), grad=g32)
+            return loss, gg.reshape(-1), [loss]
+
+        x32 = torch.zeros(n, dtype=torch.float32, device=dev)
     if args.case == "mgdecomp":
         from odil_gb300.multigrid import MultigridDecomp
         w2 = torch.randn((1025, 1025), dtype=torch.float32, device=dev)
@@ -1268,6 +1328,8 @@ def run_case(args):
                                               d32.reshape(-1)]),
                                vec.lincomb(g32.reshape(-1), u32.reshape(-1), H,
                                            2 * m, coef)),
+        "lbfgs_run": lambda: LbfgsOptimizer(graph=True).run(
+            x32, lg32, epochs=LBFGS_RUN_ITERS),
         "adam_iter": lambda: vec.adam_step(u32.reshape(-1), g32.reshape(-1),
                                            mm, vv, 1e-3, 0.9, 0.999, 1e-7),
     }[args.case]

@@ -257,13 +257,15 @@ typedef struct odil_wave_batch {
 /* Loss and fused adjoint gradient of every instance in one launch (FP32):
  * loss[i] = mean(f_i^2) over instance i's cells, grad_i = (2/N_i) J_i^T f_i
  * (util_op.py:627-654 per instance), total = sum_i loss[i] (the loss of the
- * batch as one optimisation problem).  tile_start [ninst + 1]: first tile of
- * each instance, tiles of 120 columns x 32 rows numbered instance by
- * instance (ceil(nx/120) * ceil(nt/32) per instance), ntiles the total;
- * tile_inst [ntiles]: the instance of each tile; init_u .. right_u: the
- * packed boundary arrays in FP32; partials: ntiles doubles of scratch; total
- * may be null.  Requires odil_wave_batch_setup.
+ * batch as one optimisation problem).  The work is split into items
+ * (strips of columns by tiles of rows) numbered instance by instance:
+ * odil_wave_batch_loss_grad_items(nt, nx) gives an instance's item count;
+ * tile_start [ninst + 1]: the first item of each instance (tile_start[ninst]
+ * = ntiles, the total); tile_inst [ntiles]: the instance of each item;
+ * init_u .. right_u: the packed boundary arrays in FP32; partials: ntiles
+ * doubles of scratch; total may be null.  Requires odil_wave_batch_setup.
  * The batched form of the per-run loss of vary_wave.py:37-43. */
+int64_t odil_wave_batch_loss_grad_items(int64_t nt, int64_t nx);
 int odil_wave_batch_loss_grad_f32(const odil_wave_batch* b,
                                   const int64_t* tile_start,
                                   const int32_t* tile_inst, int64_t ntiles,
@@ -695,7 +697,10 @@ int odil_lincomb_f64(double* out, const double* x, const double* M,
  *   update: ring, S^T Y, Y^T Y, gamma and the dots with the new gradient
  *           from P ([rows][3] dots of H's rows with (g_trial, s, y)) and
  *           Q ([[s.y, s.g_trial], [y.y, y.g_trial]]);
- *   commit: H rows of the updated slot <- (s, y). */
+ *   commit: H rows of the updated slot <- (s, y), and g <- g_trial when g
+ *           is given (accepted steps only; every kernel after the Wolfe test
+ *           is guarded by the status, so an iteration can be enqueued, or
+ *           captured in a CUDA graph, before the host reads it). */
 int odil_lbfgs_coef(int32_t m, int32_t gidx, const int* ring, const double* SY,
                     const double* YY, const double* dg, const double* sc,
                     double* coef, void* stream);
@@ -716,9 +721,11 @@ int odil_lbfgs_update(int* ring, double* SY, double* YY, double* dg,
                       double* sc, const double* P, int32_t rows,
                       const double* Q, void* stream);
 int odil_lbfgs_commit_f32(int64_t n, float* H, int64_t ld, const float* sy,
-                          const int* ring, const double* sc, void* stream);
+                          float* g, const float* gt, const int* ring,
+                          const double* sc, void* stream);
 int odil_lbfgs_commit_f64(int64_t n, double* H, int64_t ld, const double* sy,
-                          const int* ring, const double* sc, void* stream);
+                          double* g, const double* gt, const int* ring,
+                          const double* sc, void* stream);
 
 /* ------------------------------------------------------------------------
  * Multigrid decomposition of a field: the field is the sum over levels l of

@@ -226,8 +226,9 @@ SIGNATURES = {
     "odil_lbfgs_pair_f64": (_INT, [_I64, _P, _P, _P, _P, _P, _P]),
     "odil_lbfgs_update": (_INT, [_P, _P, _P, _P, _P, _P, ctypes.c_int32, _P,
                                  _P]),
-    "odil_lbfgs_commit_f32": (_INT, [_I64, _P, _I64, _P, _P, _P, _P]),
-    "odil_lbfgs_commit_f64": (_INT, [_I64, _P, _I64, _P, _P, _P, _P]),
+    "odil_lbfgs_commit_f32": (_INT, [_I64, _P, _I64, _P, _P, _P, _P, _P, _P]),
+    "odil_lbfgs_commit_f64": (_INT, [_I64, _P, _I64, _P, _P, _P, _P, _P, _P]),
+    "odil_wave_batch_loss_grad_items": (_I64, [_I64, _I64]),
     "odil_wave_batch_loss_grad_f32": (_INT, [_P, _P, _P, _I64, _P, _P, _P, _P,
                                              _P, _P, _P, _P, _P, _P]),
     "odil_ns_num_equations": (_INT, [_P]),

@@ -90,9 +90,11 @@ class WaveBatch:
         self.march_cfg = None
         self.graph = None
         # Fused loss + gradient of all instances: FP32 boundary data and the
-        # tile tables (120-column x 32-row tiles, instance by instance).
+        # work-item tables (the kernel's items per instance, instance by
+        # instance).
         self.bc32 = [t.float() for t in self.bc]
-        tiles = [((nx + 119) // 120) * ((nt + 31) // 32)
+        lib = _capi.load()
+        tiles = [int(lib.odil_wave_batch_loss_grad_items(nt, nx))
                  for nt, nx in self.shapes]
         self.ntiles = int(sum(tiles))
         self.tile_start = torch.as_tensor(
@@ -150,7 +152,8 @@ class WaveBatch:
             return loss, g, [loss]
 
         x0 = torch.zeros(self.total, dtype=torch.float32, device=self.device)
-        return LbfgsOptimizer(m=m).run_device(x0, lg, epochs=iters)
+        return LbfgsOptimizer(m=m, graph=True).run_device(x0, lg,
+                                                          epochs=iters)
 
     def refine(self, u0, epochs=2):
         """Mixed-precision Newton epochs from the FP64 iterate u0 (FP64

@@ -257,22 +257,54 @@ int launch_batch_march(const odil_wave_batch* b, const float* rhs, float* x, uns
     return launch_status();
 }
 
-// Fused loss + adjoint gradient of every instance in one launch (FP32): one
-// block per tile of the single-instance strip march (lg_strip, 32-row
-// tiles), blocks numbered instance by instance (tile_start: first block of
+// Fused loss + adjoint gradient of every instance in one launch (FP32).
+// Work items are strips of BLG_OUT output columns by BLG_TY rows, numbered
+// instance by instance, row tile by row tile (tile_start: first item of
 // each instance, tile_start[ninst] = total; tile_inst: the instance of each
-// block).  Each instance's gradient is (2 / N_i) J_i^T f_i, the gradient of
-// its own loss mean(f_i^2); the per-block sums go to partials.
+// item); one warp per item, BLG_WARPS independent warps per block.
+//
+// Lane l holds BLG_V = 4 contiguous columns c0 - 1 + 4 l + j of a 128-column
+// window (the first and last column are halo; lanes 0 and 31 load one more
+// column each for the halo's residual).  Per row the warp reads u once
+// (four 4-byte loads per lane: rows of uneven widths give no 16-byte
+// alignment), forms the residual of the row from registers and two
+// shuffles, and the gradient of the row two above from the residual rows
+// below it and two more shuffles.  Column classes are per-lane constants
+// (the d f/d u coefficients of the J^T gather, formed once per item), so
+// every cell takes the same instructions; only the residual at columns 0
+// and nx - 1 (one lane each: the boundary extrapolation), rows 0, 1 of the
+// residual and rows 0, nt - 2, nt - 1 of the gradient take the general
+// per-cell functions.  Rows stream in chunks of BLG_Q: the next chunk's
+// loads are issued before the current chunk is processed.  128 registers
+// (4 blocks of 4 warps per SM) hold it without spills.
+constexpr int BLG_V = 4;
+constexpr int BLG_OUT = 32 * BLG_V - 2;  // output columns per item
 constexpr int BLG_TY = 32;
+constexpr int BLG_Q = 2;
+constexpr int BLG_WARPS = 4;
 
-__global__ void __launch_bounds__(LG_WARPS * 32) batch_loss_grad_kernel(
+// Residual of an interior cell (row >= 2, 0 < column < nx - 1): the
+// expression of wave_f_with for such cells.
+__device__ __forceinline__ float blg_f(const WaveDev<float>& g, float u, float utm, float utmm,
+                                      float uxm, float uxp) {
+    const float u_t_tm = (u - utm) * g.inv_dt;
+    const float u_t_tmm = (utm - utmm) * g.inv_dt;
+    const float u_tt = (u_t_tm - u_t_tmm) * g.inv_dt;
+    const float u_xx = (uxm - 2.f * utm + uxp) * g.inv_dx2;
+    return u_tt - g.c2 * u_xx;
+}
+
+__global__ void __launch_bounds__(BLG_WARPS * 32, 4) batch_loss_grad_kernel(
     const odil_wave_instance* __restrict__ inst, const int32_t* __restrict__ tile_inst,
-    const int64_t* __restrict__ tile_start, const float* __restrict__ iu,
+    const int64_t* __restrict__ tile_start, int64_t nitems, const float* __restrict__ iu,
     const float* __restrict__ iut, const float* __restrict__ lu, const float* __restrict__ ru,
     const float* __restrict__ u, float* __restrict__ grad, double* __restrict__ partials) {
-    const int64_t blk = blockIdx.x;
-    const int lo = __ldg(tile_inst + blk);
-    const odil_wave_instance& d = inst[lo];
+    constexpr int V = BLG_V;
+    const int lane = threadIdx.x & 31;
+    const int64_t item = (int64_t)blockIdx.x * BLG_WARPS + (threadIdx.x >> 5);
+    if (item >= nitems) return;  // the whole warp
+    const int qi = __ldg(tile_inst + item);
+    const odil_wave_instance& d = inst[qi];
     WaveDev<float> g;
     g.nt = (int)d.nt;
     g.nx = (int)d.nx;
@@ -288,13 +320,153 @@ __global__ void __launch_bounds__(LG_WARPS * 32) batch_loss_grad_kernel(
     g.init_ut = iut + d.offset_x;
     g.left_u = lu + d.offset_t;
     g.right_u = ru + d.offset_t;
-    const int gx = (g.nx + LG_WARPS * LG_OUT - 1) / (LG_WARPS * LG_OUT);
-    const int64_t t = blk - __ldg(tile_start + lo);
-    const int bx = (int)(t % gx), by = (int)(t / gx);
-    const float gscale = (float)(2.0 / ((double)g.nt * (double)g.nx));
-    const float lsum = lg_strip<float, BLG_TY>(g, u + d.offset, grad + d.offset, bx, by, gscale);
-    const double sblk = block_sum((double)lsum);
-    if (threadIdx.x == 0) partials[blk] = sblk;
+    const int nt = g.nt, nx = g.nx;
+    const float A = g.A, B = g.B;
+    const int nsx = (nx + BLG_OUT - 1) / BLG_OUT;
+    const int t = (int)(item - __ldg(tile_start + qi));
+    const int ty = t / nsx, sx = t - ty * nsx;
+    const int c0 = sx * BLG_OUT;       // first output column
+    const int a0 = ty * BLG_TY;        // first output row
+    const int cb = c0 - 1 + V * lane;  // column of this lane's element 0
+    const float* __restrict__ ui = u + d.offset;
+    float* __restrict__ gi = grad + d.offset;
+    // Narrow grids (nx < 3) have no interior column: general functions only.
+    const bool gen = nx < 3;
+    const float gscale = (float)(2.0 / ((double)nt * (double)nx));
+    int off[V];
+    float ctm[V], kxm1[V], kxp1[V];
+    unsigned outm = 0, fixm = 0;
+#pragma unroll
+    for (int j = 0; j < V; ++j) {
+        const int col = cb + j;
+        const int cw = wrapn(col, nx);
+        off[j] = cw;
+        const int bp = (cw + 1 == nx) ? 0 : cw + 1;
+        const int bm = (cw == 0) ? nx - 1 : cw - 1;
+        ctm[j] = -2.f * A + B * k_tm<float>(cw, nx);
+        kxm1[j] = k_xm<float>(bp, nx);
+        kxp1[j] = k_xp<float>(bm, nx);
+        if (col >= c0 && col < c0 + BLG_OUT && col < nx) outm |= 1u << j;
+        if (col == 0 || col == nx - 1) fixm |= 1u << j;
+    }
+    const int offe = lane == 0 ? wrapn(c0 - 2, nx) : wrapn(c0 + 32 * V - 1, nx);
+    const bool xl = lane == 0 || lane == 31;
+
+    float u1[V], u2[V], f1[V], f2[V];
+#pragma unroll
+    for (int j = 0; j < V; ++j) u1[j] = u2[j] = f1[j] = f2[j] = 0.f;
+    float e1 = 0.f;
+    float lsum = 0.f;
+    float uq[BLG_Q][V], eq[BLG_Q], un[BLG_Q][V], en[BLG_Q];
+    auto load_chunk = [&](int q0, float (&uu)[BLG_Q][V], float (&ee)[BLG_Q]) {
+#pragma unroll
+        for (int jj = 0; jj < BLG_Q; ++jj) {
+            const int r = a0 - 2 + q0 + jj;
+            const bool ok = q0 + jj < BLG_TY + 4 && r >= 0 && r < nt;
+            const float* row = ui + (int64_t)r * nx;
+#pragma unroll
+            for (int j = 0; j < V; ++j) uu[jj][j] = ok ? __ldg(row + off[j]) : 0.f;
+            ee[jj] = (ok && xl) ? __ldg(row + offe) : 0.f;
+        }
+    };
+    load_chunk(0, uq, eq);
+    for (int q0 = 0; q0 < BLG_TY + 4; q0 += BLG_Q) {
+        load_chunk(q0 + BLG_Q, un, en);
+#pragma unroll
+        for (int jj = 0; jj < BLG_Q; ++jj) {
+            const int qq = q0 + jj;
+            const int r = a0 - 2 + qq;
+            // x-neighbours of row r-1 at the lane's end columns.
+            float um0 = __shfl_up_sync(0xffffffffu, u1[V - 1], 1);
+            float upv = __shfl_down_sync(0xffffffffu, u1[0], 1);
+            if (lane == 0) um0 = e1;
+            if (lane == 31) upv = e1;
+            if (qq >= 2) {
+                float f0[V];
+                if (r < nt) {
+                    if (r >= 2 && !gen) {
+#pragma unroll
+                        for (int j = 0; j < V; ++j) {
+                            const float um = j == 0 ? um0 : u1[j - 1];
+                            const float up = j == V - 1 ? upv : u1[j + 1];
+                            f0[j] = blg_f(g, uq[jj][j], u1[j], u2[j], um, up);
+                        }
+                        if (fixm) {
+#pragma unroll
+                            for (int j = 0; j < V; ++j) {
+                                if (fixm & (1u << j)) {
+                                    const float um = j == 0 ? um0 : u1[j - 1];
+                                    const float up = j == V - 1 ? upv : u1[j + 1];
+                                    f0[j] = wave_f(g, r, off[j], uq[jj][j], u1[j], u2[j], um, up);
+                                }
+                            }
+                        }
+                    } else {
+#pragma unroll
+                        for (int j = 0; j < V; ++j) {
+                            const float um = j == 0 ? um0 : u1[j - 1];
+                            const float up = j == V - 1 ? upv : u1[j + 1];
+                            f0[j] = wave_f(g, r, off[j], uq[jj][j], u1[j], u2[j], um, up);
+                        }
+                    }
+                } else {
+#pragma unroll
+                    for (int j = 0; j < V; ++j) f0[j] = 0.f;
+                }
+                // Gradient of row a = r - 2 from f rows a, a+1 (with its
+                // x-neighbours) and a+2.
+                const int a = r - 2;
+                if (qq >= 4 && a < nt) {
+                    const float fm0 = __shfl_up_sync(0xffffffffu, f1[V - 1], 1);
+                    const float fpv = __shfl_down_sync(0xffffffffu, f1[0], 1);
+                    float gv[V];
+                    if (a >= 1 && a + 2 < nt && !gen) {
+#pragma unroll
+                        for (int j = 0; j < V; ++j) {
+                            const float f1m = j == 0 ? fm0 : f1[j - 1];
+                            const float f1p = j == V - 1 ? fpv : f1[j + 1];
+                            gv[j] = A * (f2[j] + f0[j]) + ctm[j] * f1[j] -
+                                    B * (kxm1[j] * f1p + kxp1[j] * f1m);
+                        }
+                    } else {
+#pragma unroll
+                        for (int j = 0; j < V; ++j) {
+                            const float f1m = j == 0 ? fm0 : f1[j - 1];
+                            const float f1p = j == V - 1 ? fpv : f1[j + 1];
+                            gv[j] = wave_gather(g, a, off[j], f2[j], f1[j], f0[j], f1p, f1m);
+                        }
+                    }
+                    float* __restrict__ grow = gi + (int64_t)a * nx + cb;
+#pragma unroll
+                    for (int j = 0; j < V; ++j) {
+                        if (outm & (1u << j)) {
+                            grow[j] = gv[j] * gscale;
+                            lsum += f2[j] * f2[j];
+                        }
+                    }
+                }
+#pragma unroll
+                for (int j = 0; j < V; ++j) {
+                    f2[j] = f1[j];
+                    f1[j] = f0[j];
+                }
+            }
+#pragma unroll
+            for (int j = 0; j < V; ++j) {
+                u2[j] = u1[j];
+                u1[j] = uq[jj][j];
+            }
+            e1 = eq[jj];
+        }
+#pragma unroll
+        for (int jj = 0; jj < BLG_Q; ++jj) {
+#pragma unroll
+            for (int j = 0; j < V; ++j) uq[jj][j] = un[jj][j];
+            eq[jj] = en[jj];
+        }
+    }
+    const double sw = warp_sum((double)lsum);
+    if (lane == 0) partials[item] = sw;
 }
 
 // loss[i] = (sum of instance i's block sums) / N_i, one warp per instance
@@ -340,12 +512,18 @@ ODIL_API int odil_wave_batch_loss_grad_f32(const odil_wave_batch* b, const int64
         !partials || !loss)
         return ODIL_ERR_ARG;
     cudaStream_t s = as_stream(stream);
-    batch_loss_grad_kernel<<<(unsigned)ntiles, LG_WARPS * 32, 0, s>>>(
-        b->inst, tile_inst, tile_start, init_u, init_ut, left_u, right_u, u, grad, partials);
+    batch_loss_grad_kernel<<<(unsigned)((ntiles + BLG_WARPS - 1) / BLG_WARPS), BLG_WARPS * 32, 0,
+                             s>>>(b->inst, tile_inst, tile_start, ntiles, init_u, init_ut, left_u,
+                                  right_u, u, grad, partials);
     batch_loss_finish_kernel<<<(unsigned)((b->ninst * 32 + 255) / 256), 256, 0, s>>>(
         b->inst, b->ninst, tile_start, partials, loss);
     if (total) batch_loss_total_kernel<<<1, 256, 0, s>>>(loss, b->ninst, total);
     return launch_status();
+}
+
+ODIL_API int64_t odil_wave_batch_loss_grad_items(int64_t nt, int64_t nx) {
+    if (nt < 1 || nx < 1) return ODIL_ERR_SHAPE;
+    return ((nx + BLG_OUT - 1) / BLG_OUT) * ((nt + BLG_TY - 1) / BLG_TY);
 }
 
 ODIL_API int odil_wave_batch_setup(odil_wave_instance* inst, int32_t ninst, void* stream) {

@@ -28,59 +28,174 @@ constexpr int kMaxM = 128;
 
 // coef[gidx + 1] of d = sum_{row < gidx} coef[row] H[row] + coef[gidx] g =
 // -H_k g; gidx (even, 2 <= gidx <= 2m) covers every held slot.
-__global__ void __launch_bounds__(32) lbfgs_coef_kernel(int gidx, const int* __restrict__ ring,
+//
+// The k x k block R = S^T Y of the held pairs, in pair order, is staged in
+// shared memory (row stride k | 1, odd, so the column reads of warp 0 spread
+// over the banks) by the whole block, each thread issuing all of its loads
+// before its stores.  The two triangular solves are right-looking on warp 0:
+// lane l keeps the running right-hand sides of pairs l, l + 32, l + 64,
+// l + 96 in registers; per pair the owner's value times the stored
+// reciprocal of the diagonal is shuffled to every lane, which subtracts its
+// multiple -- one shuffle and one multiply-add on the dependency chain per
+// pair instead of a warp reduction.  The product with Y^T Y in between is
+// spread over all warps.
+constexpr int CT = 256;
+constexpr int CQ = kMaxM / 32;
+
+__host__ __device__ __forceinline__ int coef_ld(int k) { return k | 1; }
+
+// x <- R^-1 x (kTrans = false, R upper) or R^-T x (kTrans = true) on one
+// warp; x[q] holds the entry of pair 32 q + lane.
+template <bool kTrans>
+__device__ __forceinline__ void coef_trsv(const double* __restrict__ R, int ld,
+                                          const double* __restrict__ rinv, int k, int lane,
+                                          double (&x)[CQ]) {
+    if (!kTrans) {
+        // Backward: pair r from k-1 down; rows c < r lose R[c][r] x[r].
+#pragma unroll
+        for (int qb = CQ - 1; qb >= 0; --qb) {
+            for (int rr = 31; rr >= 0; --rr) {
+                const int r = 32 * qb + rr;
+                if (r >= k) continue;
+                const double xr = __shfl_sync(0xffffffffu, x[qb], rr) * rinv[r];
+                if (lane == rr) x[qb] = xr;
+#pragma unroll
+                for (int q = 0; q <= qb; ++q) {
+                    const int c = 32 * q + lane;
+                    if (c < r) x[q] = fma(-R[c * ld + r], xr, x[q]);
+                }
+            }
+        }
+    } else {
+        // Forward with R^T: pair r from 0 up; rows c > r lose R[r][c] x[r].
+#pragma unroll
+        for (int qb = 0; qb < CQ; ++qb) {
+            for (int rr = 0; rr < 32; ++rr) {
+                const int r = 32 * qb + rr;
+                if (r >= k) break;
+                const double xr = __shfl_sync(0xffffffffu, x[qb], rr) * rinv[r];
+                if (lane == rr) x[qb] = xr;
+#pragma unroll
+                for (int q = qb; q < CQ; ++q) {
+                    const int c = 32 * q + lane;
+                    if (c > r && c < k) x[q] = fma(-R[r * ld + c], xr, x[q]);
+                }
+            }
+        }
+    }
+}
+
+__global__ void __launch_bounds__(CT) lbfgs_coef_kernel(int mcap, int gidx,
+                                                        const int* __restrict__ ring,
                                                         const double* __restrict__ SY,
                                                         const double* __restrict__ YY,
                                                         const double* __restrict__ dg,
                                                         const double* __restrict__ sc,
                                                         double* __restrict__ coef) {
-    __shared__ double a[kMaxM], b[kMaxM], t[kMaxM], w[kMaxM], p[kMaxM];
+    extern __shared__ double Rs[];  // [k][coef_ld(k)], R in pair order
+    __shared__ double b[kMaxM], t[kMaxM], w[kMaxM], rinv[kMaxM];
     __shared__ int slot[kMaxM];
-    const int lane = threadIdx.x;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int k = ring[0], head = ring[1], m = ring[2];
-    for (int r = lane; r <= gidx; r += 32) coef[r] = 0.0;
-    __syncwarp();
-    if (k == 0) {
-        if (lane == 0) coef[gidx] = -1.0;
+    for (int r = tid; r <= gidx; r += CT) coef[r] = 0.0;
+    __syncthreads();
+    // No pair held: steepest descent.  The shared block is sized for mcap
+    // pairs; a ring that does not match (not reachable through the
+    // optimizer) takes the same fallback.
+    if (k <= 0 || m != mcap || k > m || head < 0 || head >= m) {
+        if (tid == 0) coef[gidx] = -1.0;
         return;
     }
     const double gamma = sc[1];
-    for (int c = lane; c < k; c += 32) {
-        const int j = (head + c) % m;
-        slot[c] = j;
-        a[c] = dg[2 * j];
-        b[c] = dg[2 * j + 1];
+    const int ld = coef_ld(k);
+    for (int c = tid; c < k; c += CT) slot[c] = (head + c) % m;
+    __syncthreads();
+    for (int e0 = tid; e0 < k * k; e0 += 8 * CT) {
+        double v[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            const int e = e0 + u * CT;
+            const int r = e / k, c = e - r * k;
+            v[u] = e < k * k ? SY[slot[r] * m + slot[c]] : 0.0;
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            const int e = e0 + u * CT;
+            const int r = e / k, c = e - r * k;
+            if (e < k * k) Rs[r * ld + c] = v[u];
+        }
     }
-    __syncwarp();
-    // t = R^-1 a, R = triu(S^T Y) in pair order (backward substitution).
-    for (int r = k - 1; r >= 0; --r) {
-        double s = 0.0;
-        for (int c = r + 1 + lane; c < k; c += 32) s += SY[slot[r] * m + slot[c]] * t[c];
-        s = warp_sum(s);
-        if (lane == 0) t[r] = (a[r] - s) / SY[slot[r] * m + slot[r]];
-        __syncwarp();
+    for (int c = tid; c < k; c += CT) b[c] = dg[2 * slot[c] + 1];
+    __syncthreads();
+    for (int c = tid; c < k; c += CT) rinv[c] = 1.0 / Rs[c * ld + c];
+    __syncthreads();
+    // t = R^-1 a, a = S^T g in pair order.
+    if (warp == 0) {
+        double x[CQ];
+#pragma unroll
+        for (int q = 0; q < CQ; ++q) {
+            const int c = 32 * q + lane;
+            x[q] = c < k ? dg[2 * slot[c]] : 0.0;
+        }
+        coef_trsv<false>(Rs, ld, rinv, k, lane, x);
+#pragma unroll
+        for (int q = 0; q < CQ; ++q) {
+            const int c = 32 * q + lane;
+            if (c < k) t[c] = x[q];
+        }
     }
-    // w = (D + gamma Y^T Y) t - gamma b
-    for (int c = lane; c < k; c += 32) {
-        double s = SY[slot[c] * m + slot[c]] * t[c];
-        for (int e = 0; e < k; ++e) s += gamma * YY[slot[c] * m + slot[e]] * t[e];
-        w[c] = s - gamma * b[c];
+    __syncthreads();
+    // w = (D + gamma Y^T Y) t - gamma b: one warp per pair c, lanes over e,
+    // four pairs per warp with all their loads in flight together.
+    constexpr int CW = CT / 32;
+    for (int cq = warp; cq < k; cq += 4 * CW) {
+        double v[4][CQ];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const int c = cq + i * CW;
+#pragma unroll
+            for (int q = 0; q < CQ; ++q) {
+                const int e = 32 * q + lane;
+                v[i][q] = (c < k && e < k) ? YY[(int64_t)slot[c] * m + slot[e]] : 0.0;
+            }
+        }
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const int c = cq + i * CW;
+            double s = 0.0;
+#pragma unroll
+            for (int q = 0; q < CQ; ++q) {
+                const int e = 32 * q + lane;
+                if (e < k) s = fma(v[i][q], t[e], s);
+            }
+            s = warp_sum(s);
+            if (lane == 0 && c < k) w[c] = Rs[c * ld + c] * t[c] + gamma * s - gamma * b[c];
+        }
     }
-    __syncwarp();
-    // p = R^-T w (forward substitution)
-    for (int r = 0; r < k; ++r) {
-        double s = 0.0;
-        for (int c = lane; c < r; c += 32) s += SY[slot[c] * m + slot[r]] * p[c];
-        s = warp_sum(s);
-        if (lane == 0) p[r] = (w[r] - s) / SY[slot[r] * m + slot[r]];
-        __syncwarp();
+    __syncthreads();
+    // p = R^-T w; coef of s_c is -p_c, of y_c gamma t_c.
+    if (warp == 0) {
+        double x[CQ];
+#pragma unroll
+        for (int q = 0; q < CQ; ++q) {
+            const int c = 32 * q + lane;
+            x[q] = c < k ? w[c] : 0.0;
+        }
+        coef_trsv<true>(Rs, ld, rinv, k, lane, x);
+#pragma unroll
+        for (int q = 0; q < CQ; ++q) {
+            const int c = 32 * q + lane;
+            if (c < k && 2 * slot[c] + 1 < gidx) {
+                coef[2 * slot[c]] = -x[q];
+                coef[2 * slot[c] + 1] = gamma * t[c];
+            }
+        }
+        if (lane == 0) coef[gidx] = -gamma;
     }
-    for (int c = lane; c < k; c += 32) {
-        coef[2 * slot[c]] = -p[c];
-        coef[2 * slot[c] + 1] = gamma * t[c];
-    }
-    if (lane == 0) coef[gidx] = -gamma;
 }
+
+// Dynamic shared memory of lbfgs_coef_kernel for up to m held pairs.
+inline size_t coef_smem(int m) { return (size_t)m * coef_ld(m) * sizeof(double); }
 
 // xt = x + a d with the trial step a chosen on the device from phi'(0) =
 // dots[0]: the steepest-descent step min(1, 1/|g|) while no pair is held,
@@ -211,20 +326,25 @@ __global__ void __launch_bounds__(32) lbfgs_update_kernel(int* __restrict__ ring
     }
 }
 
-// H rows of the slot written by the last update <- (s, y) (accepted only).
+// Accepted step only: H rows of the slot written by the last update <-
+// (s, y) (when the pair was kept), and g <- g_trial (when g is given).
 template <typename T>
 __global__ void __launch_bounds__(LT) lbfgs_commit_kernel(int64_t n, T* __restrict__ H, int64_t ld,
                                                           const T* __restrict__ sy,
+                                                          T* __restrict__ g,
+                                                          const T* __restrict__ gt,
                                                           const int* __restrict__ ring,
                                                           const double* __restrict__ sc) {
+    if (sc[6] != 0.0) return;
     const int slot = ring[3];
-    if (sc[6] != 0.0 || slot < 0) return;
-    T* hs = H + (int64_t)(2 * slot) * ld;
-    T* hy = hs + ld;
+    T* hs = slot >= 0 ? H + (int64_t)(2 * slot) * ld : nullptr;
     const int64_t stride = (int64_t)gridDim.x * LT;
     for (int64_t i = (int64_t)blockIdx.x * LT + threadIdx.x; i < n; i += stride) {
-        hs[i] = sy[i];
-        hy[i] = sy[n + i];
+        if (hs) {
+            hs[i] = sy[i];
+            hs[ld + i] = sy[n + i];
+        }
+        if (g) g[i] = gt[i];
     }
 }
 
@@ -253,11 +373,11 @@ int pair_impl(int64_t n, T* sy, const T* d, const T* gt, const T* g, const doubl
 }
 
 template <typename T>
-int commit_impl(int64_t n, T* H, int64_t ld, const T* sy, const int* ring, const double* sc,
-                void* stream) {
+int commit_impl(int64_t n, T* H, int64_t ld, const T* sy, T* g, const T* gt, const int* ring,
+                const double* sc, void* stream) {
     if (n < 1 || ld < n) return ODIL_ERR_SHAPE;
-    if (!H || !sy || !ring || !sc) return ODIL_ERR_ARG;
-    lbfgs_commit_kernel<T><<<lgrid(n), LT, 0, as_stream(stream)>>>(n, H, ld, sy, ring, sc);
+    if (!H || !sy || !ring || !sc || (g && !gt)) return ODIL_ERR_ARG;
+    lbfgs_commit_kernel<T><<<lgrid(n), LT, 0, as_stream(stream)>>>(n, H, ld, sy, g, gt, ring, sc);
     return launch_status();
 }
 
@@ -271,7 +391,13 @@ ODIL_API int odil_lbfgs_coef(int32_t m, int32_t gidx, const int* ring, const dou
                              void* stream) {
     if (m < 1 || m > kMaxM || gidx < 2 || gidx > 2 * m || gidx % 2) return ODIL_ERR_SHAPE;
     if (!ring || !SY || !YY || !dg || !sc || !coef) return ODIL_ERR_ARG;
-    lbfgs_coef_kernel<<<1, 32, 0, as_stream(stream)>>>(gidx, ring, SY, YY, dg, sc, coef);
+    const size_t smem = coef_smem(m);
+    if (smem > 48 * 1024) {
+        const cudaError_t e = cudaFuncSetAttribute(
+            lbfgs_coef_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return ODIL_ERR_LAUNCH;
+    }
+    lbfgs_coef_kernel<<<1, CT, smem, as_stream(stream)>>>(m, gidx, ring, SY, YY, dg, sc, coef);
     return launch_status();
 }
 
@@ -307,11 +433,13 @@ ODIL_API int odil_lbfgs_update(int* ring, double* SY, double* YY, double* dg, do
     return launch_status();
 }
 
-ODIL_API int odil_lbfgs_commit_f32(int64_t n, float* H, int64_t ld, const float* sy,
-                                   const int* ring, const double* sc, void* stream) {
-    return commit_impl<float>(n, H, ld, sy, ring, sc, stream);
+ODIL_API int odil_lbfgs_commit_f32(int64_t n, float* H, int64_t ld, const float* sy, float* g,
+                                   const float* gt, const int* ring, const double* sc,
+                                   void* stream) {
+    return commit_impl<float>(n, H, ld, sy, g, gt, ring, sc, stream);
 }
-ODIL_API int odil_lbfgs_commit_f64(int64_t n, double* H, int64_t ld, const double* sy,
-                                   const int* ring, const double* sc, void* stream) {
-    return commit_impl<double>(n, H, ld, sy, ring, sc, stream);
+ODIL_API int odil_lbfgs_commit_f64(int64_t n, double* H, int64_t ld, const double* sy, double* g,
+                                   const double* gt, const int* ring, const double* sc,
+                                   void* stream) {
+    return commit_impl<double>(n, H, ld, sy, g, gt, ring, sc, stream);
 }

@@ -309,17 +309,30 @@ __global__ void __launch_bounds__(VT, 3) multidot_vec_kernel(
         }
     }
     const int64_t nchunk = gridDim.y;
+    // All G x R sums in one pass: warp sums, one barrier, then thread o adds
+    // the warps' values of sum o in warp order (deterministic).
+    __shared__ double red[VT / 32][G * R];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
     for (int g = 0; g < G; ++g) {
 #pragma unroll
         for (int j = 0; j < R; ++j) {
-            const double sum = block_sum((double)acc[g][j]);
-            if (g0 + g < k && threadIdx.x == 0)
-                partials[((int64_t)(g0 + g) * R + j) * nchunk + c] = sum;
+            const double v = warp_sum((double)acc[g][j]);
+            if (lane == 0) red[warp][g * R + j] = v;
         }
+    }
+    __syncthreads();
+    if (threadIdx.x < G * R) {
+        const int o = threadIdx.x, g = o / R, j = o - g * R;
+        double sum = 0.0;
+#pragma unroll
+        for (int w = 0; w < VT / 32; ++w) sum += red[w][o];
+        if (g0 + g < k) partials[((int64_t)(g0 + g) * R + j) * nchunk + c] = sum;
+        __threadfence();  // each writer publishes its partial device-wide
     }
     if (counter == nullptr) return;  // multidot_finish_kernel adds them
     __shared__ bool is_last;
+    __syncthreads();  // every partial of the block is written and fenced
     if (threadIdx.x == 0) {
         __threadfence();
         unsigned prev = atomicAdd(counter, 1u);
@@ -418,10 +431,11 @@ int axpby_impl(T* z, const T* x, const T* y, int64_t n, double a, double b, void
     return launch_status();
 }
 
-// Chunk length: about kMdBlocks blocks in all (152 SMs x 3 resident blocks x
-// 4 waves, so the last wave is nearly full), chunks a multiple of 1024
-// elements and at least 4096.
-constexpr int64_t kMdBlocks = 152 * 3 * 4;
+// Chunk length: about kMdBlocks blocks in all (152 SMs x 3 resident blocks:
+// one wave of long-running blocks, so no tail wave and the per-block
+// reduction is paid once per block), chunks a multiple of 1024 elements and
+// at least 4096.
+constexpr int64_t kMdBlocks = 152 * 3;
 
 inline int64_t md_chunk(int64_t n, int k) {
     const int64_t groups = (k + MD_G - 1) / MD_G;

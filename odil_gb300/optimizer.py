@@ -59,9 +59,10 @@ class LbfgsOptimizer(Optimizer):
 
     def __init__(self, pgtol=1e-16, m=50, maxls=50, factr=0, dtype=None,
                  name="lbfgsb", displayname="L-BFGS-B", c1=1e-4, c2=0.9,
-                 **kwargs):
+                 graph=False, **kwargs):
         super().__init__(name=name, displayname=displayname, dtype=dtype)
         self.pgtol = pgtol
+        self.graph = bool(graph)
         self.m = int(m)
         self.maxls = int(maxls)
         self.factr = factr
@@ -108,7 +109,18 @@ class LbfgsOptimizer(Optimizer):
         multi-dot of the stored rows with (g_new, s, y), and one host read of
         the 16 scalars (the status).  A trial that fails the Wolfe test
         (rare once pairs are held) falls back to the host line search from
-        the same state."""
+        the same state.
+
+        With ``graph=True`` (constructor) and a loss_grad that returns device
+        tensors and can be captured (no host synchronisation, fixed
+        buffers), the whole iteration is recorded into a CUDA graph once m
+        pairs have been formed (from then on its launch shapes are fixed),
+        one graph per parity of the iterate buffers, and every later
+        iteration is one replay plus the status read.  The kernels after the
+        Wolfe test are guarded by the status on the device, so a replayed
+        iteration whose trial is rejected changes no state; the host line
+        search then runs eagerly as without graphs.  Iterates are the same
+        as without graphs."""
         from ._capi import call, ptr, stream_handle
         x = x0.detach().clone()
         n = x.numel()
@@ -138,13 +150,12 @@ class LbfgsOptimizer(Optimizer):
         sc[1] = 1.0
         sc[7], sc[8], sc[9] = self.c1, self.c2, eps
         self.last_loss, self.last_residual = float(sc[0]), res
-        info = Namespace(epochs=0, evals=1, task="", fallbacks=0)
+        info = Namespace(epochs=0, evals=1, task="", fallbacks=0, replays=0)
         epochs = epochs if epochs is not None else 1 << 30
-        accepted = 0  # upper bound of the pairs held: rows the dots need
-        st = stream_handle()
-        it = 0
-        while it < epochs:
-            rows = 2 * min(accepted, m)
+
+        def trial(x, xt, rows):
+            """Direction, trial point, loss+gradient there, Wolfe test."""
+            st = stream_handle()
             if rows:
                 call("odil_lbfgs_coef", m, rows, ptr(ring), ptr(SY), ptr(YY),
                      ptr(dg), ptr(sc), ptr(coef), st)
@@ -155,12 +166,48 @@ class LbfgsOptimizer(Optimizer):
             call("odil_lbfgs_trial_" + sfx, n, ptr(xt), ptr(x), ptr(d),
                  ptr(dots), ptr(ring), ptr(sc), st)
             ft, gt, res = loss_grad(xt, self.epoch)
-            self.evals += 1
             ft_dev = ft.reshape(1).double() if isinstance(ft, torch.Tensor) \
                 else torch.tensor([float(ft)], dtype=torch.float64, device=dev)
             dpa = md1(gt, 1, [d])
             call("odil_lbfgs_accept", ptr(ft_dev), ptr(dpa), ptr(sc), st)
-            sc_host.copy_(sc, non_blocking=True)
+            return gt, res
+
+        def update(gt, rows):
+            """Pair, dots, ring/matrix update, commit with g <- g_trial (all
+            guarded by the status on the device)."""
+            st = stream_handle()
+            call("odil_lbfgs_pair_" + sfx, n, ptr(SYp), ptr(d), ptr(gt), ptr(g),
+                 ptr(sc), st)
+            P = md(H, max(rows, 1), [gt, SYp[0], SYp[1]]) if rows else None
+            Q = md2(SYp, 2, [SYp[1], gt])
+            call("odil_lbfgs_update", ptr(ring), ptr(SY), ptr(YY), ptr(dg),
+                 ptr(sc), ptr(P), rows, ptr(Q), st)
+            call("odil_lbfgs_commit_" + sfx, n, ptr(H), n, ptr(SYp), ptr(g),
+                 ptr(gt), ptr(ring), ptr(sc), st)
+
+        graphs = {}          # x.data_ptr() -> (graph, gt, res)
+        use_graph = self.graph
+        accepted = 0  # upper bound of the pairs held: rows the dots need
+        it = 0
+        while it < epochs:
+            rows = 2 * min(accepted, m)
+            replayed = False
+            if use_graph and rows == 2 * m:
+                key = x.data_ptr()
+                if key not in graphs:
+                    graphs[key] = self._capture(
+                        lambda: trial(x, xt, rows), update, rows, sc, sc_host,
+                        dev)
+                    use_graph = graphs[key] is not None
+                if use_graph:
+                    gr, gt, res = graphs[key]
+                    gr.replay()
+                    replayed = True
+                    info.replays += 1
+            if not replayed:
+                gt, res = trial(x, xt, rows)
+                sc_host.copy_(sc, non_blocking=True)
+            self.evals += 1
             torch.cuda.current_stream(dev).synchronize()
             status = int(sc_host[6])
             if status == 2:
@@ -180,15 +227,9 @@ class LbfgsOptimizer(Optimizer):
                     info.task = "ABNORMAL_TERMINATION_IN_LNSRCH"
                     break
                 sc[3], sc[4], sc[6] = alpha, fa, 0.0
-            call("odil_lbfgs_pair_" + sfx, n, ptr(SYp), ptr(d), ptr(gt), ptr(g),
-                 ptr(sc), st)
-            P = md(H, max(rows, 1), [gt, SYp[0], SYp[1]]) if rows else None
-            Q = md2(SYp, 2, [SYp[1], gt])
-            call("odil_lbfgs_update", ptr(ring), ptr(SY), ptr(YY), ptr(dg),
-                 ptr(sc), ptr(P), rows, ptr(Q), st)
-            call("odil_lbfgs_commit_" + sfx, n, ptr(H), n, ptr(SYp), ptr(ring),
-                 ptr(sc), st)
-            g.copy_(gt)
+                update(gt, rows)
+            elif not replayed:
+                update(gt, rows)
             accepted += 1
             x, xt = xt, x
             self.last_loss = float(sc_host[4]) if status == 0 else float(fa)
@@ -200,6 +241,26 @@ class LbfgsOptimizer(Optimizer):
                 callback(x, self.epoch, opt=self)
         info.evals = self.evals
         return x, info
+
+    @staticmethod
+    def _capture(trial, update, rows, sc, sc_host, dev):
+        """One iteration (trial, update, status copy into the pinned host
+        buffer) recorded into a CUDA graph, or None when the loss_grad
+        cannot be captured (it synchronises or returns host values)."""
+        torch.cuda.synchronize(dev)
+        side = torch.cuda.Stream(dev)
+        side.wait_stream(torch.cuda.current_stream(dev))
+        gr = torch.cuda.CUDAGraph()
+        try:
+            with torch.cuda.graph(gr, stream=side):
+                gt, res = trial()
+                update(gt, rows)
+                sc_host.copy_(sc, non_blocking=True)
+        except Exception:  # noqa: BLE001 - not capturable: run eagerly
+            torch.cuda.synchronize(dev)
+            return None
+        torch.cuda.current_stream(dev).wait_stream(side)
+        return gr, gt, res
 
     def run_host(self, x0, loss_grad, epochs=None, callback=None,
                  epoch_start=0, **kwargs):

@@ -105,13 +105,19 @@ def test_batch_three_epochs(cuda):
         assert W.rel_err(u, _oracle(inst)) <= 1e-10, (inst["nt"], inst["c"])
 
 
-def test_batch_loss_grad_matches_single_instance_and_oracle(cuda):
+@pytest.mark.parametrize("sides", [(5, 70), (120, 300), (1, 4)])
+def test_batch_loss_grad_matches_single_instance_and_oracle(cuda, sides):
     """The one-launch fused loss + adjoint of the batch gives, per
     instance, the single-instance fused kernel's loss and gradient (FP32)
-    and the oracle's FP64 values (util_op.py:627-654) to FP32 accuracy."""
+    and the oracle's FP64 values (util_op.py:627-654) to FP32 accuracy.
+    Sides 5-70: one column strip per instance; 120-300: two or three
+    strips (strip edges inside the grid); 1-4: grids of one to four
+    columns (nx = 1 takes the general per-cell path)."""
     from odil_gb300.batch import WaveBatch
     from odil_gb300.wave import WaveKernels
-    insts = _small_batch()
+    from odil_gb300.workloads import wave_batch_instances
+    insts = _small_batch() if sides == (5, 70) else wave_batch_instances(
+        count=8, seed=sides[1], nmin=sides[0], nmax=sides[1])
     b = WaveBatch(insts, device=cuda)
     rng = np.random.default_rng(5)
     u = torch.as_tensor(0.1 * rng.standard_normal(b.total),

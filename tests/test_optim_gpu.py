@@ -273,3 +273,30 @@ def test_device_lbfgs_one_sync_per_iteration_fp32_1024(cuda):
     # the loss rise by up to 1e-6 of itself (below its FP32 resolution).
     assert k.loss_grad(x.reshape(n, n))[0].item() <= l0 * (1 + 1e-6)
     assert info.fallbacks <= 5
+
+
+@pytest.mark.parametrize("m", [5, 50])
+def test_device_lbfgs_graph_replay_equals_eager(cuda, m):
+    """L-BFGS with every steady-state iteration replayed from a CUDA graph
+    gives bitwise the iterates of the eager device form (the same kernels in
+    the same order), host line searches included where a trial is rejected;
+    with m = 5 the ring wraps around many times."""
+    from odil_gb300.optimizer import LbfgsOptimizer
+    n = 48
+    inst, prob = _wave_problem(n, cuda)
+    grad = torch.empty(n * n, dtype=torch.float64, device=cuda)
+
+    def lg(x, epoch):
+        loss, g = prob.kernels.loss_grad(x.reshape(n, n),
+                                         grad=grad.view(n, n))
+        return loss, g.reshape(-1), [loss]
+
+    iters = m + 30
+    x0 = torch.zeros(n * n, dtype=torch.float64, device=cuda)
+    xe, infoe = LbfgsOptimizer(m=m).run_device(x0, lg, epochs=iters)
+    xg, infog = LbfgsOptimizer(m=m, graph=True).run_device(x0, lg,
+                                                           epochs=iters)
+    assert infoe.epochs == infog.epochs == iters
+    assert infog.replays > 0
+    assert infog.fallbacks == infoe.fallbacks
+    assert torch.equal(xe, xg)
