@@ -264,24 +264,27 @@ int launch_batch_march(const odil_wave_batch* b, const float* rhs, float* x, uns
 // item); one warp per item, BLG_WARPS independent warps per block.
 //
 // Lane l holds BLG_V = 4 contiguous columns c0 - 1 + 4 l + j of a 128-column
-// window (the first and last column are halo; lanes 0 and 31 load one more
-// column each for the halo's residual).  Per row the warp reads u once
-// (four 4-byte loads per lane: rows of uneven widths give no 16-byte
-// alignment), forms the residual of the row from registers and two
-// shuffles, and the gradient of the row two above from the residual rows
-// below it and two more shuffles.  Column classes are per-lane constants
-// (the d f/d u coefficients of the J^T gather, formed once per item), so
-// every cell takes the same instructions; only the residual at columns 0
-// and nx - 1 (one lane each: the boundary extrapolation), rows 0, 1 of the
+// window (the first and last column are halo; lanes 0 and 31 also read one
+// column beyond, for the halo's residual).  Rows of uneven widths give no
+// 16-byte alignment, so rows stream into a per-warp ring of BLG_R shared-
+// memory rows by 4-byte cp.async copies, BLG_R - 1 rows in flight per warp
+// without holding registers; the ring row places the lane's four columns on
+// a 16-byte boundary, so each lane reads them back with one 16-byte shared
+// load.  Per row the warp forms the residual of the row (x-neighbours by two
+// shuffles) and the gradient of the row two above from the residual rows
+// below it (two more shuffles).  Column classes are per-lane constants (the
+// d f/d u coefficients of the J^T gather, formed once per item), so every
+// cell takes the same instructions; only the residual at columns 0 and
+// nx - 1 (one lane each: the boundary extrapolation), rows 0, 1 of the
 // residual and rows 0, nt - 2, nt - 1 of the gradient take the general
-// per-cell functions.  Rows stream in chunks of BLG_Q: the next chunk's
-// loads are issued before the current chunk is processed.  128 registers
-// (4 blocks of 4 warps per SM) hold it without spills.
+// per-cell functions.  96 registers (5 blocks of 4 warps per SM) hold it
+// without spills: 20 warps x 7 rows in flight per SM.
 constexpr int BLG_V = 4;
 constexpr int BLG_OUT = 32 * BLG_V - 2;  // output columns per item
 constexpr int BLG_TY = 32;
-constexpr int BLG_Q = 2;
 constexpr int BLG_WARPS = 4;
+constexpr int BLG_R = 8;      // ring rows per warp (power of two)
+constexpr int BLG_ROW = 136;  // floats per ring row: [3] left extra, [4 + 4 l + j], [132] right extra
 
 // Residual of an interior cell (row >= 2, 0 < column < nx - 1): the
 // expression of wave_f_with for such cells.
@@ -294,15 +297,18 @@ __device__ __forceinline__ float blg_f(const WaveDev<float>& g, float u, float u
     return u_tt - g.c2 * u_xx;
 }
 
-__global__ void __launch_bounds__(BLG_WARPS * 32, 4) batch_loss_grad_kernel(
+__global__ void __launch_bounds__(BLG_WARPS * 32, 5) batch_loss_grad_kernel(
     const odil_wave_instance* __restrict__ inst, const int32_t* __restrict__ tile_inst,
     const int64_t* __restrict__ tile_start, int64_t nitems, const float* __restrict__ iu,
     const float* __restrict__ iut, const float* __restrict__ lu, const float* __restrict__ ru,
     const float* __restrict__ u, float* __restrict__ grad, double* __restrict__ partials) {
     constexpr int V = BLG_V;
+    constexpr int NQ = BLG_TY + 4;  // rows a0 - 2 .. a0 + BLG_TY + 1
+    __shared__ __align__(16) float ring_all[BLG_WARPS][BLG_R][BLG_ROW];
     const int lane = threadIdx.x & 31;
     const int64_t item = (int64_t)blockIdx.x * BLG_WARPS + (threadIdx.x >> 5);
     if (item >= nitems) return;  // the whole warp
+    float* __restrict__ ring = &ring_all[threadIdx.x >> 5][0][0];
     const int qi = __ldg(tile_inst + item);
     const odil_wave_instance& d = inst[qi];
     WaveDev<float> g;
@@ -349,122 +355,130 @@ __global__ void __launch_bounds__(BLG_WARPS * 32, 4) batch_loss_grad_kernel(
         if (col >= c0 && col < c0 + BLG_OUT && col < nx) outm |= 1u << j;
         if (col == 0 || col == nx - 1) fixm |= 1u << j;
     }
-    const int offe = lane == 0 ? wrapn(c0 - 2, nx) : wrapn(c0 + 32 * V - 1, nx);
+    // Lanes 0 and 31 also copy the column beyond the window's edge.
     const bool xl = lane == 0 || lane == 31;
+    const int offe = lane == 0 ? wrapn(c0 - 2, nx) : wrapn(c0 + 32 * V - 1, nx);
+    const int xe = lane == 0 ? 3 : 4 + 32 * V;  // its ring index
+    // Row q (r = a0 - 2 + q) into ring slot q mod BLG_R; rows outside the
+    // grid are zero.  Every call commits one group (empty past the tile), so
+    // the wait below counts rows.
+    auto issue = [&](int q) {
+        if (q < NQ) {
+            const int r = a0 - 2 + q;
+            float* to = ring + (q & (BLG_R - 1)) * BLG_ROW;
+            if (r >= 0 && r < nt) {
+                const float* row = ui + (int64_t)r * nx;
+#pragma unroll
+                for (int j = 0; j < V; ++j) cp_async_n(to + 4 + V * lane + j, row + off[j], 4);
+                if (xl) cp_async_n(to + xe, row + offe, 4);
+            } else {
+#pragma unroll
+                for (int j = 0; j < V; ++j) to[4 + V * lane + j] = 0.f;
+                if (xl) to[xe] = 0.f;
+            }
+        }
+        cp_async_commit();
+    };
+#pragma unroll
+    for (int q = 0; q < BLG_R - 1; ++q) issue(q);
 
     float u1[V], u2[V], f1[V], f2[V];
 #pragma unroll
     for (int j = 0; j < V; ++j) u1[j] = u2[j] = f1[j] = f2[j] = 0.f;
-    float e1 = 0.f;
     float lsum = 0.f;
-    float uq[BLG_Q][V], eq[BLG_Q], un[BLG_Q][V], en[BLG_Q];
-    auto load_chunk = [&](int q0, float (&uu)[BLG_Q][V], float (&ee)[BLG_Q]) {
+    for (int qq = 0; qq < NQ; ++qq) {
+        cp_async_wait<BLG_R - 2>();  // this thread's copies of row qq have landed
+        __syncwarp();                // ... and every lane's
+        const float* cur = ring + (qq & (BLG_R - 1)) * BLG_ROW;
+        const float4 u0v = *reinterpret_cast<const float4*>(cur + 4 + V * lane);
+        const float u0[V] = {u0v.x, u0v.y, u0v.z, u0v.w};
+        // Extra column of row r-1 (lanes 0, 31), from the previous slot.
+        const float e1 = xl ? ring[((qq - 1) & (BLG_R - 1)) * BLG_ROW + xe] : 0.f;
+        __syncwarp();     // the previous slot is read: refill it
+        issue(qq + BLG_R - 1);
+        const int r = a0 - 2 + qq;
+        // x-neighbours of row r-1 at the lane's end columns.
+        float um0 = __shfl_up_sync(0xffffffffu, u1[V - 1], 1);
+        float upv = __shfl_down_sync(0xffffffffu, u1[0], 1);
+        if (lane == 0) um0 = e1;
+        if (lane == 31) upv = e1;
+        if (qq >= 2) {
+            float f0[V];
+            if (r < nt) {
+                if (r >= 2 && !gen) {
 #pragma unroll
-        for (int jj = 0; jj < BLG_Q; ++jj) {
-            const int r = a0 - 2 + q0 + jj;
-            const bool ok = q0 + jj < BLG_TY + 4 && r >= 0 && r < nt;
-            const float* row = ui + (int64_t)r * nx;
-#pragma unroll
-            for (int j = 0; j < V; ++j) uu[jj][j] = ok ? __ldg(row + off[j]) : 0.f;
-            ee[jj] = (ok && xl) ? __ldg(row + offe) : 0.f;
-        }
-    };
-    load_chunk(0, uq, eq);
-    for (int q0 = 0; q0 < BLG_TY + 4; q0 += BLG_Q) {
-        load_chunk(q0 + BLG_Q, un, en);
-#pragma unroll
-        for (int jj = 0; jj < BLG_Q; ++jj) {
-            const int qq = q0 + jj;
-            const int r = a0 - 2 + qq;
-            // x-neighbours of row r-1 at the lane's end columns.
-            float um0 = __shfl_up_sync(0xffffffffu, u1[V - 1], 1);
-            float upv = __shfl_down_sync(0xffffffffu, u1[0], 1);
-            if (lane == 0) um0 = e1;
-            if (lane == 31) upv = e1;
-            if (qq >= 2) {
-                float f0[V];
-                if (r < nt) {
-                    if (r >= 2 && !gen) {
+                    for (int j = 0; j < V; ++j) {
+                        const float um = j == 0 ? um0 : u1[j - 1];
+                        const float up = j == V - 1 ? upv : u1[j + 1];
+                        f0[j] = blg_f(g, u0[j], u1[j], u2[j], um, up);
+                    }
+                    if (fixm) {
 #pragma unroll
                         for (int j = 0; j < V; ++j) {
-                            const float um = j == 0 ? um0 : u1[j - 1];
-                            const float up = j == V - 1 ? upv : u1[j + 1];
-                            f0[j] = blg_f(g, uq[jj][j], u1[j], u2[j], um, up);
-                        }
-                        if (fixm) {
-#pragma unroll
-                            for (int j = 0; j < V; ++j) {
-                                if (fixm & (1u << j)) {
-                                    const float um = j == 0 ? um0 : u1[j - 1];
-                                    const float up = j == V - 1 ? upv : u1[j + 1];
-                                    f0[j] = wave_f(g, r, off[j], uq[jj][j], u1[j], u2[j], um, up);
-                                }
+                            if (fixm & (1u << j)) {
+                                const float um = j == 0 ? um0 : u1[j - 1];
+                                const float up = j == V - 1 ? upv : u1[j + 1];
+                                f0[j] = wave_f(g, r, off[j], u0[j], u1[j], u2[j], um, up);
                             }
-                        }
-                    } else {
-#pragma unroll
-                        for (int j = 0; j < V; ++j) {
-                            const float um = j == 0 ? um0 : u1[j - 1];
-                            const float up = j == V - 1 ? upv : u1[j + 1];
-                            f0[j] = wave_f(g, r, off[j], uq[jj][j], u1[j], u2[j], um, up);
                         }
                     }
                 } else {
 #pragma unroll
-                    for (int j = 0; j < V; ++j) f0[j] = 0.f;
-                }
-                // Gradient of row a = r - 2 from f rows a, a+1 (with its
-                // x-neighbours) and a+2.
-                const int a = r - 2;
-                if (qq >= 4 && a < nt) {
-                    const float fm0 = __shfl_up_sync(0xffffffffu, f1[V - 1], 1);
-                    const float fpv = __shfl_down_sync(0xffffffffu, f1[0], 1);
-                    float gv[V];
-                    if (a >= 1 && a + 2 < nt && !gen) {
-#pragma unroll
-                        for (int j = 0; j < V; ++j) {
-                            const float f1m = j == 0 ? fm0 : f1[j - 1];
-                            const float f1p = j == V - 1 ? fpv : f1[j + 1];
-                            gv[j] = A * (f2[j] + f0[j]) + ctm[j] * f1[j] -
-                                    B * (kxm1[j] * f1p + kxp1[j] * f1m);
-                        }
-                    } else {
-#pragma unroll
-                        for (int j = 0; j < V; ++j) {
-                            const float f1m = j == 0 ? fm0 : f1[j - 1];
-                            const float f1p = j == V - 1 ? fpv : f1[j + 1];
-                            gv[j] = wave_gather(g, a, off[j], f2[j], f1[j], f0[j], f1p, f1m);
-                        }
+                    for (int j = 0; j < V; ++j) {
+                        const float um = j == 0 ? um0 : u1[j - 1];
+                        const float up = j == V - 1 ? upv : u1[j + 1];
+                        f0[j] = wave_f(g, r, off[j], u0[j], u1[j], u2[j], um, up);
                     }
-                    float* __restrict__ grow = gi + (int64_t)a * nx + cb;
+                }
+            } else {
+#pragma unroll
+                for (int j = 0; j < V; ++j) f0[j] = 0.f;
+            }
+            // Gradient of row a = r - 2 from f rows a, a+1 (with its
+            // x-neighbours) and a+2.
+            const int a = r - 2;
+            if (qq >= 4 && a < nt) {
+                const float fm0 = __shfl_up_sync(0xffffffffu, f1[V - 1], 1);
+                const float fpv = __shfl_down_sync(0xffffffffu, f1[0], 1);
+                float gv[V];
+                if (a >= 1 && a + 2 < nt && !gen) {
 #pragma unroll
                     for (int j = 0; j < V; ++j) {
-                        if (outm & (1u << j)) {
-                            grow[j] = gv[j] * gscale;
-                            lsum += f2[j] * f2[j];
-                        }
+                        const float f1m = j == 0 ? fm0 : f1[j - 1];
+                        const float f1p = j == V - 1 ? fpv : f1[j + 1];
+                        gv[j] = A * (f2[j] + f0[j]) + ctm[j] * f1[j] -
+                                B * (kxm1[j] * f1p + kxp1[j] * f1m);
+                    }
+                } else {
+#pragma unroll
+                    for (int j = 0; j < V; ++j) {
+                        const float f1m = j == 0 ? fm0 : f1[j - 1];
+                        const float f1p = j == V - 1 ? fpv : f1[j + 1];
+                        gv[j] = wave_gather(g, a, off[j], f2[j], f1[j], f0[j], f1p, f1m);
                     }
                 }
+                float* __restrict__ grow = gi + (int64_t)a * nx + cb;
 #pragma unroll
                 for (int j = 0; j < V; ++j) {
-                    f2[j] = f1[j];
-                    f1[j] = f0[j];
+                    if (outm & (1u << j)) {
+                        grow[j] = gv[j] * gscale;
+                        lsum += f2[j] * f2[j];
+                    }
                 }
             }
 #pragma unroll
             for (int j = 0; j < V; ++j) {
-                u2[j] = u1[j];
-                u1[j] = uq[jj][j];
+                f2[j] = f1[j];
+                f1[j] = f0[j];
             }
-            e1 = eq[jj];
         }
 #pragma unroll
-        for (int jj = 0; jj < BLG_Q; ++jj) {
-#pragma unroll
-            for (int j = 0; j < V; ++j) uq[jj][j] = un[jj][j];
-            eq[jj] = en[jj];
+        for (int j = 0; j < V; ++j) {
+            u2[j] = u1[j];
+            u1[j] = u0[j];
         }
     }
+    cp_async_wait<0>();
     const double sw = warp_sum((double)lsum);
     if (lane == 0) partials[item] = sw;
 }

@@ -182,15 +182,50 @@ __device__ __forceinline__ void cluster_sync_all() {
 // only wait for their neighbours, and the solution stores need no fence.
 // `extra_wait` adds bytes that never arrive to every wait (a planted
 // failure for the bounded-wait test; 0 otherwise).
-template <typename T, int CPT, int H, int PF, bool VEC, bool DSMEM>
-__global__ void __launch_bounds__(32 * kTiledMaxWarps) wave_march_tiled_kernel(
-    WaveDev<T> g, const T* __restrict__ b, T* __restrict__ x, uint32_t extra_wait) {
+//
+// CONV (cluster-barrier exchange only): the block also holds one converter
+// warp per marching warp (warps mw .. 2 mw - 1, on SM sub-partitions the
+// marching warps leave idle).  After each cluster barrier the converter of
+// tile t writes the FP64 value of the previous batch of rows of t's owned
+// columns into u64 (exact, integer instructions: f2d_exact), while the
+// marching warps go on with the next batch; the last batch follows a block
+// barrier at the end.  x keeps the FP32 solution (the exchange reloads it).
+template <typename T, int CPT, int H, int PF, bool VEC, bool DSMEM, bool CONV = false>
+__global__ void __launch_bounds__(32 * kTiledMaxWarps * (CONV ? 2 : 1)) wave_march_tiled_kernel(
+    WaveDev<T> g, const T* __restrict__ b, T* __restrict__ x, uint32_t extra_wait,
+    double* __restrict__ u64) {
     constexpr int O = 32 * CPT - 2 * H;  // owned columns per warp
     static_assert(O > 0 && H % CPT == 0 && H % PF == 0, "tile shape");
     static_assert(!DSMEM || O >= H, "pushed columns come from one neighbour");
+    static_assert(!(CONV && DSMEM), "converter warps follow the cluster barrier");
     const int nx = g.nx, nt = g.nt;
     const int lane = threadIdx.x & 31;
-    const int tile = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const int mw = CONV ? (int)(blockDim.x >> 6) : (int)(blockDim.x >> 5);  // marching warps
+    if constexpr (CONV) {
+        const int cw = (int)(threadIdx.x >> 5) - mw;
+        if (cw >= 0) {
+            pdl_trigger();
+            const int t = blockIdx.x * mw + cw;
+            const int cfirst = t * O;
+            const int clast = cfirst + O < nx ? cfirst + O : nx;
+            auto convert = [&](int r0, int r1) {
+                for (int r = r0; r < r1; ++r) {
+                    const int64_t base = (int64_t)r * nx;
+                    for (int c = cfirst + lane; c < clast; c += 32)
+                        u64[base + c] = f2d_exact((float)__ldcg(x + base + c));
+                }
+            };
+            // One cluster barrier per batch boundary, as the marching warps.
+            for (int i0 = H; i0 < nt; i0 += H) {
+                cluster_sync_all();
+                convert(i0 - H, i0);
+            }
+            __syncthreads();  // the marching warps have stored the last batch
+            convert(((nt - 1) / H) * H, nt);
+            return;
+        }
+    }
+    const int tile = blockIdx.x * mw + (threadIdx.x >> 5);
     const int j0 = tile * O - H + lane * CPT;  // this lane's first column
     const bool own = lane >= H / CPT && lane < (H + O) / CPT;
     bool in[CPT];
@@ -304,7 +339,7 @@ __global__ void __launch_bounds__(32 * kTiledMaxWarps) wave_march_tiled_kernel(
             target = tile + 1, side = 0, off = wl - O;
         }
         if (target >= 0) {
-            const int wpb = blockDim.x >> 5;
+            const int wpb = mw;
             const uint32_t rank = (uint32_t)(target / wpb), tw = (uint32_t)(target % wpb);
             push_addr = cluster_map(smem_u32(&halo[tw][0][side][0][off]), rank);
             push_mbar = cluster_map(smem_u32(&mbar[tw][0]), rank);
@@ -397,11 +432,14 @@ __global__ void __launch_bounds__(32 * kTiledMaxWarps) wave_march_tiled_kernel(
         }
     }
     if constexpr (DSMEM) cluster_sync_all();  // no CTA leaves while pushes may target it
+    if constexpr (CONV) __syncthreads();      // hand the last batch to the converters
 }
 
 template <typename T>
 int tiled_launch(const void* kern, int clusters, int warps, const WaveDev<T>& g, const T* b,
-                 T* x, uint32_t extra_wait, cudaStream_t st) {
+                 T* x, uint32_t extra_wait, double* u64, cudaStream_t st) {
+    // Converter warps (u64 given) double the block.
+    const int threads = 32 * warps * (u64 ? 2 : 1);
     static thread_local const void* checked[64];
     static thread_local int nchecked = 0;
     bool seen = false;
@@ -412,7 +450,7 @@ int tiled_launch(const void* kern, int clusters, int warps, const WaveDev<T>& g,
     }
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)clusters);
-    cfg.blockDim = dim3((unsigned)(32 * warps));
+    cfg.blockDim = dim3((unsigned)threads);
     cfg.dynamicSmemBytes = 0;
     cfg.stream = st;
     cudaLaunchAttribute attr[2];
@@ -444,7 +482,7 @@ int tiled_launch(const void* kern, int clusters, int warps, const WaveDev<T>& g,
         if (nfits < 64) fits[nfits++] = {kern, clusters, warps, ok};
     }
     if (!ok) return ODIL_ERR_SHAPE;
-    void* args[] = {const_cast<WaveDev<T>*>(&g), &b, &x, &extra_wait};
+    void* args[] = {const_cast<WaveDev<T>*>(&g), &b, &x, &extra_wait, &u64};
     cfg.numAttrs = 2;  // the occupancy query above saw the cluster only
     if (cudaLaunchKernelExC(&cfg, kern, args) != cudaSuccess) {
         cudaGetLastError();
@@ -453,9 +491,9 @@ int tiled_launch(const void* kern, int clusters, int warps, const WaveDev<T>& g,
     return launch_status();
 }
 
-template <typename T, int CPT, int H, int PF, bool DSMEM>
+template <typename T, int CPT, int H, int PF, bool DSMEM, bool CONV = false>
 int tiled_shape_fit(const WaveDev<T>& g, const T* b, T* x, int warps, uint32_t extra_wait,
-                    cudaStream_t st) {
+                    double* u64, cudaStream_t st) {
     constexpr int O = 32 * CPT - 2 * H;
     const int64_t tiles = (g.nx + O - 1) / O;
     if (warps < 1 || warps > kTiledMaxWarps) return ODIL_ERR_SHAPE;
@@ -466,9 +504,12 @@ int tiled_shape_fit(const WaveDev<T>& g, const T* b, T* x, int warps, uint32_t e
     const bool vec = g.nx % CPT == 0 &&
                      ((reinterpret_cast<uintptr_t>(b) | reinterpret_cast<uintptr_t>(x)) % vb) == 0;
     const void* kern =
-        vec ? reinterpret_cast<const void*>(wave_march_tiled_kernel<T, CPT, H, PF, true, DSMEM>)
-            : reinterpret_cast<const void*>(wave_march_tiled_kernel<T, CPT, H, PF, false, DSMEM>);
-    return tiled_launch<T>(kern, (int)clusters, warps, g, b, x, extra_wait, st);
+        vec ? reinterpret_cast<const void*>(
+                  wave_march_tiled_kernel<T, CPT, H, PF, true, DSMEM, CONV>)
+            : reinterpret_cast<const void*>(
+                  wave_march_tiled_kernel<T, CPT, H, PF, false, DSMEM, CONV>);
+    return tiled_launch<T>(kern, (int)clusters, warps, g, b, x, extra_wait,
+                           CONV ? u64 : nullptr, st);
 }
 
 template <typename T, int CPT, int H, int PF, bool DSMEM>
@@ -478,7 +519,27 @@ int tiled_shape(const WaveDev<T>& g, const T* b, T* x, int warps, uint32_t extra
     if constexpr (CPT * PF * sizeof(T) > 512) {
         return ODIL_ERR_SHAPE;
     } else {
-        return tiled_shape_fit<T, CPT, H, PF, DSMEM>(g, b, x, warps, extra_wait, st);
+        return tiled_shape_fit<T, CPT, H, PF, DSMEM>(g, b, x, warps, extra_wait, nullptr, st);
+    }
+}
+
+// The FP32 march with converter warps writing the FP64 solution too
+// (cluster-barrier shapes).
+int tiled_to_f64_dispatch(const odil_wave_params* p, const float* b, float* x, double* u64,
+                          int cpt, int halo, int pf, int warps, void* stream) {
+    WaveDev<float> g;
+    int st = make_dev<float>(p, &g, false);
+    if (st) return st;
+    if (!b || !x || !u64) return ODIL_ERR_ARG;
+    if (g.nx < 2) return ODIL_ERR_SHAPE;
+    if (warps < 1 || warps > 2) return ODIL_ERR_SHAPE;  // one converter per spare sub-partition
+    cudaStream_t s = as_stream(stream);
+    switch (cpt * 10000 + halo * 100 + pf) {
+        case 43216:
+            return tiled_shape_fit<float, 4, 32, 16, false, true>(g, b, x, warps, 0u, u64, s);
+        case 44816:
+            return tiled_shape_fit<float, 4, 48, 16, false, true>(g, b, x, warps, 0u, u64, s);
+        default: return ODIL_ERR_SHAPE;
     }
 }
 
@@ -517,6 +578,13 @@ int tiled_dispatch(const odil_wave_params* p, const T* b, T* x, int cpt, int hal
 }  // namespace odil
 
 using odil::tiled_dispatch;
+using odil::tiled_to_f64_dispatch;
+
+ODIL_API int odil_wave_march_tiled_to_f64_f32(const odil_wave_params* p, const float* b,
+                                              float* x, double* u64, int32_t cpt, int32_t halo,
+                                              int32_t pf, int32_t warps, void* stream) {
+    return tiled_to_f64_dispatch(p, b, x, u64, cpt, halo, pf, warps, stream);
+}
 
 ODIL_API int odil_wave_march_tiled_f32(const odil_wave_params* p, const float* b, float* x,
                                        int32_t cpt, int32_t halo, int32_t pf, int32_t warps,
