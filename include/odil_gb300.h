@@ -695,6 +695,19 @@ int odil_lincomb_f32(float* out, const float* x, const float* M, int64_t ld,
 int odil_lincomb_f64(double* out, const double* x, const double* M,
                      int64_t ld, int k, const double* coef, int64_t n,
                      void* stream);
+/* odil_lincomb_* that also writes dot[0] = <out, x> (FP64, deterministic):
+ * the L-BFGS direction d and phi'(0) = g . d in one pass.  workspace: at
+ * least odil_lincomb_dot_workspace_bytes(n) bytes, zeroed before first use
+ * (the kernel leaves its counter at zero). */
+int64_t odil_lincomb_dot_workspace_bytes(int64_t n);
+int odil_lincomb_dot_f32(float* out, const float* x, const float* M,
+                         int64_t ld, int k, const double* coef, int64_t n,
+                         double* dot, void* workspace, int64_t workspace_bytes,
+                         void* stream);
+int odil_lincomb_dot_f64(double* out, const double* x, const double* M,
+                         int64_t ld, int k, const double* coef, int64_t n,
+                         double* dot, void* workspace, int64_t workspace_bytes,
+                         void* stream);
 
 /* L-BFGS with the compact-form algebra on the device (replaces the host
  * side of optimizer.py:61-99, scipy's fmin_l_bfgs_b two-loop and line-search
@@ -728,6 +741,23 @@ int odil_lbfgs_pair_f32(int64_t n, float* sy, const float* d, const float* gt,
 int odil_lbfgs_pair_f64(int64_t n, double* sy, const double* d,
                         const double* gt, const double* g, const double* sc,
                         void* stream);
+/* pair_dots: pair, its dots and the Wolfe test in one pass: s = a d,
+ * y = g_trial - g into sy (always), Q as for update, and (mode 0) the test
+ * of accept on f(trial) = ft[0] with phi'(a) = g_trial . d computed here, or
+ * (mode 1) no test: the host chose the step (sc[3], sc[4], sc[6] = 0).
+ * workspace: at least odil_lbfgs_pair_dots_workspace_bytes(n) bytes, zeroed
+ * before first use. */
+int64_t odil_lbfgs_pair_dots_workspace_bytes(int64_t n);
+int odil_lbfgs_pair_dots_f32(int64_t n, float* sy, const float* d,
+                             const float* gt, const float* g, const double* ft,
+                             int32_t mode, double* sc, double* Q,
+                             void* workspace, int64_t workspace_bytes,
+                             void* stream);
+int odil_lbfgs_pair_dots_f64(int64_t n, double* sy, const double* d,
+                             const double* gt, const double* g,
+                             const double* ft, int32_t mode, double* sc,
+                             double* Q, void* workspace,
+                             int64_t workspace_bytes, void* stream);
 int odil_lbfgs_update(int* ring, double* SY, double* YY, double* dg,
                       double* sc, const double* P, int32_t rows,
                       const double* Q, void* stream);

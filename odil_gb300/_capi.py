@@ -226,6 +226,13 @@ SIGNATURES = {
     "odil_lbfgs_accept": (_INT, [_P, _P, _P, _P]),
     "odil_lbfgs_pair_f32": (_INT, [_I64, _P, _P, _P, _P, _P, _P]),
     "odil_lbfgs_pair_f64": (_INT, [_I64, _P, _P, _P, _P, _P, _P]),
+    "odil_lbfgs_pair_dots_workspace_bytes": (_I64, [_I64]),
+    "odil_lbfgs_pair_dots_f32": (_INT, [_I64, _P, _P, _P, _P, _P,
+                                        ctypes.c_int32, _P, _P, _P, _I64,
+                                        _P]),
+    "odil_lbfgs_pair_dots_f64": (_INT, [_I64, _P, _P, _P, _P, _P,
+                                        ctypes.c_int32, _P, _P, _P, _I64,
+                                        _P]),
     "odil_lbfgs_update": (_INT, [_P, _P, _P, _P, _P, _P, ctypes.c_int32, _P,
                                  _P]),
     "odil_lbfgs_commit_f32": (_INT, [_I64, _P, _I64, _P, _P, _P, _P, _P, _P]),
@@ -278,6 +285,11 @@ SIGNATURES = {
                                  _P]),
     "odil_lincomb_f32": (_INT, [_P, _P, _P, _I64, _INT, _P, _I64, _P]),
     "odil_lincomb_f64": (_INT, [_P, _P, _P, _I64, _INT, _P, _I64, _P]),
+    "odil_lincomb_dot_workspace_bytes": (_I64, [_I64]),
+    "odil_lincomb_dot_f32": (_INT, [_P, _P, _P, _I64, ctypes.c_int, _P, _I64,
+                                    _P, _P, _I64, _P]),
+    "odil_lincomb_dot_f64": (_INT, [_P, _P, _P, _I64, ctypes.c_int, _P, _I64,
+                                    _P, _P, _I64, _P]),
     "odil_mgdecomp_refine_f32": (_INT, [ctypes.c_int32, _P, ctypes.c_int32, _P,
                                         _P, _D, _P, _D, _P]),
     "odil_mgdecomp_refine_f64": (_INT, [ctypes.c_int32, _P, ctypes.c_int32, _P,

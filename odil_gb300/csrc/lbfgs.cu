@@ -224,6 +224,17 @@ __global__ void __launch_bounds__(LT) lbfgs_trial_kernel(int64_t n, T* __restric
         xt[i] = x[i] + at * d[i];
 }
 
+// Status of a trial: 0 accepted, 1 rejected, 2 d is not a descent direction.
+__device__ __forceinline__ double wolfe_status(const double* sc, double fa, double dpa) {
+    const double f0 = sc[0], dphi0 = sc[2], a = sc[3], c1 = sc[7], c2 = sc[8];
+    const double eps = sc[9] * fabs(f0);
+    if (!(dphi0 < 0.0)) return 2.0;
+    if (!isfinite(fa) || !isfinite(dpa) || dpa < c2 * dphi0) return 1.0;
+    if (fa <= f0 + c1 * a * dphi0) return 0.0;
+    if (fa <= f0 + eps && dpa <= (2.0 * c1 - 1.0) * dphi0) return 0.0;
+    return 1.0;
+}
+
 // The Wolfe test of the trial (phi(a) <= phi(0) + c1 a phi'(0) and phi'(a) >=
 // c2 phi'(0)), or the approximate Wolfe conditions of Hager and Zhang
 // (phi(a) <= phi(0) + eps |phi(0)|, c2 phi'(0) <= phi'(a) <= (2 c1 - 1)
@@ -232,24 +243,10 @@ __global__ void lbfgs_accept_kernel(const double* __restrict__ ft,
                                     const double* __restrict__ dpa_dots,
                                     double* __restrict__ sc) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    const double f0 = sc[0], dphi0 = sc[2], a = sc[3], c1 = sc[7], c2 = sc[8];
     const double fa = ft[0], dpa = dpa_dots[0];
-    const double eps = sc[9] * fabs(f0);
     sc[4] = fa;
     sc[5] = dpa;
-    double status;
-    if (!(dphi0 < 0.0)) {
-        status = 2.0;
-    } else if (!isfinite(fa) || !isfinite(dpa) || dpa < c2 * dphi0) {
-        status = 1.0;
-    } else if (fa <= f0 + c1 * a * dphi0) {
-        status = 0.0;
-    } else if (fa <= f0 + eps && dpa <= (2.0 * c1 - 1.0) * dphi0) {
-        status = 0.0;
-    } else {
-        status = 1.0;
-    }
-    sc[6] = status;
+    sc[6] = wolfe_status(sc, fa, dpa);
 }
 
 // The new pair s = a d, y = g_trial - g into rows 0 and 1 of sy (accepted
@@ -266,6 +263,87 @@ __global__ void __launch_bounds__(LT) lbfgs_pair_kernel(int64_t n, T* __restrict
     for (int64_t i = (int64_t)blockIdx.x * LT + threadIdx.x; i < n; i += stride) {
         sy[i] = a * d[i];
         sy[n + i] = gt[i] - g[i];
+    }
+}
+
+// The pair, its dots and the Wolfe test in one pass over d, g_trial and g:
+// s = a d and y = g_trial - g into sy (scratch: written whatever the test
+// decides), and the five dots g_trial.d, s.y, s.g_trial, y.y, y.g_trial
+// (per-thread sums in the working precision, FP64 partials per block, stored
+// dot-major).  The last block adds each dot's partials in index order, then
+// mode 0: the test of lbfgs_accept_kernel on f(trial) = ft[0] and
+// phi'(a) = g_trial.d; mode 1: the host line search chose the step (sc[3],
+// sc[4], sc[6] = 0 set by the host), nothing is tested.  Q = [[s.y, s.gt],
+// [y.y, y.gt]] for the update.  Replaces the g_trial.d multi-dot, the accept
+// and pair kernels and the 2 x 2 multi-dot of the unfused iteration.
+constexpr int PD = 5;
+
+
+template <typename T>
+__global__ void __launch_bounds__(LT) lbfgs_pair_dots_kernel(
+    int64_t n, T* __restrict__ sy, const T* __restrict__ d, const T* __restrict__ gt,
+    const T* __restrict__ g, const double* __restrict__ ft, int mode, double* __restrict__ sc,
+    double* __restrict__ Q, ReduceWs ws) {
+    const T a = (T)sc[3];
+    T acc[PD];
+#pragma unroll
+    for (int j = 0; j < PD; ++j) acc[j] = T(0);
+    const int64_t stride = (int64_t)gridDim.x * LT;
+    for (int64_t i = (int64_t)blockIdx.x * LT + threadIdx.x; i < n; i += stride) {
+        const T dv = d[i], gtv = gt[i], gv = g[i];
+        const T sv = a * dv, yv = gtv - gv;
+        sy[i] = sv;
+        sy[n + i] = yv;
+        acc[0] += gtv * dv;
+        acc[1] += sv * yv;
+        acc[2] += sv * gtv;
+        acc[3] += yv * yv;
+        acc[4] += yv * gtv;
+    }
+    __shared__ double red[LT / 32][PD];
+    __shared__ bool is_last;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int j = 0; j < PD; ++j) {
+        const double v = warp_sum((double)acc[j]);
+        if (lane == 0) red[warp][j] = v;
+    }
+    __syncthreads();
+    const int64_t nb = gridDim.x;
+    if (threadIdx.x < PD) {
+        double v = 0.0;
+#pragma unroll
+        for (int w = 0; w < LT / 32; ++w) v += red[w][threadIdx.x];
+        ws.partials[threadIdx.x * nb + blockIdx.x] = v;
+        __threadfence();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const unsigned prev = atomicAdd(ws.counter, 1u);
+        is_last = prev == (unsigned)(nb - 1);
+    }
+    __syncthreads();
+    if (!is_last) return;
+    __threadfence();
+    __shared__ double tot[PD];
+    for (int j = 0; j < PD; ++j) {
+        const double v = sum_partials(ws.partials + j * nb, nb);
+        if (threadIdx.x == 0) tot[j] = v;
+    }
+    if (threadIdx.x == 0) {
+        if (mode == 0) {
+            const double fa = ft[0], dpa = tot[0];
+            sc[4] = fa;
+            sc[5] = dpa;
+            sc[6] = wolfe_status(sc, fa, dpa);
+        } else {
+            sc[5] = tot[0];
+        }
+        Q[0] = tot[1];
+        Q[1] = tot[2];
+        Q[2] = tot[3];
+        Q[3] = tot[4];
+        *ws.counter = 0u;
     }
 }
 
@@ -373,6 +451,20 @@ int pair_impl(int64_t n, T* sy, const T* d, const T* gt, const T* g, const doubl
 }
 
 template <typename T>
+int pair_dots_impl(int64_t n, T* sy, const T* d, const T* gt, const T* g, const double* ft,
+                   int mode, double* sc, double* Q, void* ws, int64_t ws_bytes, void* stream) {
+    if (n < 1) return ODIL_ERR_SHAPE;
+    if (mode != 0 && mode != 1) return ODIL_ERR_ARG;
+    if (!sy || !d || !gt || !g || !sc || !Q || (mode == 0 && !ft)) return ODIL_ERR_ARG;
+    const unsigned blocks = lgrid(n);
+    if (!ws || ws_bytes < kReduceHeader + (int64_t)PD * blocks * (int64_t)sizeof(double))
+        return ODIL_ERR_WORKSPACE;
+    lbfgs_pair_dots_kernel<T><<<blocks, LT, 0, as_stream(stream)>>>(n, sy, d, gt, g, ft, mode, sc,
+                                                                   Q, reduce_ws(ws));
+    return launch_status();
+}
+
+template <typename T>
 int commit_impl(int64_t n, T* H, int64_t ld, const T* sy, T* g, const T* gt, const int* ring,
                 const double* sc, void* stream) {
     if (n < 1 || ld < n) return ODIL_ERR_SHAPE;
@@ -423,6 +515,25 @@ ODIL_API int odil_lbfgs_pair_f32(int64_t n, float* sy, const float* d, const flo
 ODIL_API int odil_lbfgs_pair_f64(int64_t n, double* sy, const double* d, const double* gt,
                                  const double* g, const double* sc, void* stream) {
     return pair_impl<double>(n, sy, d, gt, g, sc, stream);
+}
+
+ODIL_API int64_t odil_lbfgs_pair_dots_workspace_bytes(int64_t n) {
+    if (n < 1) return 0;
+    return kReduceHeader + (int64_t)PD * lgrid(n) * (int64_t)sizeof(double);
+}
+ODIL_API int odil_lbfgs_pair_dots_f32(int64_t n, float* sy, const float* d, const float* gt,
+                                      const float* g, const double* ft, int32_t mode, double* sc,
+                                      double* Q, void* workspace, int64_t workspace_bytes,
+                                      void* stream) {
+    return pair_dots_impl<float>(n, sy, d, gt, g, ft, mode, sc, Q, workspace, workspace_bytes,
+                                 stream);
+}
+ODIL_API int odil_lbfgs_pair_dots_f64(int64_t n, double* sy, const double* d, const double* gt,
+                                      const double* g, const double* ft, int32_t mode,
+                                      double* sc, double* Q, void* workspace,
+                                      int64_t workspace_bytes, void* stream) {
+    return pair_dots_impl<double>(n, sy, d, gt, g, ft, mode, sc, Q, workspace, workspace_bytes,
+                                  stream);
 }
 
 ODIL_API int odil_lbfgs_update(int* ring, double* SY, double* YY, double* dg, double* sc,

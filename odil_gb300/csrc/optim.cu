@@ -370,12 +370,15 @@ __global__ void __launch_bounds__(256) multidot_finish_kernel(const double* __re
     if (lane == 0) out[o] = s;
 }
 
-// out = c0 * x + sum_i coef[i] * M_i  (coef, c0 read from device memory).
+// out = c0 * x + sum_i coef[i] * M_i  (coef, c0 read from device memory);
+// with dot given, also dot[0] = <out, x> (per-thread sums in the working
+// precision, FP64 across blocks, added in index order by the last block).
 template <typename T>
 __global__ void __launch_bounds__(VT) lincomb_kernel(T* __restrict__ out, const T* __restrict__ x,
                                                      const T* __restrict__ M, int64_t ld, int k,
                                                      const double* __restrict__ coef,
-                                                     int64_t n, bool vec) {
+                                                     int64_t n, bool vec, ReduceWs ws,
+                                                     double* __restrict__ dot) {
     using V = typename Vec<T>::V;
     constexpr int W = Vec<T>::W;
     __shared__ T sc[257];
@@ -385,8 +388,10 @@ __global__ void __launch_bounds__(VT) lincomb_kernel(T* __restrict__ out, const 
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int64_t nv = vec ? n / W : 0;
+    T dsum = T(0);
     for (int64_t e = tid; e < nv; e += stride) {
-        V xv = __ldcs(reinterpret_cast<const V*>(x) + e);
+        const V x0 = __ldcs(reinterpret_cast<const V*>(x) + e);
+        V xv = x0;
         T* acc = reinterpret_cast<T*>(&xv);
 #pragma unroll
         for (int w = 0; w < W; ++w) acc[w] *= c0;
@@ -398,12 +403,18 @@ __global__ void __launch_bounds__(VT) lincomb_kernel(T* __restrict__ out, const 
             for (int w = 0; w < W; ++w) acc[w] += ci * ms[w];
         }
         reinterpret_cast<V*>(out)[e] = xv;
+        const T* xs = reinterpret_cast<const T*>(&x0);
+#pragma unroll
+        for (int w = 0; w < W; ++w) dsum += acc[w] * xs[w];
     }
     for (int64_t e = nv * W + tid; e < n; e += stride) {
-        T acc = c0 * x[e];
+        const T xe = x[e];
+        T acc = c0 * xe;
         for (int i = 0; i < k; ++i) acc += sc[i] * M[(int64_t)i * ld + e];
         out[e] = acc;
+        dsum += acc * xe;
     }
+    if (dot) reduce_finish((double)dsum, blockIdx.x, gridDim.x, ws, 1.0, dot);
 }
 
 template <typename T>
@@ -532,13 +543,19 @@ int multidot_impl(const T* M, int64_t ld, int k, const void* const* q, int r, in
 
 template <typename T>
 int lincomb_impl(T* out, const T* x, const T* M, int64_t ld, int k, const double* coef, int64_t n,
-                 void* stream) {
+                 double* dot, void* ws, int64_t ws_bytes, void* stream) {
     if (k < 0 || k > 256 || n < 1 || (k > 0 && ld < n)) return ODIL_ERR_SHAPE;
     if (!out || !x || !coef || (k > 0 && !M)) return ODIL_ERR_ARG;
     const bool vec = aligned16(out) && aligned16(x) && (k == 0 || (aligned16(M) &&
                                                                   (ld * (int64_t)sizeof(T)) % 16 == 0));
-    lincomb_kernel<T><<<stream_blocks(n, Vec<T>::W), VT, 0, as_stream(stream)>>>(out, x, M, ld, k,
-                                                                                 coef, n, vec);
+    const int blocks = stream_blocks(n, Vec<T>::W);
+    ReduceWs w{nullptr, nullptr};
+    if (dot) {
+        if (!ws || ws_bytes < reduce_ws_bytes(blocks)) return ODIL_ERR_WORKSPACE;
+        w = reduce_ws(ws);
+    }
+    lincomb_kernel<T><<<blocks, VT, 0, as_stream(stream)>>>(out, x, M, ld, k, coef, n, vec, w,
+                                                            dot);
     return launch_status();
 }
 
@@ -635,11 +652,30 @@ ODIL_API int odil_multidot_f64(const double* M, int64_t ld, int k, const void* c
 }
 ODIL_API int odil_lincomb_f32(float* out, const float* x, const float* M, int64_t ld, int k,
                               const double* coef, int64_t n, void* stream) {
-    return lincomb_impl<float>(out, x, M, ld, k, coef, n, stream);
+    return lincomb_impl<float>(out, x, M, ld, k, coef, n, nullptr, nullptr, 0, stream);
 }
 ODIL_API int odil_lincomb_f64(double* out, const double* x, const double* M, int64_t ld, int k,
                               const double* coef, int64_t n, void* stream) {
-    return lincomb_impl<double>(out, x, M, ld, k, coef, n, stream);
+    return lincomb_impl<double>(out, x, M, ld, k, coef, n, nullptr, nullptr, 0, stream);
+}
+
+ODIL_API int64_t odil_lincomb_dot_workspace_bytes(int64_t n) {
+    if (n < 1) return 0;
+    const int a = stream_blocks(n, Vec<float>::W), b = stream_blocks(n, Vec<double>::W);
+    return reduce_ws_bytes(a > b ? a : b);
+}
+ODIL_API int odil_lincomb_dot_f32(float* out, const float* x, const float* M, int64_t ld, int k,
+                                  const double* coef, int64_t n, double* dot, void* workspace,
+                                  int64_t workspace_bytes, void* stream) {
+    if (!dot) return ODIL_ERR_ARG;
+    return lincomb_impl<float>(out, x, M, ld, k, coef, n, dot, workspace, workspace_bytes, stream);
+}
+ODIL_API int odil_lincomb_dot_f64(double* out, const double* x, const double* M, int64_t ld,
+                                  int k, const double* coef, int64_t n, double* dot,
+                                  void* workspace, int64_t workspace_bytes, void* stream) {
+    if (!dot) return ODIL_ERR_ARG;
+    return lincomb_impl<double>(out, x, M, ld, k, coef, n, dot, workspace, workspace_bytes,
+                                stream);
 }
 
 ODIL_API int odil_add_f32_to_f64(const double* u, const float* d, double* out, int64_t n,

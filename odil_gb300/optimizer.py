@@ -105,9 +105,11 @@ class LbfgsOptimizer(Optimizer):
         """The same iteration with the compact-form algebra, the first trial
         step, its Wolfe test and the pair/ring update on the device
         (csrc/lbfgs.cu): per iteration one direction (coefficient kernel +
-        one linear combination), one loss+gradient at the trial point, one
-        multi-dot of the stored rows with (g_new, s, y), and one host read of
-        the 16 scalars (the status).  A trial that fails the Wolfe test
+        one linear combination that also gives g . d), the trial point, one
+        loss+gradient there, one pass forming the new pair with its dots and
+        the Wolfe test, one multi-dot of the stored rows with (g_new, s, y),
+        the ring update and commit, and one host read of the 16 scalars (the
+        status).  A trial that fails the Wolfe test
         (rare once pairs are held) falls back to the host line search from
         the same state.
 
@@ -121,6 +123,7 @@ class LbfgsOptimizer(Optimizer):
         iteration whose trial is rejected changes no state; the host line
         search then runs eagerly as without graphs.  Iterates are the same
         as without graphs."""
+        from . import _capi
         from ._capi import call, ptr, stream_handle
         x = x0.detach().clone()
         n = x.numel()
@@ -131,7 +134,13 @@ class LbfgsOptimizer(Optimizer):
         SYp = torch.zeros((2, n), dtype=x.dtype, device=dev)
         md = vec.MultiDot(n, 2 * m, 3, device=dev)
         md1 = vec.MultiDot(n, 1, 1, device=dev)
-        md2 = vec.MultiDot(n, 2, 2, device=dev)
+        lib = _capi.load()
+        lc_ws = torch.zeros(int(lib.odil_lincomb_dot_workspace_bytes(n)),
+                            dtype=torch.uint8, device=dev)
+        pd_ws = torch.zeros(int(lib.odil_lbfgs_pair_dots_workspace_bytes(n)),
+                            dtype=torch.uint8, device=dev)
+        dots = torch.zeros(1, dtype=torch.float64, device=dev)
+        Q = torch.zeros(4, dtype=torch.float64, device=dev)
         coef = torch.zeros(2 * m + 1, dtype=torch.float64, device=dev)
         ring = torch.tensor([0, 0, m, -1], dtype=torch.int32, device=dev)
         SY = torch.zeros((m, m), dtype=torch.float64, device=dev)
@@ -153,33 +162,39 @@ class LbfgsOptimizer(Optimizer):
         info = Namespace(epochs=0, evals=1, task="", fallbacks=0, replays=0)
         epochs = epochs if epochs is not None else 1 << 30
 
+        def pair_dots(gt, ft_dev, mode):
+            """s, y into SYp, their dots (Q), g_trial . d and (mode 0) the
+            Wolfe test of the trial, in one pass."""
+            call("odil_lbfgs_pair_dots_" + sfx, n, ptr(SYp), ptr(d), ptr(gt),
+                 ptr(g), ptr(ft_dev), mode, ptr(sc), ptr(Q), ptr(pd_ws),
+                 pd_ws.numel(), stream_handle())
+
         def trial(x, xt, rows):
-            """Direction, trial point, loss+gradient there, Wolfe test."""
+            """Direction (with g . d), trial point, loss+gradient there, pair
+            and Wolfe test."""
             st = stream_handle()
             if rows:
                 call("odil_lbfgs_coef", m, rows, ptr(ring), ptr(SY), ptr(YY),
                      ptr(dg), ptr(sc), ptr(coef), st)
-                vec.lincomb(d, g, H, rows, coef)
+                call("odil_lincomb_dot_" + sfx, ptr(d), ptr(g), ptr(H), n, rows,
+                     ptr(coef), n, ptr(dots), ptr(lc_ws), lc_ws.numel(), st)
+                gd = dots
             else:
                 vec.axpby(d, -1.0, g, 0.0, g)
-            dots = md1(g, 1, [d])
+                gd = md1(g, 1, [d])
             call("odil_lbfgs_trial_" + sfx, n, ptr(xt), ptr(x), ptr(d),
-                 ptr(dots), ptr(ring), ptr(sc), st)
+                 ptr(gd), ptr(ring), ptr(sc), st)
             ft, gt, res = loss_grad(xt, self.epoch)
             ft_dev = ft.reshape(1).double() if isinstance(ft, torch.Tensor) \
                 else torch.tensor([float(ft)], dtype=torch.float64, device=dev)
-            dpa = md1(gt, 1, [d])
-            call("odil_lbfgs_accept", ptr(ft_dev), ptr(dpa), ptr(sc), st)
+            pair_dots(gt, ft_dev, 0)
             return gt, res
 
         def update(gt, rows):
-            """Pair, dots, ring/matrix update, commit with g <- g_trial (all
-            guarded by the status on the device)."""
+            """Dots of the stored pairs with (g_trial, s, y), ring/matrix
+            update, commit with g <- g_trial (guarded by the status)."""
             st = stream_handle()
-            call("odil_lbfgs_pair_" + sfx, n, ptr(SYp), ptr(d), ptr(gt), ptr(g),
-                 ptr(sc), st)
             P = md(H, max(rows, 1), [gt, SYp[0], SYp[1]]) if rows else None
-            Q = md2(SYp, 2, [SYp[1], gt])
             call("odil_lbfgs_update", ptr(ring), ptr(SY), ptr(YY), ptr(dg),
                  ptr(sc), ptr(P), rows, ptr(Q), st)
             call("odil_lbfgs_commit_" + sfx, n, ptr(H), n, ptr(SYp), ptr(g),
@@ -227,6 +242,7 @@ class LbfgsOptimizer(Optimizer):
                     info.task = "ABNORMAL_TERMINATION_IN_LNSRCH"
                     break
                 sc[3], sc[4], sc[6] = alpha, fa, 0.0
+                pair_dots(gt, None, 1)
                 update(gt, rows)
             elif not replayed:
                 update(gt, rows)
