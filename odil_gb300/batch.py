@@ -87,6 +87,8 @@ class WaveBatch:
         self.hi = torch.zeros(self.total, **kw32)
         self.lo = torch.zeros(self.total, **kw32)
         self.ws = torch.zeros(256, dtype=torch.uint8, device=dev)
+        # Work queue of the persistent whole-solve kernel (left zeroed by it).
+        self.ws_solve = torch.zeros(256, dtype=torch.uint8, device=dev)
         self.march_cfg = None
         self.graph = None
         # Fused loss + gradient of all instances: FP32 boundary data and the
@@ -200,6 +202,24 @@ class WaveBatch:
                 have_lo = True
         call("odil_pair_to_f64", ptr(self.hi), ptr(self.lo if have_lo else None),
              ptr(self.u), self.total, stream_handle())
+        return self.u
+
+    def solve_persistent(self, epochs=2):
+        """u <- the same mixed Newton as solve_mixed (bitwise), in ONE
+        persistent launch: each block solves whole instances from the work
+        queue, with block barriers between the steps (see
+        odil_wave_batch_solve_mixed)."""
+        if epochs < 1:
+            self.u.zero_()
+            return self.u
+        cfg = self.march_cfg or autotune.default_batch_march(self.max_nx)
+        if epochs > 2 and getattr(self, "d2", None) is None:
+            self.d2 = torch.zeros_like(self.d)
+        call("odil_wave_batch_solve_mixed", ctypes.byref(self.b), int(epochs),
+             ptr(self.rhs), ptr(self.hi), ptr(self.lo),
+             ptr(self.d2 if epochs > 2 else None), ptr(self.u),
+             cfg["threads"], cfg["cpt"], cfg["pf"], cfg["blocks_per_sm"],
+             ptr(self.ws_solve), self.ws_solve.numel(), stream_handle())
         return self.u
 
     def capture(self, epochs=2):

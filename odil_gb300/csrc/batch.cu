@@ -229,6 +229,127 @@ __global__ void __launch_bounds__(1024) batch_march_kernel(odil_wave_batch b,
     }
 }
 
+// The whole mixed Newton of the batch in one persistent launch.  Each block
+// takes the next instance (largest first) from the work queue and runs the
+// from-zero sequence of the multi-launch path on it alone, with block
+// barriers between the steps instead of grid-wide passes:
+//   rhs = float(-F(0))             (zero inside, FP64 on the boundary cells)
+//   hi = J^-1 rhs                  (march_instance, the single-block march)
+//   repeat epochs - 1 times:
+//     rhs = float(-F(hi + lo))     (float pairs inside, FP64 on the boundary)
+//     lo = J^-1 rhs, or d = J^-1 rhs and lo += d after the first of these
+//   u = hi + lo in FP64            (exact, integer instructions)
+// The instance's fields are written and read back by the same block within
+// microseconds, so they mostly stay in L2.  Counters: [0] the work queue,
+// [1] blocks done; the last block to finish resets both, so the workspace
+// needs zeroing once, before the first launch.
+template <int CPT, int PF>
+__global__ void __launch_bounds__(1024) batch_solve_kernel(odil_wave_batch b, int epochs,
+                                                           float* __restrict__ rhs,
+                                                           float* __restrict__ hi,
+                                                           float* __restrict__ lo,
+                                                           float* __restrict__ dd,
+                                                           double* __restrict__ u,
+                                                           unsigned* __restrict__ counter) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ int sh_q;
+    const int nthr = blockDim.x;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = nthr >> 5;
+    const double* iu = (const double*)b.init_u;
+    const double* iut = (const double*)b.init_ut;
+    const double* lu = (const double*)b.left_u;
+    const double* ru = (const double*)b.right_u;
+    for (;;) {
+        if (threadIdx.x == 0) sh_q = (int)atomicAdd(counter, 1u);
+        __syncthreads();
+        const int q = sh_q;
+        __syncthreads();
+        if (q >= b.ninst) break;
+        const int idx = __ldg(b.order + q);
+        const odil_wave_instance desc = b.inst[idx];
+        const WaveDev<double> g64 = dev_of<double>(desc, iu, iut, lu, ru);
+        const WaveDev<float> g32 = dev_of<float>(desc, nullptr, nullptr, nullptr, nullptr);
+        const int nt = g32.nt, nx = g32.nx;
+        const int64_t off = desc.offset, cells = (int64_t)nt * nx;
+        PairCoef k;
+        k.ah = desc.ah;
+        k.al = desc.al;
+        k.ch = desc.ch;
+        k.cl = desc.cl;
+        k.bh = desc.bh;
+        k.bl = desc.bl;
+        float* r = rhs + off;
+        float* h = hi + off;
+        float* l = lo + off;
+        float* dq = dd + off;
+        // Right-hand side of the current iterate (KIND 0: u = 0; 1: hi + lo).
+        auto residual = [&](auto kind_tag, const float* lp) {
+            constexpr int KIND = decltype(kind_tag)::value;
+            for (int i = 2 + warp; i < nt; i += nwarp) {
+                float* rrow = r + (int64_t)i * nx;
+                for (int j = 1 + lane; j < nx - 1; j += 32)
+                    rrow[j] = KIND == 0 ? 0.f
+                                        : pair_interior_rhs(k, h, lp, (int64_t)i * nx + j, nx);
+            }
+            const int64_t nb = bnd_count(nt, nx);
+            for (int64_t t = threadIdx.x; t < nb; t += nthr) {
+                int i, j;
+                bnd_cell(t, nt, nx, &i, &j);
+                r[(int64_t)i * nx + j] = bnd_cell_rhs<KIND>(g64, k, h, lp, i, j);
+            }
+            __syncthreads();
+        };
+        auto march = [&](float* x) {
+            if (nx % CPT == 0) {
+                march_instance<float, CPT, PF, true>(g32, r, x, smem_raw);
+            } else {
+                march_instance<float, CPT, PF, false>(g32, r, x, smem_raw);
+            }
+            __syncthreads();
+        };
+        residual(std::integral_constant<int, 0>{}, nullptr);
+        march(h);
+        bool have_lo = false;
+        for (int e = 1; e < epochs; ++e) {
+            residual(std::integral_constant<int, 1>{}, have_lo ? l : nullptr);
+            if (have_lo) {
+                march(dq);
+                for (int64_t c = threadIdx.x; c < cells; c += nthr) l[c] += dq[c];
+                __syncthreads();
+            } else {
+                march(l);
+                have_lo = true;
+            }
+        }
+        double* uo = u + off;
+        for (int64_t c = threadIdx.x; c < cells; c += nthr)
+            uo[c] = have_lo ? pair_sum_exact(h[c], l[c]) : f2d_exact(h[c]);
+        __syncthreads();
+    }
+    // The last block out resets the queue for the next launch.
+    if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(counter + 1, 1u) == gridDim.x - 1) {
+            counter[0] = 0u;
+            counter[1] = 0u;
+            __threadfence();
+        }
+    }
+}
+
+template <int CPT, int PF>
+int launch_batch_solve(const odil_wave_batch* b, int epochs, float* rhs, float* hi, float* lo,
+                       float* d, double* u, unsigned* counter, int threads, int blocks,
+                       cudaStream_t st) {
+    if ((int64_t)threads * CPT < b->max_nx) return ODIL_ERR_SHAPE;
+    const size_t smem = march_ring_smem_bytes<float>(b->max_nx, PF);
+    if (smem > 200 * 1024) return ODIL_ERR_SHAPE;
+    auto kern = batch_solve_kernel<CPT, PF>;
+    ensure_dynamic_smem(reinterpret_cast<const void*>(kern), smem);
+    kern<<<blocks, threads, smem, st>>>(*b, epochs, rhs, hi, lo, d, u, counter);
+    return launch_status();
+}
+
 int check_batch(const odil_wave_batch* b) {
     if (!b) return ODIL_ERR_ARG;
     if (b->ninst < 1 || b->total_cells < 1 || b->max_nx < 1 || b->max_nx > 4096)
@@ -582,6 +703,34 @@ ODIL_API int odil_wave_batch_pair_residual_mixed(const odil_wave_batch* b, const
     if (!hi || !rhs || rhs == hi || rhs == lo) return ODIL_ERR_ARG;
     if (!b->init_u || !b->init_ut || !b->left_u || !b->right_u) return ODIL_ERR_ARG;
     return launch_rhs<1>(b, hi, lo, rhs, as_stream(stream));
+}
+
+ODIL_API int odil_wave_batch_solve_mixed(const odil_wave_batch* b, int32_t epochs, float* rhs,
+                                         float* hi, float* lo, float* d, double* u,
+                                         int32_t threads, int32_t cpt, int32_t pf,
+                                         int32_t blocks_per_sm, void* workspace,
+                                         int64_t workspace_bytes, void* stream) {
+    int st = check_batch(b);
+    if (st) return st;
+    if (epochs < 1 || epochs > 16) return ODIL_ERR_ARG;
+    if (!rhs || !hi || !u || (epochs > 1 && !lo) || (epochs > 2 && !d)) return ODIL_ERR_ARG;
+    if (!b->init_u || !b->init_ut || !b->left_u || !b->right_u) return ODIL_ERR_ARG;
+    if (!workspace || workspace_bytes < 256) return ODIL_ERR_WORKSPACE;
+    if (threads < 32 || threads > 1024 || threads % 32 || blocks_per_sm < 1 || blocks_per_sm > 32)
+        return ODIL_ERR_SHAPE;
+    int blocks = sms() * blocks_per_sm;
+    if (blocks > b->ninst) blocks = b->ninst;
+    unsigned* counter = reinterpret_cast<unsigned*>(workspace);
+    cudaStream_t s = as_stream(stream);
+    switch (cpt * 100 + pf) {
+        case 108: return launch_batch_solve<1, 8>(b, epochs, rhs, hi, lo, d, u, counter, threads, blocks, s);
+        case 116: return launch_batch_solve<1, 16>(b, epochs, rhs, hi, lo, d, u, counter, threads, blocks, s);
+        case 208: return launch_batch_solve<2, 8>(b, epochs, rhs, hi, lo, d, u, counter, threads, blocks, s);
+        case 216: return launch_batch_solve<2, 16>(b, epochs, rhs, hi, lo, d, u, counter, threads, blocks, s);
+        case 408: return launch_batch_solve<4, 8>(b, epochs, rhs, hi, lo, d, u, counter, threads, blocks, s);
+        case 416: return launch_batch_solve<4, 16>(b, epochs, rhs, hi, lo, d, u, counter, threads, blocks, s);
+        default: return ODIL_ERR_SHAPE;
+    }
 }
 
 ODIL_API int odil_wave_batch_march_f32(const odil_wave_batch* b, const float* rhs, float* x,
