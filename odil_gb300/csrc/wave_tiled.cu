@@ -159,9 +159,15 @@ __device__ __forceinline__ void push_cols(uint32_t raddr, uint32_t rmbar, const 
 constexpr uint64_t kHaloWaitNs = 1000000000ull;
 __device__ unsigned long long g_tiled_wait_failures = 0;
 
-__device__ __forceinline__ void cluster_sync_all() {
+__device__ __forceinline__ void cluster_arrive() {
     asm volatile("barrier.cluster.arrive.release.aligned;\n" ::: "memory");
+}
+__device__ __forceinline__ void cluster_wait() {
     asm volatile("barrier.cluster.wait.acquire.aligned;\n" ::: "memory");
+}
+__device__ __forceinline__ void cluster_sync_all() {
+    cluster_arrive();
+    cluster_wait();
 }
 
 // VEC: nx % CPT == 0 and b, x aligned to CPT elements (capped at 16 bytes),
@@ -185,11 +191,15 @@ __device__ __forceinline__ void cluster_sync_all() {
 //
 // CONV (cluster-barrier exchange only): the block also holds one converter
 // warp per marching warp (warps mw .. 2 mw - 1, on SM sub-partitions the
-// marching warps leave idle).  After each cluster barrier the converter of
-// tile t writes the FP64 value of the previous batch of rows of t's owned
-// columns into u64 (exact, integer instructions: f2d_exact), while the
-// marching warps go on with the next batch; the last batch follows a block
-// barrier at the end.  x keeps the FP32 solution (the exchange reloads it).
+// marching warps leave idle).  After the cluster barrier that ends a batch,
+// the converter of tile t writes the FP64 value of that batch's rows of t's
+// owned columns into u64 (exact, integer instructions: f2d_exact), while the
+// marching warps go on with the next batch.  The converters split the
+// barrier: they arrive at the next one before converting, so the march never
+// waits for them; a batch's loads are all in flight together, so converting
+// it takes well under the march's time for a batch.  The last batch follows a
+// block barrier at the end.  x keeps the FP32 solution (the exchange reloads
+// it).
 template <typename T, int CPT, int H, int PF, bool VEC, bool DSMEM, bool CONV = false>
 __global__ void __launch_bounds__(32 * kTiledMaxWarps * (CONV ? 2 : 1)) wave_march_tiled_kernel(
     WaveDev<T> g, const T* __restrict__ b, T* __restrict__ x, uint32_t extra_wait,
@@ -208,16 +218,62 @@ __global__ void __launch_bounds__(32 * kTiledMaxWarps * (CONV ? 2 : 1)) wave_mar
             const int t = blockIdx.x * mw + cw;
             const int cfirst = t * O;
             const int clast = cfirst + O < nx ? cfirst + O : nx;
+            const int w = clast - cfirst;  // owned columns inside the row
             auto convert = [&](int r0, int r1) {
-                for (int r = r0; r < r1; ++r) {
-                    const int64_t base = (int64_t)r * nx;
-                    for (int c = cfirst + lane; c < clast; c += 32)
-                        u64[base + c] = f2d_exact((float)__ldcg(x + base + c));
+                if (w <= 0 || r1 <= r0) return;
+                constexpr int U = 8;  // loads in flight per lane
+                if (VEC && w % 4 == 0) {
+                    // 16-byte pieces: columns cfirst + 4 p of rows r0 .. r1.
+                    const int per = w / 4, tot = (r1 - r0) * per;
+                    for (int e0 = lane; e0 < tot; e0 += 32 * U) {
+                        float4 v[U];
+#pragma unroll
+                        for (int q = 0; q < U; ++q) {
+                            const int e = e0 + 32 * q;
+                            if (e < tot) {
+                                const int rr = r0 + e / per, cc = cfirst + 4 * (e % per);
+                                v[q] = __ldcg(reinterpret_cast<const float4*>(
+                                    x + (int64_t)rr * nx + cc));
+                            }
+                        }
+#pragma unroll
+                        for (int q = 0; q < U; ++q) {
+                            const int e = e0 + 32 * q;
+                            if (e < tot) {
+                                const int rr = r0 + e / per, cc = cfirst + 4 * (e % per);
+                                double2* o =
+                                    reinterpret_cast<double2*>(u64 + (int64_t)rr * nx + cc);
+                                o[0] = make_double2(f2d_exact(v[q].x), f2d_exact(v[q].y));
+                                o[1] = make_double2(f2d_exact(v[q].z), f2d_exact(v[q].w));
+                            }
+                        }
+                    }
+                } else {
+                    const int tot = (r1 - r0) * w;
+                    for (int e0 = lane; e0 < tot; e0 += 32 * U) {
+                        float v[U];
+#pragma unroll
+                        for (int q = 0; q < U; ++q) {
+                            const int e = e0 + 32 * q;
+                            if (e < tot)
+                                v[q] = __ldcg(x + (int64_t)(r0 + e / w) * nx + cfirst + e % w);
+                        }
+#pragma unroll
+                        for (int q = 0; q < U; ++q) {
+                            const int e = e0 + 32 * q;
+                            if (e < tot)
+                                u64[(int64_t)(r0 + e / w) * nx + cfirst + e % w] =
+                                    f2d_exact(v[q]);
+                        }
+                    }
                 }
             };
-            // One cluster barrier per batch boundary, as the marching warps.
+            // The barriers of the batch boundaries, as the marching warps
+            // take them, but split: arrive at the next before converting.
+            if (H < nt) cluster_arrive();
             for (int i0 = H; i0 < nt; i0 += H) {
-                cluster_sync_all();
+                cluster_wait();                    // rows < i0 are stored
+                if (i0 + H < nt) cluster_arrive();  // the next boundary
                 convert(i0 - H, i0);
             }
             __syncthreads();  // the marching warps have stored the last batch
