@@ -324,6 +324,10 @@ __global__ void __launch_bounds__(1024) batch_solve_kernel(odil_wave_batch b, in
         double* uo = u + off;
         for (int64_t c = threadIdx.x; c < cells; c += nthr)
             uo[c] = have_lo ? pair_sum_exact(h[c], l[c]) : f2d_exact(h[c]);
+        // The padding up to the next instance is zero, as the multi-launch
+        // path leaves it.
+        const int64_t pad_end = idx + 1 < b.ninst ? b.inst[idx + 1].offset : b.total_cells;
+        for (int64_t c = off + cells + threadIdx.x; c < pad_end; c += nthr) u[c] = 0.0;
         __syncthreads();
     }
     // The last block out resets the queue for the next launch.
