@@ -201,17 +201,6 @@ int odil_wave_march_tiled_f32(const odil_wave_params* p, const float* b,
 int odil_wave_march_tiled_f64(const odil_wave_params* p, const double* b,
                               double* x, int32_t cpt, int32_t halo, int32_t pf,
                               int32_t warps, int32_t exchange, void* stream);
-/* odil_wave_march_tiled_f32 (exchange 0; (cpt, halo, pf) in (4, 32, 16),
- * (4, 48, 16); warps 1 or 2) that also writes u64 = the FP64 value of x
- * (exact), by converter warps that follow the march one batch of `halo`
- * rows behind: the solution of a mixed Newton epoch from u = 0 in one
- * launch.  The FP32 solution is still written to x.
- * The direct solve of linsolver.py:35-45 with the update of
- * util.py:242-268 (u = 0 + d) fused. */
-int odil_wave_march_tiled_to_f64_f32(const odil_wave_params* p,
-                                     const float* b, float* x, double* u64,
-                                     int32_t cpt, int32_t halo, int32_t pf,
-                                     int32_t warps, void* stream);
 /* Test hook of the bounded halo wait: odil_wave_march_tiled_f32 with
  * exchange 1 whose every wait expects `missing_bytes` (1..65536) more than
  * ever arrive, so each wait gives up after its limit. */

@@ -17,8 +17,11 @@ from . import _capi, autotune
 from ._capi import call, ptr, stream_handle
 
 
-def _align4(n):
-    return (n + 3) // 4 * 4
+def _align32(n):
+    """Instance starts: 32 elements (128 bytes FP32, 256 bytes FP64), so
+    no cache line holds two instances' data and vector accesses stay
+    aligned."""
+    return (n + 31) // 32 * 32
 
 
 class WaveBatch:
@@ -45,7 +48,7 @@ class WaveBatch:
             d.offset, d.offset_x, d.offset_t = off, offx, offt
             self.offsets.append(off)
             self.shapes.append((nt, nx))
-            off = _align4(off + nt * nx)
+            off = _align32(off + nt * nx)
             offx += nx
             offt += nt
             bcx_u.append(np.asarray(inst["init_u"], np.float64))

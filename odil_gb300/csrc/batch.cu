@@ -240,7 +240,10 @@ __global__ void __launch_bounds__(1024) batch_march_kernel(odil_wave_batch b,
 //     lo = J^-1 rhs, or d = J^-1 rhs and lo += d after the first of these
 //   u = hi + lo in FP64            (exact, integer instructions)
 // The instance's fields are written and read back by the same block within
-// microseconds, so they mostly stay in L2.  Counters: [0] the work queue,
+// microseconds, so they mostly stay in L2.  Values written in this kernel
+// are read back through L2 (ld.global.cg), never the read-only path, and
+// instances start on 128-byte boundaries (the host's packing), so no L1
+// line holds two instances' data.  Counters: [0] the work queue,
 // [1] blocks done; the last block to finish resets both, so the workspace
 // needs zeroing once, before the first launch.
 template <int CPT, int PF>
@@ -289,13 +292,14 @@ __global__ void __launch_bounds__(1024) batch_solve_kernel(odil_wave_batch b, in
                 float* rrow = r + (int64_t)i * nx;
                 for (int j = 1 + lane; j < nx - 1; j += 32)
                     rrow[j] = KIND == 0 ? 0.f
-                                        : pair_interior_rhs(k, h, lp, (int64_t)i * nx + j, nx);
+                                        : pair_interior_rhs<false>(k, h, lp,
+                                                                   (int64_t)i * nx + j, nx);
             }
             const int64_t nb = bnd_count(nt, nx);
             for (int64_t t = threadIdx.x; t < nb; t += nthr) {
                 int i, j;
                 bnd_cell(t, nt, nx, &i, &j);
-                r[(int64_t)i * nx + j] = bnd_cell_rhs<KIND>(g64, k, h, lp, i, j);
+                r[(int64_t)i * nx + j] = bnd_cell_rhs<KIND, false>(g64, k, h, lp, i, j);
             }
             __syncthreads();
         };

@@ -289,20 +289,33 @@ __device__ __forceinline__ void pair_acc(float ch, float cl, float v, float w, f
     c = __fmaf_rn(ch, w, c);
 }
 
+// Load of an iterate value: read-only path (NC, the iterate is another
+// kernel's output) or through L2 (the iterate was written earlier in the
+// same kernel, possibly by another SM).
+template <bool NC>
+__device__ __forceinline__ float ld_iter(const float* p) {
+    if constexpr (NC) {
+        return __ldg(p);
+    } else {
+        return __ldcg(p);
+    }
+}
+
 // -F(hi + lo) at interior cell (i, j) rounded to FP32.  lo may be null.
+template <bool NC = true>
 __device__ __forceinline__ float pair_interior_rhs(const PairCoef& k, const float* __restrict__ hi,
                                                    const float* __restrict__ lo, int64_t c0,
                                                    int nx) {
     const int64_t c1 = c0 - nx, c2 = c0 - 2 * (int64_t)nx;
-    const float v0 = __ldg(hi + c0), v2 = __ldg(hi + c2), v1 = __ldg(hi + c1);
-    const float vm = __ldg(hi + c1 - 1), vp = __ldg(hi + c1 + 1);
+    const float v0 = ld_iter<NC>(hi + c0), v2 = ld_iter<NC>(hi + c2), v1 = ld_iter<NC>(hi + c1);
+    const float vm = ld_iter<NC>(hi + c1 - 1), vp = ld_iter<NC>(hi + c1 + 1);
     float w0 = 0.f, w2 = 0.f, w1 = 0.f, wm = 0.f, wp = 0.f;
     if (lo) {
-        w0 = __ldg(lo + c0);
-        w2 = __ldg(lo + c2);
-        w1 = __ldg(lo + c1);
-        wm = __ldg(lo + c1 - 1);
-        wp = __ldg(lo + c1 + 1);
+        w0 = ld_iter<NC>(lo + c0);
+        w2 = ld_iter<NC>(lo + c2);
+        w1 = ld_iter<NC>(lo + c1);
+        wm = ld_iter<NC>(lo + c1 - 1);
+        wp = ld_iter<NC>(lo + c1 + 1);
     }
     float s = 0.f, c = 0.f;
     pair_acc(k.ah, k.al, v0, w0, s, c);
@@ -315,16 +328,17 @@ __device__ __forceinline__ float pair_interior_rhs(const PairCoef& k, const floa
 
 // -F(hi + lo) at any cell: the float-pair form inside, FP64 wave_f on the
 // boundary rows and columns.
+template <bool NC = true>
 __device__ __forceinline__ float pair_cell_rhs(const WaveDev<double>& g, const PairCoef& k,
                                                const float* __restrict__ hi,
                                                const float* __restrict__ lo, int i, int j) {
     const int nx = g.nx;
     const int64_t c0 = (int64_t)i * nx + j;
-    if (i >= 2 && j >= 1 && j + 1 < nx) return pair_interior_rhs(k, hi, lo, c0, nx);
+    if (i >= 2 && j >= 1 && j + 1 < nx) return pair_interior_rhs<NC>(k, hi, lo, c0, nx);
     auto val = [&](int ii, int jj) -> double {
         const int64_t kk = (int64_t)ii * nx + jj;
-        double v = (double)__ldg(hi + kk);
-        if (lo) v += (double)__ldg(lo + kk);
+        double v = (double)ld_iter<NC>(hi + kk);
+        if (lo) v += (double)ld_iter<NC>(lo + kk);
         return v;
     };
     const double uc = val(i, j);
@@ -340,12 +354,12 @@ __device__ __forceinline__ float pair_cell_rhs(const WaveDev<double>& g, const P
 
 // -F(hi + lo) (KIND 1) or -F(0) (KIND 0) at a boundary cell (row 0 or 1,
 // column 0 or nx-1) in FP64.
-template <int KIND>
+template <int KIND, bool NC = true>
 __device__ __forceinline__ float bnd_cell_rhs(const WaveDev<double>& g, const PairCoef& k,
                                               const float* __restrict__ hi,
                                               const float* __restrict__ lo, int i, int j) {
     if (KIND == 0) return (float)(-wave_f(g, i, j, 0.0, 0.0, 0.0, 0.0, 0.0));
-    return pair_cell_rhs(g, k, hi, lo, i, j);
+    return pair_cell_rhs<NC>(g, k, hi, lo, i, j);
 }
 
 // Boundary cells of an nt x nx grid: rows 0 and 1 (all columns), then columns

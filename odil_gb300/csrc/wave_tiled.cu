@@ -159,15 +159,9 @@ __device__ __forceinline__ void push_cols(uint32_t raddr, uint32_t rmbar, const 
 constexpr uint64_t kHaloWaitNs = 1000000000ull;
 __device__ unsigned long long g_tiled_wait_failures = 0;
 
-__device__ __forceinline__ void cluster_arrive() {
-    asm volatile("barrier.cluster.arrive.release.aligned;\n" ::: "memory");
-}
-__device__ __forceinline__ void cluster_wait() {
-    asm volatile("barrier.cluster.wait.acquire.aligned;\n" ::: "memory");
-}
 __device__ __forceinline__ void cluster_sync_all() {
-    cluster_arrive();
-    cluster_wait();
+    asm volatile("barrier.cluster.arrive.release.aligned;\n" ::: "memory");
+    asm volatile("barrier.cluster.wait.acquire.aligned;\n" ::: "memory");
 }
 
 // VEC: nx % CPT == 0 and b, x aligned to CPT elements (capped at 16 bytes),
@@ -188,100 +182,15 @@ __device__ __forceinline__ void cluster_sync_all() {
 // only wait for their neighbours, and the solution stores need no fence.
 // `extra_wait` adds bytes that never arrive to every wait (a planted
 // failure for the bounded-wait test; 0 otherwise).
-//
-// CONV (cluster-barrier exchange only): the block also holds one converter
-// warp per marching warp (warps mw .. 2 mw - 1, on SM sub-partitions the
-// marching warps leave idle).  After the cluster barrier that ends a batch,
-// the converter of tile t writes the FP64 value of that batch's rows of t's
-// owned columns into u64 (exact, integer instructions: f2d_exact), while the
-// marching warps go on with the next batch.  The converters split the
-// barrier: they arrive at the next one before converting, so the march never
-// waits for them; a batch's loads are all in flight together, so converting
-// it takes well under the march's time for a batch.  The last batch follows a
-// block barrier at the end.  x keeps the FP32 solution (the exchange reloads
-// it).
-template <typename T, int CPT, int H, int PF, bool VEC, bool DSMEM, bool CONV = false>
-__global__ void __launch_bounds__(32 * kTiledMaxWarps * (CONV ? 2 : 1)) wave_march_tiled_kernel(
-    WaveDev<T> g, const T* __restrict__ b, T* __restrict__ x, uint32_t extra_wait,
-    double* __restrict__ u64) {
+template <typename T, int CPT, int H, int PF, bool VEC, bool DSMEM>
+__global__ void __launch_bounds__(32 * kTiledMaxWarps) wave_march_tiled_kernel(
+    WaveDev<T> g, const T* __restrict__ b, T* __restrict__ x, uint32_t extra_wait) {
     constexpr int O = 32 * CPT - 2 * H;  // owned columns per warp
     static_assert(O > 0 && H % CPT == 0 && H % PF == 0, "tile shape");
     static_assert(!DSMEM || O >= H, "pushed columns come from one neighbour");
-    static_assert(!(CONV && DSMEM), "converter warps follow the cluster barrier");
     const int nx = g.nx, nt = g.nt;
     const int lane = threadIdx.x & 31;
-    const int mw = CONV ? (int)(blockDim.x >> 6) : (int)(blockDim.x >> 5);  // marching warps
-    if constexpr (CONV) {
-        const int cw = (int)(threadIdx.x >> 5) - mw;
-        if (cw >= 0) {
-            pdl_trigger();
-            const int t = blockIdx.x * mw + cw;
-            const int cfirst = t * O;
-            const int clast = cfirst + O < nx ? cfirst + O : nx;
-            const int w = clast - cfirst;  // owned columns inside the row
-            auto convert = [&](int r0, int r1) {
-                if (w <= 0 || r1 <= r0) return;
-                constexpr int U = 8;  // loads in flight per lane
-                if (VEC && w % 4 == 0) {
-                    // 16-byte pieces: columns cfirst + 4 p of rows r0 .. r1.
-                    const int per = w / 4, tot = (r1 - r0) * per;
-                    for (int e0 = lane; e0 < tot; e0 += 32 * U) {
-                        float4 v[U];
-#pragma unroll
-                        for (int q = 0; q < U; ++q) {
-                            const int e = e0 + 32 * q;
-                            if (e < tot) {
-                                const int rr = r0 + e / per, cc = cfirst + 4 * (e % per);
-                                v[q] = __ldcg(reinterpret_cast<const float4*>(
-                                    x + (int64_t)rr * nx + cc));
-                            }
-                        }
-#pragma unroll
-                        for (int q = 0; q < U; ++q) {
-                            const int e = e0 + 32 * q;
-                            if (e < tot) {
-                                const int rr = r0 + e / per, cc = cfirst + 4 * (e % per);
-                                double2* o =
-                                    reinterpret_cast<double2*>(u64 + (int64_t)rr * nx + cc);
-                                o[0] = make_double2(f2d_exact(v[q].x), f2d_exact(v[q].y));
-                                o[1] = make_double2(f2d_exact(v[q].z), f2d_exact(v[q].w));
-                            }
-                        }
-                    }
-                } else {
-                    const int tot = (r1 - r0) * w;
-                    for (int e0 = lane; e0 < tot; e0 += 32 * U) {
-                        float v[U];
-#pragma unroll
-                        for (int q = 0; q < U; ++q) {
-                            const int e = e0 + 32 * q;
-                            if (e < tot)
-                                v[q] = __ldcg(x + (int64_t)(r0 + e / w) * nx + cfirst + e % w);
-                        }
-#pragma unroll
-                        for (int q = 0; q < U; ++q) {
-                            const int e = e0 + 32 * q;
-                            if (e < tot)
-                                u64[(int64_t)(r0 + e / w) * nx + cfirst + e % w] =
-                                    f2d_exact(v[q]);
-                        }
-                    }
-                }
-            };
-            // The barriers of the batch boundaries, as the marching warps
-            // take them, but split: arrive at the next before converting.
-            if (H < nt) cluster_arrive();
-            for (int i0 = H; i0 < nt; i0 += H) {
-                cluster_wait();                    // rows < i0 are stored
-                if (i0 + H < nt) cluster_arrive();  // the next boundary
-                convert(i0 - H, i0);
-            }
-            __syncthreads();  // the marching warps have stored the last batch
-            convert(((nt - 1) / H) * H, nt);
-            return;
-        }
-    }
-    const int tile = blockIdx.x * mw + (threadIdx.x >> 5);
+    const int tile = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     const int j0 = tile * O - H + lane * CPT;  // this lane's first column
     const bool own = lane >= H / CPT && lane < (H + O) / CPT;
     bool in[CPT];
@@ -395,7 +304,7 @@ __global__ void __launch_bounds__(32 * kTiledMaxWarps * (CONV ? 2 : 1)) wave_mar
             target = tile + 1, side = 0, off = wl - O;
         }
         if (target >= 0) {
-            const int wpb = mw;
+            const int wpb = blockDim.x >> 5;
             const uint32_t rank = (uint32_t)(target / wpb), tw = (uint32_t)(target % wpb);
             push_addr = cluster_map(smem_u32(&halo[tw][0][side][0][off]), rank);
             push_mbar = cluster_map(smem_u32(&mbar[tw][0]), rank);
@@ -488,14 +397,11 @@ __global__ void __launch_bounds__(32 * kTiledMaxWarps * (CONV ? 2 : 1)) wave_mar
         }
     }
     if constexpr (DSMEM) cluster_sync_all();  // no CTA leaves while pushes may target it
-    if constexpr (CONV) __syncthreads();      // hand the last batch to the converters
 }
 
 template <typename T>
 int tiled_launch(const void* kern, int clusters, int warps, const WaveDev<T>& g, const T* b,
-                 T* x, uint32_t extra_wait, double* u64, cudaStream_t st) {
-    // Converter warps (u64 given) double the block.
-    const int threads = 32 * warps * (u64 ? 2 : 1);
+                 T* x, uint32_t extra_wait, cudaStream_t st) {
     static thread_local const void* checked[64];
     static thread_local int nchecked = 0;
     bool seen = false;
@@ -506,7 +412,7 @@ int tiled_launch(const void* kern, int clusters, int warps, const WaveDev<T>& g,
     }
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)clusters);
-    cfg.blockDim = dim3((unsigned)threads);
+    cfg.blockDim = dim3((unsigned)(32 * warps));
     cfg.dynamicSmemBytes = 0;
     cfg.stream = st;
     cudaLaunchAttribute attr[2];
@@ -538,7 +444,7 @@ int tiled_launch(const void* kern, int clusters, int warps, const WaveDev<T>& g,
         if (nfits < 64) fits[nfits++] = {kern, clusters, warps, ok};
     }
     if (!ok) return ODIL_ERR_SHAPE;
-    void* args[] = {const_cast<WaveDev<T>*>(&g), &b, &x, &extra_wait, &u64};
+    void* args[] = {const_cast<WaveDev<T>*>(&g), &b, &x, &extra_wait};
     cfg.numAttrs = 2;  // the occupancy query above saw the cluster only
     if (cudaLaunchKernelExC(&cfg, kern, args) != cudaSuccess) {
         cudaGetLastError();
@@ -547,9 +453,9 @@ int tiled_launch(const void* kern, int clusters, int warps, const WaveDev<T>& g,
     return launch_status();
 }
 
-template <typename T, int CPT, int H, int PF, bool DSMEM, bool CONV = false>
+template <typename T, int CPT, int H, int PF, bool DSMEM>
 int tiled_shape_fit(const WaveDev<T>& g, const T* b, T* x, int warps, uint32_t extra_wait,
-                    double* u64, cudaStream_t st) {
+                    cudaStream_t st) {
     constexpr int O = 32 * CPT - 2 * H;
     const int64_t tiles = (g.nx + O - 1) / O;
     if (warps < 1 || warps > kTiledMaxWarps) return ODIL_ERR_SHAPE;
@@ -560,12 +466,9 @@ int tiled_shape_fit(const WaveDev<T>& g, const T* b, T* x, int warps, uint32_t e
     const bool vec = g.nx % CPT == 0 &&
                      ((reinterpret_cast<uintptr_t>(b) | reinterpret_cast<uintptr_t>(x)) % vb) == 0;
     const void* kern =
-        vec ? reinterpret_cast<const void*>(
-                  wave_march_tiled_kernel<T, CPT, H, PF, true, DSMEM, CONV>)
-            : reinterpret_cast<const void*>(
-                  wave_march_tiled_kernel<T, CPT, H, PF, false, DSMEM, CONV>);
-    return tiled_launch<T>(kern, (int)clusters, warps, g, b, x, extra_wait,
-                           CONV ? u64 : nullptr, st);
+        vec ? reinterpret_cast<const void*>(wave_march_tiled_kernel<T, CPT, H, PF, true, DSMEM>)
+            : reinterpret_cast<const void*>(wave_march_tiled_kernel<T, CPT, H, PF, false, DSMEM>);
+    return tiled_launch<T>(kern, (int)clusters, warps, g, b, x, extra_wait, st);
 }
 
 template <typename T, int CPT, int H, int PF, bool DSMEM>
@@ -575,27 +478,7 @@ int tiled_shape(const WaveDev<T>& g, const T* b, T* x, int warps, uint32_t extra
     if constexpr (CPT * PF * sizeof(T) > 512) {
         return ODIL_ERR_SHAPE;
     } else {
-        return tiled_shape_fit<T, CPT, H, PF, DSMEM>(g, b, x, warps, extra_wait, nullptr, st);
-    }
-}
-
-// The FP32 march with converter warps writing the FP64 solution too
-// (cluster-barrier shapes).
-int tiled_to_f64_dispatch(const odil_wave_params* p, const float* b, float* x, double* u64,
-                          int cpt, int halo, int pf, int warps, void* stream) {
-    WaveDev<float> g;
-    int st = make_dev<float>(p, &g, false);
-    if (st) return st;
-    if (!b || !x || !u64) return ODIL_ERR_ARG;
-    if (g.nx < 2) return ODIL_ERR_SHAPE;
-    if (warps < 1 || warps > 2) return ODIL_ERR_SHAPE;  // one converter per spare sub-partition
-    cudaStream_t s = as_stream(stream);
-    switch (cpt * 10000 + halo * 100 + pf) {
-        case 43216:
-            return tiled_shape_fit<float, 4, 32, 16, false, true>(g, b, x, warps, 0u, u64, s);
-        case 44816:
-            return tiled_shape_fit<float, 4, 48, 16, false, true>(g, b, x, warps, 0u, u64, s);
-        default: return ODIL_ERR_SHAPE;
+        return tiled_shape_fit<T, CPT, H, PF, DSMEM>(g, b, x, warps, extra_wait, st);
     }
 }
 
@@ -634,13 +517,6 @@ int tiled_dispatch(const odil_wave_params* p, const T* b, T* x, int cpt, int hal
 }  // namespace odil
 
 using odil::tiled_dispatch;
-using odil::tiled_to_f64_dispatch;
-
-ODIL_API int odil_wave_march_tiled_to_f64_f32(const odil_wave_params* p, const float* b,
-                                              float* x, double* u64, int32_t cpt, int32_t halo,
-                                              int32_t pf, int32_t warps, void* stream) {
-    return tiled_to_f64_dispatch(p, b, x, u64, cpt, halo, pf, warps, stream);
-}
 
 ODIL_API int odil_wave_march_tiled_f32(const odil_wave_params* p, const float* b, float* x,
                                        int32_t cpt, int32_t halo, int32_t pf, int32_t warps,

@@ -119,23 +119,18 @@ def _solve_pairs(k, u, rhs, d, epochs, rnorm2):
     hi = _scratch(k, "hi32", torch.float32)
     lo = _scratch(k, "lo32", torch.float32)
     k.initial_rhs(rhs)
-    # One epoch: u = float64(J^{-1} rhs), written by the march itself where
-    # the tuned shape allows (no separate FP64 pass).
-    fused = (epochs == 1 and hasattr(k, "march_tuned_to_f64") and
-             k.march_tuned_to_f64(rhs, hi, u))
-    if not fused:
-        k.march_tuned(rhs, hi)
-        have_lo = False
-        for _ in range(1, epochs):
-            k.pair_residual(hi, lo if have_lo else None, rhs)
-            if have_lo:
-                k.march_tuned(rhs, d)
-                vec.axpby(lo, 1.0, lo, 1.0, d)
-            else:
-                k.march_tuned(rhs, lo)
-                have_lo = True
-        call("odil_pair_to_f64", ptr(hi), ptr(lo if have_lo else None),
-             ptr(u), u.numel(), stream_handle())
+    k.march_tuned(rhs, hi)
+    have_lo = False
+    for _ in range(1, epochs):
+        k.pair_residual(hi, lo if have_lo else None, rhs)
+        if have_lo:
+            k.march_tuned(rhs, d)
+            vec.axpby(lo, 1.0, lo, 1.0, d)
+        else:
+            k.march_tuned(rhs, lo)
+            have_lo = True
+    call("odil_pair_to_f64", ptr(hi), ptr(lo if have_lo else None), ptr(u),
+         u.numel(), stream_handle())
     if rnorm2 is not None:
         k.update_residual_mixed(u, None, None, rhs, rnorm2)
 

@@ -229,32 +229,6 @@ class WaveKernels:
             tuned[b.dtype] = autotune.tune_march(self, dtype=b.dtype)
         return self.march_shape(b, out, tuned[b.dtype])
 
-    # FP32 march shapes that have the fused FP64 write (exchange 0).
-    _TO_F64_SHAPES = {(4, 32, 16), (4, 48, 16)}
-
-    def march_tuned_to_f64(self, b, x, u64):
-        """The tuned FP32 forward substitution x = J^{-1} b that also writes
-        u64 = float64(x) in the same launch (converter warps behind the
-        march); False (nothing launched) when the tuned shape has no such
-        form."""
-        if b.dtype != torch.float32 or u64.dtype != torch.float64:
-            raise TypeError("FP32 right-hand side and FP64 output expected")
-        tuned = self.__dict__.setdefault("_march_cfgs", {})
-        if b.dtype not in tuned:
-            from . import autotune
-            tuned[b.dtype] = autotune.tune_march(self, dtype=b.dtype)
-        cfg = tuned[b.dtype]
-        if (not cfg or cfg.get("kind") != "tiled" or cfg.get("exchange", 0) != 0
-                or int(cfg.get("warps", 1)) > 2 or
-                (int(cfg["cpt"]), int(cfg["halo"]), int(cfg["pf"]))
-                not in self._TO_F64_SHAPES):
-            return False
-        self._check(b)
-        call("odil_wave_march_tiled_to_f64_f32", ctypes.byref(self.p32),
-             ptr(b), ptr(x), ptr(u64), int(cfg["cpt"]), int(cfg["halo"]),
-             int(cfg["pf"]), int(cfg["warps"]), stream_handle())
-        return True
-
     def initial_rhs(self, rhs):
         """rhs = float32(-F(0)) (boundary cells only do FP64 work)."""
         call("odil_wave_initial_rhs_mixed", ctypes.byref(self.p64), ptr(rhs),

@@ -231,39 +231,6 @@ def test_march_tiled_matches_oracle(cuda, shape):
         assert _rel(x.cpu().numpy(), xo) < tol
 
 
-@pytest.mark.parametrize("shape", [(3, 2), (40, 70), (130, 96), (1024, 1024),
-                                   (1500, 1024)])
-def test_march_tiled_to_f64_matches_march(cuda, shape):
-    """The FP32 march whose converter warps also write the FP64 solution:
-    x is bitwise the plain tiled march's (same shape), and u64 is exactly
-    float64(x), for every fused shape, one and two marching warps per block,
-    row counts that are and are not multiples of the halo depth."""
-    s = _setup(*shape, seed=6, c=0.9)
-    k = _kernels(s, cuda)
-    b = torch.as_tensor(np.random.default_rng(7).standard_normal(shape),
-                        dtype=torch.float32, device=cuda)
-    ran = 0
-    for cpt, halo, pf in sorted(k._TO_F64_SHAPES):
-        for warps in (1, 2):
-            cfg = {"kind": "tiled", "cpt": cpt, "halo": halo, "pf": pf,
-                   "warps": warps, "exchange": 0}
-            ref = torch.full_like(b, float("nan"))
-            try:
-                k.march_shape(b, ref, cfg)
-            except Exception:  # noqa: BLE001 - shape does not fit this grid
-                continue
-            k.__dict__["_march_cfgs"] = {torch.float32: cfg}
-            x = torch.full_like(b, float("nan"))
-            u = torch.full(shape, float("nan"), dtype=torch.float64,
-                           device=cuda)
-            assert k.march_tuned_to_f64(b, x, u)
-            assert torch.equal(x, ref), cfg
-            assert torch.equal(u, ref.double()), cfg
-            ran += 1
-    k.__dict__.pop("_march_cfgs", None)
-    assert ran > 0
-
-
 def test_initial_rhs_and_f32_update(cuda):
     """rhs of u = 0 from the boundary-only kernel equals the general
     update/residual kernel's; the FP32->FP64 update is exact."""
