@@ -413,7 +413,10 @@ constexpr int BLG_OUT = 32 * BLG_V - 2;  // output columns per item
 constexpr int BLG_TY = 32;
 constexpr int BLG_WARPS = 4;
 constexpr int BLG_R = 8;      // ring rows per warp (power of two)
-constexpr int BLG_ROW = 136;  // floats per ring row: [3] left extra, [4 + 4 l + j], [132] right extra
+// floats per ring row: [3] left extra column, [4 + 4 l + j] the lanes'
+// columns, [132] right extra column, [133] / [134] the boundary values
+// left_u / right_u of the row above (for the residual at columns 0, nx-1)
+constexpr int BLG_ROW = 136;
 
 // Residual of an interior cell (row >= 2, 0 < column < nx - 1): the
 // expression of wave_f_with for such cells.
@@ -488,6 +491,13 @@ __global__ void __launch_bounds__(BLG_WARPS * 32, 5) batch_loss_grad_kernel(
     const bool xl = lane == 0 || lane == 31;
     const int offe = lane == 0 ? wrapn(c0 - 2, nx) : wrapn(c0 + 32 * V - 1, nx);
     const int xe = lane == 0 ? 3 : 4 + 32 * V;  // its ring index
+    // Lanes holding column 0 / nx - 1 also stream left_u / right_u.
+    bool has_l = false, has_r = false;
+#pragma unroll
+    for (int j = 0; j < V; ++j) {
+        has_l |= cb + j == 0;
+        has_r |= cb + j == nx - 1;
+    }
     // Row q (r = a0 - 2 + q) into ring slot q mod BLG_R; rows outside the
     // grid are zero.  Every call commits one group (empty past the tile), so
     // the wait below counts rows.
@@ -500,6 +510,8 @@ __global__ void __launch_bounds__(BLG_WARPS * 32, 5) batch_loss_grad_kernel(
 #pragma unroll
                 for (int j = 0; j < V; ++j) cp_async_n(to + 4 + V * lane + j, row + off[j], 4);
                 if (xl) cp_async_n(to + xe, row + offe, 4);
+                if (r >= 1 && has_l) cp_async_n(to + 133, g.left_u + (r - 1), 4);
+                if (r >= 1 && has_r) cp_async_n(to + 134, g.right_u + (r - 1), 4);
             } else {
 #pragma unroll
                 for (int j = 0; j < V; ++j) to[4 + V * lane + j] = 0.f;
@@ -542,12 +554,19 @@ __global__ void __launch_bounds__(BLG_WARPS * 32, 5) batch_loss_grad_kernel(
                         f0[j] = blg_f(g, u0[j], u1[j], u2[j], um, up);
                     }
                     if (fixm) {
+                        // Columns 0 / nx - 1: the extrapolated neighbour of
+                        // wave_f_with from the streamed boundary value.
 #pragma unroll
                         for (int j = 0; j < V; ++j) {
                             if (fixm & (1u << j)) {
-                                const float um = j == 0 ? um0 : u1[j - 1];
-                                const float up = j == V - 1 ? upv : u1[j + 1];
-                                f0[j] = wave_f(g, r, off[j], u0[j], u1[j], u2[j], um, up);
+                                float um = j == 0 ? um0 : u1[j - 1];
+                                float up = j == V - 1 ? upv : u1[j + 1];
+                                if (cb + j == 0) {
+                                    um = (up - 6.f * u1[j] + 8.f * cur[133]) / 3.f;
+                                } else {
+                                    up = (um - 6.f * u1[j] + 8.f * cur[134]) / 3.f;
+                                }
+                                f0[j] = blg_f(g, u0[j], u1[j], u2[j], um, up);
                             }
                         }
                     }

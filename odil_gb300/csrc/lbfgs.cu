@@ -289,8 +289,7 @@ __global__ void __launch_bounds__(LT) lbfgs_pair_dots_kernel(
 #pragma unroll
     for (int j = 0; j < PD; ++j) acc[j] = T(0);
     const int64_t stride = (int64_t)gridDim.x * LT;
-    for (int64_t i = (int64_t)blockIdx.x * LT + threadIdx.x; i < n; i += stride) {
-        const T dv = d[i], gtv = gt[i], gv = g[i];
+    auto step = [&](T dv, T gtv, T gv, int64_t i) {
         const T sv = a * dv, yv = gtv - gv;
         sy[i] = sv;
         sy[n + i] = yv;
@@ -299,7 +298,22 @@ __global__ void __launch_bounds__(LT) lbfgs_pair_dots_kernel(
         acc[2] += sv * gtv;
         acc[3] += yv * yv;
         acc[4] += yv * gtv;
+    };
+    // PU elements per thread per pass, all their loads issued first.
+    constexpr int PU = 4;
+    int64_t i = (int64_t)blockIdx.x * LT + threadIdx.x;
+    for (; i + (PU - 1) * stride < n; i += PU * stride) {
+        T dv[PU], gtv[PU], gv[PU];
+#pragma unroll
+        for (int u = 0; u < PU; ++u) {
+            dv[u] = d[i + u * stride];
+            gtv[u] = gt[i + u * stride];
+            gv[u] = g[i + u * stride];
+        }
+#pragma unroll
+        for (int u = 0; u < PU; ++u) step(dv[u], gtv[u], gv[u], i + u * stride);
     }
+    for (; i < n; i += stride) step(d[i], gt[i], g[i], i);
     __shared__ double red[LT / 32][PD];
     __shared__ bool is_last;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -450,13 +464,22 @@ int pair_impl(int64_t n, T* sy, const T* d, const T* gt, const T* g, const doubl
     return launch_status();
 }
 
+// Blocks of the pair-and-dots pass: at most 2 per SM, so the FP64 warp
+// reductions of the five dots (GB300's FP64 pipe is narrow) are paid by few
+// blocks, each streaming a long stretch.
+inline unsigned pd_grid(int64_t n) {
+    int64_t b = (n + LT - 1) / LT;
+    const int64_t cap = 152 * 2;
+    return (unsigned)(b < 1 ? 1 : (b > cap ? cap : b));
+}
+
 template <typename T>
 int pair_dots_impl(int64_t n, T* sy, const T* d, const T* gt, const T* g, const double* ft,
                    int mode, double* sc, double* Q, void* ws, int64_t ws_bytes, void* stream) {
     if (n < 1) return ODIL_ERR_SHAPE;
     if (mode != 0 && mode != 1) return ODIL_ERR_ARG;
     if (!sy || !d || !gt || !g || !sc || !Q || (mode == 0 && !ft)) return ODIL_ERR_ARG;
-    const unsigned blocks = lgrid(n);
+    const unsigned blocks = pd_grid(n);
     if (!ws || ws_bytes < kReduceHeader + (int64_t)PD * blocks * (int64_t)sizeof(double))
         return ODIL_ERR_WORKSPACE;
     lbfgs_pair_dots_kernel<T><<<blocks, LT, 0, as_stream(stream)>>>(n, sy, d, gt, g, ft, mode, sc,
@@ -519,7 +542,7 @@ ODIL_API int odil_lbfgs_pair_f64(int64_t n, double* sy, const double* d, const d
 
 ODIL_API int64_t odil_lbfgs_pair_dots_workspace_bytes(int64_t n) {
     if (n < 1) return 0;
-    return kReduceHeader + (int64_t)PD * lgrid(n) * (int64_t)sizeof(double);
+    return kReduceHeader + (int64_t)PD * pd_grid(n) * (int64_t)sizeof(double);
 }
 ODIL_API int odil_lbfgs_pair_dots_f32(int64_t n, float* sy, const float* d, const float* gt,
                                       const float* g, const double* ft, int32_t mode, double* sc,
