@@ -391,7 +391,9 @@ def run_batch(dev, with_oracle, steps=5, hbm=6800.0):
     ms_multi = statistics.mean(a.elapsed_time(c) for a, c in ts)
     u_multi = b.u.clone()
     # The same solve in ONE persistent launch (whole instances per block),
-    # replayed from a CUDA graph like the multi-launch form.
+    # blocks per SM chosen by timing, replayed from a CUDA graph like the
+    # multi-launch form.
+    pers_tune = b.tune_persistent(BATCH_EPOCHS)
     b.solve_persistent(BATCH_EPOCHS)
     torch.cuda.synchronize(dev)
     side = torch.cuda.Stream(dev)
@@ -495,6 +497,7 @@ def run_batch(dev, with_oracle, steps=5, hbm=6800.0):
            "method": ("persistent" if ms_pers <= ms_multi else
                       "multi_launch"),
            "persistent": {"ms_per_batch": ms_pers, "launches_per_batch": 1,
+                          "blocks_per_sm_ms": pers_tune,
                           "value": len(insts) / (ms_pers / 1000.0),
                           "bitwise_equal_to_multi_launch": same},
            # kernels: rhs (interior + boundary), march, then per further

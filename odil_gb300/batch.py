@@ -207,6 +207,31 @@ class WaveBatch:
              ptr(self.u), self.total, stream_handle())
         return self.u
 
+    def tune_persistent(self, epochs=2, per_sm=(1, 2, 3, 4), reps=3):
+        """Chooses blocks per SM of the persistent whole-solve launch by
+        timing it (CUDA events) with the march's threads, cpt and pf; keeps
+        the fastest in self.persistent_cfg and returns {per_sm: ms}."""
+        base = dict(self.march_cfg or autotune.default_batch_march(self.max_nx))
+        times = {}
+        for b in per_sm:
+            self.persistent_cfg = dict(base, blocks_per_sm=int(b))
+            try:
+                self.solve_persistent(epochs)
+            except _capi.OdilError:
+                continue
+            torch.cuda.synchronize(self.device)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for _ in range(reps):
+                self.solve_persistent(epochs)
+            e1.record()
+            e1.synchronize()
+            times[int(b)] = e0.elapsed_time(e1) / reps
+        best = min(times, key=times.get)
+        self.persistent_cfg = dict(base, blocks_per_sm=best)
+        return times
+
     def solve_persistent(self, epochs=2):
         """u <- the same mixed Newton as solve_mixed (bitwise), in ONE
         persistent launch: each block solves whole instances from the work
@@ -215,7 +240,8 @@ class WaveBatch:
         if epochs < 1:
             self.u.zero_()
             return self.u
-        cfg = self.march_cfg or autotune.default_batch_march(self.max_nx)
+        cfg = (getattr(self, "persistent_cfg", None) or self.march_cfg or
+               autotune.default_batch_march(self.max_nx))
         if epochs > 2 and getattr(self, "d2", None) is None:
             self.d2 = torch.zeros_like(self.d)
         call("odil_wave_batch_solve_mixed", ctypes.byref(self.b), int(epochs),
