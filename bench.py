@@ -416,7 +416,11 @@ def run_batch(dev, with_oracle, steps=5, hbm=6800.0):
     torch.cuda.synchronize(dev)
     ms_pers = statistics.mean(a.elapsed_time(c) for a, c in ts)
     same = bool(torch.equal(b.u, u_multi))
-    del u_multi
+    diff = (b.u - u_multi).abs()
+    pers_diff = {"max_abs": float(diff.max()),
+                 "entries_differing": int((diff > 0).sum()),
+                 "max_abs_multi": float(u_multi.abs().max())}
+    del u_multi, diff
     ms = min(ms_multi, ms_pers)
     u_newton = b.unpack()
     # Plain FP64 method, one instance after the other (BATCH_FP64_EPOCHS each).
@@ -499,7 +503,8 @@ def run_batch(dev, with_oracle, steps=5, hbm=6800.0):
            "persistent": {"ms_per_batch": ms_pers, "launches_per_batch": 1,
                           "blocks_per_sm_ms": pers_tune,
                           "value": len(insts) / (ms_pers / 1000.0),
-                          "bitwise_equal_to_multi_launch": same},
+                          "bitwise_equal_to_multi_launch": same,
+                          "difference_to_multi_launch": pers_diff},
            # kernels: rhs (interior + boundary), march, then per further
            # epoch rhs (2) + march, and the FP64 write.
            "multi_launch": {"ms_per_batch": ms_multi,

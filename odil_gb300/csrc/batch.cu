@@ -470,7 +470,8 @@ __global__ void __launch_bounds__(BLG_WARPS * 32, 5) batch_loss_grad_kernel(
     float* __restrict__ gi = grad + d.offset;
     // Narrow grids (nx < 3) have no interior column: general functions only.
     const bool gen = nx < 3;
-    const float gscale = (float)(2.0 / ((double)nt * (double)nx));
+    // 2 / N in FP32 (N = nt nx < 2^24 is exact): no FP64 division per item.
+    const float gscale = 2.f / ((float)nt * (float)nx);
     int off[V];
     float ctm[V], kxm1[V], kxp1[V];
     unsigned outm = 0, fixm = 0;
@@ -627,8 +628,11 @@ __global__ void __launch_bounds__(BLG_WARPS * 32, 5) batch_loss_grad_kernel(
         }
     }
     cp_async_wait<0>();
-    const double sw = warp_sum((double)lsum);
-    if (lane == 0) partials[item] = sw;
+    // The warp's 32 lane sums in FP32 (shuffles; GB300's FP64 pipe is
+    // narrow), the item's partial in FP64.
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, o);
+    if (lane == 0) partials[item] = (double)lsum;
 }
 
 // loss[i] = (sum of instance i's block sums) / N_i, one warp per instance

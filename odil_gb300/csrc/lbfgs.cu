@@ -286,11 +286,28 @@ __global__ void __launch_bounds__(LT) lbfgs_pair_dots_kernel(
     __syncthreads();
     if (!is_last) return;
     __threadfence();
-    __shared__ double tot[PD];
-    for (int j = 0; j < PD; ++j) {
-        const double v = sum_partials(ws.partials + j * nb, nb);
-        if (threadIdx.x == 0) tot[j] = v;
+    // All five sums in one pass over the block partials (fixed order).
+    double accp[PD];
+#pragma unroll
+    for (int j = 0; j < PD; ++j) accp[j] = 0.0;
+    for (int64_t q = threadIdx.x; q < nb; q += LT) {
+#pragma unroll
+        for (int j = 0; j < PD; ++j) accp[j] += __ldcg(ws.partials + j * nb + q);
     }
+#pragma unroll
+    for (int j = 0; j < PD; ++j) {
+        const double v = warp_sum(accp[j]);
+        if (lane == 0) red[warp][j] = v;
+    }
+    __syncthreads();
+    __shared__ double tot[PD];
+    if (threadIdx.x < PD) {
+        double v = 0.0;
+#pragma unroll
+        for (int w = 0; w < LT / 32; ++w) v += red[w][threadIdx.x];
+        tot[threadIdx.x] = v;
+    }
+    __syncthreads();
     if (threadIdx.x == 0) {
         if (mode == 0) {
             const double fa = ft[0], dpa = tot[0];

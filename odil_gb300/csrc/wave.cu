@@ -348,8 +348,10 @@ __device__ __forceinline__ T lg_vec_tile(const WaveDev<T>& g, const T* __restric
 // cover columns [30 V sw, 30 V (sw + 1)) and rows [TY ty, TY (ty + 1)).  The
 // tiles with 1 <= sw <= sw_hi and 1 <= ty <= ty_hi touch no boundary class
 // (interior kernel); the rest of the grid goes to the edge kernel in tiles of
-// LV_EDGE_TY rows, so that its short marches run in parallel.
+// min(TY, LV_EDGE_TY) rows, so that its short marches run in parallel.
 constexpr int LV_EDGE_TY = 16;
+
+__host__ __device__ constexpr int lv_edge_ty(int ty) { return ty < LV_EDGE_TY ? ty : LV_EDGE_TY; }
 
 struct LvGeom {
     int nsw;           // strips across
@@ -370,8 +372,9 @@ LvGeom lv_geom(int nt, int nx, int ty) {
     if (q.sw_hi < 1 || q.ty_hi < 1) q.sw_hi = q.ty_hi = 0;
     q.int_grid = dim3((q.sw_hi + LV_WARPS - 1) / LV_WARPS, q.ty_hi);
     q.n_int_blocks = (int64_t)q.int_grid.x * q.int_grid.y;
-    q.nte = (nt + LV_EDGE_TY - 1) / LV_EDGE_TY;
-    const int per = ty / LV_EDGE_TY;
+    const int ety = lv_edge_ty(ty);
+    q.nte = (nt + ety - 1) / ety;
+    const int per = ty / ety;
     if (q.ty_hi > 0) {
         q.lo = per;
         q.hi = (q.ty_hi + 1) * per - 1;
@@ -394,8 +397,9 @@ __global__ void __launch_bounds__(LV_WARPS * 32, 16) wave_loss_grad_all_kernel(
     double* loss, T gscale, double lscale) {
     static_assert(LV_WARPS == 2, "two boundary tiles per block");
     constexpr int V = Vec16<T>::n;
+    constexpr int ETY = lv_edge_ty(TY);
     __shared__ __align__(16) T ring_all[LV_WARPS][LV_RING][32 * V];
-    __shared__ T bcs_all[LV_WARPS][2 * (LV_EDGE_TY + 4)];
+    __shared__ T bcs_all[LV_WARPS][2 * (ETY + 4)];
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
     const int64_t neb = (q.n_edge + 1) / 2;  // boundary blocks
@@ -417,7 +421,7 @@ __global__ void __launch_bounds__(LV_WARPS * 32, 16) wave_loss_grad_all_kernel(
                 const int c = (int)(k - (int64_t)(ty - q.lo) * m);
                 sw = c == 0 ? 0 : q.sw_hi + c;
             }
-            lsum = lg_vec_tile<T, LV_EDGE_TY, false>(g, u, grad, ty * LV_EDGE_TY, sw * (30 * V),
+            lsum = lg_vec_tile<T, ETY, false>(g, u, grad, ty * ETY, sw * (30 * V),
                                                      lane, gscale, &ring_all[warp][0][0],
                                                      &bcs_all[warp][0]);
         }
@@ -451,7 +455,11 @@ LgPlan lg_plan(int nt, int nx, const void* u, const void* grad) {
              ((reinterpret_cast<uintptr_t>(u) | reinterpret_cast<uintptr_t>(grad)) % 16 == 0);
     if (pl.vec) {
         const int64_t cells = (int64_t)nt * nx;
-        pl.ty = cells >= (16 << 20) ? 64 : (cells >= (4 << 20) ? 32 : 16);
+        // Taller tiles on large grids (fewer halo rows), shorter ones on
+        // small grids so that enough warps run (a 1024^2 grid with 16-row
+        // tiles fills 5% of the warp slots).
+        pl.ty = cells >= (16 << 20) ? 64
+                                    : (cells >= (4 << 20) ? 32 : (cells >= (2 << 20) ? 16 : 8));
         pl.geom = lv_geom<T>(nt, nx, pl.ty);
         pl.grid = dim3(1, pl.geom.nte);
         pl.blocks = pl.geom.n_int_blocks + (pl.geom.n_edge + 1) / 2;
@@ -483,7 +491,9 @@ template <typename T>
 void lg_launch_scaled(const LgPlan& pl, const WaveDev<T>& g, const T* u, T* grad, ReduceWs ws,
                       double* loss, T gs, double ls, cudaStream_t s) {
     if (pl.vec) {
-        if (pl.ty == 16) {
+        if (pl.ty == 8) {
+            lv_launch<T, 8>(pl, g, u, grad, ws, loss, gs, ls, s);
+        } else if (pl.ty == 16) {
             lv_launch<T, 16>(pl, g, u, grad, ws, loss, gs, ls, s);
         } else if (pl.ty == 32) {
             lv_launch<T, 32>(pl, g, u, grad, ws, loss, gs, ls, s);
