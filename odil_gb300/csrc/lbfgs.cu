@@ -37,8 +37,9 @@ constexpr int kMaxM = 128;
 // so here both are matrix-vector products with no dependency chain: 256
 // threads stage the k x k block of R^-1 in pair order into shared memory
 // (row stride k | 1, all loads in flight), then one warp per pair forms
-// each entry (lanes over the other index, warp sums).  The product with
-// Y^T Y in between reads Y^T Y with four pairs' loads in flight per warp.
+// each entry (lanes over the other index, warp sums); each product is
+// refined once against R itself.  The product with Y^T Y in between reads
+// Y^T Y with four pairs' loads in flight per warp.
 constexpr int CT = 256;
 constexpr int CQ = kMaxM / 32;
 constexpr int CW = CT / 32;
@@ -54,7 +55,8 @@ __global__ void __launch_bounds__(CT) lbfgs_coef_kernel(int mcap, int gidx,
                                                         const double* __restrict__ sc,
                                                         double* __restrict__ coef) {
     extern __shared__ double Ri[];  // [k][coef_ld(k)], R^-1 in pair order
-    __shared__ double av[kMaxM], bv[kMaxM], t[kMaxM], w[kMaxM];
+    __shared__ double av[kMaxM], bv[kMaxM], t[kMaxM], w[kMaxM], pv[kMaxM], rs[kMaxM],
+        dt[kMaxM];
     __shared__ int slot[kMaxM];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int k = ring[0], head = ring[1], m = ring[2];
@@ -92,13 +94,48 @@ __global__ void __launch_bounds__(CT) lbfgs_coef_kernel(int mcap, int gidx,
         bv[c] = dg[2 * slot[c] + 1];
     }
     __syncthreads();
-    // t = R^-1 a: t_c = sum_{e >= c} Ri[c][e] a_e.
-    for (int c = warp; c < k; c += CW) {
-        double s = 0.0;
-        for (int e = c + lane; e < k; e += 32) s = fma(Ri[c * ld + e], av[e], s);
-        s = warp_sum(s);
-        if (lane == 0) t[c] = s;
-    }
+    // Products with R^-1 (staged, upper) and R (= S^T Y by slot, global).
+    // out_c = sum_{e >= c} Ri[c][e] v_e, or with TR sum_{e <= c} Ri[e][c] v_e.
+    auto ri_apply = [&](auto tr_tag, const double* v, double* out) {
+        constexpr bool TR = decltype(tr_tag)::value;
+        for (int c = warp; c < k; c += CW) {
+            double acc = 0.0;
+            if (TR) {
+                for (int e = lane; e <= c; e += 32) acc = fma(Ri[e * ld + c], v[e], acc);
+            } else {
+                for (int e = c + lane; e < k; e += 32) acc = fma(Ri[c * ld + e], v[e], acc);
+            }
+            acc = warp_sum(acc);
+            if (lane == 0) out[c] = acc;
+        }
+    };
+    // res_c = rhs_c - (R x)_c, or with TR rhs_c - (R^T x)_c.
+    auto r_residual = [&](auto tr_tag, const double* rhs, const double* xv, double* res) {
+        constexpr bool TR = decltype(tr_tag)::value;
+        for (int c = warp; c < k; c += CW) {
+            double acc = 0.0;
+            for (int e = lane; e < k; e += 32) {
+                const bool up = TR ? e <= c : e >= c;
+                if (up) {
+                    const double rv = TR ? SY[slot[e] * m + slot[c]] : SY[slot[c] * m + slot[e]];
+                    acc = fma(rv, xv[e], acc);
+                }
+            }
+            acc = warp_sum(acc);
+            if (lane == 0) res[c] = rhs[c] - acc;
+        }
+    };
+    // The kept R^-1 is applied once and refined once against R itself
+    // (x += R^-1 (rhs - R x)): the result is as accurate as a triangular
+    // solve, which an explicit inverse alone is not when R is ill-conditioned.
+    // t = R^-1 a.
+    ri_apply(std::false_type{}, av, t);
+    __syncthreads();
+    r_residual(std::false_type{}, av, t, rs);
+    __syncthreads();
+    ri_apply(std::false_type{}, rs, dt);
+    __syncthreads();
+    for (int c = tid; c < k; c += CT) t[c] += dt[c];
     __syncthreads();
     // w = (D + gamma Y^T Y) t - gamma b, D = diag(S^T Y).
     for (int cq = warp; cq < k; cq += 4 * CW) {
@@ -127,14 +164,16 @@ __global__ void __launch_bounds__(CT) lbfgs_coef_kernel(int mcap, int gidx,
         }
     }
     __syncthreads();
-    // p = R^-T w: p_c = sum_{e <= c} Ri[e][c] w_e; coef of s_c is -p_c, of
-    // y_c gamma t_c.
-    for (int c = warp; c < k; c += CW) {
-        double s = 0.0;
-        for (int e = lane; e <= c; e += 32) s = fma(Ri[e * ld + c], w[e], s);
-        s = warp_sum(s);
-        if (lane == 0 && 2 * slot[c] + 1 < gidx) {
-            coef[2 * slot[c]] = -s;
+    // p = R^-T w, refined the same way; coef of s_c is -p_c, of y_c gamma t_c.
+    ri_apply(std::true_type{}, w, pv);
+    __syncthreads();
+    r_residual(std::true_type{}, w, pv, rs);
+    __syncthreads();
+    ri_apply(std::true_type{}, rs, dt);
+    __syncthreads();
+    for (int c = tid; c < k; c += CT) {
+        if (2 * slot[c] + 1 < gidx) {
+            coef[2 * slot[c]] = -(pv[c] + dt[c]);
             coef[2 * slot[c] + 1] = gamma * t[c];
         }
     }
