@@ -731,9 +731,7 @@ int odil_lincomb_dot_f64(double* out, const double* x, const double* M,
  * side of optimizer.py:61-99, scipy's fmin_l_bfgs_b two-loop and line-search
  * driver; the state layout is documented in csrc/lbfgs.cu):
  *   coef: coef[0 .. gidx] of d = -H_k g = sum_{row < gidx} coef[row] H[row]
- *         + coef[gidx] g from the held pairs (compact representation), by
- *         products with Rinv = R^-1, R = triu(S^T Y), which update keeps
- *         (FP64 [m][m] by slot, caller-owned, no initial value needed);
+ *         + coef[gidx] g from the held pairs (compact representation);
  *   trial: xt = x + a d, a = 1 (or min(1, 1/|g|) with no pair held),
  *          phi'(0) = dots[0] recorded;
  *   accept: the Wolfe / approximate-Wolfe test of the trial -> sc[6];
@@ -746,8 +744,8 @@ int odil_lincomb_dot_f64(double* out, const double* x, const double* M,
  *           is guarded by the status, so an iteration can be enqueued, or
  *           captured in a CUDA graph, before the host reads it). */
 int odil_lbfgs_coef(int32_t m, int32_t gidx, const int* ring, const double* SY,
-                    const double* YY, const double* Rinv, const double* dg,
-                    const double* sc, double* coef, void* stream);
+                    const double* YY, const double* dg, const double* sc,
+                    double* coef, void* stream);
 int odil_lbfgs_trial_f32(int64_t n, float* xt, const float* x, const float* d,
                          const double* dots, const int* ring, double* sc,
                          void* stream);
@@ -778,8 +776,8 @@ int odil_lbfgs_pair_dots_f64(int64_t n, double* sy, const double* d,
                              const double* ft, int32_t mode, double* sc,
                              double* Q, void* workspace,
                              int64_t workspace_bytes, void* stream);
-int odil_lbfgs_update(int* ring, double* SY, double* YY, double* Rinv,
-                      double* dg, double* sc, const double* P, int32_t rows,
+int odil_lbfgs_update(int* ring, double* SY, double* YY, double* dg,
+                      double* sc, const double* P, int32_t rows,
                       const double* Q, void* stream);
 int odil_lbfgs_commit_f32(int64_t n, float* H, int64_t ld, const float* sy,
                           float* g, const float* gt, const int* ring,

@@ -223,7 +223,7 @@ SIGNATURES = {
     "odil_pcg_update_xr": (_INT, [_I64, _P, _P, _P, _P, _P, _P]),
     "odil_pcg_update_p": (_INT, [_I64, _P, _P, _P, _P]),
     "odil_lbfgs_coef": (_INT, [ctypes.c_int32, ctypes.c_int32, _P, _P, _P, _P,
-                               _P, _P, _P, _P]),
+                               _P, _P, _P]),
     "odil_lbfgs_trial_f32": (_INT, [_I64, _P, _P, _P, _P, _P, _P, _P]),
     "odil_lbfgs_trial_f64": (_INT, [_I64, _P, _P, _P, _P, _P, _P, _P]),
     "odil_lbfgs_accept": (_INT, [_P, _P, _P, _P]),
@@ -236,8 +236,8 @@ SIGNATURES = {
     "odil_lbfgs_pair_dots_f64": (_INT, [_I64, _P, _P, _P, _P, _P,
                                         ctypes.c_int32, _P, _P, _P, _I64,
                                         _P]),
-    "odil_lbfgs_update": (_INT, [_P, _P, _P, _P, _P, _P, _P, ctypes.c_int32,
-                                 _P, _P]),
+    "odil_lbfgs_update": (_INT, [_P, _P, _P, _P, _P, _P, ctypes.c_int32, _P,
+                                 _P]),
     "odil_lbfgs_commit_f32": (_INT, [_I64, _P, _I64, _P, _P, _P, _P, _P, _P]),
     "odil_lbfgs_commit_f64": (_INT, [_I64, _P, _I64, _P, _P, _P, _P, _P, _P]),
     "odil_wave_batch_loss_grad_items": (_I64, [_I64, _I64]),

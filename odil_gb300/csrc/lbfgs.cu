@@ -9,8 +9,6 @@
 //   ring  int32[4]: [0] k pairs held, [1] head (slot of the oldest pair),
 //         [2] m, [3] slot written by the last update (-1: none)
 //   SY, YY  FP64[m][m] by slot: SY[a][b] = s_a . y_b, YY[a][b] = y_a . y_b
-//   Rinv  FP64[m][m] by slot: R^-1, R = triu(S^T Y) in pair order (entries
-//         of held pairs a, b with a not newer than b; the rest unused)
 //   dg    FP64[2m]: dg[2 j] = s_j . g, dg[2 j + 1] = y_j . g at the iterate
 //   sc    FP64[16]: [0] f, [1] gamma, [2] phi'(0) = g . d, [3] trial step,
 //         [4] f at the trial, [5] phi'(step) = g_trial . d, [6] status
@@ -31,32 +29,71 @@ constexpr int kMaxM = 128;
 // coef[gidx + 1] of d = sum_{row < gidx} coef[row] H[row] + coef[gidx] g =
 // -H_k g; gidx (even, 2 <= gidx <= 2m) covers every held slot.
 //
-// With R = triu(S^T Y) in pair order, the compact form needs t = R^-1 a and
-// p = R^-T w.  The update kernel keeps R^-1 itself (Rinv, by slot: adding a
-// pair appends one column, evicting the oldest drops its row and column),
-// so here both are matrix-vector products with no dependency chain: 256
-// threads stage the k x k block of R^-1 in pair order into shared memory
-// (row stride k | 1, all loads in flight), then one warp per pair forms
-// each entry (lanes over the other index, warp sums); each product is
-// refined once against R itself.  The product with Y^T Y in between reads
-// Y^T Y with four pairs' loads in flight per warp.
+// The k x k block R = S^T Y of the held pairs, in pair order, is staged in
+// shared memory (row stride k | 1, odd, so the column reads of warp 0 spread
+// over the banks) by the whole block, each thread issuing all of its loads
+// before its stores.  The two triangular solves are right-looking on warp 0:
+// lane l keeps the running right-hand sides of pairs l, l + 32, l + 64,
+// l + 96 in registers; per pair the owner's value times the stored
+// reciprocal of the diagonal is shuffled to every lane, which subtracts its
+// multiple -- one shuffle and one multiply-add on the dependency chain per
+// pair instead of a warp reduction.  The product with Y^T Y in between is
+// spread over all warps.
 constexpr int CT = 256;
 constexpr int CQ = kMaxM / 32;
-constexpr int CW = CT / 32;
 
 __host__ __device__ __forceinline__ int coef_ld(int k) { return k | 1; }
+
+// x <- R^-1 x (kTrans = false, R upper) or R^-T x (kTrans = true) on one
+// warp; x[q] holds the entry of pair 32 q + lane.
+template <bool kTrans>
+__device__ __forceinline__ void coef_trsv(const double* __restrict__ R, int ld,
+                                          const double* __restrict__ rinv, int k, int lane,
+                                          double (&x)[CQ]) {
+    if (!kTrans) {
+        // Backward: pair r from k-1 down; rows c < r lose R[c][r] x[r].
+#pragma unroll
+        for (int qb = CQ - 1; qb >= 0; --qb) {
+            for (int rr = 31; rr >= 0; --rr) {
+                const int r = 32 * qb + rr;
+                if (r >= k) continue;
+                const double xr = __shfl_sync(0xffffffffu, x[qb], rr) * rinv[r];
+                if (lane == rr) x[qb] = xr;
+#pragma unroll
+                for (int q = 0; q <= qb; ++q) {
+                    const int c = 32 * q + lane;
+                    if (c < r) x[q] = fma(-R[c * ld + r], xr, x[q]);
+                }
+            }
+        }
+    } else {
+        // Forward with R^T: pair r from 0 up; rows c > r lose R[r][c] x[r].
+#pragma unroll
+        for (int qb = 0; qb < CQ; ++qb) {
+            for (int rr = 0; rr < 32; ++rr) {
+                const int r = 32 * qb + rr;
+                if (r >= k) break;
+                const double xr = __shfl_sync(0xffffffffu, x[qb], rr) * rinv[r];
+                if (lane == rr) x[qb] = xr;
+#pragma unroll
+                for (int q = qb; q < CQ; ++q) {
+                    const int c = 32 * q + lane;
+                    if (c > r && c < k) x[q] = fma(-R[r * ld + c], xr, x[q]);
+                }
+            }
+        }
+    }
+}
 
 __global__ void __launch_bounds__(CT) lbfgs_coef_kernel(int mcap, int gidx,
                                                         const int* __restrict__ ring,
                                                         const double* __restrict__ SY,
                                                         const double* __restrict__ YY,
-                                                        const double* __restrict__ Rinv,
                                                         const double* __restrict__ dg,
                                                         const double* __restrict__ sc,
                                                         double* __restrict__ coef) {
-    extern __shared__ double Ri[];  // [k][coef_ld(k)], R^-1 in pair order
-    __shared__ double av[kMaxM], bv[kMaxM], t[kMaxM], w[kMaxM], pv[kMaxM], rs[kMaxM],
-        dt[kMaxM];
+    extern __shared__ double Rs[];  // [k][coef_ld(k)], R in pair order
+    __shared__ double b[kMaxM], t[kMaxM], w[kMaxM], rinv[kMaxM];
     __shared__ int slot[kMaxM];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int k = ring[0], head = ring[1], m = ring[2];
@@ -79,65 +116,38 @@ __global__ void __launch_bounds__(CT) lbfgs_coef_kernel(int mcap, int gidx,
         for (int u = 0; u < 8; ++u) {
             const int e = e0 + u * CT;
             const int r = e / k, c = e - r * k;
-            // Upper triangle only (the rest of a slot's row may be stale).
-            v[u] = (e < k * k && c >= r) ? Rinv[slot[r] * m + slot[c]] : 0.0;
+            v[u] = e < k * k ? SY[slot[r] * m + slot[c]] : 0.0;
         }
 #pragma unroll
         for (int u = 0; u < 8; ++u) {
             const int e = e0 + u * CT;
             const int r = e / k, c = e - r * k;
-            if (e < k * k) Ri[r * ld + c] = v[u];
+            if (e < k * k) Rs[r * ld + c] = v[u];
         }
     }
-    for (int c = tid; c < k; c += CT) {
-        av[c] = dg[2 * slot[c]];
-        bv[c] = dg[2 * slot[c] + 1];
+    for (int c = tid; c < k; c += CT) b[c] = dg[2 * slot[c] + 1];
+    __syncthreads();
+    for (int c = tid; c < k; c += CT) rinv[c] = 1.0 / Rs[c * ld + c];
+    __syncthreads();
+    // t = R^-1 a, a = S^T g in pair order.
+    if (warp == 0) {
+        double x[CQ];
+#pragma unroll
+        for (int q = 0; q < CQ; ++q) {
+            const int c = 32 * q + lane;
+            x[q] = c < k ? dg[2 * slot[c]] : 0.0;
+        }
+        coef_trsv<false>(Rs, ld, rinv, k, lane, x);
+#pragma unroll
+        for (int q = 0; q < CQ; ++q) {
+            const int c = 32 * q + lane;
+            if (c < k) t[c] = x[q];
+        }
     }
     __syncthreads();
-    // Products with R^-1 (staged, upper) and R (= S^T Y by slot, global).
-    // out_c = sum_{e >= c} Ri[c][e] v_e, or with TR sum_{e <= c} Ri[e][c] v_e.
-    auto ri_apply = [&](auto tr_tag, const double* v, double* out) {
-        constexpr bool TR = decltype(tr_tag)::value;
-        for (int c = warp; c < k; c += CW) {
-            double acc = 0.0;
-            if (TR) {
-                for (int e = lane; e <= c; e += 32) acc = fma(Ri[e * ld + c], v[e], acc);
-            } else {
-                for (int e = c + lane; e < k; e += 32) acc = fma(Ri[c * ld + e], v[e], acc);
-            }
-            acc = warp_sum(acc);
-            if (lane == 0) out[c] = acc;
-        }
-    };
-    // res_c = rhs_c - (R x)_c, or with TR rhs_c - (R^T x)_c.
-    auto r_residual = [&](auto tr_tag, const double* rhs, const double* xv, double* res) {
-        constexpr bool TR = decltype(tr_tag)::value;
-        for (int c = warp; c < k; c += CW) {
-            double acc = 0.0;
-            for (int e = lane; e < k; e += 32) {
-                const bool up = TR ? e <= c : e >= c;
-                if (up) {
-                    const double rv = TR ? SY[slot[e] * m + slot[c]] : SY[slot[c] * m + slot[e]];
-                    acc = fma(rv, xv[e], acc);
-                }
-            }
-            acc = warp_sum(acc);
-            if (lane == 0) res[c] = rhs[c] - acc;
-        }
-    };
-    // The kept R^-1 is applied once and refined once against R itself
-    // (x += R^-1 (rhs - R x)): the result is as accurate as a triangular
-    // solve, which an explicit inverse alone is not when R is ill-conditioned.
-    // t = R^-1 a.
-    ri_apply(std::false_type{}, av, t);
-    __syncthreads();
-    r_residual(std::false_type{}, av, t, rs);
-    __syncthreads();
-    ri_apply(std::false_type{}, rs, dt);
-    __syncthreads();
-    for (int c = tid; c < k; c += CT) t[c] += dt[c];
-    __syncthreads();
-    // w = (D + gamma Y^T Y) t - gamma b, D = diag(S^T Y).
+    // w = (D + gamma Y^T Y) t - gamma b: one warp per pair c, lanes over e,
+    // four pairs per warp with all their loads in flight together.
+    constexpr int CW = CT / 32;
     for (int cq = warp; cq < k; cq += 4 * CW) {
         double v[4][CQ];
 #pragma unroll
@@ -159,25 +169,29 @@ __global__ void __launch_bounds__(CT) lbfgs_coef_kernel(int mcap, int gidx,
                 if (e < k) s = fma(v[i][q], t[e], s);
             }
             s = warp_sum(s);
-            if (lane == 0 && c < k)
-                w[c] = SY[slot[c] * m + slot[c]] * t[c] + gamma * s - gamma * bv[c];
+            if (lane == 0 && c < k) w[c] = Rs[c * ld + c] * t[c] + gamma * s - gamma * b[c];
         }
     }
     __syncthreads();
-    // p = R^-T w, refined the same way; coef of s_c is -p_c, of y_c gamma t_c.
-    ri_apply(std::true_type{}, w, pv);
-    __syncthreads();
-    r_residual(std::true_type{}, w, pv, rs);
-    __syncthreads();
-    ri_apply(std::true_type{}, rs, dt);
-    __syncthreads();
-    for (int c = tid; c < k; c += CT) {
-        if (2 * slot[c] + 1 < gidx) {
-            coef[2 * slot[c]] = -(pv[c] + dt[c]);
-            coef[2 * slot[c] + 1] = gamma * t[c];
+    // p = R^-T w; coef of s_c is -p_c, of y_c gamma t_c.
+    if (warp == 0) {
+        double x[CQ];
+#pragma unroll
+        for (int q = 0; q < CQ; ++q) {
+            const int c = 32 * q + lane;
+            x[q] = c < k ? w[c] : 0.0;
         }
+        coef_trsv<true>(Rs, ld, rinv, k, lane, x);
+#pragma unroll
+        for (int q = 0; q < CQ; ++q) {
+            const int c = 32 * q + lane;
+            if (c < k && 2 * slot[c] + 1 < gidx) {
+                coef[2 * slot[c]] = -x[q];
+                coef[2 * slot[c] + 1] = gamma * t[c];
+            }
+        }
+        if (lane == 0) coef[gidx] = -gamma;
     }
-    if (tid == 0) coef[gidx] = -gamma;
 }
 
 // Dynamic shared memory of lbfgs_coef_kernel for up to m held pairs.
@@ -368,22 +382,22 @@ __global__ void __launch_bounds__(LT) lbfgs_pair_dots_kernel(
 // stored rows with (g_trial, s, y); Q: [2][2] = [[s.y, s.g_trial],
 // [y.y, y.g_trial]].  The pair is kept when s.y > 1e-12 y.y (the curvature
 // condition, as the host version); the dots with g_trial become dg.
-__global__ void __launch_bounds__(CT) lbfgs_update_kernel(int* __restrict__ ring,
+__global__ void __launch_bounds__(32) lbfgs_update_kernel(int* __restrict__ ring,
                                                           double* __restrict__ SY,
                                                           double* __restrict__ YY,
-                                                          double* __restrict__ Rinv,
                                                           double* __restrict__ dg,
                                                           double* __restrict__ sc,
                                                           const double* __restrict__ P, int rows,
                                                           const double* __restrict__ Q) {
     __shared__ int s_slot;
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int lane = threadIdx.x;
     if (sc[6] != 0.0) return;
     const int k = ring[0], head = ring[1], m = ring[2];
     const double sy = Q[0], sgt = Q[1], yy = Q[2], ygt = Q[3];
     // dots of the held pairs with the new gradient
-    for (int r = tid; r < 2 * m; r += CT) dg[r] = r < rows ? P[r * 3] : 0.0;
-    if (tid == 0) {
+    for (int r = lane; r < 2 * m; r += 32) dg[r] = r < rows ? P[r * 3] : 0.0;
+    __syncwarp();
+    if (lane == 0) {
         s_slot = -1;
         if (isfinite(sy) && isfinite(yy) && sy > 1e-12 * yy) {
             int slot;
@@ -400,11 +414,11 @@ __global__ void __launch_bounds__(CT) lbfgs_update_kernel(int* __restrict__ ring
         ring[3] = s_slot;
         sc[0] = sc[4];
     }
-    __syncthreads();
+    __syncwarp();
     const int slot = s_slot;
     if (slot < 0) return;
-    const int k2 = ring[0], head2 = ring[1];  // the new pair is the last (order k2 - 1)
-    for (int c = tid; c < k2; c += CT) {
+    const int k2 = ring[0], head2 = ring[1];
+    for (int c = lane; c < k2; c += 32) {
         const int j = (head2 + c) % m;
         if (j == slot) continue;
         SY[slot * m + j] = P[(2 * j + 1) * 3 + 1];  // s_new . y_j
@@ -412,29 +426,12 @@ __global__ void __launch_bounds__(CT) lbfgs_update_kernel(int* __restrict__ ring
         const double v = P[(2 * j + 1) * 3 + 2];    // y_j . y_new
         YY[slot * m + j] = v;
         YY[j * m + slot] = v;
-        Rinv[slot * m + j] = 0.0;                   // the new row: older pairs
     }
-    if (tid == 0) {
+    if (lane == 0) {
         SY[slot * m + slot] = sy;
         YY[slot * m + slot] = yy;
         dg[2 * slot] = sgt;
         dg[2 * slot + 1] = ygt;
-        Rinv[slot * m + slot] = 1.0 / sy;
-    }
-    // The new column of R^-1: R_new = [[R, r], [0, rho]] with r_b = s_b . y_new
-    // and rho = s_new . y_new, so column new of R_new^-1 is -R^-1 r / rho
-    // over the older pairs; one warp per older pair a (in pair order),
-    // lanes over the pairs b >= a.
-    const double irho = 1.0 / sy;
-    for (int a = warp; a < k2 - 1; a += CW) {
-        const int sa = (head2 + a) % m;
-        double acc = 0.0;
-        for (int bo = a + lane; bo < k2 - 1; bo += 32) {
-            const int sb = (head2 + bo) % m;
-            acc = fma(Rinv[sa * m + sb], P[(2 * sb) * 3 + 2], acc);
-        }
-        acc = warp_sum(acc);
-        if (lane == 0) Rinv[sa * m + slot] = -acc * irho;
     }
 }
 
@@ -522,18 +519,17 @@ int commit_impl(int64_t n, T* H, int64_t ld, const T* sy, T* g, const T* gt, con
 using namespace odil;
 
 ODIL_API int odil_lbfgs_coef(int32_t m, int32_t gidx, const int* ring, const double* SY,
-                             const double* YY, const double* Rinv, const double* dg,
-                             const double* sc, double* coef, void* stream) {
+                             const double* YY, const double* dg, const double* sc, double* coef,
+                             void* stream) {
     if (m < 1 || m > kMaxM || gidx < 2 || gidx > 2 * m || gidx % 2) return ODIL_ERR_SHAPE;
-    if (!ring || !SY || !YY || !Rinv || !dg || !sc || !coef) return ODIL_ERR_ARG;
+    if (!ring || !SY || !YY || !dg || !sc || !coef) return ODIL_ERR_ARG;
     const size_t smem = coef_smem(m);
     if (smem > 48 * 1024) {
         const cudaError_t e = cudaFuncSetAttribute(
             lbfgs_coef_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return ODIL_ERR_LAUNCH;
     }
-    lbfgs_coef_kernel<<<1, CT, smem, as_stream(stream)>>>(m, gidx, ring, SY, YY, Rinv, dg, sc,
-                                                          coef);
+    lbfgs_coef_kernel<<<1, CT, smem, as_stream(stream)>>>(m, gidx, ring, SY, YY, dg, sc, coef);
     return launch_status();
 }
 
@@ -580,13 +576,11 @@ ODIL_API int odil_lbfgs_pair_dots_f64(int64_t n, double* sy, const double* d, co
                                   stream);
 }
 
-ODIL_API int odil_lbfgs_update(int* ring, double* SY, double* YY, double* Rinv, double* dg,
-                               double* sc, const double* P, int32_t rows, const double* Q,
-                               void* stream) {
+ODIL_API int odil_lbfgs_update(int* ring, double* SY, double* YY, double* dg, double* sc,
+                               const double* P, int32_t rows, const double* Q, void* stream) {
     if (rows < 0) return ODIL_ERR_SHAPE;
-    if (!ring || !SY || !YY || !Rinv || !dg || !sc || !Q || (rows > 0 && !P))
-        return ODIL_ERR_ARG;
-    lbfgs_update_kernel<<<1, CT, 0, as_stream(stream)>>>(ring, SY, YY, Rinv, dg, sc, P, rows, Q);
+    if (!ring || !SY || !YY || !dg || !sc || !Q || (rows > 0 && !P)) return ODIL_ERR_ARG;
+    lbfgs_update_kernel<<<1, 32, 0, as_stream(stream)>>>(ring, SY, YY, dg, sc, P, rows, Q);
     return launch_status();
 }
 

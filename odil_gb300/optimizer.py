@@ -102,10 +102,8 @@ class LbfgsOptimizer(Optimizer):
 
     def run_device(self, x0, loss_grad, epochs=None, callback=None,
                    epoch_start=0):
-        """The same iteration with the compact-form algebra (R^-1 of the
-        compact form kept up to date per pair instead of two triangular
-        solves per iteration), the first trial step, its Wolfe test and the
-        pair/ring update on the device
+        """The same iteration with the compact-form algebra, the first trial
+        step, its Wolfe test and the pair/ring update on the device
         (csrc/lbfgs.cu): per iteration one direction (coefficient kernel +
         one linear combination that also gives g . d), the trial point, one
         loss+gradient there, one pass forming the new pair with its dots and
@@ -147,7 +145,6 @@ class LbfgsOptimizer(Optimizer):
         ring = torch.tensor([0, 0, m, -1], dtype=torch.int32, device=dev)
         SY = torch.zeros((m, m), dtype=torch.float64, device=dev)
         YY = torch.zeros((m, m), dtype=torch.float64, device=dev)
-        Rinv = torch.zeros((m, m), dtype=torch.float64, device=dev)
         dg = torch.zeros(2 * m, dtype=torch.float64, device=dev)
         sc = torch.zeros(16, dtype=torch.float64, device=dev)
         sc_host = torch.zeros(16, dtype=torch.float64).pin_memory()
@@ -178,7 +175,7 @@ class LbfgsOptimizer(Optimizer):
             st = stream_handle()
             if rows:
                 call("odil_lbfgs_coef", m, rows, ptr(ring), ptr(SY), ptr(YY),
-                     ptr(Rinv), ptr(dg), ptr(sc), ptr(coef), st)
+                     ptr(dg), ptr(sc), ptr(coef), st)
                 call("odil_lincomb_dot_" + sfx, ptr(d), ptr(g), ptr(H), n, rows,
                      ptr(coef), n, ptr(dots), ptr(lc_ws), lc_ws.numel(), st)
                 gd = dots
@@ -198,8 +195,8 @@ class LbfgsOptimizer(Optimizer):
             update, commit with g <- g_trial (guarded by the status)."""
             st = stream_handle()
             P = md(H, max(rows, 1), [gt, SYp[0], SYp[1]]) if rows else None
-            call("odil_lbfgs_update", ptr(ring), ptr(SY), ptr(YY), ptr(Rinv),
-                 ptr(dg), ptr(sc), ptr(P), rows, ptr(Q), st)
+            call("odil_lbfgs_update", ptr(ring), ptr(SY), ptr(YY), ptr(dg),
+                 ptr(sc), ptr(P), rows, ptr(Q), st)
             call("odil_lbfgs_commit_" + sfx, n, ptr(H), n, ptr(SYp), ptr(g),
                  ptr(gt), ptr(ring), ptr(sc), st)
 
