@@ -201,16 +201,6 @@ int odil_wave_march_tiled_f32(const odil_wave_params* p, const float* b,
 int odil_wave_march_tiled_f64(const odil_wave_params* p, const double* b,
                               double* x, int32_t cpt, int32_t halo, int32_t pf,
                               int32_t warps, int32_t exchange, void* stream);
-/* odil_wave_march_tiled_f32 (exchange 0) on rows [r0, r1) only: r0 a
- * multiple of halo, r1 <= nt; the march starts from rows r0 - 1 and r0 - 2
- * of x, which an earlier call wrote.  Consecutive calls over [0, r1), [r1,
- * r2), ... give bitwise the solution of one call over [0, nt), and the rows
- * already solved can be used while the next ones are marched.
- * The direct solve of linsolver.py:35-45, as odil_wave_march_f32. */
-int odil_wave_march_tiled_rows_f32(const odil_wave_params* p, const float* b,
-                                   float* x, int32_t r0, int32_t r1,
-                                   int32_t cpt, int32_t halo, int32_t pf,
-                                   int32_t warps, void* stream);
 /* Test hook of the bounded halo wait: odil_wave_march_tiled_f32 with
  * exchange 1 whose every wait expects `missing_bytes` (1..65536) more than
  * ever arrive, so each wait gives up after its limit. */

@@ -171,8 +171,6 @@ SIGNATURES = {
                                   + [_P]),
     "odil_wave_march_tiled_f64": (_INT, [_P, _P, _P] + [ctypes.c_int32] * 5
                                   + [_P]),
-    "odil_wave_march_tiled_rows_f32": (_INT, [_P, _P, _P] + [ctypes.c_int32] * 6
-                                       + [_P]),
     "odil_wave_march_tiled_planted_wait_f32": (_INT, [_P, _P, _P]
                                                + [ctypes.c_int32] * 5 + [_P]),
     "odil_wave_march_tiled_wait_failures": (_INT, [_P, ctypes.c_int32]),

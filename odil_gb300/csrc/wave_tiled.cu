@@ -182,15 +182,9 @@ __device__ __forceinline__ void cluster_sync_all() {
 // only wait for their neighbours, and the solution stores need no fence.
 // `extra_wait` adds bytes that never arrive to every wait (a planted
 // failure for the bounded-wait test; 0 otherwise).
-//
-// Rows [r0, r1) only (r0 a multiple of H; cluster-barrier exchange): the
-// march starts from rows r0-1 and r0-2 of x, which an earlier launch wrote,
-// so a solve can run as several launches and the rows already solved can be
-// used (converted, copied to the host) while the next ones are marched.
 template <typename T, int CPT, int H, int PF, bool VEC, bool DSMEM>
 __global__ void __launch_bounds__(32 * kTiledMaxWarps) wave_march_tiled_kernel(
-    WaveDev<T> g, const T* __restrict__ b, T* __restrict__ x, uint32_t extra_wait, int r0,
-    int r1) {
+    WaveDev<T> g, const T* __restrict__ b, T* __restrict__ x, uint32_t extra_wait) {
     constexpr int O = 32 * CPT - 2 * H;  // owned columns per warp
     static_assert(O > 0 && H % CPT == 0 && H % PF == 0, "tile shape");
     static_assert(!DSMEM || O >= H, "pushed columns come from one neighbour");
@@ -225,10 +219,10 @@ __global__ void __launch_bounds__(32 * kTiledMaxWarps) wave_march_tiled_kernel(
     // previous kernel's output.
     pdl_trigger();
     pdl_wait();
-    const T* src = b + (int64_t)r0 * nx + j0;  // row `next` of the right-hand side
-    int next = r0;
+    const T* src = b + j0;  // row `next` of the right-hand side
+    int next = 0;
     auto issue = [&](auto checked, int slot) {
-        if (!decltype(checked)::value || next < r1) {
+        if (!decltype(checked)::value || next < nt) {
             if constexpr (VEC) {
                 if (any_in) ld_cols<T, CPT>(pre[slot], src);
             } else {
@@ -241,14 +235,7 @@ __global__ void __launch_bounds__(32 * kTiledMaxWarps) wave_march_tiled_kernel(
     };
 #pragma unroll
     for (int q = 0; q < PF - 1; ++q) issue(std::true_type{}, q);
-    T* dst = x + (int64_t)r0 * nx + j0;  // solution row i
-    if (r0 > 0) {  // rows r0 - 1, r0 - 2 from the launch before
-#pragma unroll
-        for (int c = 0; c < CPT; ++c) {
-            d1[c] = in[c] ? __ldcg(x + (int64_t)(r0 - 1) * nx + j0 + c) : T(0);
-            d2[c] = (in[c] && r0 >= 2) ? __ldcg(x + (int64_t)(r0 - 2) * nx + j0 + c) : T(0);
-        }
-    }
+    T* dst = x + j0;  // solution row i
     // One row: FIRST for rows 0 and 1 of J (identity row; no u[i-2] term),
     // CHECKED where the prefetch may pass the last row.
     auto row = [&](auto first, auto checked, int i, int s) {
@@ -328,8 +315,8 @@ __global__ void __launch_bounds__(32 * kTiledMaxWarps) wave_march_tiled_kernel(
                                 (has_r ? 1u : 0u) * 2 * H * sizeof(T) + extra_wait;
     // Byte offset between the parity-1 and parity-0 copies of halo / mbar.
     constexpr uint32_t kHaloPar = 2 * 2 * (DSMEM ? H : 1) * sizeof(T);
-    for (int i0 = r0; i0 < r1 && (!DSMEM || active); i0 += H) {
-        if (i0 > r0) {
+    for (int i0 = 0; i0 < nt && (!DSMEM || active); i0 += H) {
+        if (i0 > 0) {
             if constexpr (DSMEM) {
                 const int k = i0 / H;
                 const int par = k & 1;
@@ -372,7 +359,7 @@ __global__ void __launch_bounds__(32 * kTiledMaxWarps) wave_march_tiled_kernel(
                 }
             }
         }
-        if (i0 + H + PF <= r1) {  // no row or prefetch past the end
+        if (i0 + H + PF <= nt) {  // no row or prefetch past the end
             int h = 0;
             if (i0 == 0) {
 #pragma unroll
@@ -389,7 +376,7 @@ __global__ void __launch_bounds__(32 * kTiledMaxWarps) wave_march_tiled_kernel(
 #pragma unroll
                 for (int s = 0; s < PF; ++s) {
                     const int i = i0 + h + s;
-                    if (i >= r1) break;  // uniform over the grid
+                    if (i >= nt) break;  // uniform over the grid
                     if (i < 2) {
                         row(std::true_type{}, std::true_type{}, i, s);
                     } else {
@@ -400,7 +387,7 @@ __global__ void __launch_bounds__(32 * kTiledMaxWarps) wave_march_tiled_kernel(
         }
         if constexpr (DSMEM) {
             // Rows i0+H-2 (d2) and i0+H-1 (d1) for the neighbours' next batch.
-            if (push_addr != 0 && i0 + H < r1) {
+            if (push_addr != 0 && i0 + H < nt) {
                 const uint32_t par = (uint32_t)((i0 / H + 1) & 1);
                 const uint32_t a = push_addr + par * kHaloPar;
                 const uint32_t m = push_mbar + par * 8u;
@@ -414,7 +401,7 @@ __global__ void __launch_bounds__(32 * kTiledMaxWarps) wave_march_tiled_kernel(
 
 template <typename T>
 int tiled_launch(const void* kern, int clusters, int warps, const WaveDev<T>& g, const T* b,
-                 T* x, uint32_t extra_wait, int r0, int r1, cudaStream_t st) {
+                 T* x, uint32_t extra_wait, cudaStream_t st) {
     static thread_local const void* checked[64];
     static thread_local int nchecked = 0;
     bool seen = false;
@@ -457,7 +444,7 @@ int tiled_launch(const void* kern, int clusters, int warps, const WaveDev<T>& g,
         if (nfits < 64) fits[nfits++] = {kern, clusters, warps, ok};
     }
     if (!ok) return ODIL_ERR_SHAPE;
-    void* args[] = {const_cast<WaveDev<T>*>(&g), &b, &x, &extra_wait, &r0, &r1};
+    void* args[] = {const_cast<WaveDev<T>*>(&g), &b, &x, &extra_wait};
     cfg.numAttrs = 2;  // the occupancy query above saw the cluster only
     if (cudaLaunchKernelExC(&cfg, kern, args) != cudaSuccess) {
         cudaGetLastError();
@@ -468,7 +455,7 @@ int tiled_launch(const void* kern, int clusters, int warps, const WaveDev<T>& g,
 
 template <typename T, int CPT, int H, int PF, bool DSMEM>
 int tiled_shape_fit(const WaveDev<T>& g, const T* b, T* x, int warps, uint32_t extra_wait,
-                    int r0, int r1, cudaStream_t st) {
+                    cudaStream_t st) {
     constexpr int O = 32 * CPT - 2 * H;
     const int64_t tiles = (g.nx + O - 1) / O;
     if (warps < 1 || warps > kTiledMaxWarps) return ODIL_ERR_SHAPE;
@@ -481,18 +468,17 @@ int tiled_shape_fit(const WaveDev<T>& g, const T* b, T* x, int warps, uint32_t e
     const void* kern =
         vec ? reinterpret_cast<const void*>(wave_march_tiled_kernel<T, CPT, H, PF, true, DSMEM>)
             : reinterpret_cast<const void*>(wave_march_tiled_kernel<T, CPT, H, PF, false, DSMEM>);
-    if (r0 < 0 || r1 > g.nt || r0 >= r1 || r0 % H != 0 || (DSMEM && r0 != 0)) return ODIL_ERR_SHAPE;
-    return tiled_launch<T>(kern, (int)clusters, warps, g, b, x, extra_wait, r0, r1, st);
+    return tiled_launch<T>(kern, (int)clusters, warps, g, b, x, extra_wait, st);
 }
 
 template <typename T, int CPT, int H, int PF, bool DSMEM>
-int tiled_shape(const WaveDev<T>& g, const T* b, T* x, int warps, uint32_t extra_wait, int r0,
-                int r1, cudaStream_t st) {
+int tiled_shape(const WaveDev<T>& g, const T* b, T* x, int warps, uint32_t extra_wait,
+                cudaStream_t st) {
     // A ring above 512 bytes per thread spills (FP64 with cpt pf > 64).
     if constexpr (CPT * PF * sizeof(T) > 512) {
         return ODIL_ERR_SHAPE;
     } else {
-        return tiled_shape_fit<T, CPT, H, PF, DSMEM>(g, b, x, warps, extra_wait, r0, r1, st);
+        return tiled_shape_fit<T, CPT, H, PF, DSMEM>(g, b, x, warps, extra_wait, st);
     }
 }
 
@@ -501,8 +487,7 @@ int tiled_shape(const WaveDev<T>& g, const T* b, T* x, int warps, uint32_t extra
 // neighbours' shared memory, needs 32 cpt - 2 halo >= halo).
 template <typename T>
 int tiled_dispatch(const odil_wave_params* p, const T* b, T* x, int cpt, int halo, int pf,
-                   int warps, int exchange, uint32_t extra_wait, void* stream, int r0 = 0,
-                   int r1 = -1) {
+                   int warps, int exchange, uint32_t extra_wait, void* stream) {
     WaveDev<T> g;
     int st = make_dev<T>(p, &g, false);
     if (st) return st;
@@ -513,18 +498,17 @@ int tiled_dispatch(const odil_wave_params* p, const T* b, T* x, int cpt, int hal
         return ODIL_ERR_SHAPE;
     cudaStream_t s = as_stream(stream);
     const uint32_t e = extra_wait;
-    if (r1 < 0) r1 = g.nt;
     switch (exchange * 1000000 + cpt * 10000 + halo * 100 + pf) {
-        case 43216: return tiled_shape<T, 4, 32, 16, false>(g, b, x, warps, e, r0, r1, s);
-        case 44816: return tiled_shape<T, 4, 48, 16, false>(g, b, x, warps, e, r0, r1, s);
-        case 89616: return tiled_shape<T, 8, 96, 16, false>(g, b, x, warps, e, r0, r1, s);
-        case 1021616: return tiled_shape<T, 2, 16, 16, true>(g, b, x, warps, e, r0, r1, s);
-        case 1040808: return tiled_shape<T, 4, 8, 8, true>(g, b, x, warps, e, r0, r1, s);
-        case 1041616: return tiled_shape<T, 4, 16, 16, true>(g, b, x, warps, e, r0, r1, s);
-        case 1042408: return tiled_shape<T, 4, 24, 8, true>(g, b, x, warps, e, r0, r1, s);
-        case 1043216: return tiled_shape<T, 4, 32, 16, true>(g, b, x, warps, e, r0, r1, s);
-        case 1083216: return tiled_shape<T, 8, 32, 16, true>(g, b, x, warps, e, r0, r1, s);
-        case 1086416: return tiled_shape<T, 8, 64, 16, true>(g, b, x, warps, e, r0, r1, s);
+        case 43216: return tiled_shape<T, 4, 32, 16, false>(g, b, x, warps, e, s);
+        case 44816: return tiled_shape<T, 4, 48, 16, false>(g, b, x, warps, e, s);
+        case 89616: return tiled_shape<T, 8, 96, 16, false>(g, b, x, warps, e, s);
+        case 1021616: return tiled_shape<T, 2, 16, 16, true>(g, b, x, warps, e, s);
+        case 1040808: return tiled_shape<T, 4, 8, 8, true>(g, b, x, warps, e, s);
+        case 1041616: return tiled_shape<T, 4, 16, 16, true>(g, b, x, warps, e, s);
+        case 1042408: return tiled_shape<T, 4, 24, 8, true>(g, b, x, warps, e, s);
+        case 1043216: return tiled_shape<T, 4, 32, 16, true>(g, b, x, warps, e, s);
+        case 1083216: return tiled_shape<T, 8, 32, 16, true>(g, b, x, warps, e, s);
+        case 1086416: return tiled_shape<T, 8, 64, 16, true>(g, b, x, warps, e, s);
         default: return ODIL_ERR_SHAPE;
     }
 }
@@ -544,12 +528,6 @@ ODIL_API int odil_wave_march_tiled_f64(const odil_wave_params* p, const double* 
                                        int32_t cpt, int32_t halo, int32_t pf, int32_t warps,
                                        int32_t exchange, void* stream) {
     return tiled_dispatch<double>(p, b, x, cpt, halo, pf, warps, exchange, 0u, stream);
-}
-
-ODIL_API int odil_wave_march_tiled_rows_f32(const odil_wave_params* p, const float* b, float* x,
-                                            int32_t r0, int32_t r1, int32_t cpt, int32_t halo,
-                                            int32_t pf, int32_t warps, void* stream) {
-    return tiled_dispatch<float>(p, b, x, cpt, halo, pf, warps, 0, 0u, stream, r0, r1);
 }
 
 ODIL_API int odil_wave_march_tiled_planted_wait_f32(const odil_wave_params* p, const float* b,

@@ -77,9 +77,6 @@ def solve(problem, state, precision="mixed", epochs=None, rnorm2=None,
         rhs = _scratch(k, "rhs32", torch.float32)
         d = _scratch(k, "d32", torch.float32)
         if from_zero and epochs > 0:
-            if (epochs == 1 and host_out is not None and rnorm2 is None and
-                    _solve_one_streamed(k, u, rhs, host_out)):
-                return u
             _solve_pairs(k, u, rhs, d, epochs, rnorm2)
             if host_out is not None:
                 host_out.copy_(u, non_blocking=True)
@@ -115,53 +112,6 @@ def solve(problem, state, precision="mixed", epochs=None, rnorm2=None,
     if host_out is not None:
         host_out.copy_(u, non_blocking=True)
     return u
-
-
-# Row chunks of the pipelined one-epoch solve with a host output.
-STREAM_CHUNKS = 4
-
-
-def _solve_one_streamed(k, u, rhs, host_out, chunks=STREAM_CHUNKS):
-    """One mixed epoch from u = 0 whose solution also goes to pinned host
-    memory, with the device-to-host copy overlapped with the march: the
-    march runs as `chunks` launches over consecutive row ranges (bitwise the
-    one-launch solution), and after each one a side stream writes those
-    rows in FP64 and copies them to host_out while the next rows are
-    marched.  The march occupies one thread-block cluster and is
-    latency-bound, so the FP64 pass runs on other SMs and the copy on a copy
-    engine.  Returns False (nothing launched) where the tuned march shape
-    has no row-range form."""
-    if not hasattr(k, "march_rows"):
-        return False
-    cfg = k.march_tuned_cfg(torch.float32)
-    if (not cfg or cfg.get("kind") != "tiled" or
-            int(cfg.get("exchange", 0)) != 0):
-        return False
-    hi = _scratch(k, "hi32", torch.float32)
-    nt, nx = u.shape
-    halo = int(cfg["halo"])
-    nbatch = -(-nt // halo)
-    per = -(-nbatch // max(1, chunks))
-    bounds = sorted({min(nt, c * per * halo) for c in range(chunks + 1)})
-    main = torch.cuda.current_stream(u.device)
-    side = getattr(k, "_copy_stream", None)
-    if side is None:
-        side = k._copy_stream = torch.cuda.Stream(u.device)
-    k.initial_rhs(rhs)
-    side.wait_stream(main)
-    hv, uv = hi.view(-1), u.view(-1)
-    for r0, r1 in zip(bounds[:-1], bounds[1:]):
-        k.march_rows(rhs, hi, r0, r1)
-        done = torch.cuda.Event()
-        done.record(main)
-        side.wait_event(done)
-        with torch.cuda.stream(side):
-            a, b = r0 * nx, r1 * nx
-            call("odil_pair_to_f64", ptr(hv[a:b]), None, ptr(uv[a:b]), b - a,
-                 stream_handle())
-            host_out[r0:r1].copy_(u[r0:r1], non_blocking=True)
-    main.wait_stream(side)
-    return True
 
 
 def _solve_pairs(k, u, rhs, d, epochs, rnorm2):

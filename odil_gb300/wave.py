@@ -223,33 +223,11 @@ class WaveKernels:
     def march_tuned(self, b, out):
         """Forward substitution with the autotuned launch shape for b's
         precision (FP32 or FP64)."""
-        return self.march_shape(b, out, self.march_tuned_cfg(b.dtype))
-
-    def march_rows(self, b, x, r0, r1):
-        """Rows [r0, r1) of the tuned FP32 forward substitution x = J^{-1} b,
-        starting from rows r0-1, r0-2 of x (written by an earlier call);
-        returns the halo depth (row boundaries must be multiples of it), or
-        None, with nothing launched, when the tuned shape is not a
-        cluster-barrier tiled one."""
-        if b.dtype != torch.float32:
-            raise TypeError("FP32 right-hand side expected")
-        cfg = self.march_tuned_cfg(torch.float32)
-        if (not cfg or cfg.get("kind") != "tiled" or
-                int(cfg.get("exchange", 0)) != 0):
-            return None
-        self._check(b)
-        call("odil_wave_march_tiled_rows_f32", ctypes.byref(self.p32), ptr(b),
-             ptr(x), int(r0), int(r1), int(cfg["cpt"]), int(cfg["halo"]),
-             int(cfg["pf"]), int(cfg["warps"]), stream_handle())
-        return int(cfg["halo"])
-
-    def march_tuned_cfg(self, dtype):
-        """The autotuned march launch shape for dtype (tuned on first use)."""
         tuned = self.__dict__.setdefault("_march_cfgs", {})
-        if dtype not in tuned:
+        if b.dtype not in tuned:
             from . import autotune
-            tuned[dtype] = autotune.tune_march(self, dtype=dtype)
-        return tuned[dtype]
+            tuned[b.dtype] = autotune.tune_march(self, dtype=b.dtype)
+        return self.march_shape(b, out, tuned[b.dtype])
 
     def initial_rhs(self, rhs):
         """rhs = float32(-F(0)) (boundary cells only do FP64 work)."""

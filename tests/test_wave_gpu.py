@@ -569,48 +569,3 @@ def test_jtj_v_and_diag(cuda, shape):
     dref = (Jd**2).sum(0).reshape(shape)
     assert _rel(k.jtj_diag().cpu().numpy(), dref) < 1e-14
     assert _rel(k.jtj_diag(torch.float32).cpu().numpy(), dref) < 1e-6
-
-
-@pytest.mark.parametrize("n", [1024, 300])
-def test_streamed_solve_with_host_output_equals_plain(cuda, n):
-    """One mixed epoch from zero with a pinned host output: the march runs
-    in row chunks with the FP64 write and device-to-host copy of each chunk
-    overlapped with the next; the device state and the host copy equal the
-    one-launch solve bitwise, eagerly and replayed from a CUDA graph; the
-    chunked march equals the one-launch march bitwise."""
-    from odil_gb300 import newton
-    from odil_gb300.domain import State
-    from odil_gb300.problem import Problem
-    from odil_gb300.workloads import WaveInstance
-    inst = WaveInstance(n, n, profile="sine", seed=1, nmodes=16, device=cuda)
-    prob = Problem(inst.operator, inst.domain)
-    k = prob.kernels
-    ref = torch.zeros((n, n), dtype=torch.float64, device=cuda)
-    newton.solve(prob, State(fields={"u": ref}), "mixed", 1, from_zero=True)
-    cfg = k.march_tuned_cfg(torch.float32)
-    if cfg.get("kind") != "tiled" or cfg.get("exchange", 0) != 0:
-        pytest.skip("the tuned march shape has no row-range form")
-    b = torch.randn((n, n), dtype=torch.float32, device=cuda)
-    x1 = torch.full_like(b, float("nan"))
-    k.march_tuned(b, x1)
-    x2 = torch.full_like(b, float("nan"))
-    halo = int(cfg["halo"])
-    cuts = [0, halo, 3 * halo, n]
-    for r0, r1 in zip(cuts[:-1], cuts[1:]):
-        assert k.march_rows(b, x2, r0, r1) == halo
-    assert torch.equal(x1, x2)
-    host = torch.full((n, n), float("nan"), dtype=torch.float64).pin_memory()
-    u = torch.full((n, n), float("nan"), dtype=torch.float64, device=cuda)
-    st = State(fields={"u": u})
-    newton.solve(prob, st, "mixed", 1, from_zero=True, host_out=host)
-    torch.cuda.synchronize()
-    assert torch.equal(u, ref)
-    assert torch.equal(host, ref.cpu())
-    host.fill_(float("nan"))
-    cap = newton.CapturedSolve(prob, st, "mixed", 1, host_out=host)
-    host.fill_(float("nan"))
-    u.fill_(float("nan"))
-    cap()
-    torch.cuda.synchronize()
-    assert torch.equal(u, ref)
-    assert torch.equal(host, ref.cpu())
