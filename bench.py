@@ -1359,7 +1359,7 @@ def run_case(args):
         "batch_lg": lambda: wb.loss_grad(bu, bg),
         "pair_residual": lambda: k.pair_residual(d32, None, rhs),
         "ns_kernels": lambda: (nk.residual(*fields),
-                               mgn.linearize(*fields),
+                               mgn._linearize32(*fields),
                                mgn._smooth(0, vb, vb, vo, 2),
                                mgn._smooth(1, mgn.levels[1].x,
                                            mgn.levels[1].b,
