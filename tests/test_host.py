@@ -397,3 +397,22 @@ def test_minimal_domain_pickles():
     x, y = m.cell_center_all()
     assert np.allclose(x[:, 0], dom.cell_center_1d(0))
     assert np.allclose(y[0], dom.cell_center_1d(1))
+
+
+def test_batch_instances_stay_below_the_stability_limit():
+    """Batch instances keep the Courant number c dt / dx <= 0.9 (high wave
+    speeds get a refined time grid): the wave operator's boundary closure
+    makes forward substitution unstable above ~0.93, where the FP64
+    oracle's own march grows without bound.  With it, the oracle solution of
+    every instance is finite and close to the exact one."""
+    from odil_gb300.workloads import wave_batch_instances
+    from oracle import wave as W
+    insts = wave_batch_instances(count=48, seed=7, nmin=24, nmax=96)
+    assert any(i["nt"] != i["nx"] for i in insts)  # some were refined
+    for i in insts:
+        assert i["c"] * i["dt"] / i["dx"] <= 0.9 + 1e-12
+        s = W.WaveSetup(i["nt"], i["nx"], i["init_u"], i["init_ut"],
+                        i["left_u"], i["right_u"], c=i["c"])
+        u = W.solve_march(s, rounds=1)
+        assert np.isfinite(u).all()
+        assert W.rel_err(u, i["exact_u"]) < 0.05, (i["nt"], i["nx"], i["c"])
