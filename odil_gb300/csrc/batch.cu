@@ -410,7 +410,7 @@ int launch_batch_march(const odil_wave_batch* b, const float* rhs, float* x, uns
 // without spills: 20 warps x 7 rows in flight per SM.
 constexpr int BLG_V = 4;
 constexpr int BLG_OUT = 32 * BLG_V - 2;  // output columns per item
-constexpr int BLG_TY = 60;  // BLG_TY + 4 loaded rows: a multiple of BLG_R
+constexpr int BLG_TY = 32;
 constexpr int BLG_WARPS = 4;
 constexpr int BLG_R = 8;      // ring rows per warp (power of two)
 // floats per ring row: [3] left extra column, [4 + 4 l + j] the lanes'
@@ -436,7 +436,6 @@ __global__ void __launch_bounds__(BLG_WARPS * 32, 5) batch_loss_grad_kernel(
     const float* __restrict__ u, float* __restrict__ grad, double* __restrict__ partials) {
     constexpr int V = BLG_V;
     constexpr int NQ = BLG_TY + 4;  // rows a0 - 2 .. a0 + BLG_TY + 1
-    static_assert(NQ % BLG_R == 0, "whole ring passes");
     __shared__ __align__(16) float ring_all[BLG_WARPS][BLG_R][BLG_ROW];
     const int lane = threadIdx.x & 31;
     const int64_t item = (int64_t)blockIdx.x * BLG_WARPS + (threadIdx.x >> 5);
@@ -500,67 +499,45 @@ __global__ void __launch_bounds__(BLG_WARPS * 32, 5) batch_loss_grad_kernel(
         has_l |= cb + j == 0;
         has_r |= cb + j == nx - 1;
     }
-    // Row q (r = a0 - 2 + q) into ring slot q mod BLG_R (a compile-time slot
-    // in the unrolled loop below); rows outside the grid are zero.  srcp
-    // walks the rows by pointer increments; a lane whose four columns are
-    // contiguous in memory (all but the wrapped edge lanes) issues its copies
-    // with immediate offsets from one address.  Every call commits one group
-    // (empty past the tile), so the wait below counts rows.
-    const bool contig = off[1] == off[0] + 1 && off[2] == off[0] + 2 && off[3] == off[0] + 3;
-    bool ow[V];
-#pragma unroll
-    for (int j = 0; j < V; ++j) ow[j] = (outm >> j) & 1u;
-    float* const sdst = ring + 4 + V * lane;
-    const float* srcp = ui + (int64_t)(a0 - 2) * nx;  // row of the next issue
-    int rq = a0 - 2;                                   // its index
-    auto issue = [&](int q, int slot) {
+    // Row q (r = a0 - 2 + q) into ring slot q mod BLG_R; rows outside the
+    // grid are zero.  Every call commits one group (empty past the tile), so
+    // the wait below counts rows.
+    auto issue = [&](int q) {
         if (q < NQ) {
-            float* to = sdst + slot * BLG_ROW;
-            float* tr = ring + slot * BLG_ROW;
-            if (rq >= 0 && rq < nt) {
-                if (contig) {
-                    const float* pp = srcp + off[0];
+            const int r = a0 - 2 + q;
+            float* to = ring + (q & (BLG_R - 1)) * BLG_ROW;
+            if (r >= 0 && r < nt) {
+                const float* row = ui + (int64_t)r * nx;
 #pragma unroll
-                    for (int j = 0; j < V; ++j) cp_async_n(to + j, pp + j, 4);
-                } else {
-#pragma unroll
-                    for (int j = 0; j < V; ++j) cp_async_n(to + j, srcp + off[j], 4);
-                }
-                if (xl) cp_async_n(tr + xe, srcp + offe, 4);
-                if (rq >= 1 && has_l) cp_async_n(tr + 133, g.left_u + (rq - 1), 4);
-                if (rq >= 1 && has_r) cp_async_n(tr + 134, g.right_u + (rq - 1), 4);
+                for (int j = 0; j < V; ++j) cp_async_n(to + 4 + V * lane + j, row + off[j], 4);
+                if (xl) cp_async_n(to + xe, row + offe, 4);
+                if (r >= 1 && has_l) cp_async_n(to + 133, g.left_u + (r - 1), 4);
+                if (r >= 1 && has_r) cp_async_n(to + 134, g.right_u + (r - 1), 4);
             } else {
 #pragma unroll
-                for (int j = 0; j < V; ++j) to[j] = 0.f;
-                if (xl) tr[xe] = 0.f;
+                for (int j = 0; j < V; ++j) to[4 + V * lane + j] = 0.f;
+                if (xl) to[xe] = 0.f;
             }
         }
         cp_async_commit();
-        srcp += nx;
-        ++rq;
     };
 #pragma unroll
-    for (int q = 0; q < BLG_R - 1; ++q) issue(q, q);
+    for (int q = 0; q < BLG_R - 1; ++q) issue(q);
 
     float u1[V], u2[V], f1[V], f2[V];
 #pragma unroll
     for (int j = 0; j < V; ++j) u1[j] = u2[j] = f1[j] = f2[j] = 0.f;
     float lsum = 0.f;
-    // Gradient row a = r - 2 of row qq: a0 - 4 + qq.
-    float* __restrict__ gout = gi + (int64_t)(a0 - 4) * nx + cb;
-    for (int q0 = 0; q0 < NQ; q0 += BLG_R) {
-#pragma unroll
-        for (int jj = 0; jj < BLG_R; ++jj) {
-        const int qq = q0 + jj;
+    for (int qq = 0; qq < NQ; ++qq) {
         cp_async_wait<BLG_R - 2>();  // this thread's copies of row qq have landed
         __syncwarp();                // ... and every lane's
-        const float* cur = ring + jj * BLG_ROW;
+        const float* cur = ring + (qq & (BLG_R - 1)) * BLG_ROW;
         const float4 u0v = *reinterpret_cast<const float4*>(cur + 4 + V * lane);
         const float u0[V] = {u0v.x, u0v.y, u0v.z, u0v.w};
         // Extra column of row r-1 (lanes 0, 31), from the previous slot.
-        const float e1 = xl ? ring[((jj + BLG_R - 1) & (BLG_R - 1)) * BLG_ROW + xe] : 0.f;
+        const float e1 = xl ? ring[((qq - 1) & (BLG_R - 1)) * BLG_ROW + xe] : 0.f;
         __syncwarp();     // the previous slot is read: refill it
-        issue(qq + BLG_R - 1, (jj + BLG_R - 1) & (BLG_R - 1));
+        issue(qq + BLG_R - 1);
         const int r = a0 - 2 + qq;
         // x-neighbours of row r-1 at the lane's end columns.
         float um0 = __shfl_up_sync(0xffffffffu, u1[V - 1], 1);
@@ -629,10 +606,11 @@ __global__ void __launch_bounds__(BLG_WARPS * 32, 5) batch_loss_grad_kernel(
                         gv[j] = wave_gather(g, a, off[j], f2[j], f1[j], f0[j], f1p, f1m);
                     }
                 }
+                float* __restrict__ grow = gi + (int64_t)a * nx + cb;
 #pragma unroll
                 for (int j = 0; j < V; ++j) {
-                    if (ow[j]) {
-                        gout[j] = gv[j] * gscale;
+                    if (outm & (1u << j)) {
+                        grow[j] = gv[j] * gscale;
                         lsum += f2[j] * f2[j];
                     }
                 }
@@ -647,8 +625,6 @@ __global__ void __launch_bounds__(BLG_WARPS * 32, 5) batch_loss_grad_kernel(
         for (int j = 0; j < V; ++j) {
             u2[j] = u1[j];
             u1[j] = u0[j];
-        }
-        gout += nx;
         }
     }
     cp_async_wait<0>();
