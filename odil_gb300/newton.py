@@ -70,7 +70,7 @@ def solve(problem, state, precision="mixed", epochs=None, rnorm2=None,
         k.solve_mixed(u, epochs=3 if epochs is None else epochs,
                       rnorm2=rnorm2)
         if host_out is not None:
-            _to_host(u, host_out)
+            host_out.copy_(u, non_blocking=True)
         return u
     epochs = 2 if epochs is None else epochs
     if precision == "mixed":
@@ -79,7 +79,7 @@ def solve(problem, state, precision="mixed", epochs=None, rnorm2=None,
         if from_zero and epochs > 0:
             _solve_pairs(k, u, rhs, d, epochs, rnorm2)
             if host_out is not None:
-                _to_host(u, host_out)
+                host_out.copy_(u, non_blocking=True)
             return u
         ua, ub = u, _scratch(k, "u64", torch.float64)
         if from_zero:
@@ -110,36 +110,8 @@ def solve(problem, state, precision="mixed", epochs=None, rnorm2=None,
     else:
         raise ValueError("Unknown precision=" + precision)
     if host_out is not None:
-        _to_host(u, host_out)
+        host_out.copy_(u, non_blocking=True)
     return u
-
-
-# Concurrent device-to-host copies of a solution (row chunks).
-HOST_COPY_STREAMS = 4
-_copy_streams = {}
-
-
-def _to_host(u, host_out, parts=HOST_COPY_STREAMS):
-    """host_out <- u by `parts` copies of row chunks, each on its own side
-    stream (forked from and joined back to the current stream, so the
-    sequence also captures into a CUDA graph): one copy drives one copy
-    engine, and GB300's host link carries several at once."""
-    rows = u.shape[0]
-    parts = max(1, min(parts, rows))
-    main = torch.cuda.current_stream(u.device)
-    streams = _copy_streams.get(u.device)
-    if streams is None or len(streams) < parts:
-        streams = _copy_streams[u.device] = [torch.cuda.Stream(u.device)
-                                             for _ in range(parts)]
-    step = -(-rows // parts)
-    for p, st in zip(range(parts), streams):
-        r0, r1 = p * step, min(rows, (p + 1) * step)
-        if r0 >= r1:
-            break
-        st.wait_stream(main)
-        with torch.cuda.stream(st):
-            host_out[r0:r1].copy_(u[r0:r1], non_blocking=True)
-        main.wait_stream(st)
 
 
 def _solve_pairs(k, u, rhs, d, epochs, rnorm2):
