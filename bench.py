@@ -70,6 +70,7 @@ def parse():
                              "adam_iter", "batch", "ns_newton", "advect",
                              "ns_inverse", "ns_mg", "generic", "cavity",
                              "batch_block", "pair_residual", "batch_lg",
+                             "batch_persistent",
                              "ns_kernels", "stencil", "mgdecomp"),
                     help="run one kernel of the workload --steps times (for "
                     "profiler captures) instead of the benchmark")
@@ -1305,7 +1306,7 @@ def run_case(args):
         kb = Problem(big.operator, big.domain).kernels
         ubig = torch.randn((BIG, BIG), dtype=torch.float32, device=dev)
         gbig = torch.empty_like(ubig)
-    if args.case in ("batch", "batch_lg"):
+    if args.case in ("batch", "batch_lg", "batch_persistent"):
         from odil_gb300.batch import WaveBatch
         from odil_gb300.workloads import wave_batch_instances
         wb = WaveBatch(wave_batch_instances(count=512), device=dev)
@@ -1359,6 +1360,7 @@ def run_case(args):
     fn = {
         "loss_grad_big": lambda: kb.loss_grad(ubig, grad=gbig),
         "batch": lambda: wb.solve_mixed(),
+        "batch_persistent": lambda: wb.solve_persistent(),
         "batch_lg": lambda: wb.loss_grad(bu, bg),
         "pair_residual": lambda: k.pair_residual(d32, None, rhs),
         "ns_kernels": lambda: (nk.residual(*fields),
