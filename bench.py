@@ -509,7 +509,7 @@ def run_batch(dev, with_oracle, steps=5, hbm=6800.0):
            "method": ("persistent" if ms_pers <= ms_multi else
                       "multi_launch"),
            "persistent": {"ms_per_batch": ms_pers, "launches_per_batch": 1,
-                          "blocks_per_sm_ms": pers_tune,
+                          "cfg": b.persistent_cfg, "tune_ms": pers_tune,
                           "value": len(insts) / (ms_pers / 1000.0),
                           "bitwise_equal_to_multi_launch": same,
                           "difference_to_multi_launch": pers_diff},

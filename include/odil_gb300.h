@@ -308,19 +308,21 @@ int odil_wave_batch_march_f32(const odil_wave_batch* b, const float* rhs,
                               void* stream);
 /* The whole mixed Newton from u = 0 of every instance in ONE persistent
  * launch: each block takes the next instance (largest first, `order`) from
- * an atomic work queue and runs on it, with block barriers between the
- * steps, the sequence of the multi-launch path: rhs = float(-F(0)), hi =
- * J^-1 rhs, then epochs - 1 times rhs = float(-F(hi + lo)) and lo (or d,
- * lo += d) = J^-1 rhs, and u = hi + lo in FP64; results are bitwise those of
+ * an atomic work queue and runs its epochs as marches whose right-hand sides
+ * are formed inside the march from the previous iterate (float pairs inside,
+ * FP64 on the boundary cells, computed by the block into a table in the
+ * instance's rhs region): hi = J^-1 float(-F(0)), then epochs - 1 times
+ * x = J^-1 float(-F(hi + lo)) with lo = x (first) or lo += x, and u = hi + lo
+ * in FP64 written by the last march.  Results are bitwise those of
  * odil_wave_batch_initial_rhs_mixed / _march_f32 / _pair_residual_mixed /
- * odil_pair_to_f64 run in that order.  rhs, hi (and lo for epochs >= 2, d
- * for epochs >= 3): packed FP32 scratch; u: the packed FP64 solution.
- * Launch shape as odil_wave_batch_march_f32.  workspace: 256 bytes, zeroed
- * before the first call (the last block to finish leaves it zeroed again);
- * not shared with odil_wave_batch_march_f32.
+ * odil_pair_to_f64 run in that order.  rhs (the boundary tables), hi (and lo
+ * for epochs >= 2): packed FP32 scratch; u: the packed FP64 solution.
+ * Launch shape as odil_wave_batch_march_f32 (pf >= 8).  workspace: 256 bytes,
+ * zeroed before the first call (the last block to finish leaves it zeroed
+ * again); not shared with odil_wave_batch_march_f32.
  * util.py:242-268 per instance (the batched form of vary_wave.py:37-43). */
 int odil_wave_batch_solve_mixed(const odil_wave_batch* b, int32_t epochs,
-                                float* rhs, float* hi, float* lo, float* d,
+                                float* rhs, float* hi, float* lo,
                                 double* u, int32_t threads, int32_t cpt,
                                 int32_t pf, int32_t blocks_per_sm,
                                 void* workspace, int64_t workspace_bytes,

@@ -200,7 +200,7 @@ SIGNATURES = {
     "odil_wave_batch_march_f32": (_INT, [_P, _P, _P, ctypes.c_int32,
                                          ctypes.c_int32, ctypes.c_int32,
                                          ctypes.c_int32, _P, _I64, _P]),
-    "odil_wave_batch_solve_mixed": (_INT, [_P, ctypes.c_int32, _P, _P, _P, _P,
+    "odil_wave_batch_solve_mixed": (_INT, [_P, ctypes.c_int32, _P, _P, _P,
                                            _P] + [ctypes.c_int32] * 4 +
                                     [_P, _I64, _P]),
     "odil_nsmg_jx_f32": (_INT, [_I64, ctypes.c_int32, _P, _P, _P, _P]),

@@ -208,45 +208,54 @@ class WaveBatch:
         return self.u
 
     def tune_persistent(self, epochs=2, per_sm=(1, 2, 3, 4), reps=3):
-        """Chooses blocks per SM of the persistent whole-solve launch by
-        timing it (CUDA events) with the march's threads, cpt and pf; keeps
-        the fastest in self.persistent_cfg and returns {per_sm: ms}."""
-        base = dict(self.march_cfg or autotune.default_batch_march(self.max_nx))
-        times = {}
-        for b in per_sm:
-            self.persistent_cfg = dict(base, blocks_per_sm=int(b))
-            try:
-                self.solve_persistent(epochs)
-            except _capi.OdilError:
+        """Chooses the launch shape of the persistent whole-solve launch
+        (columns per thread, ring depth, blocks per SM) by timing every
+        candidate that fits (CUDA events); keeps the fastest in
+        self.persistent_cfg and returns {"cpt<c>_pf<p>_bps<b>": ms}."""
+        times, cfgs = {}, {}
+        for cpt in (1, 2, 4):
+            threads = max(32, ((self.max_nx + cpt - 1) // cpt + 31) // 32 * 32)
+            if threads > (1024 if cpt == 1 else 512):
                 continue
-            torch.cuda.synchronize(self.device)
-            e0 = torch.cuda.Event(enable_timing=True)
-            e1 = torch.cuda.Event(enable_timing=True)
-            e0.record()
-            for _ in range(reps):
-                self.solve_persistent(epochs)
-            e1.record()
-            e1.synchronize()
-            times[int(b)] = e0.elapsed_time(e1) / reps
-        best = min(times, key=times.get)
-        self.persistent_cfg = dict(base, blocks_per_sm=best)
+            for pf in (8, 16):
+                for b in per_sm:
+                    if b * threads > 2048:
+                        continue
+                    cfg = {"threads": threads, "cpt": cpt, "pf": pf,
+                           "blocks_per_sm": int(b)}
+                    try:
+                        self.solve_persistent(epochs, cfg=cfg)
+                    except _capi.OdilError:
+                        continue
+                    torch.cuda.synchronize(self.device)
+                    e0 = torch.cuda.Event(enable_timing=True)
+                    e1 = torch.cuda.Event(enable_timing=True)
+                    e0.record()
+                    for _ in range(reps):
+                        self.solve_persistent(epochs, cfg=cfg)
+                    e1.record()
+                    e1.synchronize()
+                    key = "cpt%d_pf%d_bps%d" % (cpt, pf, b)
+                    times[key] = e0.elapsed_time(e1) / reps
+                    cfgs[key] = cfg
+        if not times:
+            raise _capi.OdilError("no launch shape of the persistent solve "
+                                  "fits max_nx %d" % self.max_nx)
+        self.persistent_cfg = cfgs[min(times, key=times.get)]
         return times
 
-    def solve_persistent(self, epochs=2):
+    def solve_persistent(self, epochs=2, cfg=None):
         """u <- the same mixed Newton as solve_mixed (bitwise), in ONE
         persistent launch: each block solves whole instances from the work
-        queue, with block barriers between the steps (see
+        queue, forming each march's right-hand side inside the march (see
         odil_wave_batch_solve_mixed)."""
         if epochs < 1:
             self.u.zero_()
             return self.u
-        cfg = (getattr(self, "persistent_cfg", None) or self.march_cfg or
-               autotune.default_batch_march(self.max_nx))
-        if epochs > 2 and getattr(self, "d2", None) is None:
-            self.d2 = torch.zeros_like(self.d)
+        cfg = (cfg or getattr(self, "persistent_cfg", None) or
+               autotune.default_batch_solve(self.max_nx))
         call("odil_wave_batch_solve_mixed", ctypes.byref(self.b), int(epochs),
-             ptr(self.rhs), ptr(self.hi), ptr(self.lo),
-             ptr(self.d2 if epochs > 2 else None), ptr(self.u),
+             ptr(self.rhs), ptr(self.hi), ptr(self.lo), ptr(self.u),
              cfg["threads"], cfg["cpt"], cfg["pf"], cfg["blocks_per_sm"],
              ptr(self.ws_solve), self.ws_solve.numel(), stream_handle())
         return self.u

@@ -230,34 +230,309 @@ __global__ void __launch_bounds__(1024) batch_march_kernel(odil_wave_batch b,
 }
 
 // The whole mixed Newton of the batch in one persistent launch.  Each block
-// takes the next instance (largest first) from the work queue and runs the
-// from-zero sequence of the multi-launch path on it alone, with block
-// barriers between the steps instead of grid-wide passes:
-//   rhs = float(-F(0))             (zero inside, FP64 on the boundary cells)
-//   hi = J^-1 rhs                  (march_instance, the single-block march)
-//   repeat epochs - 1 times:
-//     rhs = float(-F(hi + lo))     (float pairs inside, FP64 on the boundary)
-//     lo = J^-1 rhs, or d = J^-1 rhs and lo += d after the first of these
-//   u = hi + lo in FP64            (exact, integer instructions)
-// The instance's fields are written and read back by the same block within
-// microseconds, so they mostly stay in L2.  Values written in this kernel
-// are read back through L2 (ld.global.cg), never the read-only path, and
-// instances start on 128-byte boundaries (the host's packing), so no L1
-// line holds two instances' data.  Counters: [0] the work queue,
+// takes the next instance (largest first) from the work queue and runs its
+// epochs as marches whose right-hand sides are formed inside the march, row
+// by row, from the previous iterate:
+//   march 1 (SRC 0): rhs = float(-F(0)), zero inside;
+//   march 2 (SRC 1): rhs = float(-F(hi)) inside, in float pairs;
+//   march e > 2 (SRC 2): rhs = float(-F(hi + lo)) inside, and lo += x;
+// the boundary cells' values (rows 0, 1, columns 0 and nx-1) in FP64,
+// computed by the whole block into a table before each march (the table
+// lives in the instance's rhs region).  The iterate's rows stream into
+// shared-memory rings by cp.async, PF - 3 rows ahead, so rows i, i-1 and
+// i-2 are resident when row i is formed; the column-table entries ride in
+// the same copy groups.  The last march writes u = hi + lo in FP64 (exact,
+// integer instructions) as it goes, so its correction never reaches memory:
+// with two epochs an instance costs a 4-byte write and read of hi and the
+// 8-byte write of u per cell.  The arithmetic is that of the multi-launch
+// path (batch_rows / batch_bnd, batch_march, pair_to_f64), so the results
+// are bitwise the same.  Values written in this kernel are read back
+// through L2 (ld.global.cg) or by the block that wrote them after a block
+// barrier; instances start on 128-byte boundaries (the host's packing), so
+// no L1 line holds two instances' data.  Counters: [0] the work queue,
 // [1] blocks done; the last block to finish resets both, so the workspace
 // needs zeroing once, before the first launch.
+
+struct FusedSmem {
+    float* ringh;  // [max_nx][PF + 1] rows of hi
+    float* ringl;  // [max_nx][PF + 1] rows of lo (SRC 2)
+    float* tring;  // [2][PF] column-table entries (column 0, column nx-1)
+    float* edge;   // [2 parity][2 end][kMarchMaxWarps]
+};
+
+// One march of the fused solve (see above).  x: the float result (hi for
+// SRC 0, lo otherwise; lo is updated in place for SRC 2) unless LAST, when
+// u = hi + lo goes to uo in FP64 instead.  The row step is that of
+// march_instance; the right-hand side of row i + 1 is formed during step i
+// and the FP64 value of row i - 1 is written during step i, both off the
+// row-to-row dependency chain (independent of the step's march arithmetic,
+// so their latency hides behind it).  Only the warps that hold columns of
+// this instance march (blocks are sized for the widest instance of the
+// batch); they meet at named barrier 1, the others wait at the block
+// barrier at the end.  Ring layout [column][PF + 1]: a slot is an immediate
+// offset, and a warp's 32 columns fall in distinct banks.
+template <int SRC, bool LAST, int CPT, int PF, bool VEC>
+__device__ __forceinline__ void fused_march(const WaveDev<float>& g, const PairCoef& k,
+                                            const float* tbl, const float* hs,
+                                            const float* ls, float* x, double* uo,
+                                            const FusedSmem& sm) {
+    static_assert(PF % 2 == 0 && PF >= 4, "row parity follows the ring slot");
+    constexpr int RS = PF + 1;  // ring stride per column
+    const int nx = g.nx, nt = g.nt;
+    const int nact = ((nx + CPT - 1) / CPT + 31) & ~31;  // marching threads
+    if ((int)threadIdx.x < nact) {
+        const int lane = threadIdx.x & 31;
+        const int warp = threadIdx.x >> 5;
+        const int nwarp = nact >> 5;
+        const int j0 = threadIdx.x * CPT;
+        float kxm[CPT], ktm[CPT], kxp[CPT], d1[CPT], d2[CPT];
+        // Own columns of the iterate: hb / lb row i, hc / lc row i - 1 (at
+        // the start of step i); rc: right-hand side of row i; pend: result
+        // of row i - 1 (its FP64 write is pending).
+        float hb[CPT], hc[CPT], lb[CPT], lc[CPT], rc[CPT], pend[CPT], r1[CPT];
+        const float* hcol[CPT];  // ring columns (own, clamped into the row)
+        const float* lcol[CPT];
+        bool in[CPT];       // column inside the row
+        unsigned bcol = 0;  // bit c: column j0 + c is 0 or nx - 1
+#pragma unroll
+        for (int c = 0; c < CPT; ++c) {
+            const int j = j0 + c;
+            in[c] = j < nx;
+            const int jj = in[c] ? j : 0;
+            // Columns past the row end march zeros: no coupling, zero rhs.
+            ktm[c] = in[c] ? k_tm<float>(jj, nx) : 0.f;
+            kxm[c] = in[c] ? k_xm<float>(jj, nx) : 0.f;
+            kxp[c] = in[c] ? k_xp<float>(jj, nx) : 0.f;
+            d1[c] = 0.f;
+            d2[c] = 0.f;
+            hb[c] = hc[c] = lb[c] = lc[c] = pend[c] = 0.f;
+            const int jc = in[c] ? j : nx - 1;
+            hcol[c] = sm.ringh + jc * RS;
+            lcol[c] = sm.ringl + jc * RS;
+            if (j == 0 || j == nx - 1) bcol |= 1u << c;
+            rc[c] = in[c] ? __ldcg(tbl + j) : 0.f;  // row 0: all boundary
+            r1[c] = (in[c] && nt >= 2) ? __ldcg(tbl + nx + j) : 0.f;
+        }
+        const int jl = j0 > 0 ? (j0 - 1 < nx - 1 ? j0 - 1 : nx - 1) : 0;
+        const int jr = j0 + CPT < nx ? j0 + CPT : nx - 1;
+        const float* hl = sm.ringh + jl * RS;
+        const float* hr = sm.ringh + jr * RS;
+        const float* ll = sm.ringl + jl * RS;
+        const float* lr = sm.ringl + jr * RS;
+        const bool own_l = j0 == 0;
+        const bool own_r = in[0] && nx - 1 < j0 + CPT;
+        const int wl = warp > 0 ? warp - 1 : 0;
+        const int wr = warp + 1 < nwarp ? warp + 1 : warp;
+        const bool use_l = lane == 0, use_r = lane == 31;
+        const bool self_r = nx == 1;
+        float* edge = sm.edge;
+        for (int e = threadIdx.x; e < 4 * kMarchMaxWarps; e += nact) edge[e] = 0.f;
+        // Copy sources of the next row to issue.  The table follows the
+        // bnd_cell sequence: rows 0 and 1, then the cc (= min(nx, 2))
+        // column entries (column 0, then nx - 1) of each row from 2 on.
+        const float* hsrc = hs + j0;
+        const float* lsrc = ls + j0;
+        const int cc = nx < 2 ? nx : 2;
+        const float* tsrc = tbl + (nt < 2 ? nt : 2) * nx;  // column entries of row 2
+        float* dst = x + j0;
+        double* udst = uo + j0;
+        auto bar = [&]() { asm volatile("bar.sync 1, %0;" ::"r"(nact) : "memory"); };
+        // Copy group of row rr into ring slot `slot` (one group per row,
+        // empty past the last row).
+        auto issue = [&](int rr, int slot) {
+            if (rr < nt) {
+#pragma unroll
+                for (int c = 0; c < CPT; ++c) {
+                    if (in[c]) {
+                        if constexpr (SRC >= 1)
+                            cp_async_n(sm.ringh + (j0 + c) * RS + slot, hsrc + c, 4);
+                        if constexpr (SRC == 2)
+                            cp_async_n(sm.ringl + (j0 + c) * RS + slot, lsrc + c, 4);
+                    }
+                }
+                if (rr >= 2) {
+                    if (own_l) cp_async_n(sm.tring + slot, tsrc, 4);
+                    if (own_r) cp_async_n(sm.tring + PF + slot, tsrc + (cc - 1), 4);
+                    tsrc += cc;
+                }
+            }
+            hsrc += nx;
+            lsrc += nx;
+            cp_async_commit();
+        };
+        // FP64 write of a row (result out, iterate h / l of the row).
+        auto write_u = [&](double* to, const float* out, const float* h, const float* l) {
+            double uv[CPT];
+#pragma unroll
+            for (int c = 0; c < CPT; ++c) {
+                if constexpr (SRC == 0) {
+                    uv[c] = f2d_exact(out[c]);
+                } else if constexpr (SRC == 1) {
+                    uv[c] = pair_sum_exact(h[c], out[c]);
+                } else {
+                    uv[c] = pair_sum_exact(h[c], __fadd_rn(l[c], out[c]));
+                }
+            }
+            if constexpr (VEC && CPT % 2 == 0) {
+                if (in[0]) {
+#pragma unroll
+                    for (int c = 0; c < CPT; c += 2)
+                        *reinterpret_cast<double2*>(to + c) = make_double2(uv[c], uv[c + 1]);
+                }
+            } else {
+#pragma unroll
+                for (int c = 0; c < CPT; ++c)
+                    if (in[c]) to[c] = uv[c];
+            }
+        };
+        // Rows 0 .. PF - 3 in flight; row 0 landed (own columns) before the
+        // first step, so step i finds row i resident and waits for row i + 1.
+#pragma unroll
+        for (int s = 0; s < PF - 2; ++s) issue(s, s);
+        cp_async_wait<PF - 3>();
+#pragma unroll
+        for (int c = 0; c < CPT; ++c) {
+            if constexpr (SRC >= 1) hb[c] = hcol[c][0];
+            if constexpr (SRC == 2) lb[c] = lcol[c][0];
+        }
+        bar();
+        auto row = [&](auto gen_tag, int i, int s) {
+            constexpr bool GEN = decltype(gen_tag)::value;
+            const int sn = (s + 1) % PF;  // slot of row i + 1
+            issue(i + PF - 2, (s + PF - 2) % PF);
+            const float c_rhs = GEN ? (i == 0 ? 1.f : g.dt2) : g.dt2;
+            const float c_d1 = GEN ? (i == 1 ? 1.f : 2.f) : 2.f;
+            const float c_lam = GEN ? (i == 0 ? 0.f : g.lam2) : g.lam2;
+            const float* eprv = edge + ((s & 1) ^ 1) * 2 * kMarchMaxWarps;
+            const float el = eprv[kMarchMaxWarps + wl];
+            const float er = eprv[wr];
+            const float sl = __shfl_up_sync(0xffffffffu, d1[CPT - 1], 1);
+            const float sr = __shfl_down_sync(0xffffffffu, d1[0], 1);
+            const float left = use_l ? el : sl;
+            const float right = self_r ? d1[0] : (use_r ? er : sr);
+            float out[CPT];
+#pragma unroll
+            for (int c = 0; c < CPT; ++c) {
+                const float xm = c == 0 ? left : d1[c - 1];
+                const float xp = c == CPT - 1 ? right : d1[c + 1];
+                const float tprev = c_d1 * d1[c] - d2[c];
+                out[c] = c_rhs * rc[c] + tprev +
+                         c_lam * (kxm[c] * xm - ktm[c] * d1[c] + kxp[c] * xp);
+            }
+            if constexpr (!LAST) {
+                float res[CPT];
+#pragma unroll
+                for (int c = 0; c < CPT; ++c)
+                    res[c] = SRC == 2 ? __fadd_rn(lb[c], out[c]) : out[c];
+                if constexpr (VEC) {
+                    if (in[0]) {
+                        Chunk<float, CPT> ch;
+#pragma unroll
+                        for (int c = 0; c < CPT; ++c) ch.v[c] = res[c];
+                        *reinterpret_cast<Chunk<float, CPT>*>(dst) = ch;
+                    }
+                } else {
+#pragma unroll
+                    for (int c = 0; c < CPT; ++c)
+                        if (in[c]) dst[c] = res[c];
+                }
+            }
+            float* ecur = edge + (s & 1) * 2 * kMarchMaxWarps;
+            if (use_l) ecur[warp] = out[0];
+            if (use_r) ecur[kMarchMaxWarps + warp] = out[CPT - 1];
+            // Row i - 1's FP64 write.
+            if constexpr (LAST) {
+                if (!GEN || i >= 1) write_u(udst - nx, pend, hc, lc);
+            }
+            // Right-hand side of row i + 1 from rows i + 1, i, i - 1 (row
+            // i + 1 of this thread landed here; rows i and i - 1 of every
+            // thread are resident since the last barriers).
+            cp_async_wait<PF - 3>();
+            float ha[CPT], la[CPT], rn[CPT];
+#pragma unroll
+            for (int c = 0; c < CPT; ++c) {
+                ha[c] = SRC >= 1 ? hcol[c][sn] : 0.f;
+                la[c] = SRC == 2 ? lcol[c][sn] : 0.f;
+            }
+            float hm = 0.f, hp = 0.f, lm = 0.f, lp = 0.f;  // row i at j0 - 1, j0 + CPT
+            if constexpr (SRC >= 1) {
+                hm = hl[s];
+                hp = hr[s];
+            }
+            if constexpr (SRC == 2) {
+                lm = ll[s];
+                lp = lr[s];
+            }
+            (void)hm, (void)hp, (void)lm, (void)lp;
+            const float tl = sm.tring[sn], tr = sm.tring[PF + sn];
+#pragma unroll
+            for (int c = 0; c < CPT; ++c) {
+                float v = 0.f;
+                if constexpr (SRC >= 1) {
+                    const float vm = c == 0 ? hm : hb[c - 1];
+                    const float vp = c == CPT - 1 ? hp : hb[c + 1];
+                    const float wm = c == 0 ? lm : lb[c - 1];
+                    const float wp = c == CPT - 1 ? lp : lb[c + 1];
+                    v = pair_rhs_vals(k, ha[c], hc[c], hb[c], vm, vp, la[c], lc[c], lb[c], wm, wp);
+                }
+                if ((bcol >> c) & 1u) v = j0 + c == 0 ? tl : tr;
+                if (GEN && i + 1 == 1) v = r1[c];
+                rn[c] = in[c] ? v : 0.f;
+            }
+            dst += nx;
+            udst += nx;
+#pragma unroll
+            for (int c = 0; c < CPT; ++c) {
+                d2[c] = d1[c];
+                d1[c] = out[c];
+                pend[c] = out[c];
+                hc[c] = hb[c];
+                hb[c] = ha[c];
+                lc[c] = lb[c];
+                lb[c] = la[c];
+                rc[c] = rn[c];
+            }
+            bar();
+        };
+        for (int i0 = 0; i0 < nt; i0 += PF) {
+            if (i0 == 0 || i0 + PF > nt) {
+#pragma unroll
+                for (int s = 0; s < PF; ++s) {
+                    if (i0 + s >= nt) break;
+                    row(std::true_type{}, i0 + s, s);
+                }
+            } else {
+#pragma unroll
+                for (int s = 0; s < PF; ++s) row(std::false_type{}, i0 + s, s);
+            }
+        }
+        // The last row's FP64 write (hc / lc hold its iterate after the
+        // shift).
+        if constexpr (LAST) write_u(udst - nx, pend, hc, lc);
+        cp_async_wait<0>();
+    }
+    __syncthreads();
+}
+
+// Threads per block of the fused solve: the pair stencil, three rows of the
+// iterate and the march state need more than the 64 registers a 1024-thread
+// block leaves once a thread owns more than one column.
+template <int CPT>
+constexpr int batch_solve_max_threads() { return CPT == 1 ? 1024 : 512; }
+
 template <int CPT, int PF>
-__global__ void __launch_bounds__(1024) batch_solve_kernel(odil_wave_batch b, int epochs,
-                                                           float* __restrict__ rhs,
-                                                           float* __restrict__ hi,
-                                                           float* __restrict__ lo,
-                                                           float* __restrict__ dd,
-                                                           double* __restrict__ u,
-                                                           unsigned* __restrict__ counter) {
+__global__ void __launch_bounds__(batch_solve_max_threads<CPT>()) batch_solve_kernel(
+    odil_wave_batch b, int epochs, float* __restrict__ rhs, float* __restrict__ hi, float* lo,
+    double* __restrict__ u, unsigned* __restrict__ counter) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ int sh_q;
     const int nthr = blockDim.x;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = nthr >> 5;
+    FusedSmem sm;
+    const int ring = b.max_nx * (PF + 1);
+    sm.ringh = reinterpret_cast<float*>(smem_raw);
+    sm.ringl = sm.ringh + ring;
+    sm.tring = sm.ringl + (epochs > 2 ? ring : 0);
+    sm.edge = sm.tring + 2 * PF;
     const double* iu = (const double*)b.init_u;
     const double* iut = (const double*)b.init_ut;
     const double* lu = (const double*)b.left_u;
@@ -273,7 +548,7 @@ __global__ void __launch_bounds__(1024) batch_solve_kernel(odil_wave_batch b, in
         const WaveDev<double> g64 = dev_of<double>(desc, iu, iut, lu, ru);
         const WaveDev<float> g32 = dev_of<float>(desc, nullptr, nullptr, nullptr, nullptr);
         const int nt = g32.nt, nx = g32.nx;
-        const int64_t off = desc.offset, cells = (int64_t)nt * nx;
+        const int64_t off = desc.offset;
         PairCoef k;
         k.ah = desc.ah;
         k.al = desc.al;
@@ -281,57 +556,53 @@ __global__ void __launch_bounds__(1024) batch_solve_kernel(odil_wave_batch b, in
         k.cl = desc.cl;
         k.bh = desc.bh;
         k.bl = desc.bl;
-        float* r = rhs + off;
+        float* tb = rhs + off;
         float* h = hi + off;
-        float* l = lo + off;
-        float* dq = dd + off;
-        // Right-hand side of the current iterate (KIND 0: u = 0; 1: hi + lo).
-        auto residual = [&](auto kind_tag, const float* lp) {
+        float* l = lo ? lo + off : nullptr;
+        double* uo = u + off;
+        const int64_t nb = bnd_count(nt, nx);
+        // Boundary table of the current iterate (KIND 0: u = 0; 1: hi + lo).
+        auto table = [&](auto kind_tag, const float* lp) {
             constexpr int KIND = decltype(kind_tag)::value;
-            for (int i = 2 + warp; i < nt; i += nwarp) {
-                float* rrow = r + (int64_t)i * nx;
-                for (int j = 1 + lane; j < nx - 1; j += 32)
-                    rrow[j] = KIND == 0 ? 0.f
-                                        : pair_interior_rhs<false>(k, h, lp,
-                                                                   (int64_t)i * nx + j, nx);
-            }
-            const int64_t nb = bnd_count(nt, nx);
             for (int64_t t = threadIdx.x; t < nb; t += nthr) {
                 int i, j;
                 bnd_cell(t, nt, nx, &i, &j);
-                r[(int64_t)i * nx + j] = bnd_cell_rhs<KIND, false>(g64, k, h, lp, i, j);
+                tb[t] = bnd_cell_rhs<KIND, false>(g64, k, h, lp, i, j);
             }
             __syncthreads();
         };
-        auto march = [&](float* x) {
+        auto march = [&](auto src_tag, auto last_tag, float* x) {
+            constexpr int SRC = decltype(src_tag)::value;
+            constexpr bool LAST = decltype(last_tag)::value;
             if (nx % CPT == 0) {
-                march_instance<float, CPT, PF, true>(g32, r, x, smem_raw);
+                fused_march<SRC, LAST, CPT, PF, true>(g32, k, tb, h, l, x, uo, sm);
             } else {
-                march_instance<float, CPT, PF, false>(g32, r, x, smem_raw);
+                fused_march<SRC, LAST, CPT, PF, false>(g32, k, tb, h, l, x, uo, sm);
             }
-            __syncthreads();
         };
-        residual(std::integral_constant<int, 0>{}, nullptr);
-        march(h);
-        bool have_lo = false;
-        for (int e = 1; e < epochs; ++e) {
-            residual(std::integral_constant<int, 1>{}, have_lo ? l : nullptr);
-            if (have_lo) {
-                march(dq);
-                for (int64_t c = threadIdx.x; c < cells; c += nthr) l[c] += dq[c];
-                __syncthreads();
-            } else {
-                march(l);
-                have_lo = true;
+        using I0 = std::integral_constant<int, 0>;
+        using I1 = std::integral_constant<int, 1>;
+        using I2 = std::integral_constant<int, 2>;
+        table(I0{}, nullptr);
+        if (epochs == 1) {
+            march(I0{}, std::true_type{}, h);
+        } else {
+            march(I0{}, std::false_type{}, h);
+            for (int e = 2; e <= epochs; ++e) {
+                table(I1{}, e > 2 ? l : nullptr);
+                if (e == 2) {
+                    if (e == epochs) march(I1{}, std::true_type{}, l);
+                    else march(I1{}, std::false_type{}, l);
+                } else {
+                    if (e == epochs) march(I2{}, std::true_type{}, l);
+                    else march(I2{}, std::false_type{}, l);
+                }
             }
         }
-        double* uo = u + off;
-        for (int64_t c = threadIdx.x; c < cells; c += nthr)
-            uo[c] = have_lo ? pair_sum_exact(h[c], l[c]) : f2d_exact(h[c]);
         // The padding up to the next instance is zero, as the multi-launch
         // path leaves it.
         const int64_t pad_end = idx + 1 < b.ninst ? b.inst[idx + 1].offset : b.total_cells;
-        for (int64_t c = off + cells + threadIdx.x; c < pad_end; c += nthr) u[c] = 0.0;
+        for (int64_t c = off + (int64_t)nt * nx + threadIdx.x; c < pad_end; c += nthr) u[c] = 0.0;
         __syncthreads();
     }
     // The last block out resets the queue for the next launch.
@@ -345,16 +616,24 @@ __global__ void __launch_bounds__(1024) batch_solve_kernel(odil_wave_batch b, in
     }
 }
 
+// Shared memory of the fused solve: the hi ring (and the lo ring for more
+// than two epochs), the column-table ring and the edge words.
+template <int PF>
+size_t batch_solve_smem(int max_nx, int epochs) {
+    const size_t ring = (size_t)max_nx * (PF + 1) * 4;
+    return ring * (epochs > 2 ? 2 : 1) + 2 * PF * 4 + 4 * kMarchMaxWarps * 4;
+}
+
 template <int CPT, int PF>
 int launch_batch_solve(const odil_wave_batch* b, int epochs, float* rhs, float* hi, float* lo,
-                       float* d, double* u, unsigned* counter, int threads, int blocks,
-                       cudaStream_t st) {
-    if ((int64_t)threads * CPT < b->max_nx) return ODIL_ERR_SHAPE;
-    const size_t smem = march_ring_smem_bytes<float>(b->max_nx, PF);
+                       double* u, unsigned* counter, int threads, int blocks, cudaStream_t st) {
+    if ((int64_t)threads * CPT < b->max_nx || threads > batch_solve_max_threads<CPT>())
+        return ODIL_ERR_SHAPE;
+    const size_t smem = batch_solve_smem<PF>(b->max_nx, epochs);
     if (smem > 200 * 1024) return ODIL_ERR_SHAPE;
     auto kern = batch_solve_kernel<CPT, PF>;
     ensure_dynamic_smem(reinterpret_cast<const void*>(kern), smem);
-    kern<<<blocks, threads, smem, st>>>(*b, epochs, rhs, hi, lo, d, u, counter);
+    kern<<<blocks, threads, smem, st>>>(*b, epochs, rhs, hi, lo, u, counter);
     return launch_status();
 }
 
@@ -737,14 +1016,14 @@ ODIL_API int odil_wave_batch_pair_residual_mixed(const odil_wave_batch* b, const
 }
 
 ODIL_API int odil_wave_batch_solve_mixed(const odil_wave_batch* b, int32_t epochs, float* rhs,
-                                         float* hi, float* lo, float* d, double* u,
+                                         float* hi, float* lo, double* u,
                                          int32_t threads, int32_t cpt, int32_t pf,
                                          int32_t blocks_per_sm, void* workspace,
                                          int64_t workspace_bytes, void* stream) {
     int st = check_batch(b);
     if (st) return st;
     if (epochs < 1 || epochs > 16) return ODIL_ERR_ARG;
-    if (!rhs || !hi || !u || (epochs > 1 && !lo) || (epochs > 2 && !d)) return ODIL_ERR_ARG;
+    if (!rhs || !hi || !u || (epochs > 1 && !lo)) return ODIL_ERR_ARG;
     if (!b->init_u || !b->init_ut || !b->left_u || !b->right_u) return ODIL_ERR_ARG;
     if (!workspace || workspace_bytes < 256) return ODIL_ERR_WORKSPACE;
     if (threads < 32 || threads > 1024 || threads % 32 || blocks_per_sm < 1 || blocks_per_sm > 32)
@@ -754,12 +1033,12 @@ ODIL_API int odil_wave_batch_solve_mixed(const odil_wave_batch* b, int32_t epoch
     unsigned* counter = reinterpret_cast<unsigned*>(workspace);
     cudaStream_t s = as_stream(stream);
     switch (cpt * 100 + pf) {
-        case 108: return launch_batch_solve<1, 8>(b, epochs, rhs, hi, lo, d, u, counter, threads, blocks, s);
-        case 116: return launch_batch_solve<1, 16>(b, epochs, rhs, hi, lo, d, u, counter, threads, blocks, s);
-        case 208: return launch_batch_solve<2, 8>(b, epochs, rhs, hi, lo, d, u, counter, threads, blocks, s);
-        case 216: return launch_batch_solve<2, 16>(b, epochs, rhs, hi, lo, d, u, counter, threads, blocks, s);
-        case 408: return launch_batch_solve<4, 8>(b, epochs, rhs, hi, lo, d, u, counter, threads, blocks, s);
-        case 416: return launch_batch_solve<4, 16>(b, epochs, rhs, hi, lo, d, u, counter, threads, blocks, s);
+        case 108: return launch_batch_solve<1, 8>(b, epochs, rhs, hi, lo, u, counter, threads, blocks, s);
+        case 116: return launch_batch_solve<1, 16>(b, epochs, rhs, hi, lo, u, counter, threads, blocks, s);
+        case 208: return launch_batch_solve<2, 8>(b, epochs, rhs, hi, lo, u, counter, threads, blocks, s);
+        case 216: return launch_batch_solve<2, 16>(b, epochs, rhs, hi, lo, u, counter, threads, blocks, s);
+        case 408: return launch_batch_solve<4, 8>(b, epochs, rhs, hi, lo, u, counter, threads, blocks, s);
+        case 416: return launch_batch_solve<4, 16>(b, epochs, rhs, hi, lo, u, counter, threads, blocks, s);
         default: return ODIL_ERR_SHAPE;
     }
 }

@@ -301,6 +301,20 @@ __device__ __forceinline__ float ld_iter(const float* p) {
     }
 }
 
+// -F(hi + lo) at an interior cell from its five stencil values (v: hi,
+// w: lo; rows i (0), i-2 (2), i-1 (1) at column j, row i-1 at j -+ 1).
+__device__ __forceinline__ float pair_rhs_vals(const PairCoef& k, float v0, float v2, float v1,
+                                               float vm, float vp, float w0, float w2, float w1,
+                                               float wm, float wp) {
+    float s = 0.f, c = 0.f;
+    pair_acc(k.ah, k.al, v0, w0, s, c);
+    pair_acc(k.ah, k.al, v2, w2, s, c);
+    pair_acc(k.ch, k.cl, v1, w1, s, c);
+    pair_acc(k.bh, k.bl, vm, wm, s, c);
+    pair_acc(k.bh, k.bl, vp, wp, s, c);
+    return -__fadd_rn(s, c);
+}
+
 // -F(hi + lo) at interior cell (i, j) rounded to FP32.  lo may be null.
 template <bool NC = true>
 __device__ __forceinline__ float pair_interior_rhs(const PairCoef& k, const float* __restrict__ hi,
@@ -317,13 +331,7 @@ __device__ __forceinline__ float pair_interior_rhs(const PairCoef& k, const floa
         wm = ld_iter<NC>(lo + c1 - 1);
         wp = ld_iter<NC>(lo + c1 + 1);
     }
-    float s = 0.f, c = 0.f;
-    pair_acc(k.ah, k.al, v0, w0, s, c);
-    pair_acc(k.ah, k.al, v2, w2, s, c);
-    pair_acc(k.ch, k.cl, v1, w1, s, c);
-    pair_acc(k.bh, k.bl, vm, wm, s, c);
-    pair_acc(k.bh, k.bl, vp, wp, s, c);
-    return -__fadd_rn(s, c);
+    return pair_rhs_vals(k, v0, v2, v1, vm, vp, w0, w2, w1, wm, wp);
 }
 
 // -F(hi + lo) at any cell: the float-pair form inside, FP64 wave_f on the

@@ -166,24 +166,34 @@ def test_batch_lbfgs_stage_then_newton_refinement(cuda):
     assert max(errs) <= 1e-5, max(errs)
 
 
-@pytest.mark.parametrize("sides", [(5, 70), (120, 300)])
+@pytest.mark.parametrize("sides", [(5, 70), (120, 300), (1, 4)])
 def test_batch_persistent_solve_equals_multi_launch(cuda, sides):
-    """The whole-batch mixed Newton in one persistent launch gives bitwise
-    the multi-launch sequence's solution for 1, 2 and 3 epochs, twice in a
-    row (the work queue resets itself), and meets the oracle."""
+    """The whole-batch mixed Newton in one persistent launch (right-hand
+    sides formed inside the marches) gives bitwise the multi-launch
+    sequence's solution for 1, 2 and 3 epochs, with every launch shape
+    (columns per thread 1, 2, 4; ring depth 8, 16), twice in a row (the work
+    queue resets itself), and meets the oracle."""
     from odil_gb300.batch import WaveBatch
     from odil_gb300.workloads import wave_batch_instances
     insts = _small_batch() if sides == (5, 70) else wave_batch_instances(
         count=10, seed=sides[1], nmin=sides[0], nmax=sides[1])
     b = WaveBatch(insts, device=cuda)
+    shapes = []
+    for cpt in (1, 2, 4):
+        threads = max(32, ((b.max_nx + cpt - 1) // cpt + 31) // 32 * 32)
+        for pf in (8, 16):
+            shapes.append({"threads": threads, "cpt": cpt, "pf": pf,
+                           "blocks_per_sm": 2})
     for ep in (1, 2, 3):
         ref = b.solve_mixed(epochs=ep).clone()
-        for _ in range(2):
-            b.u.fill_(float("nan"))
-            got = b.solve_persistent(epochs=ep)
-            assert torch.equal(got, ref), ep
-    for inst, u in zip(insts, b.unpack()):
-        assert W.rel_err(u, _oracle(inst)) <= 1e-8, (inst["nt"], inst["c"])
+        for cfg in shapes:
+            for _ in range(2):
+                b.u.fill_(float("nan"))
+                got = b.solve_persistent(epochs=ep, cfg=cfg)
+                assert torch.equal(got, ref), (ep, cfg)
+    if sides[0] > 1:
+        for inst, u in zip(insts, b.unpack()):
+            assert W.rel_err(u, _oracle(inst)) <= 1e-8, (inst["nt"], inst["c"])
 
 
 def test_full_batch_every_instance_meets_the_oracle(cuda):
