@@ -571,13 +571,16 @@ __global__ void __launch_bounds__(batch_solve_max_threads<CPT>()) batch_solve_ke
             }
             __syncthreads();
         };
+        // The first march (no stencil of an iterate) takes two columns per
+        // thread where the others take one: half the per-row overhead.
         auto march = [&](auto src_tag, auto last_tag, float* x) {
             constexpr int SRC = decltype(src_tag)::value;
             constexpr bool LAST = decltype(last_tag)::value;
-            if (nx % CPT == 0) {
-                fused_march<SRC, LAST, CPT, PF, true>(g32, k, tb, h, l, x, uo, sm);
+            constexpr int C = (SRC == 0 && CPT == 1) ? 2 : CPT;
+            if (nx % C == 0) {
+                fused_march<SRC, LAST, C, PF, true>(g32, k, tb, h, l, x, uo, sm);
             } else {
-                fused_march<SRC, LAST, CPT, PF, false>(g32, k, tb, h, l, x, uo, sm);
+                fused_march<SRC, LAST, C, PF, false>(g32, k, tb, h, l, x, uo, sm);
             }
         };
         using I0 = std::integral_constant<int, 0>;
