@@ -317,9 +317,10 @@ int odil_wave_batch_march_f32(const odil_wave_batch* b, const float* rhs,
  * odil_wave_batch_initial_rhs_mixed / _march_f32 / _pair_residual_mixed /
  * odil_pair_to_f64 run in that order.  rhs (the boundary tables), hi (and lo
  * for epochs >= 2): packed FP32 scratch; u: the packed FP64 solution.
- * Launch shape as odil_wave_batch_march_f32 (pf >= 8).  workspace: 256 bytes,
- * zeroed before the first call (the last block to finish leaves it zeroed
- * again); not shared with odil_wave_batch_march_f32.
+ * Launch shape as odil_wave_batch_march_f32, with (cpt, pf) in {(1, 8),
+ * (1, 16), (2, 8), (4, 8)} and threads <= 1024 (cpt 1) or 512.
+ * workspace: 256 bytes, zeroed before the first call (the last block to
+ * finish leaves it zeroed again); not shared with odil_wave_batch_march_f32.
  * util.py:242-268 per instance (the batched form of vary_wave.py:37-43). */
 int odil_wave_batch_solve_mixed(const odil_wave_batch* b, int32_t epochs,
                                 float* rhs, float* hi, float* lo,

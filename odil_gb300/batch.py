@@ -217,7 +217,7 @@ class WaveBatch:
             threads = max(32, ((self.max_nx + cpt - 1) // cpt + 31) // 32 * 32)
             if threads > (1024 if cpt == 1 else 512):
                 continue
-            for pf in (8, 16):
+            for pf in ((8, 16) if cpt == 1 else (8,)):
                 for b in per_sm:
                     if b * threads > 2048:
                         continue

@@ -1039,9 +1039,7 @@ ODIL_API int odil_wave_batch_solve_mixed(const odil_wave_batch* b, int32_t epoch
         case 108: return launch_batch_solve<1, 8>(b, epochs, rhs, hi, lo, u, counter, threads, blocks, s);
         case 116: return launch_batch_solve<1, 16>(b, epochs, rhs, hi, lo, u, counter, threads, blocks, s);
         case 208: return launch_batch_solve<2, 8>(b, epochs, rhs, hi, lo, u, counter, threads, blocks, s);
-        case 216: return launch_batch_solve<2, 16>(b, epochs, rhs, hi, lo, u, counter, threads, blocks, s);
         case 408: return launch_batch_solve<4, 8>(b, epochs, rhs, hi, lo, u, counter, threads, blocks, s);
-        case 416: return launch_batch_solve<4, 16>(b, epochs, rhs, hi, lo, u, counter, threads, blocks, s);
         default: return ODIL_ERR_SHAPE;
     }
 }
