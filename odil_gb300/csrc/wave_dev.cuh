@@ -273,20 +273,11 @@ __device__ __forceinline__ PairCoef pair_coef_dev(double A, double B) {
     return k;
 }
 
-// s + c += (ch + cl) * (v + w): exact hi product, two-sum into s, the
-// rounding errors and small products into c.  Explicit _rn intrinsics keep
-// the compiler from contracting the two-sum into an FMA.
-__device__ __forceinline__ void pair_acc(float ch, float cl, float v, float w, float& s,
-                                         float& c) {
-    const float p = __fmul_rn(ch, v);
-    const float e = __fmaf_rn(ch, v, -p);
-    const float t = __fadd_rn(s, p);
-    const float bp = __fsub_rn(t, s);
-    const float err = __fadd_rn(__fsub_rn(s, __fsub_rn(t, bp)), __fsub_rn(p, bp));
-    s = t;
-    c = __fadd_rn(c, __fadd_rn(err, e));
-    c = __fmaf_rn(cl, v, c);
-    c = __fmaf_rn(ch, w, c);
+// Rounding error of s = fl(a + b) (Knuth's two-sum): a + b = s + err
+// exactly.  Explicit _rn intrinsics keep the compiler from contracting it.
+__device__ __forceinline__ float two_sum_err(float a, float b, float s) {
+    const float bb = __fsub_rn(s, a);
+    return __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
 }
 
 // Load of an iterate value: read-only path (NC, the iterate is another
@@ -302,17 +293,33 @@ __device__ __forceinline__ float ld_iter(const float* p) {
 }
 
 // -F(hi + lo) at an interior cell from its five stencil values (v: hi,
-// w: lo; rows i (0), i-2 (2), i-1 (1) at column j, row i-1 at j -+ 1).
+// w: lo; rows i (0), i-2 (2), i-1 (1) at column j, row i-1 at j -+ 1),
+// F = A (u0 + u2) + C u1 - B (um + up) with A, C, -B as float pairs.  The
+// two sums sharing a coefficient are formed exactly (value + two-sum
+// error), the three hi-coefficient products exactly (product + FMA
+// error), and the products summed by two-sums; every rounding error and
+// the first-order small terms (lo coefficients, the sums' errors, w) go
+// into one compensation c.  Error ~2^-46 of the largest term.
 __device__ __forceinline__ float pair_rhs_vals(const PairCoef& k, float v0, float v2, float v1,
                                                float vm, float vp, float w0, float w2, float w1,
                                                float wm, float wp) {
-    float s = 0.f, c = 0.f;
-    pair_acc(k.ah, k.al, v0, w0, s, c);
-    pair_acc(k.ah, k.al, v2, w2, s, c);
-    pair_acc(k.ch, k.cl, v1, w1, s, c);
-    pair_acc(k.bh, k.bl, vm, wm, s, c);
-    pair_acc(k.bh, k.bl, vp, wp, s, c);
-    return -__fadd_rn(s, c);
+    const float a = __fadd_rn(v0, v2), ea = two_sum_err(v0, v2, a);
+    const float b = __fadd_rn(vm, vp), eb = two_sum_err(vm, vp, b);
+    const float p1 = __fmul_rn(k.ah, a), e1 = __fmaf_rn(k.ah, a, -p1);
+    const float p2 = __fmul_rn(k.ch, v1), e2 = __fmaf_rn(k.ch, v1, -p2);
+    const float p3 = __fmul_rn(k.bh, b), e3 = __fmaf_rn(k.bh, b, -p3);
+    const float s = __fadd_rn(p1, p2), es = two_sum_err(p1, p2, s);
+    const float t = __fadd_rn(s, p3), et = two_sum_err(s, p3, t);
+    float c = __fadd_rn(__fadd_rn(__fadd_rn(es, et), __fadd_rn(e1, e2)), e3);
+    c = __fmaf_rn(k.al, a, c);
+    c = __fmaf_rn(k.cl, v1, c);
+    c = __fmaf_rn(k.bl, b, c);
+    c = __fmaf_rn(k.ah, ea, c);
+    c = __fmaf_rn(k.bh, eb, c);
+    c = __fmaf_rn(k.ah, __fadd_rn(w0, w2), c);
+    c = __fmaf_rn(k.ch, w1, c);
+    c = __fmaf_rn(k.bh, __fadd_rn(wm, wp), c);
+    return -__fadd_rn(t, c);
 }
 
 // -F(hi + lo) at interior cell (i, j) rounded to FP32.  lo may be null.

@@ -37,3 +37,14 @@ def cuda(built_lib):
     from odil_gb300 import _capi
     _capi.load()
     return torch.device("cuda:0")
+
+
+@pytest.fixture(autouse=True)
+def _drain_gpu_work(request):
+    """A GPU test ends with its device work finished, so no kernel of one
+    test still runs when the next one allocates (stream-ordered memory
+    reuse across tests)."""
+    yield
+    if "cuda" in request.fixturenames:
+        import torch
+        torch.cuda.synchronize()
