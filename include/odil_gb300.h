@@ -163,6 +163,17 @@ int odil_wave_update_residual_mixed(const odil_wave_params* p, const double* u,
  * Part of the Newton step of util.py:242-268 (-F at the start state). */
 int odil_wave_initial_rhs_mixed(const odil_wave_params* p, float* rhs,
                                 void* stream);
+/* Number of boundary cells of the grid (rows 0 and 1, then columns 0 and
+ * nx-1 of each further row): the length of the table below.
+ * No counterpart in the reference (a size query). */
+int64_t odil_wave_boundary_cells(const odil_wave_params* p);
+/* tbl = (float)(-F(0)) at the boundary cells only, in the order above (rows
+ * 0 and 1 in full, then column 0 and column nx-1 of each row from 2): the
+ * input of odil_wave_march_tiled_table_f32, which takes the interior as
+ * zero.  Same values as odil_wave_initial_rhs_mixed at those cells.
+ * Part of the Newton step of util.py:242-268 (-F at the start state). */
+int odil_wave_initial_table_mixed(const odil_wave_params* p, float* tbl,
+                                  void* stream);
 /* rhs = (float)(-F(hi + lo)) for a field held as the unevaluated sum of two
  * FP32 arrays (lo may be NULL): the right-hand side of a mixed Newton epoch
  * whose iterate is kept as FP32 corrections, without an FP64 state.
@@ -201,6 +212,15 @@ int odil_wave_march_tiled_f32(const odil_wave_params* p, const float* b,
 int odil_wave_march_tiled_f64(const odil_wave_params* p, const double* b,
                               double* x, int32_t cpt, int32_t halo, int32_t pf,
                               int32_t warps, int32_t exchange, void* stream);
+/* odil_wave_march_tiled_f32 of the first correction from u = 0, reading the
+ * boundary table of odil_wave_initial_table_mixed instead of a full
+ * right-hand side (zero inside): bitwise the result of
+ * odil_wave_initial_rhs_mixed followed by odil_wave_march_tiled_f32.
+ * The direct solve of linsolver.py:35-45 on the first Newton step. */
+int odil_wave_march_tiled_table_f32(const odil_wave_params* p,
+                                    const float* tbl, float* x, int32_t cpt,
+                                    int32_t halo, int32_t pf, int32_t warps,
+                                    int32_t exchange, void* stream);
 /* Test hook of the bounded halo wait: odil_wave_march_tiled_f32 with
  * exchange 1 whose every wait expects `missing_bytes` (1..65536) more than
  * ever arrive, so each wait gives up after its limit. */

@@ -165,6 +165,10 @@ SIGNATURES = {
     "odil_wave_march_f32": (_INT, [_P, _P, _P, _P]),
     "odil_wave_march_f64": (_INT, [_P, _P, _P, _P]),
     "odil_wave_initial_rhs_mixed": (_INT, [_P, _P, _P]),
+    "odil_wave_boundary_cells": (_I64, [_P]),
+    "odil_wave_initial_table_mixed": (_INT, [_P, _P, _P]),
+    "odil_wave_march_tiled_table_f32": (_INT, [_P, _P, _P]
+                                        + [ctypes.c_int32] * 5 + [_P]),
     "odil_wave_march_shape_f32": (_INT, [_P, _P, _P, ctypes.c_int32,
                                          ctypes.c_int32, _P]),
     "odil_wave_march_tiled_f32": (_INT, [_P, _P, _P] + [ctypes.c_int32] * 5

@@ -763,7 +763,8 @@ __global__ void __launch_bounds__(256) wave_bnd_rhs_kernel(WaveDev<double> g, Pa
 __global__ void __launch_bounds__(256) wave_initial_rhs_kernel(WaveDev<double> g,
                                                                float* __restrict__ rhs,
                                                                int64_t count, int nbb) {
-    pdl_trigger();
+    // The dependent march (programmatic launch) is released only after this
+    // thread's writes (a thread that returns early releases at its exit).
     if ((int)blockIdx.x < nbb) {
         const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
         if (t >= count) return;
@@ -771,6 +772,7 @@ __global__ void __launch_bounds__(256) wave_initial_rhs_kernel(WaveDev<double> g
         bnd_cell(t, g.nt, g.nx, &i, &j);
         const PairCoef k{};
         rhs[(int64_t)i * g.nx + j] = bnd_cell_rhs<0>(g, k, nullptr, nullptr, i, j);
+        pdl_trigger();
         return;
     }
     const int w = g.nx - 2;
@@ -781,6 +783,23 @@ __global__ void __launch_bounds__(256) wave_initial_rhs_kernel(WaveDev<double> g
         const int64_t r = t / w;
         rhs[(r + 2) * g.nx + 1 + (t - r * w)] = 0.f;
     }
+    pdl_trigger();
+}
+
+// Only the boundary cells of rhs = float(-F(0)), compactly in the bnd_cell
+// order (rows 0 and 1, then columns 0 and nx-1 of each further row): the
+// table a march from zero reads in place of the full right-hand side, whose
+// interior is zero.  64-thread blocks spread the FP64 work over the SMs.
+__global__ void __launch_bounds__(64) wave_initial_table_kernel(WaveDev<double> g,
+                                                               float* __restrict__ tbl,
+                                                               int64_t count) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= count) return;
+    int i, j;
+    bnd_cell(t, g.nt, g.nx, &i, &j);
+    const PairCoef k{};
+    tbl[t] = bnd_cell_rhs<0>(g, k, nullptr, nullptr, i, j);
+    pdl_trigger();  // the dependent march is released after the write
 }
 
 template <int CPT, int PF>
@@ -919,6 +938,22 @@ ODIL_API int odil_wave_initial_rhs_mixed(const odil_wave_params* p, float* rhs, 
     int64_t nzb = (interior + 255) / 256;
     if (nzb > 4 * 152) nzb = 4 * 152;  // grid-stride beyond this
     wave_initial_rhs_kernel<<<(unsigned)(nbb + nzb), 256, 0, s>>>(g, rhs, nb, nbb);
+    return launch_status();
+}
+
+ODIL_API int64_t odil_wave_boundary_cells(const odil_wave_params* p) {
+    if (!p || p->nt < 1 || p->nx < 1) return 0;
+    return bnd_count((int)p->nt, (int)p->nx);
+}
+
+ODIL_API int odil_wave_initial_table_mixed(const odil_wave_params* p, float* tbl, void* stream) {
+    WaveDev<double> g;
+    int st = make_dev<double>(p, &g, true);
+    if (st) return st;
+    if (!tbl) return ODIL_ERR_ARG;
+    const int64_t nb = bnd_count(g.nt, g.nx);
+    wave_initial_table_kernel<<<(unsigned)((nb + 63) / 64), 64, 0, as_stream(stream)>>>(g, tbl,
+                                                                                     nb);
     return launch_status();
 }
 

@@ -182,7 +182,12 @@ __device__ __forceinline__ void cluster_sync_all() {
 // only wait for their neighbours, and the solution stores need no fence.
 // `extra_wait` adds bytes that never arrive to every wait (a planted
 // failure for the bounded-wait test; 0 otherwise).
-template <typename T, int CPT, int H, int PF, bool VEC, bool DSMEM>
+// TBL (march from u = 0): b is the boundary table of -F(0) in the bnd_cell
+// order (rows 0 and 1, then columns 0 and nx-1 of each further row); the
+// right-hand side is zero elsewhere, so rows 2.. load only the two edge
+// entries (the lanes holding columns 0 and nx-1) and the full right-hand
+// side is never written or read.
+template <typename T, int CPT, int H, int PF, bool VEC, bool DSMEM, bool TBL = false>
 __global__ void __launch_bounds__(32 * kTiledMaxWarps) wave_march_tiled_kernel(
     WaveDev<T> g, const T* __restrict__ b, T* __restrict__ x, uint32_t extra_wait) {
     constexpr int O = 32 * CPT - 2 * H;  // owned columns per warp
@@ -221,26 +226,51 @@ __global__ void __launch_bounds__(32 * kTiledMaxWarps) wave_march_tiled_kernel(
     pdl_wait();
     const T* src = b + j0;  // row `next` of the right-hand side
     int next = 0;
-    auto issue = [&](auto checked, int slot) {
-        if (!decltype(checked)::value || next < nt) {
-            if constexpr (VEC) {
-                if (any_in) ld_cols<T, CPT>(pre[slot], src);
-            } else {
+    // TBL: the lane's column-table entry of row `next` (entries 2 (r - 2)
+    // and 2 (r - 2) + 1 hold columns 0 and nx - 1 of row r >= 2; nx >= 2),
+    // for the lane holding that column, and which of its columns it is.
+    bool e_b[CPT];
+    int toff = 0;
 #pragma unroll
-                for (int c = 0; c < CPT; ++c) pre[slot][c] = in[c] ? __ldg(src + c) : T(0);
+    for (int c = 0; c < CPT; ++c) {
+        e_b[c] = TBL && (j0 + c == 0 || j0 + c == nx - 1);
+        if (TBL && j0 + c == nx - 1) toff = 1;
+    }
+    const T* tcol = b + 2 * (int64_t)nx + toff;
+    // HEAD: the prefetch before the first row (rows 0 .. PF - 2, which hold
+    // rows 0 and 1); every later issue is of a row >= PF - 1 >= 2, so with
+    // TBL it takes only the table-entry path (no branch in the row bodies).
+    static_assert(PF >= 3, "rows 0 and 1 are prefetched ahead of the march");
+    auto issue = [&](auto checked, int slot, auto head) {
+        constexpr bool HEAD = decltype(head)::value;
+        if (!decltype(checked)::value || next < nt) {
+            if (!TBL || (HEAD && next < 2)) {
+                if constexpr (VEC) {
+                    if (any_in) ld_cols<T, CPT>(pre[slot], src);
+                } else {
+#pragma unroll
+                    for (int c = 0; c < CPT; ++c) pre[slot][c] = in[c] ? __ldg(src + c) : T(0);
+                }
+            } else {
+                // Every lane loads (one or two addresses per warp, no
+                // divergence); only the boundary column keeps the value.
+                const T v = __ldg(tcol);
+#pragma unroll
+                for (int c = 0; c < CPT; ++c) pre[slot][c] = e_b[c] ? v : T(0);
+                tcol += 2;
             }
         }
         src += nx;
         ++next;
     };
 #pragma unroll
-    for (int q = 0; q < PF - 1; ++q) issue(std::true_type{}, q);
+    for (int q = 0; q < PF - 1; ++q) issue(std::true_type{}, q, std::true_type{});
     T* dst = x + j0;  // solution row i
     // One row: FIRST for rows 0 and 1 of J (identity row; no u[i-2] term),
     // CHECKED where the prefetch may pass the last row.
     auto row = [&](auto first, auto checked, int i, int s) {
         constexpr bool FIRST = decltype(first)::value;
-        issue(checked, (s + PF - 1) % PF);
+        issue(checked, (s + PF - 1) % PF, std::false_type{});
         const T c_rhs = FIRST && i == 0 ? T(1) : dt2;
         const T c_d1 = FIRST && i == 1 ? T(1) : T(2);
         const T c_lam = FIRST && i == 0 ? T(0) : lam;
@@ -455,7 +485,7 @@ int tiled_launch(const void* kern, int clusters, int warps, const WaveDev<T>& g,
 
 template <typename T, int CPT, int H, int PF, bool DSMEM>
 int tiled_shape_fit(const WaveDev<T>& g, const T* b, T* x, int warps, uint32_t extra_wait,
-                    cudaStream_t st) {
+                    bool table, cudaStream_t st) {
     constexpr int O = 32 * CPT - 2 * H;
     const int64_t tiles = (g.nx + O - 1) / O;
     if (warps < 1 || warps > kTiledMaxWarps) return ODIL_ERR_SHAPE;
@@ -468,17 +498,27 @@ int tiled_shape_fit(const WaveDev<T>& g, const T* b, T* x, int warps, uint32_t e
     const void* kern =
         vec ? reinterpret_cast<const void*>(wave_march_tiled_kernel<T, CPT, H, PF, true, DSMEM>)
             : reinterpret_cast<const void*>(wave_march_tiled_kernel<T, CPT, H, PF, false, DSMEM>);
+    if (table) {  // FP32 only (the mixed solve from zero)
+        if constexpr (sizeof(T) == 4) {
+            kern = vec ? reinterpret_cast<const void*>(
+                             wave_march_tiled_kernel<T, CPT, H, PF, true, DSMEM, true>)
+                       : reinterpret_cast<const void*>(
+                             wave_march_tiled_kernel<T, CPT, H, PF, false, DSMEM, true>);
+        } else {
+            return ODIL_ERR_ARG;
+        }
+    }
     return tiled_launch<T>(kern, (int)clusters, warps, g, b, x, extra_wait, st);
 }
 
 template <typename T, int CPT, int H, int PF, bool DSMEM>
 int tiled_shape(const WaveDev<T>& g, const T* b, T* x, int warps, uint32_t extra_wait,
-                cudaStream_t st) {
+                bool table, cudaStream_t st) {
     // A ring above 512 bytes per thread spills (FP64 with cpt pf > 64).
     if constexpr (CPT * PF * sizeof(T) > 512) {
         return ODIL_ERR_SHAPE;
     } else {
-        return tiled_shape_fit<T, CPT, H, PF, DSMEM>(g, b, x, warps, extra_wait, st);
+        return tiled_shape_fit<T, CPT, H, PF, DSMEM>(g, b, x, warps, extra_wait, table, st);
     }
 }
 
@@ -487,7 +527,8 @@ int tiled_shape(const WaveDev<T>& g, const T* b, T* x, int warps, uint32_t extra
 // neighbours' shared memory, needs 32 cpt - 2 halo >= halo).
 template <typename T>
 int tiled_dispatch(const odil_wave_params* p, const T* b, T* x, int cpt, int halo, int pf,
-                   int warps, int exchange, uint32_t extra_wait, void* stream) {
+                   int warps, int exchange, uint32_t extra_wait, void* stream,
+                   bool table = false) {
     WaveDev<T> g;
     int st = make_dev<T>(p, &g, false);
     if (st) return st;
@@ -499,16 +540,16 @@ int tiled_dispatch(const odil_wave_params* p, const T* b, T* x, int cpt, int hal
     cudaStream_t s = as_stream(stream);
     const uint32_t e = extra_wait;
     switch (exchange * 1000000 + cpt * 10000 + halo * 100 + pf) {
-        case 43216: return tiled_shape<T, 4, 32, 16, false>(g, b, x, warps, e, s);
-        case 44816: return tiled_shape<T, 4, 48, 16, false>(g, b, x, warps, e, s);
-        case 89616: return tiled_shape<T, 8, 96, 16, false>(g, b, x, warps, e, s);
-        case 1021616: return tiled_shape<T, 2, 16, 16, true>(g, b, x, warps, e, s);
-        case 1040808: return tiled_shape<T, 4, 8, 8, true>(g, b, x, warps, e, s);
-        case 1041616: return tiled_shape<T, 4, 16, 16, true>(g, b, x, warps, e, s);
-        case 1042408: return tiled_shape<T, 4, 24, 8, true>(g, b, x, warps, e, s);
-        case 1043216: return tiled_shape<T, 4, 32, 16, true>(g, b, x, warps, e, s);
-        case 1083216: return tiled_shape<T, 8, 32, 16, true>(g, b, x, warps, e, s);
-        case 1086416: return tiled_shape<T, 8, 64, 16, true>(g, b, x, warps, e, s);
+        case 43216: return tiled_shape<T, 4, 32, 16, false>(g, b, x, warps, e, table, s);
+        case 44816: return tiled_shape<T, 4, 48, 16, false>(g, b, x, warps, e, table, s);
+        case 89616: return tiled_shape<T, 8, 96, 16, false>(g, b, x, warps, e, table, s);
+        case 1021616: return tiled_shape<T, 2, 16, 16, true>(g, b, x, warps, e, table, s);
+        case 1040808: return tiled_shape<T, 4, 8, 8, true>(g, b, x, warps, e, table, s);
+        case 1041616: return tiled_shape<T, 4, 16, 16, true>(g, b, x, warps, e, table, s);
+        case 1042408: return tiled_shape<T, 4, 24, 8, true>(g, b, x, warps, e, table, s);
+        case 1043216: return tiled_shape<T, 4, 32, 16, true>(g, b, x, warps, e, table, s);
+        case 1083216: return tiled_shape<T, 8, 32, 16, true>(g, b, x, warps, e, table, s);
+        case 1086416: return tiled_shape<T, 8, 64, 16, true>(g, b, x, warps, e, table, s);
         default: return ODIL_ERR_SHAPE;
     }
 }
@@ -522,6 +563,12 @@ ODIL_API int odil_wave_march_tiled_f32(const odil_wave_params* p, const float* b
                                        int32_t cpt, int32_t halo, int32_t pf, int32_t warps,
                                        int32_t exchange, void* stream) {
     return tiled_dispatch<float>(p, b, x, cpt, halo, pf, warps, exchange, 0u, stream);
+}
+
+ODIL_API int odil_wave_march_tiled_table_f32(const odil_wave_params* p, const float* tbl,
+                                             float* x, int32_t cpt, int32_t halo, int32_t pf,
+                                             int32_t warps, int32_t exchange, void* stream) {
+    return tiled_dispatch<float>(p, tbl, x, cpt, halo, pf, warps, exchange, 0u, stream, true);
 }
 
 ODIL_API int odil_wave_march_tiled_f64(const odil_wave_params* p, const double* b, double* x,

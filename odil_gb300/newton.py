@@ -118,8 +118,11 @@ def _solve_pairs(k, u, rhs, d, epochs, rnorm2):
     """Mixed Newton from u = 0 with the iterate kept as FP32 hi + lo."""
     hi = _scratch(k, "hi32", torch.float32)
     lo = _scratch(k, "lo32", torch.float32)
-    k.initial_rhs(rhs)
-    k.march_tuned(rhs, hi)
+    if hasattr(k, "march_from_zero"):
+        k.march_from_zero(hi, rhs)
+    else:
+        k.initial_rhs(rhs)
+        k.march_tuned(rhs, hi)
     have_lo = False
     for _ in range(1, epochs):
         k.pair_residual(hi, lo if have_lo else None, rhs)

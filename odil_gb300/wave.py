@@ -235,6 +235,35 @@ class WaveKernels:
              stream_handle())
         return rhs
 
+    def initial_table(self, tbl):
+        """tbl[:n] = float32(-F(0)) at the n boundary cells (rows 0 and 1,
+        then columns 0 and nx-1 of each further row), FP64 work only."""
+        call("odil_wave_initial_table_mixed", ctypes.byref(self.p64), ptr(tbl),
+             stream_handle())
+        return tbl
+
+    def march_from_zero(self, out, rhs):
+        """out = J^-1 float32(-F(0)), the first correction of a mixed solve
+        from u = 0, with the tuned FP32 march shape.  A cluster-tiled shape
+        reads only the boundary table of -F(0) (written at the start of
+        ``rhs``; the zero interior is neither stored nor loaded); the
+        single-block march gets the full right-hand side in ``rhs``.  The
+        result is bitwise the same either way."""
+        tuned = self.__dict__.setdefault("_march_cfgs", {})
+        if torch.float32 not in tuned:
+            from . import autotune
+            tuned[torch.float32] = autotune.tune_march(self, dtype=torch.float32)
+        cfg = tuned[torch.float32]
+        if cfg.get("kind") == "tiled":
+            self.initial_table(rhs)
+            call("odil_wave_march_tiled_table_f32", ctypes.byref(self.p32),
+                 ptr(rhs), ptr(out), int(cfg["cpt"]), int(cfg["halo"]),
+                 int(cfg["pf"]), int(cfg["warps"]), int(cfg.get("exchange", 0)),
+                 stream_handle())
+            return out
+        self.initial_rhs(rhs)
+        return self.march_shape(rhs, out, cfg)
+
     # Shifts (t, x) of the Jacobian's five slots (see wave.cu).
     SLOT_SHIFTS = ((0, 0), (-1, 0), (-2, 0), (-1, -1), (-1, 1))
 

@@ -569,3 +569,52 @@ def test_jtj_v_and_diag(cuda, shape):
     dref = (Jd**2).sum(0).reshape(shape)
     assert _rel(k.jtj_diag().cpu().numpy(), dref) < 1e-14
     assert _rel(k.jtj_diag(torch.float32).cpu().numpy(), dref) < 1e-6
+
+
+@pytest.mark.parametrize("nt,nx", [(1024, 1024), (800, 1000), (700, 777),
+                                   (2, 64), (97, 130)])
+def test_table_march_from_zero_equals_full_rhs(cuda, nt, nx):
+    """The first correction from u = 0 marched from the boundary table of
+    -F(0) (the zero interior neither stored nor loaded) is bitwise the march
+    of the full right-hand side, for every cluster-tiled launch shape; the
+    table holds the full right-hand side's boundary cells in order.  Shapes
+    keep the Courant number c nx / (2 nt) below the march's stability limit
+    (~0.93), so the solutions are finite."""
+    import ctypes
+    from odil_gb300 import autotune, _capi
+    from odil_gb300._capi import call, ptr, stream_handle
+    s = _setup(nt, nx, seed=4)
+    k = _kernels(s, cuda)
+    rhs = torch.empty((nt, nx), dtype=torch.float32, device=cuda)
+    k.initial_rhs(rhs)
+    nb = _capi.load().odil_wave_boundary_cells(ctypes.byref(k.p64))
+    rows = [(i, j) for i in range(min(nt, 2)) for j in range(nx)]
+    rows += [(i, j) for i in range(2, nt) for j in (0, nx - 1)]
+    assert nb == len(rows)
+    tbl = torch.full((nt * nx, ), float("nan"), dtype=torch.float32,
+                     device=cuda)
+    call("odil_wave_initial_table_mixed", ctypes.byref(k.p64), ptr(tbl),
+         stream_handle())
+    ii, jj = (torch.as_tensor(v, device=cuda) for v in zip(*rows))
+    assert torch.equal(tbl[:nb], rhs[ii, jj])
+    tried = 0
+    for cfg in autotune.candidates_march(nx, torch.float32):
+        if cfg["kind"] != "tiled":
+            continue
+        x1 = torch.full_like(rhs, float("nan"))
+        x2 = torch.full_like(rhs, float("nan"))
+        try:
+            k.march_shape(rhs, x1, cfg)
+        except _capi.OdilError:
+            continue  # the cluster does not fit
+        call("odil_wave_march_tiled_table_f32", ctypes.byref(k.p32), ptr(tbl),
+             ptr(x2), cfg["cpt"], cfg["halo"], cfg["pf"], cfg["warps"],
+             cfg["exchange"], stream_handle())
+        assert torch.equal(x1, x2), cfg
+        tried += 1
+    assert tried > 0
+    assert torch.isfinite(x1).all()
+    # The tuned entry point, whichever kind of march it picked.
+    x3 = torch.empty_like(rhs)
+    k.march_from_zero(x3, torch.empty_like(rhs))
+    assert torch.equal(x3, k.march_tuned(rhs, torch.empty_like(rhs)))
