@@ -242,6 +242,18 @@ class WaveKernels:
              stream_handle())
         return tbl
 
+    def march_table(self, tbl, out):
+        """out = J^-1 b for b = 0 except the boundary table ``tbl`` (see
+        initial_table), with the tuned cluster-tiled FP32 shape."""
+        cfg = self.__dict__.get("_march_cfgs", {}).get(torch.float32)
+        if not cfg or cfg.get("kind") != "tiled":
+            raise ValueError("the table march needs a tuned cluster-tiled shape")
+        call("odil_wave_march_tiled_table_f32", ctypes.byref(self.p32),
+             ptr(tbl), ptr(out), int(cfg["cpt"]), int(cfg["halo"]),
+             int(cfg["pf"]), int(cfg["warps"]), int(cfg.get("exchange", 0)),
+             stream_handle())
+        return out
+
     def march_from_zero(self, out, rhs):
         """out = J^-1 float32(-F(0)), the first correction of a mixed solve
         from u = 0, with the tuned FP32 march shape.  A cluster-tiled shape
@@ -256,11 +268,7 @@ class WaveKernels:
         cfg = tuned[torch.float32]
         if cfg.get("kind") == "tiled":
             self.initial_table(rhs)
-            call("odil_wave_march_tiled_table_f32", ctypes.byref(self.p32),
-                 ptr(rhs), ptr(out), int(cfg["cpt"]), int(cfg["halo"]),
-                 int(cfg["pf"]), int(cfg["warps"]), int(cfg.get("exchange", 0)),
-                 stream_handle())
-            return out
+            return self.march_table(rhs, out)
         self.initial_rhs(rhs)
         return self.march_shape(rhs, out, cfg)
 
