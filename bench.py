@@ -992,13 +992,13 @@ def run_ours(args):
     h2d = sum(b.numel() * 8 for b in bc_host)
     d2h = out_host.numel() * 8
 
-    # newton.CapturedSolve: new boundary data H2D (and its FP32 copies),
-    # the solve, the solution D2H into pinned host memory, replayed as one
-    # CUDA graph per step.
+    # newton.CapturedSolve: new boundary data H2D, the solve, the solution
+    # D2H into pinned host memory, replayed as one CUDA graph per step.  The
+    # mixed solve reads the boundary data only in FP64 (its FP32 kernels,
+    # the marches, take none), so the FP32 copies are not refreshed.
     cap = newton.CapturedSolve(
         problem, state, "mixed", MIXED_EPOCHS,
-        inputs=list(zip(bc_host, k.bc64)) + list(zip(k.bc64, k.bc32)),
-        host_out=out_host)
+        inputs=list(zip(bc_host, k.bc64)), host_out=out_host)
     t_e2e = timed(cap, args.steps, args.warmup)
     if with_oracle:
         e2e_u = out_host.numpy().copy()
