@@ -618,3 +618,37 @@ def test_table_march_from_zero_equals_full_rhs(cuda, nt, nx):
     x3 = torch.empty_like(rhs)
     k.march_from_zero(x3, torch.empty_like(rhs))
     assert torch.equal(x3, k.march_tuned(rhs, torch.empty_like(rhs)))
+
+
+def test_captured_table_solve_follows_new_inputs_1024(cuda):
+    """The headline solve (1024^2, one mixed epoch: boundary table, table
+    march, FP64 write, each kernel released by the one before it) replayed
+    from a CUDA graph with new boundary data every replay equals the eager
+    solve of that data bitwise: no kernel reads its predecessor's output
+    from the previous replay."""
+    from odil_gb300 import newton
+    from odil_gb300.domain import State
+    from odil_gb300.problem import Problem
+    from odil_gb300.workloads import WaveInstance
+    n = 1024
+    inst = WaveInstance(n, n, profile="sine", seed=1, nmodes=16, device=cuda)
+    prob = Problem(inst.operator, inst.domain)
+    k = prob.kernels
+    u = torch.zeros((n, n), dtype=torch.float64, device=cuda)
+    host = [k.bc64[i].cpu().pin_memory() for i in range(4)]
+    out = torch.empty((n, n), dtype=torch.float64).pin_memory()
+    cap = newton.CapturedSolve(prob, State(fields={"u": u}), "mixed", 1,
+                               inputs=list(zip(host, k.bc64)),
+                               outputs=[(u, out)])
+    for scale in (1.0, -0.5, 2.0, -1.0):
+        for h in host:
+            h.mul_(scale)
+        cap()
+        torch.cuda.synchronize()
+        got = out.clone()
+        ref = torch.zeros_like(u)
+        for h, d in zip(host, k.bc64):
+            d.copy_(h)
+        newton.solve(prob, State(fields={"u": ref}), "mixed", 1,
+                     from_zero=True)
+        assert torch.equal(got, ref.cpu()), scale
