@@ -216,6 +216,7 @@ int odil_wave_march_tiled_f64(const odil_wave_params* p, const double* b,
  * boundary table of odil_wave_initial_table_mixed instead of a full
  * right-hand side (zero inside): bitwise the result of
  * odil_wave_initial_rhs_mixed followed by odil_wave_march_tiled_f32.
+ * Needs nx > cpt (ODIL_ERR_SHAPE otherwise).
  * The direct solve of linsolver.py:35-45 on the first Newton step. */
 int odil_wave_march_tiled_table_f32(const odil_wave_params* p,
                                     const float* tbl, float* x, int32_t cpt,

@@ -534,6 +534,8 @@ int tiled_dispatch(const odil_wave_params* p, const T* b, T* x, int cpt, int hal
     if (st) return st;
     if (!b || !x) return ODIL_ERR_ARG;
     if (g.nx < 2) return ODIL_ERR_SHAPE;
+    // Table mode: a lane holds at most one of columns 0 and nx - 1.
+    if (table && g.nx <= cpt) return ODIL_ERR_SHAPE;
     if (cpt < 1 || cpt > 9 || halo < 1 || halo > 99 || pf < 1 || pf > 99 || exchange < 0 ||
         exchange > 1)
         return ODIL_ERR_SHAPE;

@@ -266,7 +266,7 @@ class WaveKernels:
             from . import autotune
             tuned[torch.float32] = autotune.tune_march(self, dtype=torch.float32)
         cfg = tuned[torch.float32]
-        if cfg.get("kind") == "tiled":
+        if cfg.get("kind") == "tiled" and self.nx > cfg["cpt"]:
             self.initial_table(rhs)
             return self.march_table(rhs, out)
         self.initial_rhs(rhs)

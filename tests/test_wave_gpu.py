@@ -572,7 +572,7 @@ def test_jtj_v_and_diag(cuda, shape):
 
 
 @pytest.mark.parametrize("nt,nx", [(1024, 1024), (800, 1000), (700, 777),
-                                   (2, 64), (97, 130)])
+                                   (2, 64), (97, 130), (12, 6)])
 def test_table_march_from_zero_equals_full_rhs(cuda, nt, nx):
     """The first correction from u = 0 marched from the boundary table of
     -F(0) (the zero interior neither stored nor loaded) is bitwise the march
@@ -607,14 +607,24 @@ def test_table_march_from_zero_equals_full_rhs(cuda, nt, nx):
             k.march_shape(rhs, x1, cfg)
         except _capi.OdilError:
             continue  # the cluster does not fit
-        call("odil_wave_march_tiled_table_f32", ctypes.byref(k.p32), ptr(tbl),
-             ptr(x2), cfg["cpt"], cfg["halo"], cfg["pf"], cfg["warps"],
-             cfg["exchange"], stream_handle())
+        try:
+            call("odil_wave_march_tiled_table_f32", ctypes.byref(k.p32),
+                 ptr(tbl), ptr(x2), cfg["cpt"], cfg["halo"], cfg["pf"],
+                 cfg["warps"], cfg["exchange"], stream_handle())
+        except _capi.OdilError:
+            # A lane would hold both edge columns: refused, and the solve
+            # from zero takes the full right-hand side instead.
+            assert nx <= cfg["cpt"], cfg
+            k._march_cfgs = {torch.float32: cfg}
+            x3 = k.march_from_zero(torch.empty_like(rhs), torch.empty_like(rhs))
+            assert torch.equal(x1, x3), cfg
+            continue
         assert torch.equal(x1, x2), cfg
         tried += 1
     assert tried > 0
     assert torch.isfinite(x1).all()
     # The tuned entry point, whichever kind of march it picked.
+    k._march_cfgs = {}
     x3 = torch.empty_like(rhs)
     k.march_from_zero(x3, torch.empty_like(rhs))
     assert torch.equal(x3, k.march_tuned(rhs, torch.empty_like(rhs)))
