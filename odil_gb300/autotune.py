@@ -56,13 +56,13 @@ def default_batch_march(max_nx):
 
 
 def default_batch_solve(max_nx):
-    """Heuristic shape of the persistent whole-batch solve: one column per
-    thread while a block holds the row (up to 1024 columns; more warps hide
-    the per-row latency), else 4 (at most 512 threads with more than one
-    column), 8 ring rows, 2 blocks per SM."""
-    cpt = 1 if max_nx <= 1024 else 4
+    """Heuristic shape of the persistent whole-batch solve: two columns per
+    thread up to 1024 columns, else 4 (at most 512 threads with more than
+    one column), 8 ring rows, 4 blocks per SM (the fastest measured on the
+    512-instance batch, sides 64-512)."""
+    cpt = 2 if max_nx <= 1024 else 4
     threads = max(32, ((max_nx + cpt - 1) // cpt + 31) // 32 * 32)
-    return {"threads": threads, "cpt": cpt, "pf": 8, "blocks_per_sm": 2}
+    return {"threads": threads, "cpt": cpt, "pf": 8, "blocks_per_sm": 4}
 
 
 def candidates_batch_march(max_nx, smem_limit=200 * 1024):

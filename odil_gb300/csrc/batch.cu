@@ -241,8 +241,11 @@ __global__ void __launch_bounds__(1024) batch_march_kernel(odil_wave_batch b,
 // lives in the instance's rhs region).  The iterate's rows stream into
 // shared-memory rings by cp.async, PF - 3 rows ahead, so rows i, i-1 and
 // i-2 are resident when row i is formed; the column-table entries ride in
-// the same copy groups.  The last march writes u = hi + lo in FP64 (exact,
-// integer instructions) as it goes, so its correction never reaches memory:
+// the same copy groups.  The last march writes u = hi + lo in FP64 as it
+// goes (one FP64 add of the two widened floats: exact wherever the sum fits
+// a double, and the value pair_to_f64 forms with integer instructions; the
+// FP64 pipe is otherwise idle here, the integer form would load the issue
+// slots the march needs), so its correction never reaches memory:
 // with two epochs an instance costs a 4-byte write and read of hi and the
 // 8-byte write of u per cell.  The arithmetic is that of the multi-launch
 // path (batch_rows / batch_bnd, batch_march, pair_to_f64), so the results
@@ -360,17 +363,19 @@ __device__ __forceinline__ void fused_march(const WaveDev<float>& g, const PairC
             lsrc += nx;
             cp_async_commit();
         };
-        // FP64 write of a row (result out, iterate h / l of the row).
+        // FP64 write of a row (result out, iterate h / l of the row): the
+        // widening is exact and the FP64 add rounds only where the sum does
+        // not fit a double, as pair_sum_exact does.
         auto write_u = [&](double* to, const float* out, const float* h, const float* l) {
             double uv[CPT];
 #pragma unroll
             for (int c = 0; c < CPT; ++c) {
                 if constexpr (SRC == 0) {
-                    uv[c] = f2d_exact(out[c]);
+                    uv[c] = (double)out[c];
                 } else if constexpr (SRC == 1) {
-                    uv[c] = pair_sum_exact(h[c], out[c]);
+                    uv[c] = __dadd_rn((double)h[c], (double)out[c]);
                 } else {
-                    uv[c] = pair_sum_exact(h[c], __fadd_rn(l[c], out[c]));
+                    uv[c] = __dadd_rn((double)h[c], (double)__fadd_rn(l[c], out[c]));
                 }
             }
             if constexpr (VEC && CPT % 2 == 0) {
