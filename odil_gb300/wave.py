@@ -100,8 +100,16 @@ class WaveKernels:
             if np.asarray(a).shape != (s, ):
                 raise ValueError("boundary array has shape %s, expected (%d,)"
                                  % (np.asarray(a).shape, s))
-        self.bc64 = [torch.as_tensor(np.asarray(a, np.float64),
-                                     device=self.device) for a in bc]
+        # The four FP64 arrays are views of one buffer (each segment starts
+        # on a 16-byte boundary), so new boundary data arrive in one copy.
+        offs, o = [], 0
+        for s in sizes:
+            offs.append(o)
+            o += (s + 1) // 2 * 2
+        self.bc64_all = torch.zeros(o, dtype=torch.float64, device=self.device)
+        self.bc64 = [self.bc64_all[q:q + s] for q, s in zip(offs, sizes)]
+        for d, a in zip(self.bc64, bc):
+            d.copy_(torch.as_tensor(np.asarray(a, np.float64)))
         self.bc32 = [a.float() for a in self.bc64]
         self.p64 = self._params(self.bc64)
         self.p32 = self._params(self.bc32)
