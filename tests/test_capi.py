@@ -61,3 +61,23 @@ def test_shape_errors_without_gpu(built_lib):
     assert lib.odil_wave_march_f64(ctypes.byref(p), ctypes.c_void_p(16),
                                    ctypes.c_void_p(16), None) == -1
     assert lib.odil_wave_workspace_bytes(ctypes.byref(p)) > 256
+
+
+def test_boundary_table_size_and_refusals_without_gpu(built_lib):
+    """The boundary table of a solve from zero holds rows 0 and 1 in full
+    and columns 0 and nx-1 of every further row; the table march refuses,
+    on the host, grids where one lane would hold both edge columns."""
+    lib = _capi.load()
+    p = _capi.OdilWaveParams()
+    p.dt, p.dx, p.c = 0.1, 0.1, 1.0
+    for nt, nx in ((1, 5), (2, 5), (3, 1), (7, 2), (1024, 1024), (300, 777)):
+        p.nt, p.nx = nt, nx
+        want = min(nt, 2) * nx + max(nt - 2, 0) * min(nx, 2)
+        assert lib.odil_wave_boundary_cells(ctypes.byref(p)) == want
+    p.nt, p.nx = 0, 4
+    assert lib.odil_wave_boundary_cells(ctypes.byref(p)) == 0
+    p.nt, p.nx = 16, 4  # nx <= cpt 4: refused before anything launches
+    st = lib.odil_wave_march_tiled_table_f32(
+        ctypes.byref(p), ctypes.c_void_p(256), ctypes.c_void_p(256), 4, 48,
+        16, 1, 0, None)
+    assert st == -1  # ODIL_ERR_SHAPE
