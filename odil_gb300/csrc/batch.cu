@@ -239,8 +239,9 @@ __global__ void __launch_bounds__(1024) batch_march_kernel(odil_wave_batch b,
 // the boundary cells' values (rows 0, 1, columns 0 and nx-1) in FP64,
 // computed by the whole block into a table before each march (the table
 // lives in the instance's rhs region).  The iterate's rows stream into
-// shared-memory rings by cp.async, PF - 3 rows ahead, so rows i, i-1 and
-// i-2 are resident when row i is formed; the column-table entries ride in
+// shared-memory rings by cp.async, PF - 2 rows ahead of the march step,
+// so rows i + 1, i and i - 1 are resident when the right-hand side of row
+// i + 1 is formed during step i; the column-table entries ride in
 // the same copy groups.  The last march writes u = hi + lo in FP64 as it
 // goes (one FP64 add of the two widened floats: exact wherever the sum fits
 // a double, and the value pair_to_f64 forms with integer instructions; the
